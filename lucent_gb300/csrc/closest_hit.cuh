@@ -1,0 +1,127 @@
+// Closest-hit decisions of the reference's CPU intersector, reproduced on the
+// GPU: f32 tests with proven error bounds decide every case they can, and the
+// rest are recomputed in binary64 with the reference's exact operation order.
+#pragma once
+#include "common.cuh"
+
+namespace lucent {
+
+// Inputs whose f32 images stay far from overflow and underflow, so the error
+// bounds below hold: |coordinate| <= 2^30 and 2^-30 <= |dir component| <= 2^30.
+constexpr float kSafeCoord = 1073741824.0f;  // 2^30
+constexpr float kSafeDirLo = 9.3132257e-10f; // 2^-30
+
+LUCENT_DEV bool safe_ray(float3 o, float3 d) {
+  const bool fo = fabsf(o.x) <= kSafeCoord && fabsf(o.y) <= kSafeCoord && fabsf(o.z) <= kSafeCoord;
+  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  const bool fd = ax >= kSafeDirLo && ay >= kSafeDirLo && az >= kSafeDirLo && ax <= kSafeCoord &&
+                  ay <= kSafeCoord && az <= kSafeCoord;
+  return fo && fd;
+}
+
+// Per-ray f32 state. `inv` is the correctly rounded f32 reciprocal.
+struct Ray32 {
+  float3 o, d, inv;
+  int negx, negy, negz;  // sign of inv: which slab bound is the entry
+};
+
+LUCENT_DEV Ray32 make_ray32(float3 o, float3 d) {
+  Ray32 r;
+  r.o = o;
+  r.d = d;
+  r.inv = make_float3(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
+  r.negx = r.inv.x < 0.f;
+  r.negy = r.inv.y < 0.f;
+  r.negz = r.inv.z < 0.f;
+  return r;
+}
+
+// Slab-test classification against the reference's binary64 slab test
+// (src/math/aabb.ts:84-98) with running closest `c` given as f32 bounds.
+enum SlabClass { kCulled = 0, kPass = 1, kAmbiguous = 2 };
+
+// t = (b - o) * inv computed with 3 roundings in f32 and ~3 in f64; the two
+// differ by at most 4 ulp(f32) relative plus an absolute floor for results
+// that fall into the f32 subnormal range.
+constexpr float kSlabRel = 2.384185791e-07f;  // 2^-22
+constexpr float kAbsFloor = 7.8886091e-31f;   // 2^-100
+
+LUCENT_DEV float slab_t(float b, float o, float inv) { return __fmul_rn(__fsub_rn(b, o), inv); }
+LUCENT_DEV float widen(float t) { return __fmaf_ru(fabsf(t), kSlabRel, kAbsFloor); }
+
+LUCENT_DEV SlabClass classify_slab(const Ray32& r, float4 mn, float4 mx, float c_lo, float c_hi) {
+  // Entry/exit per axis: after the reference's swap the entry is the bound the
+  // ray meets first, fixed by the sign of the direction.
+  const float ax0 = slab_t(mn.x, r.o.x, r.inv.x), ax1 = slab_t(mx.x, r.o.x, r.inv.x);
+  const float ay0 = slab_t(mn.y, r.o.y, r.inv.y), ay1 = slab_t(mx.y, r.o.y, r.inv.y);
+  const float az0 = slab_t(mn.z, r.o.z, r.inv.z), az1 = slab_t(mx.z, r.o.z, r.inv.z);
+  const float ex = r.negx ? ax1 : ax0, xx = r.negx ? ax0 : ax1;
+  const float ey = r.negy ? ay1 : ay0, xy = r.negy ? ay0 : ay1;
+  const float ez = r.negz ? az1 : az0, xz = r.negz ? az0 : az1;
+  const float wex = widen(ex), wey = widen(ey), wez = widen(ez);
+  const float wxx = widen(xx), wxy = widen(xy), wxz = widen(xz);
+  const float ex_lo = ex - wex, ey_lo = ey - wey, ez_lo = ez - wez;
+  const float ex_hi = ex + wex, ey_hi = ey + wey, ez_hi = ez + wez;
+  const float xx_lo = xx - wxx, xy_lo = xy - wxy, xz_lo = xz - wxz;
+  const float xx_hi = xx + wxx, xy_hi = xy + wxy, xz_hi = xz + wxz;
+  // Culled for sure: some exit (or c) lies below some entry (or 0). A same-axis
+  // pair can never qualify, since exit >= entry on one axis in both precisions.
+  const float emax_lo = fmaxf(fmaxf(ex_lo, ey_lo), fmaxf(ez_lo, 0.f));
+  const float xmin_hi = fminf(fminf(xx_hi, xy_hi), fminf(xz_hi, c_hi));
+  if (xmin_hi < emax_lo) return kCulled;
+  // Passes for sure: every cross-axis pair, every exit vs 0 and c vs every
+  // entry is ordered with margin. Same-axis pairs are exact (flat boxes).
+  const bool okx = xx_lo >= fmaxf(fmaxf(ey_hi, ez_hi), 0.f);
+  const bool oky = xy_lo >= fmaxf(fmaxf(ex_hi, ez_hi), 0.f);
+  const bool okz = xz_lo >= fmaxf(fmaxf(ex_hi, ey_hi), 0.f);
+  const bool okc = c_lo >= fmaxf(fmaxf(ex_hi, ey_hi), ez_hi);
+  return (okx && oky && okz && okc) ? kPass : kAmbiguous;
+}
+
+// Moller-Trumbore f32 prefilter. Returns false only when the reference's
+// binary64 intersectTriangle (src/math/ray.ts:22-45) with (tMin, c) certainly
+// rejects. Every numerator is bounded by 2^-19 x its absolute-value
+// evaluation (>= 4x the worst-case rounding of either precision: at most 8
+// roundings deep) plus an absolute floor.
+constexpr float kMtRel = 1.9073486e-06f;  // 2^-19
+
+LUCENT_DEV bool mt_candidate(const Ray32& r, float4 a, float4 b, float4 c3, float tmin_lo, float c_hi) {
+  const float3 e1 = make_float3(b.x - a.x, b.y - a.y, b.z - a.z);
+  const float3 e2 = make_float3(c3.x - a.x, c3.y - a.y, c3.z - a.z);
+  const float3 d = r.d;
+  const float3 p = make_float3(d.y * e2.z - d.z * e2.y, d.z * e2.x - d.x * e2.z, d.x * e2.y - d.y * e2.x);
+  const float det = e1.x * p.x + e1.y * p.y + e1.z * p.z;
+  const float3 s = make_float3(r.o.x - a.x, r.o.y - a.y, r.o.z - a.z);
+  const float U = s.x * p.x + s.y * p.y + s.z * p.z;
+  const float3 q = make_float3(s.y * e1.z - s.z * e1.y, s.z * e1.x - s.x * e1.z, s.x * e1.y - s.y * e1.x);
+  const float V = d.x * q.x + d.y * q.y + d.z * q.z;
+  const float T = e2.x * q.x + e2.y * q.y + e2.z * q.z;
+  // Absolute-value evaluations.
+  const float3 ad = make_float3(fabsf(d.x), fabsf(d.y), fabsf(d.z));
+  const float3 ae1 = make_float3(fabsf(e1.x), fabsf(e1.y), fabsf(e1.z));
+  const float3 ae2 = make_float3(fabsf(e2.x), fabsf(e2.y), fabsf(e2.z));
+  const float3 as = make_float3(fabsf(s.x), fabsf(s.y), fabsf(s.z));
+  const float3 ap = make_float3(ad.y * ae2.z + ad.z * ae2.y, ad.z * ae2.x + ad.x * ae2.z, ad.x * ae2.y + ad.y * ae2.x);
+  const float3 aq = make_float3(as.y * ae1.z + as.z * ae1.y, as.z * ae1.x + as.x * ae1.z, as.x * ae1.y + as.y * ae1.x);
+  const float eD = fmaf(ae1.x * ap.x + ae1.y * ap.y + ae1.z * ap.z, kMtRel, kAbsFloor);
+  const float eU = fmaf(as.x * ap.x + as.y * ap.y + as.z * ap.z, kMtRel, kAbsFloor);
+  const float eV = fmaf(ad.x * aq.x + ad.y * aq.y + ad.z * aq.z, kMtRel, kAbsFloor);
+  const float eT = fmaf(ae2.x * aq.x + ae2.y * aq.y + ae2.z * aq.z, kMtRel, kAbsFloor);
+
+  const float A = fabsf(det);
+  if (A + eD < 9.9e-13f) return false;  // |det| < 1e-12 for sure
+  if (A <= eD) return true;             // sign of det unknown: decide in f64
+  const float sg = det < 0.f ? -1.f : 1.f;
+  const float Ua = U * sg, Va = V * sg, Ta = T * sg;
+  const float Ahi = A + eD, Alo = A - eD;
+  if (Ua + eU < 0.f) return false;              // u < 0
+  if (Ua - eU > Ahi) return false;              // u > 1
+  if (Va + eV < 0.f) return false;              // v < 0
+  if (Ua + Va - (eU + eV) > Ahi) return false;  // u + v > 1
+  if (Ta + eT < 0.f) return false;              // t < 0 <= tMin
+  if (Ta + eT <= tmin_lo * Alo * 0.99999905f) return false;          // t <= tMin  (factor 1 - 2^-20)
+  if (Ta - eT >= c_hi * Ahi * 1.00000095f) return false;             // t >= closest (c_hi may be inf)
+  return true;
+}
+
+}  // namespace lucent

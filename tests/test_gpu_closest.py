@@ -1,0 +1,125 @@
+"""GPU closest-hit parity: hit ids equal the oracle's restatement of the
+reference's intersectBVH (src/math/bvh.ts:265-320) bit for bit; t, u, v equal
+the oracle's binary64 values rounded to binary32 (0 ulp; the bar is 2 ulp)."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from lucent_gb300 import DeviceBVH, mesh, workloads
+from lucent_gb300.bvh import BVH, AABB, intersect_bvh
+from refcases import LCG, bvh_vs_brute_rays, random_soup, torus_rays
+
+pytestmark = pytest.mark.gpu
+
+
+def _compare(dev, ob, pos, rays32, t_min=1e-5, t_max=math.inf):
+    ids_o, t_o, u_o, v_o = oracle.intersect_bvh(ob, pos, rays32, t_min, t_max)
+    for exact in (False, True):
+        dev.set_mode(exact)
+        prim, t, u, v = dev.intersect(rays32, t_min, t_max)
+        bad = np.nonzero(prim != ids_o)[0]
+        assert bad.size == 0, "mode=%s: %d id mismatches, first ray %d: gpu %d oracle %d" % (
+            exact, bad.size, bad[:1], prim[bad[:1]], ids_o[bad[:1]])
+        hit = ids_o >= 0
+        assert np.array_equal(t[hit], t_o[hit].astype(np.float32))
+        assert np.array_equal(u[hit], u_o[hit].astype(np.float32))
+        assert np.array_equal(v[hit], v_o[hit].astype(np.float32))
+        assert np.all(np.isinf(t[~hit]))
+    dev.set_mode(False)
+    return ids_o
+
+
+def _dev(pos):
+    ob = oracle.build_bvh(pos)
+    return ob, DeviceBVH(ob.nodes, ob.tri_indices, pos, ob.node_count)
+
+
+def test_reference_soup_case():  # test/bvh.test.ts:90-110 inputs
+    rand = LCG(42)
+    soup = random_soup(2000, rand)
+    ob, dev = _dev(soup)
+    rays = bvh_vs_brute_rays(rand, 400)
+    prim, t, u, v = dev.intersect_f64(rays)
+    ids, to, uo, vo = oracle.intersect_bvh(ob, soup, rays)
+    assert np.array_equal(prim, ids)
+    hit = ids >= 0
+    assert np.array_equal(t[hit], to[hit]) and np.array_equal(u[hit], uo[hit]) and np.array_equal(v[hit], vo[hit])
+    _compare(dev, ob, soup, rays.astype(np.float32))
+
+
+def test_reference_torus_case():  # test/bvh.test.ts:112-124 inputs
+    m = mesh.torus_knot(tubular_segments=80, radial_segments=10)
+    ob, dev = _dev(m.positions)
+    rays = torus_rays(LCG(99), 200)
+    prim, t, _, _ = dev.intersect_f64(rays)
+    ids, to, _, _ = oracle.intersect_bvh(ob, m.positions, rays)
+    assert np.array_equal(prim, ids) and np.array_equal(t[ids >= 0], to[ids >= 0])
+
+
+def test_random_soup_subset():
+    pos, rays = workloads.soup_and_rays(seed=0, n_tri=65536, n_rays=200_000)
+    ob, dev = _dev(pos)
+    ids = _compare(dev, ob, pos, rays)
+    assert (ids >= 0).mean() > 0.3
+
+
+def test_adversarial_rays_mesh():
+    m = mesh.merge_meshes([mesh.torus_knot(tubular_segments=120, radial_segments=16),
+                           mesh.box([-2, -2, -2], [2, 2, 2], inward=True),
+                           mesh.transform(mesh.box([-0.5, -0.5, -0.5], [0.5, 0.5, 0.5]), rotate_y=0.3)])
+    ob, dev = _dev(m.positions)
+    rng = np.random.Generator(np.random.PCG64(5))
+    rays = workloads.adversarial_rays(m.positions, rng, 1500)
+    for t_min, t_max in ((1e-5, math.inf), (0.0, math.inf), (1e-6, 2.5), (0.5, 3.0)):
+        _compare(dev, ob, m.positions, rays, t_min, t_max)
+
+
+def test_adversarial_rays_soup():
+    pos, _ = workloads.soup_and_rays(seed=3, n_tri=4096, n_rays=1)
+    ob, dev = _dev(pos)
+    rays = workloads.adversarial_rays(pos, np.random.Generator(np.random.PCG64(9)), 2000)
+    _compare(dev, ob, pos, rays)
+
+
+def test_coincident_and_duplicate_triangles():  # bvh.test.ts:78-86 plus exact ties
+    one = np.array([0, 0, 0, 1, 0, 0, 0, 1, 0], np.float32)
+    soup = np.tile(one, 64)
+    ob, dev = _dev(soup)
+    rays = np.array([[0.2, 0.2, -1, 0, 0, 1], [0.25, 0.25, 1, 0, 0, -1], [0.5, 0.5, -1, 0, 0, 1],
+                     [0.1, 0.1, -1, 0.01, 0.02, 1]], np.float32)
+    ids = _compare(dev, ob, soup, rays)
+    assert ids[0] >= 0
+
+
+def test_empty_and_single():
+    ob = oracle.build_bvh(np.zeros(0, np.float32))
+    dev = DeviceBVH(ob.nodes, ob.tri_indices, np.zeros(0, np.float32), ob.node_count)
+    prim, t, _, _ = dev.intersect(np.array([[0, 0, 0, 0, 0, 1]], np.float32))
+    assert prim[0] == -1 and np.isinf(t[0])
+    tri = np.array([0, 0, 0, 1, 0, 0, 0, 1, 0], np.float32)
+    ob, dev = _dev(tri)
+    _compare(dev, ob, tri, np.array([[0.2, 0.2, -1, 0, 0, 1], [2, 2, -1, 0, 0, 1]], np.float32))
+
+
+def test_pick_api_mirrors_reference():
+    soup = random_soup(300, LCG(3))
+    ob = oracle.build_bvh(soup)
+    bvh = BVH(ob.nodes, ob.node_count, ob.tri_indices, AABB(ob.bounds[:3], ob.bounds[3:]))
+    ray = {"origin": [0.0, 0.0, -20.0], "dir": [0.0, 0.0, 1.0]}
+    h = intersect_bvh(bvh, soup, ray)
+    ids, t, u, v = oracle.intersect_bvh(ob, soup, np.array([[0, 0, -20, 0, 0, 1.0]]))
+    if ids[0] < 0:
+        assert h is None
+    else:
+        assert (h.tri_index, h.t, h.u, h.v) == (ids[0], t[0], u[0], v[0])
+
+
+def test_invalid_bvh_rejected():
+    from lucent_gb300 import LucentError
+    ob = oracle.build_bvh(random_soup(50, LCG(1)))
+    bad = ob.nodes.copy()
+    bad[3] = 1e6  # root's children far outside the node array
+    with pytest.raises(LucentError):
+        DeviceBVH(bad, ob.tri_indices, random_soup(50, LCG(1)), ob.node_count)
