@@ -40,15 +40,37 @@ int32_t lucent_version(void);
  * ------------------------------------------------------------------------- */
 typedef struct lucent_bvh_opts {
   uint32_t max_leaf_size; /* BVHOptions.maxLeafSize, default 4 (bvh.ts:33) */
-  uint32_t bins;          /* BVHOptions.bins, default 12 (bvh.ts:33) */
+  uint32_t bins;          /* BVHOptions.bins, default 12 (bvh.ts:33); at most 32 */
 } lucent_bvh_opts;
+
+typedef struct lucent_bvh lucent_bvh;
+
+/* buildBVH(positions, opts) (bvh.ts:52). `positions` = n_floats host floats,
+ * 9 per triangle (n_floats % 9 != 0 fails as in bvh.ts:55-57; non-finite
+ * values and more than 2^23 triangles are rejected). `opts` may be NULL for
+ * the reference's defaults. Outputs (each may be NULL): nodes_out holds
+ * max(1, 2N-1) * 8 floats (the reference's allocation, bvh.ts:79),
+ * tri_indices_out N u32, bounds_out 6 doubles [min.xyz, max.xyz]. When
+ * handle_out is non-NULL the built BVH also stays on the device as a
+ * lucent_bvh ready for lucent_bvh_intersect (no re-upload). Node bounds equal
+ * the reference's as numbers (the sign of a zero bound is not reproduced). */
+lucent_status lucent_bvh_build(const float* positions, uint64_t n_floats, const lucent_bvh_opts* opts,
+                               float* nodes_out, uint32_t* node_count_out, uint32_t* tri_indices_out,
+                               double* bounds_out, lucent_bvh** handle_out, void* stream);
+/* Same over device-resident positions (9 floats per triangle); creates the
+ * device BVH only. The replacement for buildBVHAsync (bvh-async.ts:8): the
+ * build never runs on the calling CPU thread's critical path. */
+lucent_status lucent_bvh_build_device(const float* positions_d, uint32_t tri_count, const lucent_bvh_opts* opts,
+                                      lucent_bvh** handle_out, void* stream);
+/* Copies a device BVH back in the reference's layout (buffers sized by the
+ * caller: node_count * 8 floats, tri_count u32). */
+lucent_status lucent_bvh_download(const lucent_bvh* bvh, float* nodes_out, uint32_t* tri_indices_out);
 
 /* ---------------------------------------------------------------------------
  * Closest hit: intersectBVH (src/math/bvh.ts:265-320). Hit ids equal the
  * reference's on identical rays; t, u, v are the reference's binary64 values
  * rounded to binary32.
  * ------------------------------------------------------------------------- */
-typedef struct lucent_bvh lucent_bvh;
 
 /* Uploads a BVH in the reference's layout: `nodes` = node_count * 8 floats
  * [min.xyz, leftFirst, max.xyz, count] (bvh.ts:6-16), `tri_indices` = the

@@ -7,6 +7,6 @@ include/lucent.h. Modules:
   workloads seeded synthetic scenes and ray sets
 """
 from ._native import LucentError, NativeMissing, lib  # noqa: F401
-from .bvh import BVH, BVHHit, DeviceBVH, NODE_STRIDE, intersect_bvh  # noqa: F401
+from .bvh import BVH, BVHHit, DeviceBVH, NODE_STRIDE, build_bvh, build_bvh_async, intersect_bvh  # noqa: F401
 
-__all__ = ["BVH", "BVHHit", "DeviceBVH", "NODE_STRIDE", "intersect_bvh", "LucentError", "NativeMissing", "lib"]
+__all__ = ["BVH", "BVHHit", "DeviceBVH", "NODE_STRIDE", "build_bvh", "build_bvh_async", "intersect_bvh", "LucentError", "NativeMissing", "lib"]

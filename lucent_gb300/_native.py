@@ -29,6 +29,12 @@ class NativeMissing(ImportError):
 
 _lib = None
 P = C.POINTER
+
+
+class BvhOpts(C.Structure):
+    """lucent_bvh_opts (include/lucent.h)."""
+    _fields_ = [("max_leaf_size", C.c_uint32), ("bins", C.c_uint32)]
+
 F32P, F64P, I32P, U32P, U8P = P(C.c_float), P(C.c_double), P(C.c_int32), P(C.c_uint32), P(C.c_uint8)
 VP = C.c_void_p
 
@@ -42,6 +48,9 @@ def _sig(L, name, args, res=C.c_int32):
 def _declare(L):
     _sig(L, "lucent_last_error", [], C.c_char_p)
     _sig(L, "lucent_version", [])
+    _sig(L, "lucent_bvh_build", [F32P, C.c_uint64, VP, F32P, U32P, U32P, F64P, P(VP), VP])
+    _sig(L, "lucent_bvh_build_device", [VP, C.c_uint32, VP, P(VP), VP])
+    _sig(L, "lucent_bvh_download", [VP, F32P, U32P])
     _sig(L, "lucent_bvh_create", [F32P, C.c_uint32, U32P, C.c_uint32, F32P, P(VP)])
     _sig(L, "lucent_bvh_destroy", [VP], None)
     _sig(L, "lucent_bvh_info", [VP, U32P, U32P])

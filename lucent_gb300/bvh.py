@@ -121,3 +121,67 @@ def intersect_bvh(bvh: BVH, positions, ray, t_min=1e-5, t_max=math.inf) -> Optio
     if prim[0] < 0:
         return None
     return BVHHit(float(t[0]), int(prim[0]), float(u[0]), float(v[0]))
+
+
+def _wrap_handle(h, node_count, tri_count):
+    dev = DeviceBVH.__new__(DeviceBVH)
+    dev._h = h
+    dev.node_count = node_count
+    dev.tri_count = tri_count
+    return dev
+
+
+def build_bvh(positions, max_leaf_size=4, bins=12, stream=None) -> BVH:
+    """buildBVH (bvh.ts:52-252) on the GPU: the reference's node array, triIndices and bounds.
+
+    The returned BVH also keeps its device copy, so intersect calls need no upload.
+    """
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1)
+    if pos.size % 9:
+        raise ValueError("positions length %d is not a multiple of 9" % pos.size)  # bvh.ts:55-57
+    n = pos.size // 9
+    nodes = np.zeros(max(1, 2 * n - 1) * NODE_STRIDE, np.float32)
+    tri = np.zeros(max(n, 1), np.uint32)
+    cnt = C.c_uint32()
+    bounds = np.zeros(6, np.float64)
+    opts = N.BvhOpts(max_leaf_size, bins)
+    h = C.c_void_p()
+    N.check(N.lib().lucent_bvh_build(N.ptr(pos, C.c_float), pos.size, C.byref(opts), N.ptr(nodes, C.c_float),
+                                     C.byref(cnt), N.ptr(tri, C.c_uint32), N.ptr(bounds, C.c_double), C.byref(h),
+                                     stream))
+    nc = cnt.value
+    b = BVH(nodes[: nc * NODE_STRIDE].copy(), nc, tri[:n].copy(), AABB(bounds[:3], bounds[3:]))
+    b._device = _wrap_handle(h, nc, n)
+    return b
+
+
+def build_bvh_async(positions, max_leaf_size=4, bins=12):
+    """buildBVHAsync (bvh-async.ts:8): a future resolving to the BVH.
+
+    The GPU build does not occupy the page's thread in the reference's sense;
+    the future runs it on a worker thread so callers keep their own loop going.
+    """
+    import concurrent.futures as cf
+    ex = cf.ThreadPoolExecutor(max_workers=1)
+    fut = ex.submit(build_bvh, positions, max_leaf_size, bins)
+    ex.shutdown(wait=False)
+    return fut
+
+
+def build_device(positions_ptr, tri_count, max_leaf_size=4, bins=12, stream=None) -> DeviceBVH:
+    """Builds from device-resident positions (an int pointer); returns only the device BVH."""
+    opts = N.BvhOpts(max_leaf_size, bins)
+    h = C.c_void_p()
+    N.check(N.lib().lucent_bvh_build_device(positions_ptr, tri_count, C.byref(opts), C.byref(h), stream))
+    nc = C.c_uint32()
+    tc = C.c_uint32()
+    N.check(N.lib().lucent_bvh_info(h, C.byref(nc), C.byref(tc)))
+    return _wrap_handle(h, nc.value, tc.value)
+
+
+def download(dev: DeviceBVH):
+    """Reference-layout (nodes, triIndices) of a device BVH."""
+    nodes = np.zeros(dev.node_count * NODE_STRIDE, np.float32)
+    tri = np.zeros(max(dev.tri_count, 1), np.uint32)
+    N.check(N.lib().lucent_bvh_download(dev.handle, N.ptr(nodes, C.c_float), N.ptr(tri, C.c_uint32)))
+    return nodes, tri[: dev.tri_count]

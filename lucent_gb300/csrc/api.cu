@@ -1,5 +1,6 @@
 // C ABI: status codes, thread-local error text, BVH handle for closest-hit.
 #include <cmath>
+#include <cstring>
 #include <cstdarg>
 #include <cstdio>
 #include <string>
@@ -132,6 +133,71 @@ lucent_status lucent_bvh_create(const float* nodes, uint32_t node_count, const u
   return LUCENT_OK;
 }
 
+static lucent_status build_common(const float* pos_d, uint32_t n, const lucent_bvh_opts* opts, cudaStream_t s,
+                                  float* nodes_out, uint32_t* node_count_out, uint32_t* tri_out, double* bounds_out,
+                                  lucent_bvh** handle_out) {
+  const int max_leaf = opts ? (int)opts->max_leaf_size : 4;  // bvh.ts:33 defaults
+  const int bins = opts ? (int)opts->bins : 12;
+  std::vector<float> nodes;
+  std::vector<uint32_t> tri;
+  double bounds[6];
+  lucent_bvh* b = handle_out ? new lucent_bvh() : nullptr;
+  lucent_status st = gpu_build_bvh(pos_d, n, max_leaf, bins, s, nodes, tri, bounds, b ? &b->nodes : nullptr,
+                                   b ? &b->tris : nullptr);
+  if (st) {
+    lucent_bvh_destroy(b);
+    return st;
+  }
+  const uint32_t nc = (uint32_t)(nodes.size() / 8);
+  if (nodes_out) memcpy(nodes_out, nodes.data(), nodes.size() * 4);
+  if (node_count_out) *node_count_out = nc;
+  if (tri_out && n) memcpy(tri_out, tri.data(), (size_t)n * 4);
+  if (bounds_out) memcpy(bounds_out, bounds, sizeof bounds);
+  if (b) {
+    b->node_count = nc;
+    b->tri_count = n;
+    *handle_out = b;
+  }
+  return LUCENT_OK;
+}
+
+lucent_status lucent_bvh_build(const float* positions, uint64_t n_floats, const lucent_bvh_opts* opts,
+                               float* nodes_out, uint32_t* node_count_out, uint32_t* tri_indices_out,
+                               double* bounds_out, lucent_bvh** handle_out, void* stream) {
+  clear_error();
+  if (handle_out) *handle_out = nullptr;
+  if (n_floats % 9 != 0)  // bvh.ts:55-57
+    return fail(LUCENT_ERR_INVALID, "positions length %llu is not a multiple of 9", (unsigned long long)n_floats);
+  if (n_floats && !positions) return fail(LUCENT_ERR_INVALID, "null positions");
+  const uint64_t n = n_floats / 9;
+  if (n > (1u << 23)) return fail(LUCENT_ERR_UNSUPPORTED, "%llu triangles; the limit is 2^23", (unsigned long long)n);
+  for (uint64_t i = 0; i < n_floats; i++)
+    if (!std::isfinite(positions[i])) return fail(LUCENT_ERR_UNSUPPORTED, "positions[%llu] is not finite", (unsigned long long)i);
+  cudaStream_t s = (cudaStream_t)stream;
+  DeviceBuffer pos;
+  lucent_status st = pos.reserve(n_floats * 4 + 4);
+  if (st) return st;
+  cudaError_t e = cudaMemcpyAsync(pos.ptr, positions, n_floats * 4, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) {
+    pos.release();
+    return cuda_fail(e, "upload positions");
+  }
+  st = build_common((const float*)pos.ptr, (uint32_t)n, opts, s, nodes_out, node_count_out, tri_indices_out,
+                    bounds_out, handle_out);
+  cudaStreamSynchronize(s);
+  pos.release();
+  return st;
+}
+
+lucent_status lucent_bvh_build_device(const float* positions_d, uint32_t tri_count, const lucent_bvh_opts* opts,
+                                      lucent_bvh** handle_out, void* stream) {
+  clear_error();
+  if (!handle_out || (tri_count && !positions_d)) return fail(LUCENT_ERR_INVALID, "null argument");
+  *handle_out = nullptr;
+  return build_common(positions_d, tri_count, opts, (cudaStream_t)stream, nullptr, nullptr, nullptr, nullptr,
+                      handle_out);
+}
+
 void lucent_bvh_destroy(lucent_bvh* b) {
   if (!b) return;
   b->nodes.release();
@@ -147,6 +213,22 @@ lucent_status lucent_bvh_info(const lucent_bvh* b, uint32_t* node_count, uint32_
   if (node_count) *node_count = b->node_count;
   if (tri_count) *tri_count = b->tri_count;
   return LUCENT_OK;
+}
+
+lucent_status lucent_bvh_download(const lucent_bvh* b, float* nodes_out, uint32_t* tri_indices_out) {
+  clear_error();
+  if (!b || !nodes_out || (b->tri_count && !tri_indices_out)) return fail(LUCENT_ERR_INVALID, "null argument");
+  DeviceBuffer tmp;
+  lucent_status st = tmp.reserve((size_t)b->node_count * 32 + (size_t)b->tri_count * 4 + 16);
+  if (st) return st;
+  float* ref_d = (float*)tmp.ptr;
+  uint32_t* idx_d = (uint32_t*)((char*)tmp.ptr + (size_t)b->node_count * 32);
+  launch_unpack((const Node*)b->nodes.ptr, b->node_count, (const float4*)b->tris.ptr, b->tri_count, ref_d, idx_d, 0);
+  cudaError_t e = cudaMemcpy(nodes_out, ref_d, (size_t)b->node_count * 32, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && b->tri_count)
+    e = cudaMemcpy(tri_indices_out, idx_d, (size_t)b->tri_count * 4, cudaMemcpyDeviceToHost);
+  tmp.release();
+  return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "download bvh");
 }
 
 lucent_status lucent_bvh_set_mode(lucent_bvh* b, int32_t mode) {

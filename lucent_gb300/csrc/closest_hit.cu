@@ -225,6 +225,20 @@ __global__ void k_gather_tris(const float* __restrict__ pos, const uint32_t* __r
   }
 }
 
+// Inverse of the two kernels above: back to the reference's layout.
+__global__ void k_unpack(const Node* __restrict__ nodes, uint32_t count, const float4* __restrict__ tris,
+                         uint32_t tri_count, float* __restrict__ ref, uint32_t* __restrict__ tri_indices) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count || i < tri_count; i += gridDim.x * blockDim.x) {
+    if (i < count) {
+      const Node nd = nodes[i];
+      float* r = ref + (size_t)i * 8;
+      r[0] = nd.lo.x, r[1] = nd.lo.y, r[2] = nd.lo.z, r[3] = (float)node_first(nd);
+      r[4] = nd.hi.x, r[5] = nd.hi.y, r[6] = nd.hi.z, r[7] = (float)node_count(nd);
+    }
+    if (i < tri_count) tri_indices[i] = (uint32_t)__float_as_int(tris[3 * (size_t)i].w);
+  }
+}
+
 static int grid_for(uint32_t n, int block) {
   int g = (int)((n + block - 1) / block);
   return g < 1 ? 1 : (g > 65535 * 16 ? 65535 * 16 : g);
@@ -237,6 +251,12 @@ void launch_pack_nodes(const float* ref_d, uint32_t count, Node* out_d, cudaStre
 void launch_gather_tris(const float* pos_d, const uint32_t* idx_d, uint32_t tri_count, float4* out_d,
                         cudaStream_t s) {
   k_gather_tris<<<grid_for(tri_count, 256), 256, 0, s>>>(pos_d, idx_d, tri_count, out_d);
+}
+
+void launch_unpack(const Node* nodes, uint32_t count, const float4* tris, uint32_t tri_count, float* ref_d,
+                   uint32_t* idx_d, cudaStream_t s) {
+  k_unpack<<<grid_for(count > tri_count ? count : tri_count, 256), 256, 0, s>>>(nodes, count, tris, tri_count, ref_d,
+                                                                                idx_d);
 }
 
 void launch_closest(const Node* nodes, uint32_t node_count, const float4* tris, const float* rays_d, uint32_t n, double tMin,

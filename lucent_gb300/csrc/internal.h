@@ -3,6 +3,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
+#include "../../include/lucent.h"
 #include "common.cuh"
 
 namespace lucent {
@@ -10,10 +13,17 @@ namespace lucent {
 void launch_pack_nodes(const float* ref_d, uint32_t count, Node* out_d, cudaStream_t s);
 void launch_gather_tris(const float* pos_d, const uint32_t* idx_d, uint32_t tri_count, float4* out_d,
                         cudaStream_t s);
+void launch_unpack(const Node* nodes, uint32_t count, const float4* tris, uint32_t tri_count, float* ref_d,
+                   uint32_t* idx_d, cudaStream_t s);
 void launch_closest(const Node* nodes, uint32_t node_count, const float4* tris, const float* rays_d, uint32_t n, double tMin,
                     double tMax, int32_t* prim, float* t, float* u, float* v, uint32_t* queue, uint32_t* queue_len,
                     unsigned* err, bool exact_only, cudaStream_t s);
 void launch_closest_d(const Node* nodes, uint32_t node_count, const float4* tris, const double* rays_d, uint32_t n, double tMin,
                       double tMax, int32_t* prim, double* t, double* u, double* v, unsigned* err, cudaStream_t s);
+
+struct DeviceBuffer;
+lucent_status gpu_build_bvh(const float* pos_d, uint32_t n, int max_leaf, int bins, cudaStream_t s,
+                            std::vector<float>& nodes_ref, std::vector<uint32_t>& tri_out, double bounds[6],
+                            DeviceBuffer* nodes_dev, DeviceBuffer* tris_dev);
 
 }  // namespace lucent

@@ -49,6 +49,8 @@ def _declare(L):
     L.orc_aabb_intersect.restype = _D
     L.orc_glsl_traversal_counts.argtypes = [P(_F), _U32, P(_F), _U32, P(_F), C.c_uint64, _F, P(_U32),
                                             P(_U32), P(_I32), C.c_int]
+    L.orc_ts_traversal_counts.argtypes = [P(_F), P(_U32), _U32, P(_F), P(_F), C.c_uint64, _D, _D, P(_U32),
+                                          P(_U32), C.c_int]
     L.orc_build_alias.argtypes = [P(_D), _U32, P(_F), P(_U32), P(_D), P(_D)]
     L.orc_build_env_sampler.argtypes = [P(_F), _U32, _U32, _U32, P(_U32), P(_U32), P(_F), P(_D)]
     L.orc_sheen_albedo.argtypes = [_D, _D, C.c_int]
@@ -173,6 +175,27 @@ def glsl_traversal_counts(nodes, node_count, geo, rays, t_min=1e-6, threads=0):
                                     g.size // 12, _p(r, _F), n, t_min, _p(inner, _U32), _p(tris, _U32),
                                     _p(slot, _I32), threads)
     return inner, tris, slot
+
+
+def ts_traversal_counts(bvh, positions, rays, t_min=1e-5, t_max=np.inf, threads=0):
+    """Nodes popped / triangles tested per ray in intersectBVH's left-first order."""
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+    n = r.shape[0]
+    popped = np.empty(n, np.uint32)
+    tests = np.empty(n, np.uint32)
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1)
+    lib().orc_ts_traversal_counts(_p(bvh.nodes, _F), _p(np.ascontiguousarray(bvh.tri_indices, np.uint32), _U32),
+                                  bvh.tri_indices.size, _p(pos, _F), _p(r, _F), n, t_min, t_max,
+                                  _p(popped, _U32), _p(tests, _U32), threads)
+    return popped, tests
+
+
+def leaf_order_geometry(bvh, positions):
+    """Triangles gathered into slot order, 12 floats each (the GLSL geo layout)."""
+    tri = np.asarray(positions, np.float32).reshape(-1, 3, 3)[bvh.tri_indices]
+    g = np.zeros((tri.shape[0], 3, 4), np.float32)
+    g[:, :, :3] = tri
+    return g.reshape(-1)
 
 
 def build_alias(weights):

@@ -417,6 +417,51 @@ int orc_intersect_bvh_f32(const float* nodes, uint32_t node_count, const uint32_
   return overflow ? ORC_ERR_STACK : ORC_OK;
 }
 
+// Work counts of intersectBVH's own order (bvh.ts:283-318): nodes popped and
+// triangles tested per ray.
+int orc_ts_traversal_counts(const float* nodes, const uint32_t* tri, uint32_t tri_count, const float* positions,
+                            const float* rays, uint64_t n, double t_min, double t_max, uint32_t* popped_out,
+                            uint32_t* tests_out, int threads) {
+  parallel_for(n, threads, [&](uint64_t b, uint64_t e) {
+    for (uint64_t r = b; r < e; r++) {
+      const float* ry = rays + r * 6;
+      const V3 o{ry[0], ry[1], ry[2]}, d{ry[3], ry[4], ry[5]};
+      const double org[3] = {o.x, o.y, o.z};
+      const double inv[3] = {1.0 / d.x, 1.0 / d.y, 1.0 / d.z};
+      uint32_t popped = 0, tests = 0;
+      if (tri_count) {
+        int32_t stack[64];
+        int sp = 0;
+        stack[sp++] = 0;
+        double closest = t_max;
+        while (sp > 0) {
+          const int32_t nn = stack[--sp];
+          popped++;
+          const float* nd = nodes + (uint64_t)nn * 8;
+          const double mn[3] = {nd[0], nd[1], nd[2]}, mx[3] = {nd[4], nd[5], nd[6]};
+          if (slab(mn, mx, org, inv, closest) == INF) continue;
+          if (nd[7] > 0) {
+            for (int i = 0; i < (int)nd[7]; i++) {
+              const uint32_t t = tri[(uint64_t)nd[3] + i];
+              tests++;
+              double th, uh, vh;
+              if (tri_hit(o, d, vtx(positions, t, 0), vtx(positions, t, 1), vtx(positions, t, 2), t_min, closest,
+                          th, uh, vh))
+                closest = th;
+            }
+          } else if (sp + 2 <= 64) {
+            stack[sp++] = (int32_t)nd[3] + 1;
+            stack[sp++] = (int32_t)nd[3];
+          }
+        }
+      }
+      popped_out[r] = popped;
+      tests_out[r] = tests;
+    }
+  });
+  return ORC_OK;
+}
+
 int orc_intersect_all(const float* positions, uint32_t tri_count, const double* rays, uint64_t n, double t_min,
                       double t_max, int32_t* id_out, double* t_out, double* u_out, double* v_out, int threads) {
   parallel_for(n, threads, [&](uint64_t b, uint64_t e) {

@@ -45,6 +45,11 @@ int orc_intersect_bvh_f32(const float* nodes, uint32_t node_count, const uint32_
                           const float* positions, const float* rays, uint64_t n, double t_min, double t_max,
                           int32_t* id_out, double* t_out, double* u_out, double* v_out, int threads);
 
+/* Nodes popped / triangles tested per ray in intersectBVH's own order. */
+int orc_ts_traversal_counts(const float* nodes, const uint32_t* tri, uint32_t tri_count, const float* positions,
+                            const float* rays, uint64_t n, double t_min, double t_max, uint32_t* popped_out,
+                            uint32_t* tests_out, int threads);
+
 /* intersectAllTriangles (src/math/bvh.ts:323-348), brute force. */
 int orc_intersect_all(const float* positions, uint32_t tri_count, const double* rays, uint64_t n,
                       double t_min, double t_max, int32_t* id_out, double* t_out, double* u_out,

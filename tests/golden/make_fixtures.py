@@ -1,0 +1,53 @@
+"""Generates the committed fixtures in tests/golden/ from the oracle.
+
+algorithmic_bytes.json: per-ray algorithmic bytes of each benchmark workload,
+counted by the oracle under the reference's GLSL traversal order
+(src/shaders/scene.glsl:218-267: near-first, both child boxes read per inner
+node): 64 B per inner node visited + 48 B per triangle tested + 24 B ray in +
+16 B hit out. bench.py divides these by the measured kernel time for its
+roofline; tests/test_fixtures.py re-derives them so they cannot go stale.
+
+Run: python tests/golden/make_fixtures.py
+"""
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+import oracle  # noqa: E402
+from lucent_gb300 import workloads  # noqa: E402
+
+
+def closest_bytes(n_rays=200_000):
+    """Random soup workload; the mean over the first n_rays of its 10^6 rays."""
+    pos, rays = workloads.soup_and_rays(seed=0, n_tri=65536, n_rays=1_000_000)
+    ob = oracle.build_bvh(pos)
+    geo = oracle.leaf_order_geometry(ob, pos)
+    inner, tris, _ = oracle.glsl_traversal_counts(ob.nodes, ob.node_count, geo, rays[:n_rays], 1e-5)
+    popped, tests = oracle.ts_traversal_counts(ob, pos, rays[:n_rays])
+    per_ray = 64.0 * inner.mean() + 48.0 * tris.mean() + 24 + 16
+    return {"bytes_per_ray": round(float(per_ray), 2), "inner_nodes_per_ray": round(float(inner.mean()), 3),
+            "triangles_per_ray": round(float(tris.mean()), 3), "rays_sampled": n_rays,
+            "reference_order_nodes_per_ray": round(float(popped.mean()), 3),
+            "reference_order_triangles_per_ray": round(float(tests.mean()), 3)}
+
+
+def main():
+    path = os.path.join(HERE, "algorithmic_bytes.json")
+    out = json.load(open(path)) if os.path.exists(path) else {}
+    out["closest"] = closest_bytes()
+    try:
+        from tests.golden import make_render_fixtures  # noqa: F401
+    except ImportError:
+        pass
+    json.dump(out, open(path, "w"), indent=1, sort_keys=True)
+    print(json.dumps(out, indent=1))
+
+
+if __name__ == "__main__":
+    main()
