@@ -59,6 +59,9 @@ void DeviceBuffer::release() {
 
 struct lucent_bvh {
   uint32_t node_count = 0, tri_count = 0;
+  // Tree depth (root = 0). Trees whose depth could overflow the reference's
+  // 64-entry stack take the all-binary64 path, which reproduces the overflow.
+  uint32_t depth = 0;
   int mode = LUCENT_TRAVERSE_FAST;
   DeviceBuffer nodes, tris, scratch, stage;
 };
@@ -67,6 +70,24 @@ extern "C" {
 
 const char* lucent_last_error(void) { return g_last_error.c_str(); }
 int32_t lucent_version(void) { return 100; }
+
+// Depth of a (validated) reference-layout tree; root = 0.
+static uint32_t tree_depth(const float* nodes, uint32_t node_count, uint32_t tri_count) {
+  if (tri_count == 0 || node_count == 0) return 0;
+  std::vector<std::pair<uint32_t, uint32_t>> st{{0u, 0u}};
+  uint32_t depth = 0;
+  while (!st.empty()) {
+    const auto [n, d] = st.back();
+    st.pop_back();
+    depth = d > depth ? d : depth;
+    const float* r = nodes + (size_t)n * 8;
+    if (r[7] > 0) continue;
+    const uint32_t l = (uint32_t)r[3];
+    st.push_back({l, d + 1});
+    st.push_back({l + 1, d + 1});
+  }
+  return depth;
+}
 
 // Validates the reference layout so that no kernel can read out of bounds:
 // children inside the array, leaf ranges inside triIndices, indices in range.
@@ -103,6 +124,7 @@ lucent_status lucent_bvh_create(const float* nodes, uint32_t node_count, const u
   lucent_bvh* b = new lucent_bvh();
   b->node_count = node_count;
   b->tri_count = tri_count;
+  b->depth = tree_depth(nodes, node_count, tri_count);
   DeviceBuffer ref, pos, idx;
   cudaStream_t s = 0;
   auto cleanup = [&](lucent_status code) {
@@ -156,6 +178,7 @@ static lucent_status build_common(const float* pos_d, uint32_t n, const lucent_b
   if (b) {
     b->node_count = nc;
     b->tri_count = n;
+    b->depth = tree_depth(nodes.data(), nc, n);
     *handle_out = b;
   }
   return LUCENT_OK;
@@ -244,16 +267,17 @@ static lucent_status check_tmin(double t_min, double t_max) {
   return LUCENT_OK;
 }
 
-// Scratch layout: [err word][queue length][pad..][queue: n u32]
+// Scratch layout: [err word][queue length][work counter][pad..][queue: n u32]
 static lucent_status prepare_scratch(lucent_bvh* b, uint32_t n, cudaStream_t s, unsigned** err, uint32_t** qlen,
-                                     uint32_t** queue) {
+                                     uint32_t** queue, uint32_t** work = nullptr) {
   lucent_status st = b->scratch.reserve(256 + (size_t)n * 4);
   if (st) return st;
   char* base = (char*)b->scratch.ptr;
   *err = (unsigned*)base;
   *qlen = (uint32_t*)(base + 4);
+  if (work) *work = (uint32_t*)(base + 8);
   *queue = (uint32_t*)(base + 256);
-  cudaError_t e = cudaMemsetAsync(base, 0, 8, s);
+  cudaError_t e = cudaMemsetAsync(base, 0, 12, s);
   if (e != cudaSuccess) return cuda_fail(e, "memset scratch");
   return LUCENT_OK;
 }
@@ -267,15 +291,15 @@ lucent_status lucent_bvh_intersect_device(lucent_bvh* b, const float* rays_d, ui
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
   unsigned* err;
-  uint32_t *qlen, *queue;
-  if ((st = prepare_scratch(b, n, s, &err, &qlen, &queue))) return st;
+  uint32_t *qlen, *queue, *work;
+  if ((st = prepare_scratch(b, n, s, &err, &qlen, &queue, &work))) return st;
   if (n == 0) return LUCENT_OK;
   if (b->tri_count == 0) {  // bvh.ts:274: an empty BVH never hits
     cudaError_t e = cudaMemsetAsync(prim_d, 0xff, (size_t)n * 4, s);
     return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "memset");
   }
   launch_closest((const Node*)b->nodes.ptr, b->node_count, (const float4*)b->tris.ptr, rays_d, n, t_min, t_max, prim_d, t_d, u_d,
-                 v_d, queue, qlen, err, b->mode == LUCENT_TRAVERSE_EXACT, s);
+                 v_d, queue, qlen, work, err, b->mode == LUCENT_TRAVERSE_EXACT || b->depth + 2 > kTsStack, s);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "closest-hit launch");
 }

@@ -134,71 +134,195 @@ __global__ void k_closest_exact_d(const Node* __restrict__ nodes, uint32_t node_
   }
 }
 
-// Fast path. Rays outside the bounded-error range are queued for the slow path.
-__global__ void __launch_bounds__(256) k_closest_fast(const Node* __restrict__ nodes, uint32_t node_limit,
+// Fast path: persistent warps, one ray per lane, lanes refill from a global
+// counter as their rays finish. The reference's traversal order is kept:
+// both children of an inner node are tested with the current closest `c`
+// (exactly what the reference's pop of the left child, and of the right one if
+// the left is culled, would test); a right child that passes is pushed with an
+// upper bound on its entry distance, and is re-tested when popped only if `c`
+// has since dropped below that bound (the cull test is monotone in `c`).
+// `c` is carried as binary32 bounds [c_lo, c_hi] of the reference's binary64
+// value; the binary64 value itself is computed only when a decision needs it.
+// Rays outside the bounded-error range are queued for the slow path.
+struct PendingNode {
+  int node;
+  float ehi;
+};
+
+__device__ __forceinline__ D3 inv_exact(float3 d) {
+  return {ddiv(1.0, (double)d.x), ddiv(1.0, (double)d.y), ddiv(1.0, (double)d.z)};
+}
+
+__global__ void __launch_bounds__(256, 3) k_closest_fast(const Node* __restrict__ nodes, uint32_t node_limit,
                                                       const float4* __restrict__ tris,
                                                       const float* __restrict__ rays, uint32_t n, double tMin,
                                                       double tMax, int32_t* __restrict__ prim,
                                                       float* __restrict__ tout, float* __restrict__ uout,
                                                       float* __restrict__ vout, uint32_t* __restrict__ queue,
-                                                      uint32_t* __restrict__ queue_len, unsigned* err) {
-  const float tmin_lo = __double2float_rd(tMin);
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float3 o, d;
-    load_ray(rays, i, o, d);
-    if (!safe_ray(o, d)) {
-      queue[atomicAdd(queue_len, 1u)] = i;
-      continue;
-    }
-    const Ray32 r = make_ray32(o, d);
-    const D3 o64 = {o.x, o.y, o.z}, d64 = {d.x, d.y, d.z};
-    const D3 inv64 = {ddiv(1.0, d64.x), ddiv(1.0, d64.y), ddiv(1.0, d64.z)};
-    double closest = tMax;
-    float c_lo = __double2float_rd(closest), c_hi = __double2float_ru(closest);
-    HitOut h;
-    h.slot = -1;
-    int stack[kTsStack];
-    int sp = 0;
-    stack[sp++] = 0;
-    bool ok = true;
-    uint32_t iters = 0;
-    while (sp > 0) {
-      if (++iters > node_limit) {
-        atomicOr(err, kErrIterations);
-        ok = false;
-        break;
-      }
-      const int nidx = stack[--sp];
-      const Node nd = load_node(nodes, nidx);
-      SlabClass cls = classify_slab(r, nd.lo, nd.hi, c_lo, c_hi);
-      if (cls == kAmbiguous) cls = ts_slab_culled(nd.lo, nd.hi, o64, inv64, closest) ? kCulled : kPass;
-      if (cls == kCulled) continue;
-      const int cnt = node_count(nd), first = node_first(nd);
-      if (cnt > 0) {
-        for (int k = 0; k < cnt; k++) {
-          const int slot = first + k;
-          const float4 a = __ldg(tris + 3 * (size_t)slot), b = __ldg(tris + 3 * (size_t)slot + 1),
-                       c = __ldg(tris + 3 * (size_t)slot + 2);
-          if (!mt_candidate(r, a, b, c, tmin_lo, c_hi)) continue;
-          double t, u, v;
-          if (ts_triangle(o64, d64, d3f(a), d3f(b), d3f(c), tMin, closest, t, u, v)) {
-            closest = t;
-            c_lo = __double2float_rd(t);
-            c_hi = __double2float_ru(t);
-            h = {slot, t, u, v};
+                                                      uint32_t* __restrict__ queue_len,
+                                                      uint32_t* __restrict__ work, unsigned* err) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const float tmin_lo = __double2float_rd(tMin), tmin_hi = __double2float_ru(tMin);
+  const float cmax_lo = __double2float_rd(tMax), cmax_hi = __double2float_ru(tMax);
+  const double INF64 = __longlong_as_double(0x7ff0000000000000ll);
+
+  bool active = false, exhausted = false, have_cur = false, c_exact = true;
+  uint32_t ri = 0, iters = 0;
+  Ray32 r;
+  float c_lo = 0.f, c_hi = 0.f;
+  double c64 = tMax;
+  int best = -1, sp = 0;
+  Node cur;
+  PendingNode stack[kTsStack];
+
+  while (true) {
+    // Lanes without a ray take the next ones (one atomic per warp).
+    const bool need = !active && !exhausted;
+    const unsigned m = __ballot_sync(FULL, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(work, (uint32_t)__popc(m));
+      base = __shfl_sync(FULL, base, leader);
+      if (need) {
+        ri = base + __popc(m & lt);
+        if (ri >= n) {
+          exhausted = true;
+        } else {
+          float3 o, d;
+          load_ray(rays, ri, o, d);
+          if (!safe_ray(o, d)) {
+            queue[atomicAdd(queue_len, 1u)] = ri;
+          } else {
+            r = make_ray32(o, d);
+            c_lo = cmax_lo;
+            c_hi = cmax_hi;
+            c64 = tMax;
+            c_exact = true;
+            best = -1;
+            sp = 0;
+            iters = 0;
+            // The reference pops the root first and tests its box.
+            cur = load_node(nodes, 0);
+            SlabClass cl = classify_slab(r, cur.lo, cur.hi, c_lo, c_hi);
+            if (cl == kAmbiguous)
+              cl = ts_slab_culled(cur.lo, cur.hi, {o.x, o.y, o.z}, inv_exact(d), c64) ? kCulled : kPass;
+            have_cur = cl != kCulled;
+            active = true;
           }
         }
-      } else {
-        if (sp + 2 > kTsStack) {
-          atomicOr(err, kErrStack);
-          ok = false;
-          break;
-        }
-        stack[sp++] = first + 1;
-        stack[sp++] = first;
       }
     }
-    write_hit(tris, h, ok, i, prim, tout, uout, vout);
+    if (__all_sync(FULL, exhausted)) break;
+    if (!active) continue;
+
+    // Binary64 value of c, computed on demand (the reference's t of `best`).
+    auto exact_c = [&]() {
+      if (!c_exact) {
+        const float4 a = __ldg(tris + 3 * (size_t)best), b = __ldg(tris + 3 * (size_t)best + 1),
+                     c = __ldg(tris + 3 * (size_t)best + 2);
+        double t, u, v;
+        ts_triangle({r.o.x, r.o.y, r.o.z}, {r.d.x, r.d.y, r.d.z}, d3f(a), d3f(b), d3f(c), tMin, INF64, t, u, v);
+        c64 = t;
+        c_exact = true;
+        c_lo = __double2float_rd(t);
+        c_hi = __double2float_ru(t);
+      }
+      return c64;
+    };
+    auto slab_decide = [&](const Node& nd, SlabClass cl) {
+      if (cl != kAmbiguous) return cl;
+      return ts_slab_culled(nd.lo, nd.hi, {r.o.x, r.o.y, r.o.z}, inv_exact(r.d), exact_c()) ? kCulled : kPass;
+    };
+
+    if (!have_cur) {
+      if (sp == 0) {  // traversal finished: write the hit in the reference's binary64
+        if (best < 0) {
+          prim[ri] = -1;
+          if (tout) tout[ri] = __int_as_float(0x7f800000);
+          if (uout) uout[ri] = 0.f;
+          if (vout) vout[ri] = 0.f;
+        } else {
+          const float4 a = __ldg(tris + 3 * (size_t)best), b = __ldg(tris + 3 * (size_t)best + 1),
+                       c = __ldg(tris + 3 * (size_t)best + 2);
+          double t = 0, u = 0, v = 0;
+          ts_triangle({r.o.x, r.o.y, r.o.z}, {r.d.x, r.d.y, r.d.z}, d3f(a), d3f(b), d3f(c), tMin, INF64, t, u, v);
+          prim[ri] = __float_as_int(a.w);
+          if (tout) tout[ri] = __double2float_rn(t);
+          if (uout) uout[ri] = __double2float_rn(u);
+          if (vout) vout[ri] = __double2float_rn(v);
+        }
+        active = false;
+        continue;
+      }
+      const PendingNode e = stack[--sp];
+      const Node nd = load_node(nodes, e.node);
+      if (e.ehi > c_lo) {
+        if (slab_decide(nd, classify_slab(r, nd.lo, nd.hi, c_lo, c_hi)) == kCulled) continue;
+      }
+      cur = nd;
+      have_cur = true;
+    }
+    if (++iters > node_limit) {  // a valid BVH visits each node at most once per ray
+      atomicOr(err, kErrIterations);
+      prim[ri] = -2;
+      active = false;
+      have_cur = false;
+      continue;
+    }
+    const int cnt = node_count(cur), first = node_first(cur);
+    if (cnt > 0) {
+      for (int k = 0; k < cnt; k++) {
+        const int slot = first + k;
+        const float4 a = __ldg(tris + 3 * (size_t)slot), b = __ldg(tris + 3 * (size_t)slot + 1),
+                     c = __ldg(tris + 3 * (size_t)slot + 2);
+        float tl, th;
+        const TriClass tc = mt_classify(r, a, b, c, tmin_lo, tmin_hi, c_lo, c_hi, tl, th);
+        if (tc == kTriReject) continue;
+        if (tc == kTriAccept) {
+          best = slot;
+          c_exact = false;
+          c_lo = tl;
+          c_hi = th;
+          continue;
+        }
+        double t, u, v;
+        const double cc = exact_c();
+        if (ts_triangle({r.o.x, r.o.y, r.o.z}, {r.d.x, r.d.y, r.d.z}, d3f(a), d3f(b), d3f(c), tMin, cc, t, u, v)) {
+          best = slot;
+          c64 = t;
+          c_exact = true;
+          c_lo = __double2float_rd(t);
+          c_hi = __double2float_ru(t);
+        }
+      }
+      have_cur = false;
+    } else {
+      // Children pair (first, first + 1): one contiguous 64-byte read.
+      const Node L = load_node(nodes, first), R = load_node(nodes, first + 1);
+      float ehl, ehr;
+      const SlabClass cl = slab_decide(L, classify_slab_e(r, L.lo, L.hi, c_lo, c_hi, ehl));
+      const SlabClass cr = slab_decide(R, classify_slab_e(r, R.lo, R.hi, c_lo, c_hi, ehr));
+      if (cl == kPass) {
+        if (cr == kPass) {
+          if (sp >= kTsStack) {  // cannot happen for BVHs shallower than the reference's stack
+            atomicOr(err, kErrStack);
+            prim[ri] = -2;
+            active = false;
+            have_cur = false;
+            continue;
+          }
+          stack[sp++] = {first + 1, ehr};
+        }
+        cur = L;
+      } else if (cr == kPass) {
+        cur = R;
+      } else {
+        have_cur = false;
+      }
+    }
   }
 }
 
@@ -261,15 +385,24 @@ void launch_unpack(const Node* nodes, uint32_t count, const float4* tris, uint32
 
 void launch_closest(const Node* nodes, uint32_t node_count, const float4* tris, const float* rays_d, uint32_t n, double tMin,
                     double tMax, int32_t* prim, float* t, float* u, float* v, uint32_t* queue, uint32_t* queue_len,
-                    unsigned* err, bool exact_only, cudaStream_t s) {
+                    uint32_t* work, unsigned* err, bool exact_only, cudaStream_t s) {
   if (n == 0) return;
   if (exact_only) {
     k_closest_exact<<<grid_for(n, 128), 128, 0, s>>>(nodes, node_count, tris, rays_d, n, nullptr, nullptr, tMin, tMax, prim,
                                                       t, u, v, err);
     return;
   }
-  k_closest_fast<<<grid_for(n, 256), 256, 0, s>>>(nodes, node_count, tris, rays_d, n, tMin, tMax, prim, t, u, v, queue,
-                                                   queue_len, err);
+  static int blocks = 0;
+  if (!blocks) {  // persistent grid: every SM filled to the kernel's occupancy
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_closest_fast, 256, 0);
+    blocks = (sms > 0 ? sms : 152) * (per > 0 ? per : 2);
+  }
+  const int want = (int)((n + 255) / 256);
+  k_closest_fast<<<want < blocks ? want : blocks, 256, 0, s>>>(nodes, node_count, tris, rays_d, n, tMin, tMax, prim,
+                                                                t, u, v, queue, queue_len, work, err);
   // Slow path over the queued rays; the queue length is read on the device.
   k_closest_exact<<<grid_for(n < 4096 ? n : 4096, 128), 128, 0, s>>>(nodes, node_count, tris, rays_d, n, queue, queue_len,
                                                                       tMin, tMax, prim, t, u, v, err);

@@ -49,6 +49,29 @@ constexpr float kAbsFloor = 7.8886091e-31f;   // 2^-100
 LUCENT_DEV float slab_t(float b, float o, float inv) { return __fmul_rn(__fsub_rn(b, o), inv); }
 LUCENT_DEV float widen(float t) { return __fmaf_ru(fabsf(t), kSlabRel, kAbsFloor); }
 
+// Same classification; also returns an upper bound on the reference's entry
+// distance max(0, entries), which decides later re-tests after `c` shrinks.
+LUCENT_DEV SlabClass classify_slab_e(const Ray32& r, float4 mn, float4 mx, float c_lo, float c_hi, float& ehi) {
+  const float ax0 = slab_t(mn.x, r.o.x, r.inv.x), ax1 = slab_t(mx.x, r.o.x, r.inv.x);
+  const float ay0 = slab_t(mn.y, r.o.y, r.inv.y), ay1 = slab_t(mx.y, r.o.y, r.inv.y);
+  const float az0 = slab_t(mn.z, r.o.z, r.inv.z), az1 = slab_t(mx.z, r.o.z, r.inv.z);
+  const float ex = r.negx ? ax1 : ax0, xx = r.negx ? ax0 : ax1;
+  const float ey = r.negy ? ay1 : ay0, xy = r.negy ? ay0 : ay1;
+  const float ez = r.negz ? az1 : az0, xz = r.negz ? az0 : az1;
+  const float wex = widen(ex), wey = widen(ey), wez = widen(ez);
+  const float wxx = widen(xx), wxy = widen(xy), wxz = widen(xz);
+  const float ex_hi = ex + wex, ey_hi = ey + wey, ez_hi = ez + wez;
+  const float xx_lo = xx - wxx, xy_lo = xy - wxy, xz_lo = xz - wxz;
+  const float emax_lo = fmaxf(fmaxf(ex - wex, ey - wey), fmaxf(ez - wez, 0.f));
+  const float xmin_hi = fminf(fminf(xx + wxx, xy + wxy), fminf(xz + wxz, c_hi));
+  ehi = fmaxf(fmaxf(ex_hi, ey_hi), fmaxf(ez_hi, 0.f));
+  if (xmin_hi < emax_lo) return kCulled;
+  const bool okx = xx_lo >= fmaxf(fmaxf(ey_hi, ez_hi), 0.f);
+  const bool oky = xy_lo >= fmaxf(fmaxf(ex_hi, ez_hi), 0.f);
+  const bool okz = xz_lo >= fmaxf(fmaxf(ex_hi, ey_hi), 0.f);
+  return (okx && oky && okz && c_lo >= ehi) ? kPass : kAmbiguous;
+}
+
 LUCENT_DEV SlabClass classify_slab(const Ray32& r, float4 mn, float4 mx, float c_lo, float c_hi) {
   // Entry/exit per axis: after the reference's swap the entry is the bound the
   // ray meets first, fixed by the sign of the direction.
@@ -122,6 +145,57 @@ LUCENT_DEV bool mt_candidate(const Ray32& r, float4 a, float4 b, float4 c3, floa
   if (Ta + eT <= tmin_lo * Alo * 0.99999905f) return false;          // t <= tMin  (factor 1 - 2^-20)
   if (Ta - eT >= c_hi * Ahi * 1.00000095f) return false;             // t >= closest (c_hi may be inf)
   return true;
+}
+
+// Three-way Moller-Trumbore decision against the reference's binary64 test
+// (src/math/ray.ts:22-45) with tMin and the running closest c in [c_lo, c_hi]:
+//   kTriReject  the reference certainly rejects,
+//   kTriAccept  the reference certainly accepts; [t_lo, t_hi] bounds its t,
+//   kTriExact   undecided: recompute in binary64.
+// Numerator bounds as in mt_candidate (2^-19 x absolute-value evaluation).
+enum TriClass { kTriReject = 0, kTriAccept = 1, kTriExact = 2 };
+
+LUCENT_DEV TriClass mt_classify(const Ray32& r, float4 a, float4 b, float4 c3, float tmin_lo, float tmin_hi,
+                                float c_lo, float c_hi, float& t_lo, float& t_hi) {
+  const float3 e1 = make_float3(b.x - a.x, b.y - a.y, b.z - a.z);
+  const float3 e2 = make_float3(c3.x - a.x, c3.y - a.y, c3.z - a.z);
+  const float3 d = r.d;
+  const float3 p = make_float3(d.y * e2.z - d.z * e2.y, d.z * e2.x - d.x * e2.z, d.x * e2.y - d.y * e2.x);
+  const float det = e1.x * p.x + e1.y * p.y + e1.z * p.z;
+  const float3 s = make_float3(r.o.x - a.x, r.o.y - a.y, r.o.z - a.z);
+  const float U = s.x * p.x + s.y * p.y + s.z * p.z;
+  const float3 q = make_float3(s.y * e1.z - s.z * e1.y, s.z * e1.x - s.x * e1.z, s.x * e1.y - s.y * e1.x);
+  const float V = d.x * q.x + d.y * q.y + d.z * q.z;
+  const float T = e2.x * q.x + e2.y * q.y + e2.z * q.z;
+  const float3 ad = make_float3(fabsf(d.x), fabsf(d.y), fabsf(d.z));
+  const float3 ae1 = make_float3(fabsf(e1.x), fabsf(e1.y), fabsf(e1.z));
+  const float3 ae2 = make_float3(fabsf(e2.x), fabsf(e2.y), fabsf(e2.z));
+  const float3 as = make_float3(fabsf(s.x), fabsf(s.y), fabsf(s.z));
+  const float3 ap = make_float3(ad.y * ae2.z + ad.z * ae2.y, ad.z * ae2.x + ad.x * ae2.z, ad.x * ae2.y + ad.y * ae2.x);
+  const float3 aq = make_float3(as.y * ae1.z + as.z * ae1.y, as.z * ae1.x + as.x * ae1.z, as.x * ae1.y + as.y * ae1.x);
+  const float eD = fmaf(ae1.x * ap.x + ae1.y * ap.y + ae1.z * ap.z, kMtRel, kAbsFloor);
+  const float eU = fmaf(as.x * ap.x + as.y * ap.y + as.z * ap.z, kMtRel, kAbsFloor);
+  const float eV = fmaf(ad.x * aq.x + ad.y * aq.y + ad.z * aq.z, kMtRel, kAbsFloor);
+  const float eT = fmaf(ae2.x * aq.x + ae2.y * aq.y + ae2.z * aq.z, kMtRel, kAbsFloor);
+
+  const float A = fabsf(det);
+  if (A + eD < 9.9e-13f) return kTriReject;  // |det| < 1e-12 for sure
+  if (A <= eD) return kTriExact;
+  const float sg = det < 0.f ? -1.f : 1.f;
+  const float Ua = U * sg, Va = V * sg, Ta = T * sg;
+  const float Ahi = __fadd_ru(A, eD), Alo = __fsub_rd(A, eD);
+  if (Ua + eU < 0.f || Ua - eU > Ahi || Va + eV < 0.f || Ua + Va - (eU + eV) > Ahi) return kTriReject;
+  if (Ta + eT < 0.f || Ta + eT <= tmin_lo * Alo * 0.99999905f) return kTriReject;  // t <= tMin
+  if (Ta - eT >= c_hi * Ahi * 1.00000095f) return kTriReject;                       // t >= closest
+  // Certain acceptance: every reference condition holds with margin.
+  const bool inside = Ua - eU >= 0.f && Va - eV >= 0.f && Ua + Va + (eU + eV) <= Alo && Alo >= 1.0000001e-12f;
+  const bool t_ok = Ta - eT > tmin_hi * Ahi * 1.00000095f && Ta + eT < c_lo * Alo * 0.99999905f;
+  if (!(inside && t_ok)) return kTriExact;
+  // t = T/det lies in [(Ta-eT)/Ahi, (Ta+eT)/Alo]; round outward and widen by
+  // one more ulp for the reference's own binary64 rounding.
+  t_lo = __fmul_rd(__fdiv_rd(__fsub_rd(Ta, eT), Ahi), 0.99999994f);
+  t_hi = __fmul_ru(__fdiv_ru(__fadd_ru(Ta, eT), Alo), 1.00000012f);
+  return kTriAccept;
 }
 
 }  // namespace lucent
