@@ -3,6 +3,9 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
 Workloads:
+  pt       (default) path tracing of the box scene (81,956 triangles) at
+           512x512, 16 spp, depth 8: one step = one 16-spp frame; the metric
+           is closest-hit rays per second inside the renderer, with spp/s
   closest  random soup, 65,536 triangles, 10^6 rays, seed 0: one step = one
            closest-hit pass over all rays (the reference's intersectBVH)
 Under torchrun (N > 1) every rank runs an independent replica of the same
@@ -103,9 +106,7 @@ def run_ours_closest(args, rank, world, local):
 
     torch.cuda.set_device(local)
     pos, rays = workloads.soup_and_rays(seed=0, n_tri=65536, n_rays=1_000_000)
-    gb = B.build_bvh(pos) if hasattr(B, "build_bvh") else None
-    if gb is None:  # pragma: no cover - the GPU builder is part of the package
-        raise RuntimeError("GPU BVH builder missing")
+    gb = B.build_bvh(pos)
     dev = DeviceBVH(gb.nodes, gb.tri_indices, pos, gb.node_count)
     n = rays.shape[0]
     rays_d = torch.from_numpy(rays).cuda()
@@ -198,6 +199,138 @@ def cpu_closest(threads, sample_rays=1_000_000, reps=3):
     return sample_rays * reps / dt / 1e6, "%d rays x %d reps of the same workload" % (sample_rays, reps)
 
 
+# ----------------------------------------------------------------------------- path-tracing workload
+PT_W, PT_H, PT_SPP, PT_DEPTH = 512, 512, 16, 8
+PT_METRIC = ("closest-hit Mrays/s inside path tracing: box scene (81,956 triangles), 512x512, 16 spp, "
+             "max depth 8 (also spp/s)")
+
+
+def run_ours_pt(args, rank, world, local):
+    import ctypes as C
+
+    import torch
+    from lucent_gb300 import _native as N
+    from lucent_gb300 import workloads as W
+    from lucent_gb300 import _native_render as NR
+    from lucent_gb300.renderer import Renderer
+
+    torch.cuda.set_device(local)
+    r = Renderer(PT_W, PT_H)
+    r.settings.max_bounces = PT_DEPTH
+    r.load_scene(W.box_scene(0, 6))
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        r.reset()
+        r.trace_samples(PT_SPP, sp)
+
+    for _ in range(args.warmup):
+        step()
+    r.check(sp)
+    s0 = r.stats()
+    barrier(world)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(float(k))  # evict L2 (256 MB > 129 MB) between timed frames
+            evs[k][0].record(stream)
+            step()
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    r.check(sp)
+    s1 = r.stats()
+    ms = [a.elapsed_time(b) for a, b in evs]
+    dev_s = max_over_ranks(sum(ms) / 1000.0, world)
+    closest = (s1["closest_rays"] - s0["closest_rays"]) * world
+    shadow = (s1["shadow_rays"] - s0["shadow_rays"]) * world
+    value = closest / dev_s / 1e6
+    paths = PT_W * PT_H * PT_SPP * args.steps * world
+    spp_per_s = PT_SPP * args.steps / dev_s  # per GPU frame stream; all ranks render the same size
+    # Per-phase device time of one frame (events between the renderer's kernels).
+    r.set_profiling(True)
+    step()
+    r.check(sp)
+    ph = r.stats()["phase_ms"]
+    r.set_profiling(False)
+
+    # End to end through the C ABI with host buffers: camera and settings from
+    # host structs, trace, colour target (512 x 512 x RGBA32F) back to pinned host memory.
+    L = N.lib()
+    out = torch.empty(PT_W * PT_H * 4, dtype=torch.float32).pin_memory()
+    cam = r.camera_state
+    settings = NR.SettingsDesc(PT_DEPTH, r.settings.firefly_clamp)
+
+    def e2e_step():
+        N.check(L.lucent_renderer_upload_camera(r.handle, C.byref(cam)))
+        N.check(L.lucent_renderer_apply_settings(r.handle, C.byref(settings)))
+        N.check(L.lucent_renderer_trace(r.handle, PT_SPP, sp))
+        N.check(L.lucent_renderer_read(r.handle, C.cast(out.data_ptr(), N.F32P), None, None, None))
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    per_frame_closest = closest / (args.steps * world)
+    e2e = {"value": round(per_frame_closest * args.steps * world / e2e_s / 1e6, 2), "unit": "Mrays/s",
+           "h2d_bytes_per_step": C.sizeof(cam) + C.sizeof(settings), "d2h_bytes_per_step": PT_W * PT_H * 16,
+           "spp_per_s": round(PT_SPP * args.steps / e2e_s, 2)}
+
+    alg = json.load(open(ALG_BYTES)).get("pt_box") if os.path.exists(ALG_BYTES) else None
+    peak, which = peaks()
+    roof = None
+    if alg and ph.get("closest"):
+        per_frame = alg["bytes_per_closest_ray"] * per_frame_closest
+        achieved = per_frame / (ph["closest"] / 1000.0) / 1e9
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": alg.get("ncu_dram_bytes_per_launch"),
+                "peak_source": which, "kernel": "k_closest_fast_t<PathClosest> (+ slow path)",
+                "bytes_per_closest_ray": alg["bytes_per_closest_ray"],
+                "closest_ms_per_frame": round(ph["closest"], 3)}
+    launches_per_frame = 2 + 8 * (PT_DEPTH + 1)
+    return {
+        "metric": PT_METRIC, "value": round(value, 2), "unit": "Mrays/s", "ms_per_step": round(sum(ms) / len(ms), 4),
+        "wall_s": round(wall, 3), "e2e": e2e, "roofline": roof, "clocks": clk.summary(),
+        "gpu_launches": launches_per_frame * args.steps, "dtype": "f32 (+f64 exact hit decisions)",
+        "spp_per_s": round(spp_per_s, 2),
+        "extra": {"mpaths_per_s": round(paths / dev_s / 1e6, 2), "shadow_mrays_per_s": round(shadow / dev_s / 1e6, 2),
+                  "closest_rays_per_frame": int(per_frame_closest),
+                  "phase_ms_per_frame": {k: round(v, 3) for k, v in ph.items()}},
+        "config": {"workload": "pt: box scene seed 0 (5 Lambert walls, quad light 15, 2 rotated boxes, "
+                               "81,920-triangle icosphere, layered BSDF), 512x512, 16 spp, depth 8, RR from bounce 2",
+                   "l2": "flushed between timed frames (256 MB write)",
+                   "hit_ids": "bit-exact vs intersectBVH (tMin 1e-6, tMax 1e30)"},
+    }
+
+
+def cpu_pt(threads, reps=1, crop=512):
+    """The oracle (C++ restatement of trace.frag with the binary64 intersectBVH
+    restatement) on a centred crop of the same frame; closest-hit rays it traced
+    per second."""
+    from oracle import render as R
+    from lucent_gb300 import workloads as W
+    prep = R.prepare(W.box_scene(0, 6))
+    x0 = (PT_W - crop) // 2
+    crop_box = (x0, x0, crop, crop)
+    R.render_work(prep, PT_W, PT_H, 0, 1, max_bounces=PT_DEPTH, crop=(x0, x0, 16, 16), threads=threads,
+                  detailed=False)
+    t0 = time.perf_counter()
+    rays = 0
+    for _ in range(reps):
+        w = R.render_work(prep, PT_W, PT_H, 0, PT_SPP, max_bounces=PT_DEPTH, crop=crop_box, threads=threads,
+                          detailed=False)
+        rays += w["closest_rays"]
+    dt = time.perf_counter() - t0
+    return rays / dt / 1e6, "%dx%d centre crop of the 512x512 frame, 16 spp x %d reps" % (crop, crop, reps)
+
+
 # ----------------------------------------------------------------------------- plumbing
 _pg = None
 
@@ -227,8 +360,8 @@ def max_over_ranks(x, world):
     return float(t.item())
 
 
-WORKLOADS = {"closest": (run_ours_closest, cpu_closest, "Mrays/s")}
-DEFAULT_WORKLOAD = "closest"
+WORKLOADS = {"closest": (run_ours_closest, cpu_closest, "Mrays/s"), "pt": (run_ours_pt, cpu_pt, "Mrays/s")}
+DEFAULT_WORKLOAD = "pt"
 
 
 def main():
@@ -263,7 +396,7 @@ def main():
                                  "sample": sample + " (oracle: C++ restatement of the reference's TypeScript, "
                                                     "binary64, std::thread on all host cores; not V8)"},
                 "e2e": {"value": round(v, 3), "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        ours_metric = {"closest": "closest-hit Mrays/s (intersectBVH, 65,536-triangle soup, 1e6 rays)"}
+        ours_metric = {"closest": "closest-hit Mrays/s (intersectBVH, 65,536-triangle soup, 1e6 rays)", "pt": PT_METRIC}
         line["metric"] = ours_metric.get(args.workload, args.workload)
         line["config"] = {"workload": args.workload}
         print(json.dumps(line), flush=True)

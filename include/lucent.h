@@ -106,6 +106,124 @@ lucent_status lucent_bvh_intersect_f64(lucent_bvh* bvh, const double* rays, uint
                                        double t_max, int32_t* prim_out, double* t_out, double* u_out,
                                        double* v_out, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Renderer: the Renderer class of src/renderer.ts:171-871 without its WebGL
+ * plumbing. Accumulation targets, scene data and the path state live on the
+ * GPU; host buffers are copied in and out by the calls that take them.
+ * ------------------------------------------------------------------------- */
+typedef struct lucent_renderer lucent_renderer;
+
+/* PackedScene inputs before the BVH-order gather (scene.ts:106-134, 162-305).
+ * Per triangle in mergeMeshes order: positions (9 floats), normals (9),
+ * optional uvs (6), material index, light index (-1 = none) and alpha-test
+ * flag. The BVH is built on the GPU unless a reference-layout BVH over the
+ * same triangles is supplied (packScene's `prebuilt`, scene.ts:206-209).
+ * Materials are packed by packMaterials (40 floats each, material.ts:121-131);
+ * texture maps must be -1 (texture layers are not part of this ABI).
+ * Lights are 16 floats each (scene.ts:88-95), at most 8; spheres are
+ * (centre, radius), at most 64. ground_material: the packed ground material
+ * (the plane itself is switched by lucent_renderer_upload_ground). */
+typedef struct lucent_scene_desc {
+  uint32_t tri_count;
+  const float* positions;
+  const float* normals;
+  const float* uvs;
+  const int32_t* tri_material;
+  const int32_t* tri_light;
+  const uint8_t* tri_alpha;
+  const float* bvh_nodes;
+  uint32_t bvh_node_count;
+  const uint32_t* bvh_tri_indices;
+  const float* materials;
+  uint32_t material_count;
+  const float* spheres;
+  const int32_t* sphere_materials;
+  const int32_t* sphere_lights;
+  uint32_t sphere_count;
+  const float* lights;
+  uint32_t light_count;
+  int32_t ground_material;
+} lucent_scene_desc;
+
+/* uploadLighting (renderer.ts:355-413): the analytic sun and an equirect
+ * radiance map (RGB floats, rows top to bottom). The map's importance
+ * sampler (buildEnvSampler, environment.ts:52-85, max grid width 1024) is
+ * built here. A map whose luminance sums to 0 disables environment sampling. */
+typedef struct lucent_lighting {
+  int32_t sun_enabled;
+  float sun_dir[3];
+  float sun_radiance[3];
+  float sun_cos_angle;
+  float sun_pdf;
+  uint32_t env_width, env_height;
+  const float* env_rgb;
+  float env_rotation_cos, env_rotation_sin;
+  float env_intensity;
+  int32_t env_background;
+  float backdrop[3];
+} lucent_lighting;
+
+/* uploadCamera (renderer.ts:424-439): basis already normalised. */
+typedef struct lucent_camera {
+  float position[3], right[3], up[3], forward[3];
+  float tan_half_fov, aperture, focus_distance;
+} lucent_camera;
+
+/* applySettings (renderer.ts:454-460): RenderSettings.maxBounces / fireflyClamp. */
+typedef struct lucent_settings {
+  uint32_t max_bounces;
+  float firefly_clamp;
+} lucent_settings;
+
+/* stats() (renderer.ts:832-854) plus ray counters. */
+typedef struct lucent_render_stats {
+  uint32_t samples;        /* samples behind the current average (frame) */
+  uint32_t seed;           /* next RNG stream index (uSeed) */
+  uint32_t width, height;
+  uint32_t triangles, bvh_nodes;
+  uint64_t closest_rays;   /* closest-hit rays traced since creation */
+  uint64_t shadow_rays;    /* shadow rays traced since creation */
+  double last_trace_ms;    /* device time of the last lucent_renderer_trace */
+  /* device ms of the last trace per phase (camera, closest hit, shade, shadow
+   * rays, resolve + queue upkeep, accumulate); zero unless profiling is on */
+  double phase_ms[6];
+  /* closest-hit traversal counters accumulated while profiling is on: rays,
+   * slab tests decided in binary64, triangle tests decided in binary64,
+   * binary64 recomputations of the running closest distance, binary64 final
+   * hit reports */
+  uint64_t traversal[5];
+} lucent_render_stats;
+
+lucent_status lucent_renderer_create(uint32_t width, uint32_t height, lucent_renderer** out);
+void lucent_renderer_destroy(lucent_renderer* r);
+/* loadScene(scene, bvh?) (renderer.ts:279-312). */
+lucent_status lucent_renderer_load_scene(lucent_renderer* r, const lucent_scene_desc* scene);
+lucent_status lucent_renderer_upload_lighting(lucent_renderer* r, const lucent_lighting* lighting);
+/* uploadGround (renderer.ts:415-421). */
+lucent_status lucent_renderer_upload_ground(lucent_renderer* r, int32_t enabled, float height);
+lucent_status lucent_renderer_upload_camera(lucent_renderer* r, const lucent_camera* camera);
+lucent_status lucent_renderer_apply_settings(lucent_renderer* r, const lucent_settings* settings);
+/* resize (renderer.ts:476-496): new accumulation targets, history cleared. */
+lucent_status lucent_renderer_resize(lucent_renderer* r, uint32_t width, uint32_t height);
+/* reset (renderer.ts:463-473). The RNG stream index is not reset (it never is). */
+lucent_status lucent_renderer_reset(lucent_renderer* r);
+/* Sets the next RNG stream index (uSeed); the reference starts at 0. */
+lucent_status lucent_renderer_set_seed(lucent_renderer* r, uint32_t seed);
+/* traceSamples(count) (renderer.ts:702-737): `samples` more samples per
+ * pixel into the running average. Asynchronous on `stream`. */
+lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* stream);
+/* Synchronises and reports the device error word. */
+lucent_status lucent_renderer_check(lucent_renderer* r, void* stream);
+/* Copies the accumulation targets to the host (each may be NULL):
+ * color4 / albedo4 / normal4 as width*height*4 floats, history width*height.
+ * Row 0 is the bottom row (gl_FragCoord convention). */
+lucent_status lucent_renderer_read(lucent_renderer* r, float* color4, float* albedo4, float* normal4, float* history);
+lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out);
+/* Records CUDA events between the kernels of each trace (the counterpart of
+ * the reference's GPU timer queries, renderer.ts:668-700); results appear in
+ * lucent_render_stats.phase_ms after lucent_renderer_check. */
+lucent_status lucent_renderer_set_profiling(lucent_renderer* r, int32_t enabled);
+
 #ifdef __cplusplus
 }
 #endif

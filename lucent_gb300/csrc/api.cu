@@ -72,7 +72,7 @@ const char* lucent_last_error(void) { return g_last_error.c_str(); }
 int32_t lucent_version(void) { return 100; }
 
 // Depth of a (validated) reference-layout tree; root = 0.
-static uint32_t tree_depth(const float* nodes, uint32_t node_count, uint32_t tri_count) {
+uint32_t tree_depth(const float* nodes, uint32_t node_count, uint32_t tri_count) {
   if (tri_count == 0 || node_count == 0) return 0;
   std::vector<std::pair<uint32_t, uint32_t>> st{{0u, 0u}};
   uint32_t depth = 0;
@@ -91,7 +91,7 @@ static uint32_t tree_depth(const float* nodes, uint32_t node_count, uint32_t tri
 
 // Validates the reference layout so that no kernel can read out of bounds:
 // children inside the array, leaf ranges inside triIndices, indices in range.
-static lucent_status validate_bvh(const float* nodes, uint32_t node_count, const uint32_t* tri, uint32_t tri_count) {
+lucent_status validate_bvh(const float* nodes, uint32_t node_count, const uint32_t* tri, uint32_t tri_count) {
   if (node_count == 0) return fail(LUCENT_ERR_INVALID, "BVH has no nodes");
   if (tri_count > (1u << 23)) return fail(LUCENT_ERR_UNSUPPORTED, "%u triangles; the limit is 2^23", tri_count);
   for (uint32_t i = 0; i < tri_count; i++)

@@ -20,3 +20,9 @@ struct DeviceBuffer {
 };
 
 }  // namespace lucent
+
+extern "C" {
+// Reference-layout BVH checks shared by the C-ABI files (defined in api.cu).
+uint32_t tree_depth(const float* nodes, uint32_t node_count, uint32_t tri_count);
+lucent_status validate_bvh(const float* nodes, uint32_t node_count, const uint32_t* tri, uint32_t tri_count);
+}

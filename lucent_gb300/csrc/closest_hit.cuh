@@ -156,7 +156,7 @@ LUCENT_DEV bool mt_candidate(const Ray32& r, float4 a, float4 b, float4 c3, floa
 enum TriClass { kTriReject = 0, kTriAccept = 1, kTriExact = 2 };
 
 LUCENT_DEV TriClass mt_classify(const Ray32& r, float4 a, float4 b, float4 c3, float tmin_lo, float tmin_hi,
-                                float c_lo, float c_hi, float& t_lo, float& t_hi) {
+                                float c_lo, float c_hi, float& t_lo, float& t_hi, float3& est) {
   const float3 e1 = make_float3(b.x - a.x, b.y - a.y, b.z - a.z);
   const float3 e2 = make_float3(c3.x - a.x, c3.y - a.y, c3.z - a.z);
   const float3 d = r.d;
@@ -195,6 +195,9 @@ LUCENT_DEV TriClass mt_classify(const Ray32& r, float4 a, float4 b, float4 c3, f
   // one more ulp for the reference's own binary64 rounding.
   t_lo = __fmul_rd(__fdiv_rd(__fsub_rd(Ta, eT), Ahi), 0.99999994f);
   t_hi = __fmul_ru(__fdiv_ru(__fadd_ru(Ta, eT), Alo), 1.00000012f);
+  // Binary32 estimates of (t, u, v), as the GLSL's own hitTriangle computes them.
+  const float inv = 1.f / det;
+  est = make_float3(T * inv, U * inv, V * inv);
   return kTriAccept;
 }
 

@@ -10,6 +10,8 @@
 
 namespace lucent {
 
+int grid_for(uint32_t n, int block);
+int persistent_blocks(const void* kernel, int block);
 void launch_pack_nodes(const float* ref_d, uint32_t count, Node* out_d, cudaStream_t s);
 void launch_gather_tris(const float* pos_d, const uint32_t* idx_d, uint32_t tri_count, float4* out_d,
                         cudaStream_t s);

@@ -1,0 +1,493 @@
+// Wavefront path tracer: the reference's trace.frag (src/shaders/trace.frag)
+// restructured as kernels over queues of paths.
+//
+// One batch holds S samples of every pixel (path p = s * W * H + pixel). Each
+// path keeps the reference's per-pixel PCG stream (trace.frag:326-328, seed =
+// pixel * 1973 + sampleSeed * 9277 + 26699) and draws its numbers in the
+// reference's order, so a path makes the reference's choices. Per bounce:
+//   closest  -> triangle hit per active path (traverse.cuh, hit ids equal to
+//               the reference's CPU intersector with tMin = EPS, tMax = INF)
+//   shade    -> spheres / ground, surface, emission + MIS, dielectric or
+//               opaque: next-event estimation (sun, environment, one light)
+//               into per-path shadow slots, BSDF sample, Russian roulette
+//   any-hit  -> shadow rays
+//   resolve  -> unoccluded NEE added in the reference's order (sun, env, light)
+// Accumulation replays the running mean (trace.frag:350-354) sample by
+// sample per pixel, so a batch equals S sequential draws.
+#include <cuda_fp16.h>
+
+#include "internal.h"
+#include "render_internal.h"
+#include "shade.cuh"
+#include "traverse.cuh"
+
+namespace lucent {
+
+using namespace sh;
+
+// ------------------------------------------------------------ traversal policies
+struct PathClosest {
+  const uint32_t* cnt;
+  const uint32_t* queue;
+  const float4* ro;
+  const float4* rd;
+  const uint32_t* rng;
+  float4* hits;
+  const float4* geo;
+  const float4* mats;
+  int any_alpha;
+  __device__ uint32_t count() const { return *cnt; }
+  __device__ void ray(uint32_t k, float3& o, float3& d) const {
+    const uint32_t p = queue[k];
+    const float4 a = ro[p], b = rd[p];
+    o = make_float3(a.x, a.y, a.z);
+    d = make_float3(b.x, b.y, b.z);
+  }
+  __device__ uint32_t key(uint32_t k) const { return rng[queue[k]]; }
+  __device__ bool alpha_any() const { return any_alpha != 0; }
+  // alphaOpaque (scene.glsl:284-297) with constant alpha.
+  __device__ bool alpha(int slot, uint32_t key) const {
+    if (__ldg(&geo[3 * (size_t)slot + 2].w) < 0.5f) return true;
+    const int m = (int)__ldg(&geo[3 * (size_t)slot].w);
+    const float alpha = __ldg(&mats[m * 10 + 2].w);
+    if ((int)__ldg(&mats[m * 10 + 3].w) == 1) return alpha >= __ldg(&mats[m * 10 + 5].w);
+    return alpha_rand(key, (uint32_t)slot) < alpha;
+  }
+  // Shading uses binary32 t and barycentrics (as the GLSL does); only the
+  // choice of triangle must be the reference's.
+  __device__ bool exact_output() const { return false; }
+  __device__ void hit32(uint32_t k, int slot, float3 e) const {
+    hits[queue[k]] = make_float4(e.x, e.y, e.z, __int_as_float(slot));
+  }
+  __device__ void hit(uint32_t k, int slot, double t, double u, double v) const {
+    hits[queue[k]] = make_float4(__double2float_rn(t), __double2float_rn(u), __double2float_rn(v), __int_as_float(slot));
+  }
+  __device__ void miss(uint32_t k) const { hits[queue[k]] = make_float4(INF, 0.f, 0.f, __int_as_float(-1)); }
+  __device__ void fail(uint32_t k) const { miss(k); }
+};
+
+struct PathShadow {
+  const uint32_t* cnt;
+  const uint32_t* queue;
+  const float4* so;  // origin xyz, tmax
+  const float4* sd;  // dir xyz, alpha key bits
+  uint8_t* occ;
+  const float4* geo;
+  const float4* mats;
+  int any_alpha;
+  __device__ uint32_t count() const { return *cnt; }
+  __device__ void ray(uint32_t k, float3& o, float3& d) const {
+    const uint32_t s = queue[k];
+    const float4 a = so[s], b = sd[s];
+    o = make_float3(a.x, a.y, a.z);
+    d = make_float3(b.x, b.y, b.z);
+  }
+  __device__ double tmax(uint32_t k) const { return (double)so[queue[k]].w; }
+  __device__ uint32_t key(uint32_t k) const { return __float_as_uint(sd[queue[k]].w); }
+  __device__ bool alpha_any() const { return any_alpha != 0; }
+  __device__ bool alpha(int slot, uint32_t key) const {
+    return PathClosest{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, geo, mats, any_alpha}.alpha(slot, key);
+  }
+  __device__ void shadow(uint32_t k, bool occluded) const { occ[queue[k]] = occluded ? 1 : 0; }
+};
+
+// ------------------------------------------------------------ kernels
+constexpr unsigned kSpecular = 1u, kGuideDone = 2u;
+
+__global__ void k_camera(Paths P, CameraDev cam, int W, int H, int S, uint32_t seed0) {
+  const uint32_t WH = (uint32_t)W * H, total = WH * S;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+    const uint32_t pixel = p % WH, s = p / WH;
+    const uint32_t x = pixel % W, y = pixel / W;
+    uint32_t st = pixel * 1973u + (seed0 + s) * 9277u + 26699u;  // trace.frag:327-328
+    pcg(st);
+    // cameraRay (trace.frag:53-62)
+    const float j0 = rnd(st), j1 = rnd(st);
+    const float ux = ((float)x + 0.5f + j0) / (float)W * 2.f - 1.f;
+    const float uy = ((float)y + 0.5f + j1) / (float)H * 2.f - 1.f;
+    const float aspect = (float)W / (float)H;
+    const float3 dir = norm3(cam.forward + cam.right * (ux * aspect * cam.tan_half_fov) + cam.up * (uy * cam.tan_half_fov));
+    const float3 focus = cam.pos + dir * (cam.focus / dot3(dir, cam.forward));
+    const float l0 = rnd(st), l1 = rnd(st);
+    const float2 lens = concentric_disk(l0, l1);
+    const float3 ro = cam.pos + cam.right * (lens.x * cam.aperture) + cam.up * (lens.y * cam.aperture);
+    const float3 rd = norm3(focus - ro);
+    P.ro[p] = make_float4(ro.x, ro.y, ro.z, 0.f);
+    P.rd[p] = make_float4(rd.x, rd.y, rd.z, 0.f);
+    P.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+    P.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    P.tint[p] = make_float4(1.f, 1.f, 1.f, __uint_as_float(kSpecular));
+    P.galb[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+    P.gnrm[p] = make_float4(-rd.x, -rd.y, -rd.z, 1e4f);
+    P.rng[p] = st;
+    P.q[0][p] = p;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) P.ctr[kCtrQ0] = total;
+}
+
+__device__ __forceinline__ float3 clamp_c(float3 c, int bounce, float uclamp) {  // trace.frag:65-69
+  if (bounce == 0 || uclamp <= 0.f) return c;
+  const float l = lum(c);
+  return l > uclamp ? c * (uclamp / l) : c;
+}
+
+// Shadow slot: origin + tmax, direction + alpha key, contribution + pending.
+__device__ __forceinline__ void emit_shadow(const Paths& P, uint32_t p, int j, float3 o, float3 d, float tmax,
+                                            uint32_t key, float3 c) {
+  const uint32_t s = 3 * p + j;
+  P.sh_o[s] = make_float4(o.x, o.y, o.z, tmax);
+  P.sh_d[s] = make_float4(d.x, d.y, d.z, __uint_as_float(key));
+  P.sh_c[s] = make_float4(c.x, c.y, c.z, 1.f);
+  P.qs[atomicAdd(&P.ctr[kCtrShadow], 1u)] = s;
+}
+
+__device__ __forceinline__ bool analytic_occluded(const SceneDev& S, float3 ro, float3 rd, float tmax) {
+  for (int i = 0; i < S.sphere_count; i++)  // scene.glsl:337-340
+    if (hit_sphere(ro, rd, __ldg(&S.spheres[i]), tmax) < tmax) return true;
+  return hit_ground(S, ro, rd, tmax) < tmax;
+}
+
+__global__ void __launch_bounds__(128) k_shade(Paths P, SceneDev S, LightingDev L, int cur, int bounce,
+                                               int max_bounces, float uclamp) {
+  const uint32_t n = P.ctr[kCtrQ0 + cur];
+  const uint32_t* q = P.q[cur];
+  uint32_t* qn = P.q[cur ^ 1];
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const uint32_t p = q[k];
+    float3 ro = f3(P.ro[p]), rd = f3(P.rd[p]);
+    const float4 thr4 = P.thr[p], tint4 = P.tint[p];
+    float3 thr = f3(thr4), rad = f3(P.rad[p]), tint = f3(tint4);
+    float bsdf_pdf = thr4.w;
+    unsigned flags = __float_as_uint(tint4.w);
+    bool spec = flags & kSpecular, done = flags & kGuideDone;
+    float4 galb = P.galb[p], gnrm = P.gnrm[p];
+    uint32_t st = P.rng[p];
+    const float4 hv = P.hit[p];
+    bool alive = false;
+
+    // traceScene (scene.glsl:192-333): spheres, ground, then the triangle hit.
+    float closest = INF;
+    int best_sphere = -1;
+    bool ground = false;
+    for (int i = 0; i < S.sphere_count; i++) {
+      const float t = hit_sphere(ro, rd, __ldg(&S.spheres[i]), closest);
+      if (t < closest) {
+        closest = t;
+        best_sphere = i;
+      }
+    }
+    const float tg = hit_ground(S, ro, rd, closest);
+    if (tg < closest) {
+      closest = tg;
+      best_sphere = -1;
+      ground = true;
+    }
+    const int slot = __float_as_int(hv.w);
+    bool tri = false;
+    if (slot >= 0 && hv.x < closest) {
+      closest = hv.x;
+      tri = true;
+      best_sphere = -1;
+      ground = false;
+    }
+    do {
+      if (!tri && best_sphere < 0 && !ground) {  // miss (trace.frag:146-155)
+        const float3 env = bounce == 0 && !L.env_background ? L.backdrop : environment(L, rd, spec, bsdf_pdf);
+        rad = rad + clamp_c(thr * env, bounce, uclamp);
+        if (!done) {
+          galb = make_float4(tint.x, tint.y, tint.z, galb.w);
+          gnrm = make_float4(-rd.x, -rd.y, -rd.z, gnrm.w);
+          done = true;
+        }
+        break;
+      }
+      if (bounce == 0) {
+        gnrm.w = closest;
+        galb.w = 1.f;
+      }
+      // Hit record.
+      const float3 pos = ro + rd * closest;
+      float3 normal, gn;
+      bool front;
+      int material, light = -1;
+      if (ground) {
+        front = rd.y < 0.f;
+        normal = f3(0.f, front ? 1.f : -1.f, 0.f);
+        gn = normal;
+        material = S.ground_material;
+      } else if (best_sphere >= 0) {
+        const float4 sp = __ldg(&S.spheres[best_sphere]);
+        const float3 nn = (pos - f3(sp)) / sp.w;
+        front = dot3(rd, nn) < 0.f;
+        normal = front ? nn : -nn;
+        gn = normal;
+        material = __ldg(&S.sphere_materials[best_sphere]);
+        light = __ldg(&S.sphere_lights[best_sphere]);
+      } else {  // scene.glsl:407-440
+        const float4 g0 = __ldg(&S.geo[3 * (size_t)slot]), g1 = __ldg(&S.geo[3 * (size_t)slot + 1]),
+                     g2 = __ldg(&S.geo[3 * (size_t)slot + 2]);
+        const float4 a0 = __ldg(&S.attr[4 * (size_t)slot]), a1 = __ldg(&S.attr[4 * (size_t)slot + 1]),
+                     a2 = __ldg(&S.attr[4 * (size_t)slot + 2]);
+        const float bu = hv.y, bv = hv.z, w = 1.f - bu - bv;
+        const float3 e1 = f3(g1) - f3(g0), e2 = f3(g2) - f3(g0);
+        float3 ng = norm3(cross3(e1, e2));
+        float3 ns = norm3(f3(a0) * w + f3(a1) * bu + f3(a2) * bv);
+        front = dot3(rd, ng) < 0.f;
+        if (!front) {
+          ng = -ng;
+          ns = -ns;
+        }
+        if (dot3(ns, ng) < 0.05f) ns = ng;
+        normal = ns;
+        gn = ng;
+        material = (int)g0.w;
+        light = (int)g1.w;
+      }
+      // surfaceAt (trace.frag:72-124), no texture maps.
+      const float4* M = S.materials + (size_t)material * 10;
+      const float4 m0 = __ldg(M), m1 = __ldg(M + 1), m2 = __ldg(M + 2), m3 = __ldg(M + 3), m5 = __ldg(M + 5),
+                   m6 = __ldg(M + 6), m7 = __ldg(M + 7), m8 = __ldg(M + 8);
+      Surface s;
+      s.albedo = f3(m0);
+      if (m1.w > 0.f) {
+        const float qx = floorf(pos.x * m1.w + 0.5f), qy = floorf(pos.y * m1.w + 0.5f), qz = floorf(pos.z * m1.w + 0.5f);
+        const float sum = qx + qy + qz;
+        if (sum - 2.f * floorf(sum / 2.f) >= 0.5f) s.albedo = f3(m3);
+      }
+      s.metallic = m0.w;
+      s.roughness = m1.x;
+      const float3 emission = f3(m2);
+      s.nc = normal;
+      s.n = normal;
+      s.ior = m1.y;
+      s.transmission = m1.z * (1.f - s.metallic);
+      s.clearcoat = m5.y;
+      s.clearcoat_roughness = m5.z;
+      s.sheen_color = f3(m6);
+      s.sheen_roughness = m6.w;
+      s.thin = m8.w > 0.5f;
+      if (m7.w > 0.f) {
+        s.absorption = f3(-logf(fmaxf(m7.x, 1e-4f)), -logf(fmaxf(m7.y, 1e-4f)), -logf(fmaxf(m7.z, 1e-4f))) / m7.w;
+      } else {
+        s.absorption = f3(0.f, 0.f, 0.f);
+      }
+      const float3 wo = -rd;
+      if (!front && !s.thin && s.transmission > 0.f)  // trace.frag:168
+        thr = thr * f3(expf(-s.absorption.x * closest), expf(-s.absorption.y * closest), expf(-s.absorption.z * closest));
+      if (emission.x > 0.f || emission.y > 0.f || emission.z > 0.f) {  // :170-184
+        float w = 1.f;
+        if (!spec && light >= 0) w = mis(bsdf_pdf, light_pdf(S, light, ro, rd, closest) / (float)S.light_count);
+        rad = rad + clamp_c(thr * emission * w, bounce, uclamp);
+        if (!done) {
+          galb = make_float4(tint.x, tint.y, tint.z, galb.w);
+          gnrm = make_float4(s.n.x, s.n.y, s.n.z, gnrm.w);
+          done = true;
+        }
+        if (light >= 0) break;
+      }
+      const bool glass = s.transmission > 0.f && rnd(st) < s.transmission;
+      const bool mirror = !glass && s.metallic > 0.9f && s.roughness < 0.1f;
+      if (!done && !((glass || mirror) && bounce < 3)) {
+        galb = make_float4(tint.x * s.albedo.x, tint.y * s.albedo.y, tint.z * s.albedo.z, galb.w);
+        gnrm = make_float4(s.n.x, s.n.y, s.n.z, gnrm.w);
+        done = true;
+      }
+      auto U = [&]() { return rnd(st); };
+      if (glass) {
+        float3 wi, weight;
+        bool refl;
+        if (!sample_dielectric(s, front, gn, wo, wi, weight, refl, U)) break;
+        thr = thr * weight;
+        if (!done) tint = tint * weight;
+        ro = offset_ray(pos, refl ? gn : -gn);
+        rd = wi;
+        spec = true;
+      } else {
+        if (!done) tint = tint * s.albedo;
+        const float3 so = offset_ray(pos, gn);
+        const float3 n = s.n;
+        if (L.sun_enabled) {  // :216-225
+          const float u0 = rnd(st), u1 = rnd(st);
+          float3 t, b;
+          basis(L.sun_dir, t, b);
+          const float3 wi = to_world(uniform_cone(u0, u1, L.sun_cos), t, b, L.sun_dir);
+          const float NdotL = dot3(n, wi);
+          if (NdotL > 0.f && dot3(gn, wi) > 0.f && !analytic_occluded(S, so, wi, INF)) {
+            float pb;
+            const float3 f = eval_opaque(L, s, wo, wi, pb);
+            const float w = mis(L.sun_pdf, pb);
+            emit_shadow(P, p, 0, so, wi, INF, st, clamp_c(thr * f * NdotL * L.sun_radiance * (w / L.sun_pdf), bounce, uclamp));
+          }
+        }
+        if (L.env_sampling) {  // :228-237
+          const LightSample ls = sample_environment(L, st);
+          const float NdotL = dot3(n, ls.dir);
+          if (ls.pdf > 0.f && NdotL > 0.f && dot3(gn, ls.dir) > 0.f && !analytic_occluded(S, so, ls.dir, INF)) {
+            float pb;
+            const float3 f = eval_opaque(L, s, wo, ls.dir, pb);
+            const float w = mis(ls.pdf, pb);
+            emit_shadow(P, p, 1, so, ls.dir, INF, st, clamp_c(thr * f * NdotL * ls.radiance * (w / ls.pdf), bounce, uclamp));
+          }
+        }
+        if (S.light_count > 0) {  // :240-252
+          const int li = min((int)(rnd(st) * (float)S.light_count), S.light_count - 1);
+          const float u0 = rnd(st), u1 = rnd(st);
+          const LightSample ls = sample_light(S, li, pos, u0, u1);
+          const float NdotL = dot3(n, ls.dir);
+          const float tmax = ls.dist * (1.f - 1e-4f);
+          if (ls.pdf > 0.f && NdotL > 0.f && dot3(gn, ls.dir) > 0.f && !analytic_occluded(S, so, ls.dir, tmax)) {
+            const float pl = ls.pdf / (float)S.light_count;
+            float pb;
+            const float3 f = eval_opaque(L, s, wo, ls.dir, pb);
+            const float w = mis(pl, pb);
+            emit_shadow(P, p, 2, so, ls.dir, tmax, st, clamp_c(thr * f * NdotL * ls.radiance * (w / pl), bounce, uclamp));
+          }
+        }
+        const BsdfSample bs = sample_opaque(L, s, wo, U);  // :255-261
+        if (bs.pdf <= 0.f || dot3(bs.dir, gn) <= 0.f) break;
+        thr = thr * bs.weight;
+        bsdf_pdf = bs.pdf;
+        spec = false;
+        ro = so;
+        rd = bs.dir;
+      }
+      if (bounce >= 2) {  // Russian roulette (:265-269)
+        const float pr = fminf(0.95f, max3(thr));
+        if (rnd(st) >= pr) break;
+        thr = thr / pr;
+      }
+      alive = bounce < max_bounces;
+    } while (false);
+
+    P.rad[p] = make_float4(rad.x, rad.y, rad.z, 0.f);
+    P.galb[p] = galb;
+    P.gnrm[p] = gnrm;
+    P.rng[p] = st;
+    if (alive) {
+      P.ro[p] = make_float4(ro.x, ro.y, ro.z, 0.f);
+      P.rd[p] = make_float4(rd.x, rd.y, rd.z, 0.f);
+      P.thr[p] = make_float4(thr.x, thr.y, thr.z, bsdf_pdf);
+      P.tint[p] = make_float4(tint.x, tint.y, tint.z, __uint_as_float((spec ? kSpecular : 0u) | (done ? kGuideDone : 0u)));
+      qn[atomicAdd(&P.ctr[kCtrQ0 + (cur ^ 1)], 1u)] = p;
+    }
+  }
+}
+
+// Adds the unoccluded next-event contributions of this bounce, per path, in
+// the reference's order (sun, environment, light).
+__global__ void k_resolve(Paths P, int cur) {
+  const uint32_t n = P.ctr[kCtrQ0 + cur];
+  const uint32_t* q = P.q[cur];
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const uint32_t p = q[k];
+    float4 r = P.rad[p];
+    bool any = false;
+    for (int j = 0; j < 3; j++) {
+      const uint32_t s = 3 * p + j;
+      const float4 c = P.sh_c[s];
+      if (c.w == 0.f) continue;
+      any = true;
+      if (!P.sh_occ[s]) {
+        r.x += c.x;
+        r.y += c.y;
+        r.z += c.z;
+      }
+      P.sh_c[s].w = 0.f;
+    }
+    if (any) P.rad[p] = r;
+  }
+}
+
+// Running means (trace.frag:335-354), one thread per pixel, samples in order.
+__global__ void k_accumulate(Paths P, AccumDev A, int W, int H, int S) {
+  const uint32_t WH = (uint32_t)W * H;
+  for (uint32_t px = blockIdx.x * blockDim.x + threadIdx.x; px < WH; px += gridDim.x * blockDim.x) {
+    float4 col = A.color[px];
+    float4 alb = make_float4(__half2float(A.albedo[px].x), __half2float(A.albedo[px].y), __half2float(A.albedo[px].z),
+                             __half2float(A.albedo[px].w));
+    float4 nrm = make_float4(__half2float(A.normal[px].x), __half2float(A.normal[px].y), __half2float(A.normal[px].z),
+                             __half2float(A.normal[px].w));
+    float n = A.history[px];
+    for (int s = 0; s < S; s++) {
+      const uint32_t p = (uint32_t)s * WH + px;
+      float4 c = P.rad[p];
+      if (isnan(c.x) || isnan(c.y) || isnan(c.z) || isinf(c.x) || isinf(c.y) || isinf(c.z)) c = make_float4(0.f, 0.f, 0.f, 0.f);
+      const float l = lum(f3(c));
+      const float k = 1.f / (n + 1.f);
+      const float4 ga = P.galb[p], gn = P.gnrm[p];
+      col = make_float4(mixf(col.x, c.x, k), mixf(col.y, c.y, k), mixf(col.z, c.z, k), mixf(col.w, l * l, k));
+      // RGBA16F targets (renderer.ts:490): every store rounds to half.
+      alb = make_float4(__half2float(__float2half_rn(mixf(alb.x, ga.x, k))), __half2float(__float2half_rn(mixf(alb.y, ga.y, k))),
+                        __half2float(__float2half_rn(mixf(alb.z, ga.z, k))), __half2float(__float2half_rn(mixf(alb.w, ga.w, k))));
+      nrm = make_float4(__half2float(__float2half_rn(mixf(nrm.x, gn.x, k))), __half2float(__float2half_rn(mixf(nrm.y, gn.y, k))),
+                        __half2float(__float2half_rn(mixf(nrm.z, gn.z, k))), __half2float(__float2half_rn(mixf(nrm.w, gn.w, k))));
+      n = n + 1.f;
+    }
+    A.color[px] = col;
+    A.albedo[px] = make_half4(alb);
+    A.normal[px] = make_half4(nrm);
+    A.history[px] = n;
+  }
+}
+
+__global__ void k_zero_counters(uint32_t* ctr, int nxt) {
+  if (threadIdx.x == 0) {
+    ctr[kCtrQ0 + nxt] = 0;
+    ctr[kCtrShadow] = 0;
+    ctr[kCtrWork] = 0;
+    ctr[kCtrSlow] = 0;
+    ctr[kCtrWork2] = 0;
+    ctr[kCtrSlow2] = 0;
+  }
+}
+
+__global__ void k_count_rays(uint32_t* ctr, int cur) {  // statistics: rays traced this bounce
+  if (threadIdx.x == 0) {
+    atomicAdd((unsigned long long*)(ctr + kCtrStatClosest), (unsigned long long)ctr[kCtrQ0 + cur]);
+    atomicAdd((unsigned long long*)(ctr + kCtrStatShadow), (unsigned long long)ctr[kCtrShadow]);
+  }
+}
+
+// ------------------------------------------------------------ one batch
+void render_batch(const RenderLaunch& R, cudaStream_t s, PhaseEvents* pe) {
+  const Paths& P = R.paths;
+  const uint32_t total = (uint32_t)R.W * R.H * R.S;
+  const int blocks = grid_for(total, 256);
+  PhaseEvents none{nullptr, nullptr, 0, 0};
+  PhaseEvents& E = pe ? *pe : none;
+  E.mark(-1, s);
+  k_camera<<<blocks, 256, 0, s>>>(P, R.cam, R.W, R.H, R.S, R.seed0);
+  E.mark(kPhCamera, s);
+  static int closest_blocks = 0, shade_blocks = 0;
+  if (!closest_blocks) {
+    closest_blocks = persistent_blocks((const void*)k_closest_fast_t<PathClosest>, 256);
+    shade_blocks = persistent_blocks((const void*)k_shade, 128);
+  }
+  for (int b = 0; b <= R.max_bounces; b++) {
+    const int cur = b & 1;
+    k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
+    E.mark(kPhResolve, s);
+    PathClosest pc{P.ctr + kCtrQ0 + cur, P.q[cur], P.ro, P.rd, P.rng, P.hit, R.scene.geo, R.scene.materials,
+                   R.scene.any_alpha};
+    TravArgs A{R.scene.nodes, R.scene.node_count, R.scene.geo, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow,
+               P.ctr + kCtrWork, P.ctr + kCtrErr, R.trav_stats};
+    k_closest_fast_t<PathClosest><<<closest_blocks, 256, 0, s>>>(A, pc);
+    k_closest_exact_t<PathClosest><<<64, 128, 0, s>>>(A, pc);
+    E.mark(kPhClosest, s);
+    k_shade<<<shade_blocks, 128, 0, s>>>(P, R.scene, R.light, cur, b, R.max_bounces, R.clamp);
+    E.mark(kPhShade, s);
+    PathShadow ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, R.scene.geo, R.scene.materials, R.scene.any_alpha};
+    TravArgs B{R.scene.nodes, R.scene.node_count, R.scene.geo, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2,
+               P.ctr + kCtrWork2, P.ctr + kCtrErr};
+    k_anyhit_fast_t<PathShadow><<<shade_blocks * 2, 256, 0, s>>>(B, ps);
+    k_anyhit_exact_t<PathShadow><<<64, 128, 0, s>>>(B, ps);
+    E.mark(kPhShadow, s);
+    k_resolve<<<shade_blocks, 128, 0, s>>>(P, cur);
+    k_count_rays<<<1, 32, 0, s>>>(P.ctr, cur);
+  }
+  E.mark(kPhResolve, s);
+  k_accumulate<<<grid_for((uint32_t)R.W * R.H, 256), 256, 0, s>>>(P, R.accum, R.W, R.H, R.S);
+  E.mark(kPhAccumulate, s);
+}
+
+}  // namespace lucent

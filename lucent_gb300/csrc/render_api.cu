@@ -1,0 +1,649 @@
+// Renderer C ABI: scene / lighting / camera upload, accumulation targets,
+// trace, readback. Mirrors the Renderer class of src/renderer.ts.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/lucent.h"
+#include "api_util.h"
+#include "internal.h"
+#include "render_internal.h"
+
+using namespace lucent;
+
+namespace lucent {
+
+// Packs the scene's triangles into BVH leaf order (scene.ts:215-235):
+// geo = (v0, material), (v1, light), (v2, alpha flag);
+// attr = (n0, u0), (n1, u1), (n2, u2), (v0, v1, v2, 0).
+__global__ void k_pack_scene(const float* __restrict__ pos, const float* __restrict__ nrm,
+                             const float* __restrict__ uvs, const int32_t* __restrict__ mat,
+                             const int32_t* __restrict__ light, const uint8_t* __restrict__ alpha,
+                             const uint32_t* __restrict__ tri_indices, uint32_t n, float4* __restrict__ geo,
+                             float4* __restrict__ attr) {
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const uint32_t src = tri_indices[s];
+    const float* p = pos + (size_t)src * 9;
+    const float* q = nrm + (size_t)src * 9;
+    const float* u = uvs ? uvs + (size_t)src * 6 : nullptr;
+    geo[3 * (size_t)s] = make_float4(p[0], p[1], p[2], (float)mat[src]);
+    geo[3 * (size_t)s + 1] = make_float4(p[3], p[4], p[5], light ? (float)light[src] : -1.f);
+    geo[3 * (size_t)s + 2] = make_float4(p[6], p[7], p[8], alpha ? (float)alpha[src] : 0.f);
+    for (int v = 0; v < 3; v++)
+      attr[4 * (size_t)s + v] = make_float4(q[v * 3], q[v * 3 + 1], q[v * 3 + 2], u ? u[v * 2] : 0.f);
+    attr[4 * (size_t)s + 3] = make_float4(u ? u[1] : 0.f, u ? u[3] : 0.f, u ? u[5] : 0.f, 0.f);
+  }
+}
+
+__global__ void k_clear_accum(AccumDev A, uint32_t n) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    A.color[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    A.albedo[i] = make_half4(make_float4(0.f, 0.f, 0.f, 0.f));
+    A.normal[i] = make_half4(make_float4(0.f, 0.f, 0.f, 0.f));
+    A.history[i] = 0.f;
+  }
+}
+
+__global__ void k_unpack_accum(AccumDev A, uint32_t n, float* alb, float* nrm) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const half4 a = A.albedo[i], b = A.normal[i];
+    if (alb) {
+      alb[4 * i] = __half2float(a.x), alb[4 * i + 1] = __half2float(a.y);
+      alb[4 * i + 2] = __half2float(a.z), alb[4 * i + 3] = __half2float(a.w);
+    }
+    if (nrm) {
+      nrm[4 * i] = __half2float(b.x), nrm[4 * i + 1] = __half2float(b.y);
+      nrm[4 * i + 2] = __half2float(b.z), nrm[4 * i + 3] = __half2float(b.w);
+    }
+  }
+}
+
+// ------------------------------------------------------------ host precompute
+// buildAliasTable (src/math/alias.ts:17-65), Vose's method.
+static bool alias_table(const std::vector<double>& w, std::vector<float>& prob, std::vector<uint32_t>& alias,
+                        std::vector<double>& pmf, double& total) {
+  const size_t n = w.size();
+  if (n == 0) return false;
+  total = 0;
+  for (double x : w) {
+    if (!(x >= 0) || !std::isfinite(x)) return false;
+    total += x;
+  }
+  pmf.resize(n);
+  for (size_t i = 0; i < n; i++) pmf[i] = total > 0 ? w[i] / total : 1.0 / (double)n;
+  std::vector<double> scaled(n);
+  std::vector<uint32_t> small, large;
+  small.reserve(n);
+  large.reserve(n);
+  for (size_t i = 0; i < n; i++) {
+    scaled[i] = pmf[i] * (double)n;
+    (scaled[i] < 1 ? small : large).push_back((uint32_t)i);
+  }
+  prob.assign(n, 0.f);
+  alias.assign(n, 0u);
+  while (!small.empty() && !large.empty()) {
+    const uint32_t s = small.back(), l = large.back();
+    small.pop_back();
+    large.pop_back();
+    prob[s] = (float)scaled[s];
+    alias[s] = l;
+    scaled[l] = scaled[l] + scaled[s] - 1;
+    (scaled[l] < 1 ? small : large).push_back(l);
+  }
+  while (!large.empty()) {
+    prob[large.back()] = 1;
+    alias[large.back()] = large.back();
+    large.pop_back();
+  }
+  while (!small.empty()) {
+    prob[small.back()] = 1;
+    alias[small.back()] = small.back();
+    small.pop_back();
+  }
+  return true;
+}
+
+// buildEnvSampler (src/scene/environment.ts:52-85): cells of a grid at most
+// max_w wide, weight = mean luminance x sin(theta), then the alias table; 4
+// floats per cell (keep probability, alias cell, pdfUV, alias pdfUV).
+static bool env_sampler(const float* rgb, uint32_t w, uint32_t h, uint32_t max_w, uint32_t& gw, uint32_t& gh,
+                        std::vector<float>& table, double& total) {
+  gw = std::max(1u, std::min(w, max_w));
+  gh = std::max(1u, std::min(h, (uint32_t)std::floor((double)h * gw / w + 0.5)));
+  std::vector<double> weights((size_t)gw * gh);
+  for (uint32_t cy = 0; cy < gh; cy++) {
+    const uint64_t y0 = (uint64_t)std::floor((double)cy * h / gh);
+    const uint64_t y1 = std::max(y0 + 1, (uint64_t)std::floor((double)(cy + 1) * h / gh));
+    const double st = std::sin(M_PI * (cy + 0.5) / gh);
+    for (uint32_t cx = 0; cx < gw; cx++) {
+      const uint64_t x0 = (uint64_t)std::floor((double)cx * w / gw);
+      const uint64_t x1 = std::max(x0 + 1, (uint64_t)std::floor((double)(cx + 1) * w / gw));
+      double sum = 0;
+      for (uint64_t y = y0; y < y1; y++)
+        for (uint64_t x = x0; x < x1; x++) {
+          const float* p = rgb + (y * w + x) * 3;
+          sum += 0.2126 * (double)p[0] + 0.7152 * (double)p[1] + 0.0722 * (double)p[2];
+        }
+      weights[(size_t)cy * gw + cx] = (sum / (double)((y1 - y0) * (x1 - x0))) * st;
+    }
+  }
+  std::vector<float> prob;
+  std::vector<uint32_t> alias;
+  std::vector<double> pmf;
+  if (!alias_table(weights, prob, alias, pmf, total)) return false;
+  const size_t n = weights.size();
+  table.resize(n * 4);
+  for (size_t i = 0; i < n; i++) {
+    table[i * 4] = prob[i];
+    table[i * 4 + 1] = (float)alias[i];
+    table[i * 4 + 2] = (float)(pmf[i] * (double)n);
+    table[i * 4 + 3] = (float)(pmf[alias[i]] * (double)n);
+  }
+  return true;
+}
+
+// sheenAlbedoLUT (src/scene/sheen.ts:13-60): 16 x 16, 96 quadrature steps,
+// then rounded to half precision like the reference's R16F upload.
+static void sheen_lut(float* out) {
+  const int size = 16, steps = 96;
+  for (int y = 0; y < size; y++)
+    for (int x = 0; x < size; x++) {
+      const double cosV = std::max(1e-3, (double)x / (size - 1));
+      const double r = std::max(0.07, (double)y / (size - 1));
+      const double alpha = r * r, inv = 1 / alpha;
+      const double v0 = std::sqrt(std::max(0.0, 1 - cosV * cosV)), v2 = cosV;
+      const int phi_steps = steps / 2;
+      const double dth = M_PI / 2 / steps, dph = M_PI / phi_steps;
+      double e = 0;
+      for (int i = 0; i < steps; i++) {
+        const double th = (i + 0.5) * dth, ch = std::cos(th), shh = std::sin(th);
+        const double d = ((2 + inv) * std::pow(std::max(0.0, 1 - ch * ch), inv * 0.5)) / (2 * M_PI);
+        for (int j = 0; j < phi_steps; j++) {
+          const double ph = (j + 0.5) * dph;
+          const double vh = v0 * (shh * std::cos(ph)) + v2 * ch;
+          if (vh <= 0) continue;
+          const double cosL = 2 * vh * ch - v2;
+          if (cosL <= 0) continue;
+          e += d * (1 / (4 * (cosL + cosV - cosL * cosV))) * cosL * 4 * vh * shh * dth * dph;
+        }
+      }
+      out[y * size + x] = __half2float(__float2half_rn((float)std::min(1.0, 2 * e)));
+    }
+}
+
+}  // namespace lucent
+
+struct lucent_renderer {
+  uint32_t W = 1, H = 1;
+  // scene
+  DeviceBuffer nodes, geo, attr, mats, spheres, sph_mat, sph_light, lights;
+  uint32_t node_count = 0, tri_count = 0, material_count = 0, sphere_count = 0, light_count = 0;
+  int32_t ground_material = -1, ground_enabled = 0, any_alpha = 0;
+  float ground_height = 0;
+  bool has_scene = false;
+  // lighting
+  DeviceBuffer env_rgb, env_alias, sheen;
+  sh::LightingDev light{};
+  bool has_lighting = false;
+  // camera and settings (renderer.ts DEFAULT_SETTINGS: maxBounces 6, fireflyClamp 8)
+  sh::CameraDev cam{};
+  uint32_t max_bounces = 6;
+  float clamp = 8.f;
+  // targets and path state
+  DeviceBuffer color, albedo, normal, history, paths, ctr;
+  uint32_t path_cap = 0;
+  Paths P{};
+  uint32_t frame = 0, seed = 0;
+  double last_ms = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // optional per-phase timing (lucent_renderer_set_profiling)
+  bool profiling = false;
+  std::vector<cudaEvent_t> pev;
+  std::vector<int> ptag;
+  int pn = 0;
+  double phase_ms[kPhases] = {0, 0, 0, 0, 0, 0};
+};
+
+static AccumDev accum_of(lucent_renderer* r) {
+  return {(float4*)r->color.ptr, (half4*)r->albedo.ptr, (half4*)r->normal.ptr, (float*)r->history.ptr};
+}
+
+static lucent_status alloc_targets(lucent_renderer* r, uint32_t w, uint32_t h) {
+  const size_t n = (size_t)w * h;
+  lucent_status st;
+  if ((st = r->color.reserve(n * 16)) || (st = r->albedo.reserve(n * 8)) || (st = r->normal.reserve(n * 8)) ||
+      (st = r->history.reserve(n * 4)))
+    return st;
+  r->W = w;
+  r->H = h;
+  k_clear_accum<<<grid_for((uint32_t)n, 256), 256>>>(accum_of(r), (uint32_t)n);
+  r->frame = 0;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "clear targets");
+}
+
+// Path buffers for `cap` paths (bytes per path: 8 float4 + rng + 2 queue
+// entries + 3 shadow slots of 3 float4, a flag and a queue entry).
+static lucent_status alloc_paths(lucent_renderer* r, uint32_t cap) {
+  if (cap <= r->path_cap) return LUCENT_OK;
+  // Per-path arrays in allocation order (bytes per path); each starts on a 256-byte boundary.
+  static const size_t kPer[] = {16, 16, 16, 16, 16, 16, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12};
+  size_t total = 0;
+  for (size_t b : kPer) total += ((size_t)cap * b + 255) & ~(size_t)255;
+  lucent_status st = r->paths.reserve(total);
+  if (st) return st;
+  if ((st = r->ctr.reserve(kCtrWords * 4))) return st;
+  char* b = (char*)r->paths.ptr;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* p = b + off;
+    off += (bytes + 255) & ~(size_t)255;
+    return (void*)p;
+  };
+  Paths& P = r->P;
+  P.ro = (float4*)take((size_t)cap * 16);
+  P.rd = (float4*)take((size_t)cap * 16);
+  P.thr = (float4*)take((size_t)cap * 16);
+  P.rad = (float4*)take((size_t)cap * 16);
+  P.tint = (float4*)take((size_t)cap * 16);
+  P.galb = (float4*)take((size_t)cap * 16);
+  P.gnrm = (float4*)take((size_t)cap * 16);
+  P.hit = (float4*)take((size_t)cap * 16);
+  P.sh_o = (float4*)take((size_t)cap * 48);
+  P.sh_d = (float4*)take((size_t)cap * 48);
+  P.sh_c = (float4*)take((size_t)cap * 48);
+  P.rng = (uint32_t*)take((size_t)cap * 4);
+  P.sh_occ = (uint8_t*)take((size_t)cap * 3);
+  P.q[0] = (uint32_t*)take((size_t)cap * 4);
+  P.q[1] = (uint32_t*)take((size_t)cap * 4);
+  P.qs = (uint32_t*)take((size_t)cap * 12);
+  P.slow = (uint32_t*)take((size_t)cap * 4);
+  P.slow2 = (uint32_t*)take((size_t)cap * 12);
+  if (off > r->paths.cap) return fail(LUCENT_ERR_DEVICE, "path buffer layout overflow");
+  P.ctr = (uint32_t*)r->ctr.ptr;
+  cudaError_t e = cudaMemset(P.sh_c, 0, (size_t)cap * 48);
+  if (e == cudaSuccess) e = cudaMemset(P.ctr, 0, kCtrWords * 4);
+  if (e != cudaSuccess) return cuda_fail(e, "clear path buffers");
+  r->path_cap = cap;
+  return LUCENT_OK;
+}
+
+extern "C" {
+
+lucent_status lucent_renderer_create(uint32_t width, uint32_t height, lucent_renderer** out) {
+  clear_error();
+  if (!out) return fail(LUCENT_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (width == 0 || height == 0 || (uint64_t)width * height > (1u << 26))
+    return fail(LUCENT_ERR_INVALID, "bad size %ux%u", width, height);
+  lucent_renderer* r = new lucent_renderer();
+  lucent_status st = alloc_targets(r, width, height);
+  if (!st) st = r->sheen.reserve(256 * 4);
+  if (!st) {
+    float lut[256];
+    sheen_lut(lut);
+    cudaError_t e = cudaMemcpy(r->sheen.ptr, lut, sizeof lut, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaEventCreate(&r->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&r->ev1);
+    if (e != cudaSuccess) st = cuda_fail(e, "renderer setup");
+  }
+  if (st) {
+    lucent_renderer_destroy(r);
+    return st;
+  }
+  r->light.sheen_lut = (const float*)r->sheen.ptr;
+  *out = r;
+  return LUCENT_OK;
+}
+
+void lucent_renderer_destroy(lucent_renderer* r) {
+  if (!r) return;
+  for (DeviceBuffer* b : {&r->nodes, &r->geo, &r->attr, &r->mats, &r->spheres, &r->sph_mat, &r->sph_light,
+                          &r->lights, &r->env_rgb, &r->env_alias, &r->sheen, &r->color, &r->albedo, &r->normal,
+                          &r->history, &r->paths, &r->ctr})
+    b->release();
+  if (r->ev0) cudaEventDestroy(r->ev0);
+  if (r->ev1) cudaEventDestroy(r->ev1);
+  for (cudaEvent_t e : r->pev) cudaEventDestroy(e);
+  delete r;
+}
+
+static lucent_status upload(DeviceBuffer& b, const void* src, size_t bytes) {
+  lucent_status st = b.reserve(bytes ? bytes : 16);
+  if (st) return st;
+  if (!bytes) return LUCENT_OK;
+  cudaError_t e = cudaMemcpy(b.ptr, src, bytes, cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "upload");
+}
+
+lucent_status lucent_renderer_load_scene(lucent_renderer* r, const lucent_scene_desc* d) {
+  clear_error();
+  if (!r || !d) return fail(LUCENT_ERR_INVALID, "null argument");
+  const uint32_t n = d->tri_count;
+  if (n && (!d->positions || !d->normals || !d->tri_material))
+    return fail(LUCENT_ERR_INVALID, "triangles need positions, normals and material ids");
+  if (n > (1u << 23)) return fail(LUCENT_ERR_UNSUPPORTED, "%u triangles; the limit is 2^23", n);
+  if (d->sphere_count > 64) return fail(LUCENT_ERR_INVALID, "scene has %u spheres; max is 64", d->sphere_count);
+  if (d->light_count > 8) return fail(LUCENT_ERR_INVALID, "scene has %u lights; max is 8", d->light_count);
+  if (d->material_count == 0 || !d->materials) return fail(LUCENT_ERR_INVALID, "scene has no materials");
+  const uint32_t M = d->material_count;
+  for (uint32_t m = 0; m < M; m++)
+    for (int k = 16; k < 20; k++)
+      if (d->materials[m * 40 + k] >= 0)
+        return fail(LUCENT_ERR_UNSUPPORTED, "material %u uses a texture map; texture layers are not supported", m);
+  for (uint32_t i = 0; i < n; i++) {
+    if (d->tri_material[i] < 0 || (uint32_t)d->tri_material[i] >= M)
+      return fail(LUCENT_ERR_INVALID, "triangle %u has material %d", i, d->tri_material[i]);
+    if (d->tri_light && (d->tri_light[i] < -1 || d->tri_light[i] >= (int32_t)d->light_count))
+      return fail(LUCENT_ERR_INVALID, "triangle %u has light %d", i, d->tri_light[i]);
+  }
+  for (uint32_t i = 0; i < d->sphere_count; i++) {
+    if (d->sphere_materials[i] < 0 || (uint32_t)d->sphere_materials[i] >= M)
+      return fail(LUCENT_ERR_INVALID, "sphere %u has material %d", i, d->sphere_materials[i]);
+    if (d->sphere_lights && (d->sphere_lights[i] < -1 || d->sphere_lights[i] >= (int32_t)d->light_count))
+      return fail(LUCENT_ERR_INVALID, "sphere %u has light %d", i, d->sphere_lights[i]);
+  }
+  if (d->ground_material >= (int32_t)M) return fail(LUCENT_ERR_INVALID, "ground material %d", d->ground_material);
+  for (uint64_t i = 0; i < (uint64_t)n * 9; i++)
+    if (!std::isfinite(d->positions[i])) return fail(LUCENT_ERR_UNSUPPORTED, "positions[%llu] is not finite", (unsigned long long)i);
+  if (d->bvh_nodes) {
+    if (!d->bvh_tri_indices) return fail(LUCENT_ERR_INVALID, "prebuilt BVH without triIndices");
+    lucent_status st = validate_bvh(d->bvh_nodes, d->bvh_node_count, d->bvh_tri_indices, n);
+    if (st) return st;
+  }
+  cudaStream_t s = 0;
+  DeviceBuffer pos, nrm, uvs, mat, lgt, alp, idx;
+  auto cleanup = [&](lucent_status st) {
+    for (DeviceBuffer* b : {&pos, &nrm, &uvs, &mat, &lgt, &alp, &idx}) b->release();
+    return st;
+  };
+  lucent_status st;
+  if ((st = upload(pos, d->positions, (size_t)n * 36)) || (st = upload(nrm, d->normals, (size_t)n * 36)) ||
+      (st = upload(mat, d->tri_material, (size_t)n * 4)))
+    return cleanup(st);
+  if (d->uvs && (st = upload(uvs, d->uvs, (size_t)n * 24))) return cleanup(st);
+  if (d->tri_light && (st = upload(lgt, d->tri_light, (size_t)n * 4))) return cleanup(st);
+  if (d->tri_alpha && (st = upload(alp, d->tri_alpha, (size_t)n))) return cleanup(st);
+  std::vector<float> ref;
+  std::vector<uint32_t> tri;
+  double bounds[6];
+  if (d->bvh_nodes) {
+    ref.assign(d->bvh_nodes, d->bvh_nodes + (size_t)d->bvh_node_count * 8);
+    tri.assign(d->bvh_tri_indices, d->bvh_tri_indices + n);
+    DeviceBuffer rb;
+    if ((st = upload(rb, ref.data(), ref.size() * 4)) || (st = r->nodes.reserve((size_t)d->bvh_node_count * 32))) {
+      rb.release();
+      return cleanup(st);
+    }
+    launch_pack_nodes((const float*)rb.ptr, d->bvh_node_count, (Node*)r->nodes.ptr, s);
+    cudaStreamSynchronize(s);
+    rb.release();
+  } else {
+    if ((st = gpu_build_bvh((const float*)pos.ptr, n, 4, 12, s, ref, tri, bounds, &r->nodes, nullptr)))
+      return cleanup(st);
+  }
+  const uint32_t nc = (uint32_t)(ref.size() / 8);
+  if (tree_depth(ref.data(), nc, n) + 2 > kTsStack)
+    return cleanup(fail(LUCENT_ERR_UNSUPPORTED, "BVH deeper than the reference's 64-entry traversal stack"));
+  if ((st = upload(idx, tri.data(), (size_t)n * 4)) || (st = r->geo.reserve((size_t)(n ? n : 1) * 48)) ||
+      (st = r->attr.reserve((size_t)(n ? n : 1) * 64)))
+    return cleanup(st);
+  if (n)
+    k_pack_scene<<<grid_for(n, 256), 256, 0, s>>>((const float*)pos.ptr, (const float*)nrm.ptr,
+                                                   d->uvs ? (const float*)uvs.ptr : nullptr, (const int32_t*)mat.ptr,
+                                                   d->tri_light ? (const int32_t*)lgt.ptr : nullptr,
+                                                   d->tri_alpha ? (const uint8_t*)alp.ptr : nullptr,
+                                                   (const uint32_t*)idx.ptr, n, (float4*)r->geo.ptr,
+                                                   (float4*)r->attr.ptr);
+  if ((st = upload(r->mats, d->materials, (size_t)M * 160))) return cleanup(st);
+  std::vector<float> sph(256 * 4, 0.f);
+  std::vector<int32_t> sm(64, 0), sl(64, -1);
+  for (uint32_t i = 0; i < d->sphere_count; i++) {
+    for (int k = 0; k < 4; k++) sph[i * 4 + k] = d->spheres[i * 4 + k];
+    sm[i] = d->sphere_materials[i];
+    sl[i] = d->sphere_lights ? d->sphere_lights[i] : -1;
+  }
+  std::vector<float> lts(8 * 16, 0.f);
+  if (d->light_count) std::memcpy(lts.data(), d->lights, (size_t)d->light_count * 64);
+  if ((st = upload(r->spheres, sph.data(), sph.size() * 4)) || (st = upload(r->sph_mat, sm.data(), 256)) ||
+      (st = upload(r->sph_light, sl.data(), 256)) || (st = upload(r->lights, lts.data(), lts.size() * 4)))
+    return cleanup(st);
+  int any_alpha = 0;
+  if (d->tri_alpha)
+    for (uint32_t i = 0; i < n && !any_alpha; i++) any_alpha = d->tri_alpha[i] != 0;
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return cleanup(cuda_fail(e, "scene upload"));
+  r->node_count = nc;
+  r->tri_count = n;
+  r->material_count = M;
+  r->sphere_count = d->sphere_count;
+  r->light_count = d->light_count;
+  r->ground_material = d->ground_material;
+  r->any_alpha = any_alpha;
+  r->has_scene = true;
+  cleanup(LUCENT_OK);
+  return lucent_renderer_reset(r);
+}
+
+lucent_status lucent_renderer_upload_lighting(lucent_renderer* r, const lucent_lighting* l) {
+  clear_error();
+  if (!r || !l) return fail(LUCENT_ERR_INVALID, "null argument");
+  if (!l->env_rgb || l->env_width == 0 || l->env_height == 0) return fail(LUCENT_ERR_INVALID, "lighting needs an environment map");
+  const size_t texels = (size_t)l->env_width * l->env_height;
+  for (size_t i = 0; i < texels * 3; i++)
+    if (!(l->env_rgb[i] >= 0) || !std::isfinite(l->env_rgb[i]))
+      return fail(LUCENT_ERR_INVALID, "environment texel %zu is negative or not finite", i / 3);
+  uint32_t gw, gh;
+  std::vector<float> table;
+  double total;
+  if (!env_sampler(l->env_rgb, l->env_width, l->env_height, 1024, gw, gh, table, total))
+    return fail(LUCENT_ERR_INVALID, "environment sampler failed");
+  lucent_status st;
+  if ((st = upload(r->env_rgb, l->env_rgb, texels * 12)) || (st = upload(r->env_alias, table.data(), table.size() * 4)))
+    return st;
+  sh::LightingDev& L = r->light;
+  L.sun_enabled = l->sun_enabled;
+  L.sun_dir = make_float3(l->sun_dir[0], l->sun_dir[1], l->sun_dir[2]);
+  L.sun_radiance = make_float3(l->sun_radiance[0], l->sun_radiance[1], l->sun_radiance[2]);
+  L.sun_cos = l->sun_cos_angle;
+  L.sun_pdf = l->sun_pdf;
+  L.env_rgb = (const float*)r->env_rgb.ptr;
+  L.env_w = (int)l->env_width;
+  L.env_h = (int)l->env_height;
+  L.env_alias = (const float4*)r->env_alias.ptr;
+  L.grid_w = (int)gw;
+  L.grid_h = (int)gh;
+  L.env_cos = l->env_rotation_cos;
+  L.env_sin = l->env_rotation_sin;
+  L.env_intensity = l->env_intensity;
+  L.env_sampling = total > 0 ? 1 : 0;  // renderer.ts:412
+  L.env_background = l->env_background;
+  L.backdrop = make_float3(l->backdrop[0], l->backdrop[1], l->backdrop[2]);
+  L.sheen_lut = (const float*)r->sheen.ptr;
+  r->has_lighting = true;
+  return lucent_renderer_reset(r);
+}
+
+lucent_status lucent_renderer_upload_ground(lucent_renderer* r, int32_t enabled, float height) {
+  clear_error();
+  if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  r->ground_enabled = enabled;
+  r->ground_height = height;
+  return lucent_renderer_reset(r);
+}
+
+lucent_status lucent_renderer_upload_camera(lucent_renderer* r, const lucent_camera* c) {
+  clear_error();
+  if (!r || !c) return fail(LUCENT_ERR_INVALID, "null argument");
+  r->cam.pos = make_float3(c->position[0], c->position[1], c->position[2]);
+  r->cam.right = make_float3(c->right[0], c->right[1], c->right[2]);
+  r->cam.up = make_float3(c->up[0], c->up[1], c->up[2]);
+  r->cam.forward = make_float3(c->forward[0], c->forward[1], c->forward[2]);
+  r->cam.tan_half_fov = c->tan_half_fov;
+  r->cam.aperture = c->aperture;
+  r->cam.focus = c->focus_distance;
+  return lucent_renderer_reset(r);  // the view changed; no temporal reprojection here
+}
+
+lucent_status lucent_renderer_apply_settings(lucent_renderer* r, const lucent_settings* s) {
+  clear_error();
+  if (!r || !s) return fail(LUCENT_ERR_INVALID, "null argument");
+  if (s->max_bounces > 64) return fail(LUCENT_ERR_INVALID, "max_bounces %u", s->max_bounces);
+  r->max_bounces = s->max_bounces;
+  r->clamp = s->firefly_clamp;
+  return LUCENT_OK;
+}
+
+lucent_status lucent_renderer_resize(lucent_renderer* r, uint32_t w, uint32_t h) {
+  clear_error();
+  if (!r || w == 0 || h == 0 || (uint64_t)w * h > (1u << 26)) return fail(LUCENT_ERR_INVALID, "bad size");
+  return alloc_targets(r, w, h);
+}
+
+lucent_status lucent_renderer_reset(lucent_renderer* r) {
+  clear_error();
+  if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  const uint32_t n = r->W * r->H;
+  k_clear_accum<<<grid_for(n, 256), 256>>>(accum_of(r), n);
+  r->frame = 0;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "reset");
+}
+
+lucent_status lucent_renderer_set_seed(lucent_renderer* r, uint32_t seed) {
+  clear_error();
+  if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  r->seed = seed;
+  return LUCENT_OK;
+}
+
+lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* stream) {
+  clear_error();
+  if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  if (!r->has_scene || !r->has_lighting) return fail(LUCENT_ERR_INVALID, "trace before load_scene / upload_lighting");
+  if (samples == 0) return LUCENT_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const uint32_t WH = r->W * r->H;
+  const uint32_t max_paths = 1u << 23;
+  uint32_t batch = std::max(1u, std::min(samples, max_paths / std::max(1u, WH)));
+  lucent_status st = alloc_paths(r, batch * WH);
+  if (st) return st;
+  RenderLaunch R;
+  R.paths = r->P;
+  R.scene = {(const Node*)r->nodes.ptr, r->node_count, (const float4*)r->geo.ptr, (const float4*)r->attr.ptr,
+             (const float4*)r->mats.ptr, (const float4*)r->spheres.ptr, (const int*)r->sph_mat.ptr,
+             (const int*)r->sph_light.ptr, (int)r->sphere_count, (const float4*)r->lights.ptr, (int)r->light_count,
+             r->ground_enabled ? r->ground_material : -1, r->ground_height, r->any_alpha};
+  R.light = r->light;
+  R.cam = r->cam;
+  R.accum = accum_of(r);
+  R.W = (int)r->W;
+  R.H = (int)r->H;
+  R.max_bounces = (int)r->max_bounces;
+  R.clamp = r->clamp;
+  R.trav_stats = r->profiling ? (unsigned long long*)((uint32_t*)r->ctr.ptr + kCtrTrav) : nullptr;
+  cudaEventRecord(r->ev0, s);
+  PhaseEvents pe{r->pev.data(), r->ptag.data(), (int)r->pev.size(), 0};
+  for (uint32_t done = 0; done < samples; done += batch) {
+    R.S = (int)std::min(batch, samples - done);
+    R.seed0 = r->seed;
+    render_batch(R, s, r->profiling ? &pe : nullptr);
+    r->seed += (uint32_t)R.S;
+    r->frame += (uint32_t)R.S;
+  }
+  cudaEventRecord(r->ev1, s);
+  r->pn = pe.n;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "trace launch");
+}
+
+lucent_status lucent_renderer_set_profiling(lucent_renderer* r, int32_t enabled) {
+  clear_error();
+  if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  r->profiling = enabled != 0;
+  if (r->profiling && r->pev.empty()) {
+    r->pev.resize(1024);
+    r->ptag.resize(1024);
+    for (cudaEvent_t& e : r->pev) {
+      cudaError_t err = cudaEventCreate(&e);
+      if (err != cudaSuccess) return cuda_fail(err, "profiling events");
+    }
+  }
+  return LUCENT_OK;
+}
+
+lucent_status lucent_renderer_check(lucent_renderer* r, void* stream) {
+  clear_error();
+  if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "synchronize");
+  if (!r->ctr.ptr) return LUCENT_OK;
+  uint32_t word = 0;
+  e = cudaMemcpy(&word, (uint32_t*)r->ctr.ptr + kCtrErr, 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "read error word");
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, r->ev0, r->ev1) == cudaSuccess) r->last_ms = ms;
+  if (r->profiling && r->pn > 1) {
+    for (double& v : r->phase_ms) v = 0;
+    for (int i = 1; i < r->pn; i++) {
+      if (r->ptag[i] < 0) continue;
+      float d = 0;
+      if (cudaEventElapsedTime(&d, r->pev[i - 1], r->pev[i]) == cudaSuccess) r->phase_ms[r->ptag[i]] += d;
+    }
+    r->pn = 0;
+  }
+  if (word) {
+    cudaMemset((uint32_t*)r->ctr.ptr + kCtrErr, 0, 4);
+    return fail(LUCENT_ERR_DEVICE, "render raised device error word 0x%x", word);
+  }
+  return LUCENT_OK;
+}
+
+lucent_status lucent_renderer_read(lucent_renderer* r, float* color4, float* albedo4, float* normal4, float* history) {
+  lucent_status st = lucent_renderer_check(r, nullptr);
+  if (st) return st;
+  const uint32_t n = r->W * r->H;
+  cudaError_t e = cudaSuccess;
+  if (color4) e = cudaMemcpy(color4, r->color.ptr, (size_t)n * 16, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && history) e = cudaMemcpy(history, r->history.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && (albedo4 || normal4)) {
+    DeviceBuffer tmp;
+    if ((st = tmp.reserve((size_t)n * 32))) return st;
+    float* a = (float*)tmp.ptr;
+    float* b = a + (size_t)n * 4;
+    k_unpack_accum<<<grid_for(n, 256), 256>>>(accum_of(r), n, albedo4 ? a : nullptr, normal4 ? b : nullptr);
+    if (albedo4) e = cudaMemcpy(albedo4, a, (size_t)n * 16, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && normal4) e = cudaMemcpy(normal4, b, (size_t)n * 16, cudaMemcpyDeviceToHost);
+    tmp.release();
+  }
+  return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "read targets");
+}
+
+lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out) {
+  clear_error();
+  if (!r || !out) return fail(LUCENT_ERR_INVALID, "null argument");
+  std::memset(out, 0, sizeof *out);
+  out->samples = r->frame;
+  out->seed = r->seed;
+  out->width = r->W;
+  out->height = r->H;
+  out->triangles = r->tri_count;
+  out->bvh_nodes = r->node_count;
+  if (r->ctr.ptr) {
+    uint64_t c[2] = {0, 0};
+    cudaError_t e = cudaMemcpy(c, (uint32_t*)r->ctr.ptr + kCtrStatClosest, 16, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "read stats");
+    out->closest_rays = c[0];
+    out->shadow_rays = c[1];
+  }
+  out->last_trace_ms = r->last_ms;
+  for (int k = 0; k < kPhases; k++) out->phase_ms[k] = r->phase_ms[k];
+  if (r->ctr.ptr) {
+    cudaError_t e = cudaMemcpy(out->traversal, (uint32_t*)r->ctr.ptr + kCtrTrav, 40, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "read traversal counters");
+  }
+  return LUCENT_OK;
+}
+
+}  // extern "C"

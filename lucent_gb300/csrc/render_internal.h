@@ -1,0 +1,87 @@
+// Device-side state of the wavefront renderer, shared by its kernels and the C ABI.
+#pragma once
+#include <cuda_fp16.h>
+
+#include "shade.cuh"
+
+namespace lucent {
+
+// Counter words (uint32) in Paths::ctr.
+enum : int {
+  kCtrQ0 = 0,           // active-queue lengths [0], [1]
+  kCtrShadow = 2,       // shadow-queue length
+  kCtrWork = 3,         // closest-hit persistent ray counter
+  kCtrSlow = 4,         // closest-hit slow-path queue length
+  kCtrWork2 = 5,        // any-hit work counter (unused by the grid-stride kernel)
+  kCtrSlow2 = 6,        // any-hit slow-path queue length
+  kCtrErr = 7,          // device error word
+  kCtrStatClosest = 8,  // u64: closest-hit rays traced (words 8-9)
+  kCtrStatShadow = 10,  // u64: shadow rays traced (words 10-11)
+  kCtrTrav = 16,        // 5 x u64 closest-hit traversal counters (words 16-25), profiling only
+  kCtrWords = 32,
+};
+
+struct __align__(8) half4 {
+  __half x, y, z, w;
+};
+__device__ __forceinline__ half4 make_half4(float4 v) {
+  half4 h;
+  h.x = __float2half_rn(v.x);
+  h.y = __float2half_rn(v.y);
+  h.z = __float2half_rn(v.z);
+  h.w = __float2half_rn(v.w);
+  return h;
+}
+
+// Structure-of-arrays path state; shadow slots are 3 per path (sun, env, light).
+struct Paths {
+  float4 *ro, *rd, *thr, *rad, *tint, *galb, *gnrm, *hit;
+  float4 *sh_o, *sh_d, *sh_c;
+  uint32_t* rng;
+  uint8_t* sh_occ;
+  uint32_t* q[2];
+  uint32_t* qs;
+  uint32_t* slow;
+  uint32_t* slow2;
+  uint32_t* ctr;
+};
+
+// Accumulation targets (renderer.ts:490): RGBA32F colour + lum^2, RGBA16F
+// albedo + coverage, RGBA16F normal + depth, R32F history.
+struct AccumDev {
+  float4* color;
+  half4* albedo;
+  half4* normal;
+  float* history;
+};
+
+struct RenderLaunch {
+  Paths paths;
+  sh::SceneDev scene;
+  sh::LightingDev light;
+  sh::CameraDev cam;
+  AccumDev accum;
+  int W, H, S, max_bounces;
+  uint32_t seed0;
+  float clamp;
+  unsigned long long* trav_stats;  // closest-hit traversal counters or nullptr
+};
+
+// Optional per-phase timing: events recorded between launches, each tagged
+// with the phase of the interval that ends at it.
+enum Phase : int { kPhCamera = 0, kPhClosest, kPhShade, kPhShadow, kPhResolve, kPhAccumulate, kPhases };
+struct PhaseEvents {
+  cudaEvent_t* ev;  // pool
+  int* tag;         // phase of the interval ending at ev[i]
+  int cap, n;
+  void mark(int phase, cudaStream_t s) {
+    if (ev && n < cap) {
+      cudaEventRecord(ev[n], s);
+      tag[n++] = phase;
+    }
+  }
+};
+
+void render_batch(const RenderLaunch& R, cudaStream_t s, PhaseEvents* pe);
+
+}  // namespace lucent

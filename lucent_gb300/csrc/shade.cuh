@@ -1,0 +1,538 @@
+// Device shading for the wavefront path tracer: the reference's surface,
+// light and BSDF model (src/shaders/common.glsl, lights.glsl, bsdf.glsl,
+// trace.frag) on packed device buffers. Binary32 throughout, like the GLSL.
+#pragma once
+#include <cuda_fp16.h>
+
+#include "common.cuh"
+
+namespace lucent {
+namespace sh {
+
+constexpr float PI = 3.14159265358979323846f;
+constexpr float INV_PI = 0.31830988618379067154f;
+constexpr float TWO_PI = 6.28318530717958647692f;
+constexpr float INF = 1e30f;
+constexpr float EPS = 1e-6f;
+
+// ------------------------------------------------------------ float3 helpers
+LUCENT_DEV float3 f3(float a, float b, float c) { return make_float3(a, b, c); }
+LUCENT_DEV float3 f3(float4 v) { return make_float3(v.x, v.y, v.z); }
+LUCENT_DEV float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+LUCENT_DEV float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+LUCENT_DEV float3 operator-(float3 a) { return f3(-a.x, -a.y, -a.z); }
+LUCENT_DEV float3 operator*(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+LUCENT_DEV float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+LUCENT_DEV float3 operator*(float s, float3 a) { return f3(s * a.x, s * a.y, s * a.z); }
+LUCENT_DEV float3 operator/(float3 a, float s) { return f3(a.x / s, a.y / s, a.z / s); }
+LUCENT_DEV float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+LUCENT_DEV float3 cross3(float3 a, float3 b) {
+  return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+LUCENT_DEV float len3(float3 a) { return sqrtf(dot3(a, a)); }
+LUCENT_DEV float3 norm3(float3 a) { return a / len3(a); }
+LUCENT_DEV float clampf(float x, float a, float b) { return fminf(fmaxf(x, a), b); }
+LUCENT_DEV float mixf(float x, float y, float a) { return x * (1.f - a) + y * a; }
+LUCENT_DEV float3 mix3(float3 x, float3 y, float a) { return x * (1.f - a) + y * a; }
+LUCENT_DEV float max3(float3 v) { return fmaxf(v.x, fmaxf(v.y, v.z)); }
+LUCENT_DEV float lum(float3 c) { return dot3(c, f3(0.2126f, 0.7152f, 0.0722f)); }
+LUCENT_DEV float3 reflect3(float3 I, float3 N) { return I - 2.f * dot3(N, I) * N; }
+LUCENT_DEV float3 refract3(float3 I, float3 N, float eta) {
+  const float c = dot3(N, I);
+  const float k = 1.f - eta * eta * (1.f - c * c);
+  if (k < 0.f) return f3(0.f, 0.f, 0.f);
+  return eta * I - (eta * c + sqrtf(k)) * N;
+}
+LUCENT_DEV float smooth(float e0, float e1, float x) {
+  const float t = clampf((x - e0) / (e1 - e0), 0.f, 1.f);
+  return t * t * (3.f - 2.f * t);
+}
+
+// ------------------------------------------------------------ RNG (common.glsl:13-25)
+LUCENT_DEV uint32_t pcg(uint32_t& state) {
+  const uint32_t s = state;
+  state = s * 747796405u + 2891336453u;
+  const uint32_t word = ((s >> ((s >> 28u) + 4u)) ^ s) * 277803737u;
+  return (word >> 22u) ^ word;
+}
+LUCENT_DEV float rnd(uint32_t& st) { return (float)pcg(st) * (1.0f / 4294967296.0f); }
+// Alpha any-hit uniform from (path RNG state, slot): the path's own stream is
+// never drawn inside a traversal.
+LUCENT_DEV float alpha_rand(uint32_t key, uint32_t slot) {
+  uint32_t s = key ^ (slot * 0x9E3779B9u);
+  return (float)pcg(s) * (1.0f / 4294967296.0f);
+}
+
+// ------------------------------------------------------------ sampling helpers (common.glsl)
+LUCENT_DEV void basis(float3 n, float3& t, float3& b) {
+  const float s = n.z >= 0.f ? 1.f : -1.f;
+  const float a = -1.f / (s + n.z);
+  const float c = n.x * n.y * a;
+  t = f3(1.f + s * n.x * n.x * a, s * c, -s * n.x);
+  b = f3(c, s + n.y * n.y * a, -n.y);
+}
+LUCENT_DEV float3 to_world(float3 v, float3 t, float3 b, float3 n) { return t * v.x + b * v.y + n * v.z; }
+LUCENT_DEV float3 to_local(float3 v, float3 t, float3 b, float3 n) { return f3(dot3(v, t), dot3(v, b), dot3(v, n)); }
+LUCENT_DEV float3 cosine_hemisphere(float u0, float u1) {
+  const float r = sqrtf(u0), phi = TWO_PI * u1;
+  float sp, cp;
+  sincosf(phi, &sp, &cp);
+  return f3(r * cp, r * sp, sqrtf(fmaxf(0.f, 1.f - u0)));
+}
+LUCENT_DEV float3 uniform_cone(float u0, float u1, float cos_max) {
+  const float ct = 1.f - u0 * (1.f - cos_max);
+  const float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
+  float sp, cp;
+  sincosf(TWO_PI * u1, &sp, &cp);
+  return f3(st * cp, st * sp, ct);
+}
+LUCENT_DEV float2 concentric_disk(float u0, float u1) {
+  const float ox = 2.f * u0 - 1.f, oy = 2.f * u1 - 1.f;
+  if (ox == 0.f && oy == 0.f) return make_float2(0.f, 0.f);
+  float r, th;
+  if (fabsf(ox) > fabsf(oy)) {
+    r = ox;
+    th = (PI / 4.f) * (oy / ox);
+  } else {
+    r = oy;
+    th = (PI / 2.f) - (PI / 4.f) * (ox / oy);
+  }
+  float s, c;
+  sincosf(th, &s, &c);
+  return make_float2(r * c, r * s);
+}
+LUCENT_DEV float mis(float a, float b) {
+  const float a2 = a * a, b2 = b * b;
+  return a2 / fmaxf(a2 + b2, 1e-10f);
+}
+// Wachter-Binder offset (common.glsl:95-108): integer ULP nudge along n.
+LUCENT_DEV float3 offset_ray(float3 p, float3 n) {
+  const int ox = (int)(256.f * n.x), oy = (int)(256.f * n.y), oz = (int)(256.f * n.z);
+  const float px = __int_as_float(__float_as_int(p.x) + (p.x < 0.f ? -ox : ox));
+  const float py = __int_as_float(__float_as_int(p.y) + (p.y < 0.f ? -oy : oy));
+  const float pz = __int_as_float(__float_as_int(p.z) + (p.z < 0.f ? -oz : oz));
+  const float o = 1.f / 32.f, fs = 1.f / 65536.f;
+  return f3(fabsf(p.x) < o ? p.x + fs * n.x : px, fabsf(p.y) < o ? p.y + fs * n.y : py,
+            fabsf(p.z) < o ? p.z + fs * n.z : pz);
+}
+
+// ------------------------------------------------------------ device scene
+struct SceneDev {
+  const Node* nodes;
+  uint32_t node_count;
+  const float4* geo;        // 3 per slot: (v0, material), (v1, light), (v2, alpha flag)
+  const float4* attr;       // 4 per slot: (n0, u0), (n1, u1), (n2, u2), (v0, v1, v2, 0)
+  const float4* materials;  // 10 per material (material.ts:121-131)
+  const float4* spheres;
+  const int* sphere_materials;
+  const int* sphere_lights;
+  int sphere_count;
+  const float4* lights;     // 4 per light (scene.ts:88-95)
+  int light_count;
+  int ground_material;      // -1: no ground plane
+  float ground_height;
+  int any_alpha;
+};
+
+struct LightingDev {
+  int sun_enabled;
+  float3 sun_dir, sun_radiance;
+  float sun_cos, sun_pdf;
+  const float* env_rgb;  // equirect RGB f32, rows top to bottom
+  int env_w, env_h;
+  const float4* env_alias;  // per cell: keep probability, alias, pdfUV, alias pdfUV
+  int grid_w, grid_h;
+  float env_cos, env_sin, env_intensity;
+  int env_sampling, env_background;
+  float3 backdrop;
+  const float* sheen_lut;  // 16 x 16, values already rounded to half precision
+};
+
+struct CameraDev {
+  float3 pos, right, up, forward;
+  float tan_half_fov, aperture, focus;
+};
+
+// Software GL LINEAR sample (the reference samples these with hardware
+// bilinear filtering): u wraps (REPEAT) or clamps, v clamps.
+LUCENT_DEV void bilinear(const float* img, int w, int h, int ch, float u, float v, bool repeat_s, float* out) {
+  const float x = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
+  const float fx = floorf(x), fy = floorf(y);
+  const float ax = x - fx, ay = y - fy;
+  int x0 = (int)fx, y0 = (int)fy, x1 = x0 + 1, y1 = y0 + 1;
+  if (repeat_s) {
+    x0 %= w;
+    x0 = x0 < 0 ? x0 + w : x0;
+    x1 %= w;
+    x1 = x1 < 0 ? x1 + w : x1;
+  } else {
+    x0 = min(max(x0, 0), w - 1);
+    x1 = min(max(x1, 0), w - 1);
+  }
+  y0 = min(max(y0, 0), h - 1);
+  y1 = min(max(y1, 0), h - 1);
+  for (int c = 0; c < ch; c++) {
+    const float a = __ldg(img + ((size_t)y0 * w + x0) * ch + c), b = __ldg(img + ((size_t)y0 * w + x1) * ch + c);
+    const float cc = __ldg(img + ((size_t)y1 * w + x0) * ch + c), d = __ldg(img + ((size_t)y1 * w + x1) * ch + c);
+    const float top = a * (1.f - ax) + b * ax, bot = cc * (1.f - ax) + d * ax;
+    out[c] = top * (1.f - ay) + bot * ay;
+  }
+}
+
+// ------------------------------------------------------------ lights.glsl
+LUCENT_DEV float3 env_to_local(const LightingDev& L, float3 d) {
+  return f3(L.env_cos * d.x - L.env_sin * d.z, d.y, L.env_sin * d.x + L.env_cos * d.z);
+}
+LUCENT_DEV float3 env_to_world(const LightingDev& L, float3 l) {
+  return f3(L.env_cos * l.x + L.env_sin * l.z, l.y, -L.env_sin * l.x + L.env_cos * l.z);
+}
+LUCENT_DEV float2 equirect_uv(float3 l) {
+  return make_float2(atan2f(l.z, l.x) * (0.5f * INV_PI) + 0.5f, acosf(clampf(l.y, -1.f, 1.f)) * INV_PI);
+}
+LUCENT_DEV float3 env_tex(const LightingDev& L, float2 uv) {
+  float o[3];
+  bilinear(L.env_rgb, L.env_w, L.env_h, 3, uv.x, uv.y, true, o);
+  return f3(o[0], o[1], o[2]);
+}
+LUCENT_DEV float3 env_radiance(const LightingDev& L, float3 d) {
+  return env_tex(L, equirect_uv(env_to_local(L, d))) * L.env_intensity;
+}
+LUCENT_DEV float env_pdf(const LightingDev& L, float3 d) {
+  const float3 l = env_to_local(L, d);
+  const float st = sqrtf(fmaxf(0.f, 1.f - l.y * l.y));
+  if (st < 1e-6f) return 0.f;
+  const float2 uv = equirect_uv(l);
+  const int cx = min((int)(uv.x * (float)L.grid_w), L.grid_w - 1);
+  const int cy = min((int)(uv.y * (float)L.grid_h), L.grid_h - 1);
+  return __ldg(&L.env_alias[(size_t)cy * L.grid_w + cx].z) / (2.f * PI * PI * st);
+}
+
+struct LightSample {
+  float3 dir;
+  float dist, pdf;
+  float3 radiance;
+};
+
+LUCENT_DEV LightSample sample_environment(const LightingDev& L, uint32_t& rng) {
+  LightSample ls;
+  const int n = L.grid_w * L.grid_h;
+  const int i = min((int)(rnd(rng) * (float)n), n - 1);
+  const float4 e = __ldg(&L.env_alias[i]);
+  int cell = i;
+  float pdfUV = e.z;
+  if (rnd(rng) >= e.x) {
+    cell = (int)e.y;
+    pdfUV = e.w;
+  }
+  const float j0 = rnd(rng), j1 = rnd(rng);
+  const float u = ((float)(cell % L.grid_w) + j0) / (float)L.grid_w;
+  const float v = ((float)(cell / L.grid_w) + j1) / (float)L.grid_h;
+  const float phi = (u - 0.5f) * TWO_PI, theta = v * PI;
+  float st, ct, sp, cp;
+  sincosf(theta, &st, &ct);
+  sincosf(phi, &sp, &cp);
+  ls.dir = env_to_world(L, f3(st * cp, ct, st * sp));
+  ls.dist = INF;
+  ls.pdf = st > 1e-6f ? pdfUV / (2.f * PI * PI * st) : 0.f;
+  ls.radiance = env_tex(L, make_float2(u, v)) * L.env_intensity;
+  return ls;
+}
+
+LUCENT_DEV float3 environment(const LightingDev& L, float3 d, bool specular, float bsdf_pdf) {
+  float3 r = env_radiance(L, d);
+  if (!specular && L.env_sampling) r = r * mis(bsdf_pdf, env_pdf(L, d));
+  if (L.sun_enabled && dot3(d, L.sun_dir) >= L.sun_cos) {
+    const float w = specular ? 1.f : mis(bsdf_pdf, L.sun_pdf);
+    r = r + L.sun_radiance * w;
+  }
+  return r;
+}
+
+LUCENT_DEV float hit_sphere(float3 ro, float3 rd, float4 s, float tmax) {  // scene.glsl:132-144
+  const float3 oc = ro - f3(s);
+  const float b = dot3(oc, rd);
+  const float c = dot3(oc, oc) - s.w * s.w;
+  const float disc = b * b - c;
+  if (disc < 0.f) return INF;
+  const float sq = sqrtf(disc);
+  float t = -b - sq;
+  if (t > EPS && t < tmax) return t;
+  t = -b + sq;
+  if (t > EPS && t < tmax) return t;
+  return INF;
+}
+
+LUCENT_DEV float hit_ground(const SceneDev& S, float3 ro, float3 rd, float tmax) {  // scene.glsl:146-150
+  if (S.ground_material < 0 || fabsf(rd.y) < 1e-9f) return INF;
+  const float t = (S.ground_height - ro.y) / rd.y;
+  return t > EPS && t < tmax ? t : INF;
+}
+
+LUCENT_DEV LightSample sample_light(const SceneDev& S, int index, float3 p, float u0, float u1) {  // :99-138
+  LightSample ls;
+  ls.pdf = 0.f;
+  ls.dir = f3(0.f, 0.f, 0.f);
+  ls.dist = 0.f;
+  const float4 l0 = __ldg(S.lights + index * 4), l1 = __ldg(S.lights + index * 4 + 1),
+               l2 = __ldg(S.lights + index * 4 + 2), l3 = __ldg(S.lights + index * 4 + 3);
+  ls.radiance = f3(l3);
+  if (l0.w < 0.5f) {
+    const float3 toC = f3(l0) - p;
+    const float d2 = dot3(toC, toC);
+    const float r = l1.w;
+    if (d2 <= r * r) return ls;
+    const float cos_max = sqrtf(fmaxf(0.f, 1.f - r * r / d2));
+    const float3 axis = toC * rsqrtf(d2);
+    float3 t, b;
+    basis(axis, t, b);
+    ls.dir = to_world(uniform_cone(u0, u1, cos_max), t, b, axis);
+    ls.pdf = 1.f / (TWO_PI * (1.f - cos_max));
+    const float t0 = hit_sphere(p, ls.dir, make_float4(l0.x, l0.y, l0.z, r), INF);
+    ls.dist = t0 < INF ? t0 : sqrtf(d2);
+  } else {
+    const float3 e1 = f3(l1), e2 = f3(l2);
+    const float3 q = f3(l0) + e1 * u0 + e2 * u1;
+    const float3 toQ = q - p;
+    const float d2 = dot3(toQ, toQ);
+    const float d = sqrtf(d2);
+    ls.dir = toQ / d;
+    ls.dist = d;
+    const float3 nc = cross3(e1, e2);
+    const float area = len3(nc);
+    const float cosL = fabsf(dot3(nc / area, ls.dir));
+    if (cosL < 1e-4f) return ls;
+    ls.pdf = d2 / (cosL * area);
+  }
+  return ls;
+}
+
+LUCENT_DEV float light_pdf(const SceneDev& S, int index, float3 p, float3 dir, float dist) {  // :141-158
+  const float4 l0 = __ldg(S.lights + index * 4), l1 = __ldg(S.lights + index * 4 + 1),
+               l2 = __ldg(S.lights + index * 4 + 2);
+  if (l0.w < 0.5f) {
+    const float3 toC = f3(l0) - p;
+    const float d2 = dot3(toC, toC);
+    const float r = l1.w;
+    if (d2 <= r * r) return 0.f;
+    const float cos_max = sqrtf(fmaxf(0.f, 1.f - r * r / d2));
+    return 1.f / (TWO_PI * (1.f - cos_max));
+  }
+  const float3 nc = cross3(f3(l1), f3(l2));
+  const float area = len3(nc);
+  const float cosL = fabsf(dot3(nc / area, dir));
+  if (cosL < 1e-4f) return 0.f;
+  return dist * dist / (cosL * area);
+}
+
+// ------------------------------------------------------------ bsdf.glsl
+struct Surface {
+  float3 albedo;
+  float metallic, roughness, ior, transmission;
+  float clearcoat, clearcoat_roughness;
+  float3 sheen_color;
+  float sheen_roughness;
+  bool thin;
+  float3 absorption, n, nc;
+};
+
+LUCENT_DEV float d_ggx(float NdotH, float a) {
+  const float a2 = a * a;
+  const float d = NdotH * NdotH * (a2 - 1.f) + 1.f;
+  return a2 / (PI * d * d);
+}
+LUCENT_DEV float g1_ggx(float NdotX, float a) {
+  const float a2 = a * a;
+  return 2.f * NdotX / (NdotX + sqrtf(a2 + (1.f - a2) * NdotX * NdotX));
+}
+LUCENT_DEV float schlick_w(float c) {
+  const float m = 1.f - clampf(c, 0.f, 1.f);
+  const float m2 = m * m;
+  return m2 * m2 * m;  // pow(m, 5) for m in [0, 1]
+}
+LUCENT_DEV float3 fresnel3(float c, float3 F0) { return F0 + (f3(1.f, 1.f, 1.f) - F0) * schlick_w(c); }
+LUCENT_DEV float fresnel1(float c, float F0) { return F0 + (1.f - F0) * schlick_w(c); }
+LUCENT_DEV float dielectric_f0(float ior) {
+  const float r = (ior - 1.f) / (ior + 1.f);
+  return r * r;
+}
+LUCENT_DEV float alpha_of(float r) { return fmaxf(r * r, 1e-3f); }
+
+LUCENT_DEV float3 sample_vndf(float3 Ve, float a, float u0, float u1) {  // Heitz 2018 (bsdf.glsl:59-72)
+  const float3 Vh = norm3(f3(a * Ve.x, a * Ve.y, Ve.z));
+  const float lensq = Vh.x * Vh.x + Vh.y * Vh.y;
+  const float3 T1 = lensq > 0.f ? f3(-Vh.y, Vh.x, 0.f) * rsqrtf(lensq) : f3(1.f, 0.f, 0.f);
+  const float3 T2 = cross3(Vh, T1);
+  const float r = sqrtf(u0);
+  float sp, cp;
+  sincosf(TWO_PI * u1, &sp, &cp);
+  const float t1 = r * cp;
+  float t2 = r * sp;
+  const float s = 0.5f * (1.f + Vh.z);
+  t2 = (1.f - s) * sqrtf(fmaxf(0.f, 1.f - t1 * t1)) + s * t2;
+  const float3 Nh = t1 * T1 + t2 * T2 + sqrtf(fmaxf(0.f, 1.f - t1 * t1 - t2 * t2)) * Vh;
+  return norm3(f3(a * Nh.x, a * Nh.y, fmaxf(0.f, Nh.z)));
+}
+
+// Charlie sheen D (bsdf.glsl:79-83): (2 + 1/a) sin^(1/a) / 2pi with
+// sin^2 = 1 - cos^2 evaluated as sin2 = (1 - c)(1 + c) to keep precision for
+// exponents up to ~204.
+LUCENT_DEV float d_charlie(float alpha, float NdotH) {
+  const float inv = 1.f / alpha;
+  const float sin2 = fmaxf((1.f - NdotH) * (1.f + NdotH), 0.f);
+  return (2.f + inv) * powf(sin2, inv * 0.5f) / TWO_PI;
+}
+LUCENT_DEV float v_neubelt(float NdotL, float NdotV) { return 1.f / (4.f * (NdotL + NdotV - NdotL * NdotV)); }
+
+LUCENT_DEV float sheen_albedo(const LightingDev& L, float NdotV, float r) {  // LINEAR-filtered 16x16 LUT
+  float o;
+  bilinear(L.sheen_lut, 16, 16, 1, (NdotV * 15.f + 0.5f) / 16.f, (r * 15.f + 0.5f) / 16.f, false, &o);
+  return o;
+}
+LUCENT_DEV float spec_prob(float3 F0, float metallic, float NdotV) {
+  const float f = lum(fresnel3(NdotV, F0));
+  return mixf(clampf(f, 0.1f, 0.9f), 1.f, metallic);
+}
+LUCENT_DEV float coat_prob(const Surface& s, float3 wo) {
+  if (s.clearcoat <= 0.f) return 0.f;
+  const float Fc = s.clearcoat * fresnel1(fmaxf(dot3(s.nc, wo), 0.f), 0.04f);
+  const float base = (1.f - Fc) * fmaxf(lum(s.albedo), 0.04f);
+  return clampf(Fc / (Fc + base), 0.15f, 0.85f);
+}
+LUCENT_DEV float3 base_f0(const Surface& s) {
+  const float d = dielectric_f0(s.ior);
+  return mix3(f3(d, d, d), s.albedo, s.metallic);
+}
+
+// evalOpaque (bsdf.glsl:114-166): f (not cosine-weighted) and the mixture pdf.
+LUCENT_DEV float3 eval_opaque(const LightingDev& L, const Surface& s, float3 wo, float3 wi, float& pdf) {
+  const float3 n = s.n;
+  const float NdotL = dot3(n, wi), NdotV = dot3(n, wo);
+  pdf = 0.f;
+  if (NdotL <= 0.f || NdotV <= 0.f) return f3(0.f, 0.f, 0.f);
+  const float a = alpha_of(s.roughness);
+  const float3 H = norm3(wo + wi);
+  const float NdotH = fmaxf(dot3(n, H), 0.f), VdotH = fmaxf(dot3(wo, H), 0.f);
+  const float3 F0 = base_f0(s);
+  const float3 F = fresnel3(VdotH, F0);
+  const float D = d_ggx(NdotH, a);
+  const float G1v = g1_ggx(NdotV, a);
+  const float G = G1v * g1_ggx(NdotL, a);
+  const float3 spec = (D * G) * F / fmaxf(4.f * NdotV * NdotL, 1e-6f);
+  const float3 diff = (f3(1.f, 1.f, 1.f) - F) * s.albedo * (1.f - s.metallic) * INV_PI;
+  float3 f = diff + spec;
+  const float pspec = spec_prob(F0, s.metallic, NdotV);
+  pdf = mixf(NdotL * INV_PI, G1v * D / fmaxf(4.f * NdotV, 1e-6f), pspec);
+  const float smax = max3(s.sheen_color);
+  if (smax > 0.f) {
+    const float sr = fmaxf(s.sheen_roughness, 0.07f);
+    const float3 sheen = s.sheen_color * d_charlie(sr * sr, NdotH) * v_neubelt(NdotL, NdotV);
+    const float scale = 1.f - smax * fmaxf(sheen_albedo(L, NdotV, sr), sheen_albedo(L, NdotL, sr));
+    f = sheen + f * scale;
+  }
+  const float pcoat = coat_prob(s, wo);
+  if (pcoat > 0.f) {
+    const float cV = dot3(s.nc, wo), cL = dot3(s.nc, wi);
+    float coat = 0.f, pdf_coat = 0.f;
+    if (cV > 0.f && cL > 0.f) {
+      const float ac = alpha_of(s.clearcoat_roughness);
+      const float cH = fmaxf(dot3(s.nc, H), 0.f);
+      const float Dc = d_ggx(cH, ac), G1c = g1_ggx(cV, ac);
+      coat = Dc * G1c * g1_ggx(cL, ac) * fresnel1(VdotH, 0.04f) / (4.f * cV * cL);
+      pdf_coat = G1c * Dc / (4.f * cV);
+    }
+    const float Fcv = fresnel1(fmaxf(cV, 0.f), 0.04f);
+    f = f * (1.f - s.clearcoat * Fcv) + f3(coat, coat, coat) * s.clearcoat;
+    pdf = mixf(pdf, pdf_coat, pcoat);
+  }
+  return f;
+}
+
+struct BsdfSample {
+  float3 dir, weight;
+  float pdf;
+};
+
+// sampleOpaque (bsdf.glsl:174-211); `U` draws the uniforms in the GLSL order.
+template <class UF>
+LUCENT_DEV BsdfSample sample_opaque(const LightingDev& L, const Surface& s, float3 wo, UF&& U) {
+  BsdfSample bs;
+  bs.pdf = 0.f;
+  bs.weight = f3(0.f, 0.f, 0.f);
+  bs.dir = f3(0.f, 0.f, 0.f);
+  float3 wi;
+  const float uc = U();
+  if (uc < coat_prob(s, wo)) {
+    float3 t, b;
+    basis(s.nc, t, b);
+    const float3 woL = to_local(wo, t, b, s.nc);
+    if (woL.z <= 0.f) return bs;
+    const float a0 = U(), a1 = U();
+    const float3 H = sample_vndf(woL, alpha_of(s.clearcoat_roughness), a0, a1);
+    wi = to_world(reflect3(-woL, H), t, b, s.nc);
+  } else {
+    float3 t, b;
+    basis(s.n, t, b);
+    const float3 woL = to_local(wo, t, b, s.n);
+    if (woL.z <= 0.f) return bs;
+    float3 wiL;
+    const float us = U();
+    if (us < spec_prob(base_f0(s), s.metallic, woL.z)) {
+      const float a0 = U(), a1 = U();
+      wiL = reflect3(-woL, sample_vndf(woL, alpha_of(s.roughness), a0, a1));
+    } else {
+      const float a0 = U(), a1 = U();
+      wiL = cosine_hemisphere(a0, a1);
+    }
+    wi = to_world(wiL, t, b, s.n);
+  }
+  const float NdotL = dot3(s.n, wi);
+  if (NdotL <= 0.f) return bs;
+  float pdf;
+  const float3 f = eval_opaque(L, s, wo, wi, pdf);
+  if (pdf <= 0.f) return bs;
+  bs.dir = wi;
+  bs.pdf = pdf;
+  bs.weight = f * NdotL / pdf;
+  return bs;
+}
+
+// sampleDielectric (bsdf.glsl:216-248).
+template <class UF>
+LUCENT_DEV bool sample_dielectric(const Surface& s, bool front, float3 ng, float3 wo, float3& wi, float3& weight,
+                                  bool& reflected, UF&& U) {
+  const float3 n = s.n;
+  float3 t, b;
+  basis(n, t, b);
+  const float3 woL = to_local(wo, t, b, n);
+  if (woL.z <= 0.f) return false;
+  float3 H = n;
+  if (s.roughness > 0.f) {
+    const float a0 = U(), a1 = U();
+    H = to_world(sample_vndf(woL, alpha_of(s.roughness), a0, a1), t, b, n);
+  }
+  float cosI = dot3(wo, H);
+  if (cosI <= 0.f) {
+    H = n;
+    cosI = woL.z;
+  }
+  const float eta = front ? 1.f / s.ior : s.ior;
+  const float sin2T = eta * eta * (1.f - cosI * cosI);
+  float Fr = fresnel1(cosI, dielectric_f0(s.ior));
+  if (s.thin)
+    Fr = 2.f * Fr / (1.f + Fr);
+  else if (sin2T > 1.f)
+    Fr = 1.f;
+  if (U() < Fr) {
+    wi = reflect3(-wo, H);
+    weight = f3(1.f, 1.f, 1.f);
+    reflected = true;
+    return dot3(wi, ng) > 0.f;
+  }
+  wi = s.thin ? -wo : refract3(-wo, H, eta);
+  weight = s.albedo;
+  reflected = false;
+  return dot3(wi, ng) < 0.f;
+}
+
+}  // namespace sh
+}  // namespace lucent

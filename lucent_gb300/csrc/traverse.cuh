@@ -1,0 +1,438 @@
+// Traversal kernels shared by the BVH API and the renderer, templated on a
+// policy that supplies rays and consumes hits.
+//
+// Closest hit reproduces the reference's CPU intersector, intersectBVH
+// (src/math/bvh.ts:265-320): its traversal order (explicit stack, left child
+// first, a node's box tested against the running closest distance `c` when it
+// is popped) and its binary64 decisions. Each decision is first tried with
+// binary32 arithmetic whose error is bounded (closest_hit.cuh); binary64 runs
+// only when the bound cannot decide, and once for the final hit.
+//
+// Any hit (shadow rays) answers: does some triangle pass the reference's
+// binary64 Moller-Trumbore in (tMin, tMax) inside boxes its slab test at tMax
+// accepts? With `c` fixed at tMax the answer does not depend on visiting order.
+//
+// Policies:
+//   uint32_t count() const                        rays in this launch
+//   void ray(uint32_t k, float3& o, float3& d)   k-th ray
+//   uint32_t key(uint32_t k) const                alpha any-hit key (RNG state)
+//   bool alpha(int slot, uint32_t key) const      true if a hit on `slot` counts
+//   bool alpha_any() const                        false: no alpha-tested triangles
+//   void hit(uint32_t k, int slot, double t, double u, double v)   (closest)
+//   void miss(uint32_t k); void fail(uint32_t k)
+//   void shadow(uint32_t k, bool occluded)        (any hit)
+#pragma once
+#include "closest_hit.cuh"
+
+namespace lucent {
+
+__device__ __forceinline__ Node load_node(const Node* nodes, int n) {
+  const float4* p = reinterpret_cast<const float4*>(nodes) + 2 * (size_t)n;
+  Node r;
+  r.lo = __ldg(p);
+  r.hi = __ldg(p + 1);
+  return r;
+}
+
+__device__ __forceinline__ D3 inv_exact(float3 d) {
+  return {ddiv(1.0, (double)d.x), ddiv(1.0, (double)d.y), ddiv(1.0, (double)d.z)};
+}
+
+struct TravArgs {
+  const Node* nodes;
+  uint32_t node_limit;
+  const float4* tris;  // 3 float4 per slot, vertices in xyz
+  double tMin, tMax;
+  uint32_t* queue;     // rays outside the bounded-error range (slow path)
+  uint32_t* queue_len;
+  uint32_t* work;      // persistent-kernel ray counter (zeroed before launch)
+  unsigned* err;
+  // Optional counters (nullptr = off): rays, binary64 slab decisions,
+  // binary64 triangle decisions, binary64 closest values, binary64 final hits.
+  unsigned long long* stats = nullptr;
+};
+
+__device__ __forceinline__ void count_stat(const TravArgs& A, int k) {
+  if (A.stats) atomicAdd(A.stats + k, 1ull);
+}
+
+struct PendingNode {
+  int node;
+  float ehi;
+};
+
+// Entire reference algorithm in binary64 for one ray (slow path, f64 rays).
+// Returns false if the traversal was aborted (error word set).
+template <class Pol>
+__device__ bool trace_exact(const TravArgs& A, const Pol& P, D3 o, D3 d, uint32_t key, int& slot, double& t_out,
+                            double& u_out, double& v_out) {
+  const D3 inv = {ddiv(1.0, d.x), ddiv(1.0, d.y), ddiv(1.0, d.z)};
+  int stack[kTsStack];
+  int sp = 0;
+  stack[sp++] = 0;
+  double closest = A.tMax;
+  slot = -1;
+  uint32_t iters = 0;
+  while (sp > 0) {
+    if (++iters > A.node_limit) {
+      atomicOr(A.err, kErrIterations);
+      return false;
+    }
+    const int n = stack[--sp];
+    const Node nd = load_node(A.nodes, n);
+    if (ts_slab_culled(nd.lo, nd.hi, o, inv, closest)) continue;
+    const int cnt = node_count(nd), first = node_first(nd);
+    if (cnt > 0) {
+      for (int k = 0; k < cnt; k++) {
+        const int s = first + k;
+        const float4 a = __ldg(A.tris + 3 * (size_t)s), b = __ldg(A.tris + 3 * (size_t)s + 1),
+                     c = __ldg(A.tris + 3 * (size_t)s + 2);
+        double t, u, v;
+        if (ts_triangle(o, d, d3f(a), d3f(b), d3f(c), A.tMin, closest, t, u, v) && P.alpha(s, key)) {
+          closest = t;
+          slot = s;
+          t_out = t;
+          u_out = u;
+          v_out = v;
+        }
+      }
+    } else {
+      if (sp + 2 > kTsStack) {
+        atomicOr(A.err, kErrStack);
+        return false;
+      }
+      stack[sp++] = first + 1;
+      stack[sp++] = first;
+    }
+  }
+  return true;
+}
+
+template <class Pol>
+__global__ void k_closest_exact_t(TravArgs A, Pol P) {
+  const uint32_t limit = A.queue ? *A.queue_len : P.count();
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < limit; q += gridDim.x * blockDim.x) {
+    const uint32_t k = A.queue ? A.queue[q] : q;
+    float3 o, d;
+    P.ray(k, o, d);
+    int slot;
+    double t = 0, u = 0, v = 0;
+    if (!trace_exact(A, P, {o.x, o.y, o.z}, {d.x, d.y, d.z}, P.key(k), slot, t, u, v))
+      P.fail(k);
+    else if (slot < 0)
+      P.miss(k);
+    else
+      P.hit(k, slot, t, u, v);
+  }
+}
+
+// Fast path: persistent warps, one ray per lane; lanes refill from A.work as
+// their rays finish. Both children of an inner node are tested with the
+// current `c` (what the reference tests when it pops the left child, and the
+// right one if the left is culled); a right child that passes is pushed with
+// an upper bound on its entry distance and re-tested on pop only if `c` has
+// dropped below it (the cull test is monotone in `c`). `c` is carried as
+// binary32 bounds [c_lo, c_hi] of the reference's binary64 value.
+template <class Pol>
+__global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const float tmin_lo = __double2float_rd(A.tMin), tmin_hi = __double2float_ru(A.tMin);
+  const float cmax_lo = __double2float_rd(A.tMax), cmax_hi = __double2float_ru(A.tMax);
+  const double INF64 = __longlong_as_double(0x7ff0000000000000ll);
+  const uint32_t n = P.count();
+  const bool use_alpha = P.alpha_any();
+
+  bool active = false, exhausted = false, have_cur = false, c_exact = true, best_exact = false;
+  uint32_t ri = 0, iters = 0, key = 0;
+  Ray32 r;
+  float c_lo = 0.f, c_hi = 0.f;
+  double c64 = A.tMax, bu64 = 0, bv64 = 0;  // binary64 (t, u, v) of `best` when best_exact
+  float3 best_est = make_float3(0.f, 0.f, 0.f);  // binary32 (t, u, v) of a certainly accepted `best`
+  int best = -1, sp = 0;
+  Node cur;
+  PendingNode stack[kTsStack];
+
+  while (true) {
+    const bool need = !active && !exhausted;
+    const unsigned m = __ballot_sync(FULL, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(A.work, (uint32_t)__popc(m));
+      base = __shfl_sync(FULL, base, leader);
+      if (need) {
+        ri = base + __popc(m & lt);
+        if (ri >= n) {
+          exhausted = true;
+        } else {
+          float3 o, d;
+          P.ray(ri, o, d);
+          if (!safe_ray(o, d)) {
+            A.queue[atomicAdd(A.queue_len, 1u)] = ri;
+          } else {
+            r = make_ray32(o, d);
+            key = P.key(ri);
+            c_lo = cmax_lo;
+            c_hi = cmax_hi;
+            c64 = A.tMax;
+            c_exact = true;
+            best_exact = false;
+            best = -1;
+            sp = 0;
+            iters = 0;
+            count_stat(A, 0);
+            cur = load_node(A.nodes, 0);  // the reference pops the root first and tests its box
+            SlabClass cl = classify_slab(r, cur.lo, cur.hi, c_lo, c_hi);
+            if (cl == kAmbiguous) {
+              count_stat(A, 1);
+              cl = ts_slab_culled(cur.lo, cur.hi, {o.x, o.y, o.z}, inv_exact(d), c64) ? kCulled : kPass;
+            }
+            have_cur = cl != kCulled;
+            active = true;
+          }
+        }
+      }
+    }
+    if (__all_sync(FULL, exhausted)) break;
+    if (!active) continue;
+
+    auto exact_c = [&]() {  // the reference's binary64 `closest`, on demand
+      if (!c_exact) {
+        count_stat(A, 3);
+        const float4 a = __ldg(A.tris + 3 * (size_t)best), b = __ldg(A.tris + 3 * (size_t)best + 1),
+                     c = __ldg(A.tris + 3 * (size_t)best + 2);
+        double t, u, v;
+        ts_triangle({r.o.x, r.o.y, r.o.z}, {r.d.x, r.d.y, r.d.z}, d3f(a), d3f(b), d3f(c), A.tMin, INF64, t, u, v);
+        c64 = t;
+        bu64 = u;
+        bv64 = v;
+        c_exact = true;
+        best_exact = true;
+        c_lo = __double2float_rd(t);
+        c_hi = __double2float_ru(t);
+      }
+      return c64;
+    };
+    auto slab_decide = [&](const Node& nd, SlabClass cl) {
+      if (cl != kAmbiguous) return cl;
+      count_stat(A, 1);
+      return ts_slab_culled(nd.lo, nd.hi, {r.o.x, r.o.y, r.o.z}, inv_exact(r.d), exact_c()) ? kCulled : kPass;
+    };
+
+    if (!have_cur) {
+      if (sp == 0) {  // finished
+        if (best < 0) {
+          P.miss(ri);
+        } else if (best_exact) {
+          P.hit(ri, best, c64, bu64, bv64);
+        } else if (P.exact_output()) {  // the reference's binary64 t, u, v
+          count_stat(A, 4);
+          const float4 a = __ldg(A.tris + 3 * (size_t)best), b = __ldg(A.tris + 3 * (size_t)best + 1),
+                       c = __ldg(A.tris + 3 * (size_t)best + 2);
+          double t = 0, u = 0, v = 0;
+          ts_triangle({r.o.x, r.o.y, r.o.z}, {r.d.x, r.d.y, r.d.z}, d3f(a), d3f(b), d3f(c), A.tMin, INF64, t, u, v);
+          P.hit(ri, best, t, u, v);
+        } else {  // same triangle; binary32 t, u, v like the GLSL's own
+          P.hit32(ri, best, best_est);
+        }
+        active = false;
+        continue;
+      }
+      const PendingNode e = stack[--sp];
+      const Node nd = load_node(A.nodes, e.node);
+      if (e.ehi > c_lo && slab_decide(nd, classify_slab(r, nd.lo, nd.hi, c_lo, c_hi)) == kCulled) continue;
+      cur = nd;
+      have_cur = true;
+    }
+    if (++iters > A.node_limit) {  // a valid BVH visits each node at most once per ray
+      atomicOr(A.err, kErrIterations);
+      P.fail(ri);
+      active = false;
+      have_cur = false;
+      continue;
+    }
+    const int cnt = node_count(cur), first = node_first(cur);
+    if (cnt > 0) {
+      for (int k = 0; k < cnt; k++) {
+        const int slot = first + k;
+        const float4 a = __ldg(A.tris + 3 * (size_t)slot), b = __ldg(A.tris + 3 * (size_t)slot + 1),
+                     c = __ldg(A.tris + 3 * (size_t)slot + 2);
+        float tl, th;
+        float3 est;
+        const TriClass tc = mt_classify(r, a, b, c, tmin_lo, tmin_hi, c_lo, c_hi, tl, th, est);
+        if (tc == kTriReject) continue;
+        if (use_alpha && !P.alpha(slot, key)) continue;  // alpha depends on (key, slot) only
+        if (tc == kTriAccept) {
+          best = slot;
+          best_est = est;
+          best_exact = false;
+          c_exact = false;
+          c_lo = tl;
+          c_hi = th;
+          continue;
+        }
+        count_stat(A, 2);
+        double t, u, v;
+        const double cc = exact_c();
+        if (ts_triangle({r.o.x, r.o.y, r.o.z}, {r.d.x, r.d.y, r.d.z}, d3f(a), d3f(b), d3f(c), A.tMin, cc, t, u, v)) {
+          best = slot;
+          c64 = t;
+          bu64 = u;
+          bv64 = v;
+          c_exact = true;
+          best_exact = true;
+          c_lo = __double2float_rd(t);
+          c_hi = __double2float_ru(t);
+        }
+      }
+      have_cur = false;
+    } else {
+      const Node L = load_node(A.nodes, first), R = load_node(A.nodes, first + 1);  // one 64-byte pair
+      float ehl, ehr;
+      const SlabClass cl = slab_decide(L, classify_slab_e(r, L.lo, L.hi, c_lo, c_hi, ehl));
+      const SlabClass cr = slab_decide(R, classify_slab_e(r, R.lo, R.hi, c_lo, c_hi, ehr));
+      if (cl == kPass) {
+        if (cr == kPass) {
+          if (sp >= kTsStack) {  // unreachable for trees shallower than the reference's stack
+            atomicOr(A.err, kErrStack);
+            P.fail(ri);
+            active = false;
+            have_cur = false;
+            continue;
+          }
+          stack[sp++] = {first + 1, ehr};
+        }
+        cur = L;
+      } else if (cr == kPass) {
+        cur = R;
+      } else {
+        have_cur = false;
+      }
+    }
+  }
+}
+
+// Any hit in binary64 (slow path).
+template <class Pol>
+__device__ bool any_exact(const TravArgs& A, const Pol& P, D3 o, D3 d, uint32_t key, double tMax, bool& ok) {
+  const D3 inv = {ddiv(1.0, d.x), ddiv(1.0, d.y), ddiv(1.0, d.z)};
+  int stack[kTsStack];
+  int sp = 0;
+  stack[sp++] = 0;
+  uint32_t iters = 0;
+  ok = true;
+  while (sp > 0) {
+    if (++iters > A.node_limit) {
+      atomicOr(A.err, kErrIterations);
+      ok = false;
+      return false;
+    }
+    const int n = stack[--sp];
+    const Node nd = load_node(A.nodes, n);
+    if (ts_slab_culled(nd.lo, nd.hi, o, inv, tMax)) continue;
+    const int cnt = node_count(nd), first = node_first(nd);
+    if (cnt > 0) {
+      for (int k = 0; k < cnt; k++) {
+        const int s = first + k;
+        const float4 a = __ldg(A.tris + 3 * (size_t)s), b = __ldg(A.tris + 3 * (size_t)s + 1),
+                     c = __ldg(A.tris + 3 * (size_t)s + 2);
+        double t, u, v;
+        if (ts_triangle(o, d, d3f(a), d3f(b), d3f(c), A.tMin, tMax, t, u, v) && P.alpha(s, key)) return true;
+      }
+    } else if (sp + 2 <= kTsStack) {
+      stack[sp++] = first + 1;
+      stack[sp++] = first;
+    } else {
+      atomicOr(A.err, kErrStack);
+      ok = false;
+      return false;
+    }
+  }
+  return false;
+}
+
+// Any-hit rays carry their own tMax: P.tmax(k).
+template <class Pol>
+__global__ void k_anyhit_exact_t(TravArgs A, Pol P) {
+  const uint32_t limit = *A.queue_len;
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < limit; q += gridDim.x * blockDim.x) {
+    const uint32_t k = A.queue[q];
+    float3 o, d;
+    P.ray(k, o, d);
+    bool ok;
+    const bool occ = any_exact(A, P, {o.x, o.y, o.z}, {d.x, d.y, d.z}, P.key(k), P.tmax(k), ok);
+    P.shadow(k, ok ? occ : true);
+  }
+}
+
+// Fast any hit: one ray per thread (grid-stride), depth-first, exits on the
+// first triangle the reference's test certainly (or, in binary64, exactly)
+// accepts. Culling at the fixed tMax.
+template <class Pol>
+__global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
+  const float tmin_lo = __double2float_rd(A.tMin), tmin_hi = __double2float_ru(A.tMin);
+  const uint32_t n = P.count();
+  const bool use_alpha = P.alpha_any();
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    float3 o, d;
+    P.ray(k, o, d);
+    if (!safe_ray(o, d)) {
+      A.queue[atomicAdd(A.queue_len, 1u)] = k;
+      continue;
+    }
+    const Ray32 r = make_ray32(o, d);
+    const uint32_t key = P.key(k);
+    const double tmax = P.tmax(k);
+    const float c_lo = __double2float_rd(tmax), c_hi = __double2float_ru(tmax);
+    int stack[kTsStack];
+    int sp = 0;
+    stack[sp++] = 0;
+    bool occ = false, ok = true;
+    uint32_t iters = 0;
+    while (sp > 0 && !occ) {
+      if (++iters > A.node_limit) {
+        atomicOr(A.err, kErrIterations);
+        ok = false;
+        break;
+      }
+      const Node nd = load_node(A.nodes, stack[--sp]);
+      SlabClass cl = classify_slab(r, nd.lo, nd.hi, c_lo, c_hi);
+      if (cl == kAmbiguous) cl = ts_slab_culled(nd.lo, nd.hi, {o.x, o.y, o.z}, inv_exact(d), tmax) ? kCulled : kPass;
+      if (cl == kCulled) continue;
+      const int cnt = node_count(nd), first = node_first(nd);
+      if (cnt > 0) {
+        for (int q = 0; q < cnt && !occ; q++) {
+          const int slot = first + q;
+          const float4 a = __ldg(A.tris + 3 * (size_t)slot), b = __ldg(A.tris + 3 * (size_t)slot + 1),
+                       c = __ldg(A.tris + 3 * (size_t)slot + 2);
+          float tl, th;
+          float3 est;
+          const TriClass tc = mt_classify(r, a, b, c, tmin_lo, tmin_hi, c_lo, c_hi, tl, th, est);
+          if (tc == kTriReject) continue;
+          if (use_alpha && !P.alpha(slot, key)) continue;
+          if (tc == kTriAccept) {
+            occ = true;
+          } else {
+            double t, u, v;
+            occ = ts_triangle({o.x, o.y, o.z}, {d.x, d.y, d.z}, d3f(a), d3f(b), d3f(c), A.tMin, tmax, t, u, v);
+          }
+        }
+      } else {
+        if (sp + 2 > kTsStack) {
+          atomicOr(A.err, kErrStack);
+          ok = false;
+          break;
+        }
+        stack[sp++] = first + 1;
+        stack[sp++] = first;
+      }
+    }
+    P.shadow(k, ok ? occ : true);
+  }
+}
+
+int persistent_blocks(const void* kernel, int block);
+
+}  // namespace lucent

@@ -1,0 +1,187 @@
+"""Renderer mirroring the reference's Renderer class (src/renderer.ts:171-871).
+
+Same calls and meaning: load_scene, upload_lighting, upload_ground,
+upload_camera, apply_settings, reset, resize, trace_samples, render,
+benchmark, stats, dispose. WebGL state is replaced by device buffers owned by
+a lucent_renderer handle; the canvas is replaced by explicit width/height.
+"""
+import ctypes as C
+import math
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as N
+from . import _native_render as NR
+from . import scene as S
+
+ATROUS_STEPS = [1, 2, 4, 8, 16]  # renderer.ts:140
+PHASES = ("camera", "closest", "shade", "shadow", "resolve", "accumulate")
+
+
+def atrous_levels(spp):  # renderer.ts:142
+    return 5 if spp <= 4 else 4 if spp <= 16 else 3 if spp <= 64 else 2 if spp <= 256 else 1
+
+
+def denoise_weight(spp):  # renderer.ts:144
+    return min(1.0, max(0.0, (1024 - spp) / (1024 - 128)))
+
+
+@dataclass
+class RenderSettings:
+    """RenderSettings / DEFAULT_SETTINGS (renderer.ts:42-84), the fields this build uses."""
+    max_bounces: int = 6
+    exposure: float = 1.0
+    tonemap: str = "aces"
+    firefly_clamp: float = 8.0
+    denoise: bool = True
+
+
+def _f(a):
+    return N.ptr(a, C.c_float) if a is not None else None
+
+
+class Renderer:
+    def __init__(self, width, height):
+        self.settings = RenderSettings()
+        h = C.c_void_p()
+        N.check(N.lib().lucent_renderer_create(width, height, C.byref(h)))
+        self._h = h
+        self.width, self.height = width, height
+        self.scene = None
+        self._keep = []
+        self.camera_state = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def dispose(self):
+        if getattr(self, "_h", None):
+            N.lib().lucent_renderer_destroy(self._h)
+            self._h = None
+
+    __del__ = dispose
+
+    # ------------------------------------------------------------------ scene
+    def load_scene(self, scene: S.Scene, bvh=None):
+        """loadScene (renderer.ts:279-312); `bvh` is a prebuilt reference-layout BVH."""
+        p = S.pack_scene(scene)
+        self.packed = p
+        d = NR.SceneDesc()
+        d.tri_count = p.tri_count
+        keep = [p.positions, p.normals, p.tri_material, p.tri_light, p.tri_alpha, p.materials, p.spheres,
+                p.sphere_materials, p.sphere_lights, p.lights]
+        d.positions, d.normals = _f(p.positions), _f(p.normals)
+        d.uvs = _f(p.uvs) if p.uvs is not None else None
+        if p.uvs is not None:
+            keep.append(p.uvs)
+        d.tri_material = N.ptr(p.tri_material, C.c_int32)
+        d.tri_light = N.ptr(p.tri_light, C.c_int32)
+        d.tri_alpha = N.ptr(p.tri_alpha, C.c_uint8)
+        if bvh is not None:
+            nodes = np.ascontiguousarray(bvh.nodes, np.float32)
+            tri = np.ascontiguousarray(bvh.tri_indices, np.uint32)
+            keep += [nodes, tri]
+            d.bvh_nodes, d.bvh_node_count, d.bvh_tri_indices = _f(nodes), bvh.node_count, N.ptr(tri, C.c_uint32)
+        d.materials, d.material_count = _f(p.materials), p.material_count
+        d.spheres, d.sphere_count = _f(p.spheres), len(scene.spheres)
+        d.sphere_materials = N.ptr(p.sphere_materials, C.c_int32)
+        d.sphere_lights = N.ptr(p.sphere_lights, C.c_int32)
+        d.lights, d.light_count = _f(p.lights), p.light_count
+        d.ground_material = p.ground_material
+        N.check(N.lib().lucent_renderer_load_scene(self._h, C.byref(d)))
+        self.scene = scene
+        self.upload_ground(scene.ground)
+        self.upload_lighting(scene)
+        self.upload_camera(scene.camera, False)
+        self.apply_settings()
+        self.reset()
+
+    def upload_lighting(self, scene: S.Scene):
+        """uploadLighting (renderer.ts:355-387)."""
+        L = S.lighting(scene)
+        env = np.ascontiguousarray(L.env.data, np.float32)
+        self._env = env
+        d = NR.LightingDesc()
+        d.sun_enabled = L.sun_enabled
+        d.sun_dir[:] = L.sun_dir
+        d.sun_radiance[:] = L.sun_radiance
+        d.sun_cos_angle, d.sun_pdf = L.sun_cos_angle, L.sun_pdf
+        d.env_width, d.env_height, d.env_rgb = L.env.width, L.env.height, _f(env)
+        d.env_rotation_cos, d.env_rotation_sin = L.env_rotation
+        d.env_intensity, d.env_background = L.env_intensity, L.env_background
+        d.backdrop[:] = L.backdrop
+        N.check(N.lib().lucent_renderer_upload_lighting(self._h, C.byref(d)))
+
+    def upload_ground(self, ground: S.Ground):
+        N.check(N.lib().lucent_renderer_upload_ground(self._h, 1 if ground.enabled else 0, ground.height))
+
+    def upload_camera(self, cam: S.Camera, moving=True):
+        """uploadCamera (renderer.ts:424-439); any camera change restarts the average."""
+        f, r, u = S.camera_basis(cam)
+        d = NR.CameraDesc()
+        d.position[:] = cam.position
+        d.right[:], d.up[:], d.forward[:] = r, u, f
+        d.tan_half_fov = math.tan(cam.fov * math.pi / 360)
+        d.aperture, d.focus_distance = cam.aperture, cam.focus_distance
+        self.camera_state = d
+        N.check(N.lib().lucent_renderer_upload_camera(self._h, C.byref(d)))
+
+    def apply_settings(self):
+        d = NR.SettingsDesc(self.settings.max_bounces, self.settings.firefly_clamp)
+        N.check(N.lib().lucent_renderer_apply_settings(self._h, C.byref(d)))
+
+    def reset(self):
+        N.check(N.lib().lucent_renderer_reset(self._h))
+
+    def resize(self, width, height):
+        N.check(N.lib().lucent_renderer_resize(self._h, width, height))
+        self.width, self.height = width, height
+
+    def set_seed(self, seed):
+        N.check(N.lib().lucent_renderer_set_seed(self._h, seed))
+
+    # ------------------------------------------------------------------ work
+    def trace_samples(self, count, stream=None):
+        """traceSamples (renderer.ts:702-737), asynchronous on `stream`."""
+        N.check(N.lib().lucent_renderer_trace(self._h, count, stream))
+
+    def check(self, stream=None):
+        N.check(N.lib().lucent_renderer_check(self._h, stream))
+
+    def read(self):
+        """(color4, albedo4, normal4, history) as numpy arrays [H, W, ...], row 0 = bottom."""
+        n = self.width * self.height
+        col = np.empty(n * 4, np.float32)
+        alb = np.empty(n * 4, np.float32)
+        nrm = np.empty(n * 4, np.float32)
+        hist = np.empty(n, np.float32)
+        N.check(N.lib().lucent_renderer_read(self._h, _f(col), _f(alb), _f(nrm), _f(hist)))
+        sh = (self.height, self.width)
+        return col.reshape(*sh, 4), alb.reshape(*sh, 4), nrm.reshape(*sh, 4), hist.reshape(sh)
+
+    def stats(self):
+        st = NR.RenderStats()
+        N.check(N.lib().lucent_renderer_stats(self._h, C.byref(st)))
+        out = {k: getattr(st, k) for k, _ in NR.RenderStats._fields_}
+        out["phase_ms"] = dict(zip(PHASES, list(st.phase_ms)))
+        out["traversal"] = dict(zip(("rays", "slab_f64", "triangle_f64", "closest_f64", "final_f64"),
+                                    [int(x) for x in st.traversal]))
+        return out
+
+    def set_profiling(self, enabled=True):
+        N.check(N.lib().lucent_renderer_set_profiling(self._h, 1 if enabled else 0))
+
+    def benchmark(self, samples):
+        """benchmark(n) (renderer.ts:745-777): one warm-up sample, then `samples` timed."""
+        self.reset()
+        self.trace_samples(1)
+        self.check()
+        t0 = time.perf_counter()
+        self.trace_samples(samples)
+        self.check()
+        trace_ms = (time.perf_counter() - t0) * 1e3
+        return {"trace_ms": trace_ms, "mpaths_per_sec": samples * self.width * self.height / (trace_ms / 1e3) / 1e6,
+                "width": self.width, "height": self.height}

@@ -12,6 +12,7 @@
  * Build flags (see oracle/build_oracle.py): -O2 -ffp-contract=off -fno-fast-math.
  */
 #include "lucent_oracle.h"
+#include "oracle_core.h"
 
 #include <algorithm>
 #include <atomic>
@@ -23,62 +24,8 @@
 
 namespace {
 
-const double INF = std::numeric_limits<double>::infinity();
-
-// ---------------------------------------------------------------------------
-// src/math/vec3.ts:15-25 (sub, dot, cross) on binary64 triples.
-// ---------------------------------------------------------------------------
-struct V3 {
-  double x, y, z;
-};
-inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-inline V3 cross(V3 a, V3 b) {
-  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
-}
-
-// ---------------------------------------------------------------------------
-// intersectTriangle, src/math/ray.ts:22-45 (two-sided Moller-Trumbore, f64).
-// ---------------------------------------------------------------------------
-inline bool tri_hit(V3 o, V3 d, V3 v0, V3 v1, V3 v2, double tMin, double tMax, double& t, double& u,
-                    double& v) {
-  V3 e1 = sub(v1, v0);
-  V3 e2 = sub(v2, v0);
-  V3 p = cross(d, e2);
-  double det = dot(e1, p);
-  if (std::fabs(det) < 1e-12) return false;
-  double invDet = 1.0 / det;
-  V3 s = sub(o, v0);
-  double uu = dot(s, p) * invDet;
-  if (uu < 0 || uu > 1) return false;
-  V3 q = cross(s, e1);
-  double vv = dot(d, q) * invDet;
-  if (vv < 0 || uu + vv > 1) return false;
-  double tt = dot(e2, q) * invDet;
-  if (tt <= tMin || tt >= tMax) return false;
-  t = tt;
-  u = uu;
-  v = vv;
-  return true;
-}
-
-// ---------------------------------------------------------------------------
-// AABB.intersect, src/math/aabb.ts:84-98 (slab test, f64). NaN comparisons
-// are false exactly as in JavaScript.
-// ---------------------------------------------------------------------------
-inline double slab(const double* mn, const double* mx, const double* o, const double* inv, double tMax) {
-  double tmin = 0;
-  double tmax = tMax;
-  for (int i = 0; i < 3; i++) {
-    double t0 = (mn[i] - o[i]) * inv[i];
-    double t1 = (mx[i] - o[i]) * inv[i];
-    if (t0 > t1) std::swap(t0, t1);
-    if (t0 > tmin) tmin = t0;
-    if (t1 < tmax) tmax = t1;
-    if (tmax < tmin) return INF;
-  }
-  return tmin;
-}
+// Binary64 vector / slab / triangle arithmetic (vec3.ts, aabb.ts, ray.ts).
+using namespace orc;
 
 inline V3 vtx(const float* pos, uint32_t tri, int k) {
   const float* p = pos + (uint64_t)tri * 9 + k * 3;

@@ -1,0 +1,92 @@
+/*
+ * Oracle renderer: CPU restatement of the reference's path tracer
+ * (src/shaders/trace.frag with common.glsl, scene.glsl, lights.glsl,
+ * bsdf.glsl) and its denoise / display passes (variance.frag, atrous.frag,
+ * denoise.glsl, display.frag). TEST INFRASTRUCTURE ONLY (the checker).
+ *
+ * Precision 32 evaluates the shading in binary32 like the GLSL; precision 64
+ * evaluates it in binary64 (the FP64 reference render). Triangle hits use the
+ * binary64 restatement of intersectBVH (src/math/bvh.ts:265-320) with
+ * tMin = EPS (common.glsl:8) and tMax = INF (1e30), then analytic spheres and
+ * the ground plane override them when closer, as traceScene does.
+ */
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_scene {
+  uint32_t tri_count;
+  const float* positions;     /* 9 per triangle, original order (for intersectBVH) */
+  const float* geo;           /* 12 per slot: packScene triGeometry (scene.ts:213-235) */
+  const float* attr;          /* 16 per slot: packScene triAttributes */
+  const float* nodes;         /* reference layout, 8 per node */
+  uint32_t node_count;
+  const uint32_t* tri_indices;
+  const float* materials;     /* 40 per material (material.ts:121-131) */
+  uint32_t material_count;
+  const float* spheres;       /* 4 per sphere */
+  const int32_t* sphere_materials;
+  const int32_t* sphere_lights;
+  uint32_t sphere_count;
+  const float* lights;        /* 16 per light (scene.ts:88-95) */
+  uint32_t light_count;
+  int32_t ground_material;    /* -1: no ground */
+  float ground_height;
+  /* lighting uniforms (renderer.ts:355-413) */
+  int32_t sun_enabled;
+  float sun_dir[3], sun_radiance[3], sun_cos_angle, sun_pdf;
+  uint32_t env_width, env_height;
+  const float* env_rgb;       /* equirect RGB, rows top to bottom */
+  uint32_t env_grid_w, env_grid_h;
+  const float* env_alias;     /* 4 per cell */
+  float env_rot_cos, env_rot_sin, env_intensity;
+  int32_t env_sampling, env_background;
+  float backdrop[3];
+  const float* sheen_lut;     /* 16x16, already rounded to half precision */
+} orc_scene;
+
+typedef struct orc_camera {
+  float pos[3], right[3], up[3], forward[3];
+  float tan_half_fov, aperture, focus_dist;
+} orc_camera;
+
+/* Renders samples [seed0, seed0 + samples) into the crop [x0,x0+cw) x [y0,y0+ch)
+ * of a width x height image (pixel y = 0 is the bottom row, like
+ * gl_FragCoord), accumulating like trace.frag:324-354 with uReproject = 0.
+ * Outputs per crop pixel: color4 (rgb mean, mean lum^2), albedo4, normal4,
+ * history. albedo/normal are rounded to half precision at every store
+ * (RGBA16F targets, renderer.ts:490) when precision == 32. */
+int orc_render(const orc_scene* s, const orc_camera* cam, uint32_t max_bounces, float clamp_lum, uint32_t width,
+               uint32_t height, uint32_t x0, uint32_t y0, uint32_t cw, uint32_t ch, uint32_t seed0,
+               uint32_t samples, int precision, float* color4, float* albedo4, float* normal4, float* history,
+               int threads);
+
+/* orc_render (precision 32) that also counts the rays it traces and, when
+ * `detailed`, the reference GLSL traversal work of each: work_out = [closest
+ * rays, inner nodes visited, triangles tested, shadow rays, shadow nodes
+ * visited, shadow triangles]. */
+int orc_render_work(const orc_scene* s, const orc_camera* cam, uint32_t max_bounces, float clamp_lum,
+                    uint32_t width, uint32_t height, uint32_t x0, uint32_t y0, uint32_t cw, uint32_t ch,
+                    uint32_t seed0, uint32_t samples, float* color4, float* albedo4, float* normal4,
+                    float* history, int threads, int detailed, uint64_t* work_out);
+
+/* BSDF tuples (bsdf.glsl): for each tuple evaluates evalOpaque, and
+ * sampleOpaque / sampleDielectric driven by the given uniforms instead of the
+ * RNG. Tuple layout and outputs documented in oracle_render.cpp. */
+int orc_bsdf_tuples(const float* in, uint64_t n, int precision, double* out, int threads);
+void orc_bsdf_set_lut(const float* lut);
+
+/* Denoiser and display (variance.frag, atrous.frag, display.frag) on full
+ * W x H images; see oracle_render.cpp for buffer layouts. */
+int orc_denoise(const float* color4, const float* albedo4, const float* normal4, const float* history,
+                uint32_t w, uint32_t h, const orc_camera* cam, uint32_t levels, float sigma_l, float sigma_n,
+                float sigma_p, float* out4);
+int orc_display(const float* color4, const float* albedo4, const float* denoised4, uint32_t w, uint32_t h,
+                float denoise_weight, float exposure, int tonemap, float* out_rgb);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,164 @@
+"""Oracle renderer wrapper (TEST INFRASTRUCTURE ONLY: the checker).
+
+Prepares everything the reference computes on the CPU before drawing, with
+the oracle's own code: buildBVH over the merged triangles, packScene's gather
+into BVH leaf order (src/scene/scene.ts:215-235), buildEnvSampler
+(environment.ts:52-85) and the sheen LUT rounded to half precision
+(renderer.ts:241-242), then runs the C++ restatement of trace.frag.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _p, build_bvh, build_env_sampler, lib, sheen_lut
+
+P = C.POINTER
+F, D, U32, I32 = C.c_float, C.c_double, C.c_uint32, C.c_int32
+
+
+class OrcScene(C.Structure):
+    _fields_ = [("tri_count", U32), ("positions", P(F)), ("geo", P(F)), ("attr", P(F)), ("nodes", P(F)),
+                ("node_count", U32), ("tri_indices", P(U32)), ("materials", P(F)), ("material_count", U32),
+                ("spheres", P(F)), ("sphere_materials", P(I32)), ("sphere_lights", P(I32)),
+                ("sphere_count", U32), ("lights", P(F)), ("light_count", U32), ("ground_material", I32),
+                ("ground_height", F), ("sun_enabled", I32), ("sun_dir", F * 3), ("sun_radiance", F * 3),
+                ("sun_cos_angle", F), ("sun_pdf", F), ("env_width", U32), ("env_height", U32),
+                ("env_rgb", P(F)), ("env_grid_w", U32), ("env_grid_h", U32), ("env_alias", P(F)),
+                ("env_rot_cos", F), ("env_rot_sin", F), ("env_intensity", F), ("env_sampling", I32),
+                ("env_background", I32), ("backdrop", F * 3), ("sheen_lut", P(F))]
+
+
+class OrcCamera(C.Structure):
+    _fields_ = [("pos", F * 3), ("right", F * 3), ("up", F * 3), ("forward", F * 3), ("tan_half_fov", F),
+                ("aperture", F), ("focus_dist", F)]
+
+
+def declare(L):
+    L.orc_render.argtypes = [P(OrcScene), P(OrcCamera), U32, F, U32, U32, U32, U32, U32, U32, U32, U32, C.c_int,
+                             P(F), P(F), P(F), P(F), C.c_int]
+    L.orc_render_work.argtypes = [P(OrcScene), P(OrcCamera), U32, F, U32, U32, U32, U32, U32, U32, U32, U32, P(F),
+                                  P(F), P(F), P(F), C.c_int, C.c_int, P(C.c_uint64)]
+    L.orc_bsdf_tuples.argtypes = [P(F), C.c_uint64, C.c_int, P(D), C.c_int]
+    L.orc_bsdf_set_lut.argtypes = [P(F)]
+    if hasattr(L, "orc_denoise"):
+        L.orc_denoise.argtypes = [P(F), P(F), P(F), P(F), U32, U32, P(OrcCamera), U32, F, F, F, P(F)]
+        L.orc_display.argtypes = [P(F), P(F), P(F), U32, U32, F, F, C.c_int, P(F)]
+
+
+def half_lut():
+    """The 16x16 sheen LUT as the reference uploads it: R16F (half) values."""
+    return sheen_lut(16, 96).astype(np.float16).astype(np.float32)
+
+
+class Prepared:
+    """A packed scene + lighting ready for orc_render (arrays kept alive here)."""
+
+    def __init__(self, packed, lighting, camera, ground=None):
+        from lucent_gb300 import scene as S
+        self.keep = []
+        keep = self.keep.append
+        p = packed
+        n = p.tri_count
+        bvh = build_bvh(p.positions)
+        self.bvh = bvh
+        src = bvh.tri_indices.astype(np.int64)
+        pos = p.positions.reshape(-1, 3, 3)[src] if n else np.zeros((0, 3, 3), np.float32)
+        nrm = p.normals.reshape(-1, 3, 3)[src] if n else np.zeros((0, 3, 3), np.float32)
+        geo = np.zeros((n, 3, 4), np.float32)  # scene.ts:213-235
+        geo[:, :, :3] = pos
+        geo[:, 0, 3] = p.tri_material[src]
+        geo[:, 1, 3] = p.tri_light[src]
+        geo[:, 2, 3] = p.tri_alpha[src]
+        attr = np.zeros((n, 4, 4), np.float32)
+        attr[:, :3, :3] = nrm
+        if p.uvs is not None and n:
+            uv = p.uvs.reshape(-1, 3, 2)[src]
+            attr[:, :3, 3] = uv[:, :, 0]
+            attr[:, 3, :3] = uv[:, :, 1]
+        s = OrcScene()
+        s.tri_count = n
+        for name, arr, ct in (("positions", p.positions, F), ("geo", geo, F), ("attr", attr, F),
+                              ("nodes", bvh.nodes, F), ("tri_indices", bvh.tri_indices, U32),
+                              ("materials", p.materials, F), ("spheres", p.spheres, F),
+                              ("sphere_materials", p.sphere_materials, I32), ("sphere_lights", p.sphere_lights, I32),
+                              ("lights", p.lights, F)):
+            a = np.ascontiguousarray(arr, np.float32 if ct is F else (np.uint32 if ct is U32 else np.int32))
+            if a.size == 0:
+                a = np.zeros(4, a.dtype)
+            keep(a)
+            setattr(s, name, _p(a, ct))
+        s.node_count = bvh.node_count
+        s.material_count = p.material_count
+        s.sphere_count = p.sphere_materials.size
+        s.light_count = p.light_count
+        g = ground if ground is not None else S.Ground()
+        s.ground_material = p.ground_material if g.enabled else -1
+        s.ground_height = g.height
+        L = lighting
+        s.sun_enabled = L.sun_enabled
+        s.sun_dir[:] = L.sun_dir
+        s.sun_radiance[:] = L.sun_radiance
+        s.sun_cos_angle, s.sun_pdf = L.sun_cos_angle, L.sun_pdf
+        env = np.ascontiguousarray(L.env.data, np.float32)
+        keep(env)
+        s.env_width, s.env_height, s.env_rgb = L.env.width, L.env.height, _p(env, F)
+        gw, gh, table, total = build_env_sampler(env, L.env.width, L.env.height, 1024)
+        keep(table)
+        s.env_grid_w, s.env_grid_h, s.env_alias = gw, gh, _p(table, F)
+        s.env_rot_cos, s.env_rot_sin = L.env_rotation
+        s.env_intensity = L.env_intensity
+        s.env_sampling = 1 if total > 0 else 0
+        s.env_background = L.env_background
+        s.backdrop[:] = L.backdrop
+        lut = half_lut()
+        keep(lut)
+        s.sheen_lut = _p(lut, F)
+        self.scene = s
+        f, r, u = S.camera_basis(camera)
+        cam = OrcCamera()
+        cam.pos[:] = camera.position
+        cam.right[:], cam.up[:], cam.forward[:] = r, u, f
+        cam.tan_half_fov = float(np.tan(camera.fov * np.pi / 360))
+        cam.aperture, cam.focus_dist = camera.aperture, camera.focus_distance
+        self.camera = cam
+
+
+def prepare(scene):
+    from lucent_gb300 import scene as S
+    return Prepared(S.pack_scene(scene), S.lighting(scene), scene.camera, scene.ground)
+
+
+def render(prep, width, height, seed0, samples, max_bounces=6, clamp=8.0, precision=32, crop=None, threads=0):
+    """orc_render over a crop (x0, y0, w, h) of a width x height image.
+    Returns (color4, albedo4, normal4, history) shaped [h, w, ...] (row 0 = bottom)."""
+    x0, y0, cw, ch = crop if crop is not None else (0, 0, width, height)
+    col = np.zeros(cw * ch * 4, np.float32)
+    alb = np.zeros(cw * ch * 4, np.float32)
+    nrm = np.zeros(cw * ch * 4, np.float32)
+    his = np.zeros(cw * ch, np.float32)
+    st = lib().orc_render(C.byref(prep.scene), C.byref(prep.camera), max_bounces, clamp, width, height, x0, y0, cw,
+                          ch, seed0, samples, precision, _p(col, F), _p(alb, F), _p(nrm, F), _p(his, F), threads)
+    if st:
+        raise RuntimeError("orc_render failed")
+    return col.reshape(ch, cw, 4), alb.reshape(ch, cw, 4), nrm.reshape(ch, cw, 4), his.reshape(ch, cw)
+
+
+def render_work(prep, width, height, seed0, samples, max_bounces=6, clamp=8.0, crop=None, threads=0, detailed=True):
+    """Rays traced by the render and, if `detailed`, their reference GLSL traversal work."""
+    x0, y0, cw, ch = crop if crop is not None else (0, 0, width, height)
+    bufs = [np.zeros(cw * ch * 4, np.float32) for _ in range(3)] + [np.zeros(cw * ch, np.float32)]
+    work = np.zeros(6, np.uint64)
+    lib().orc_render_work(C.byref(prep.scene), C.byref(prep.camera), max_bounces, clamp, width, height, x0, y0, cw,
+                          ch, seed0, samples, *[_p(b, F) for b in bufs], threads, 1 if detailed else 0,
+                          work.ctypes.data_as(P(C.c_uint64)))
+    keys = ["closest_rays", "closest_inner", "closest_tris", "shadow_rays", "shadow_nodes", "shadow_tris"]
+    return dict(zip(keys, (int(x) for x in work)))
+
+
+def bsdf_tuples(tuples, precision=64, threads=0):
+    t = np.ascontiguousarray(tuples, np.float32).reshape(-1, 32)
+    lut = half_lut()
+    lib().orc_bsdf_set_lut(_p(lut, F))
+    out = np.zeros((t.shape[0], 24), np.float64)
+    lib().orc_bsdf_tuples(_p(t, F), t.shape[0], precision, _p(out, D), threads)
+    return out

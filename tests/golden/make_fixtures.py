@@ -37,14 +37,30 @@ def closest_bytes(n_rays=200_000):
             "reference_order_triangles_per_ray": round(float(tests.mean()), 3)}
 
 
+def box_scene_bytes(samples=1):
+    """Path-tracing workload (box scene, seed 0, 81,956 triangles, 512 x 512,
+    depth 8): the oracle renders `samples` spp of the full frame and tallies,
+    for every closest-hit ray, the reference GLSL traversal's inner nodes and
+    triangles (64 B / 48 B each) and, for every shadow ray, the occluded()
+    traversal's visited nodes and triangles (32 B / 48 B); + 24 B ray in and
+    16 B result out per ray."""
+    from oracle import render as R
+    prep = R.prepare(workloads.box_scene(0, 6))
+    w = R.render_work(prep, 512, 512, 0, samples, max_bounces=8)
+    c, s = w["closest_rays"], w["shadow_rays"]
+    return {"bytes_per_closest_ray": round((64.0 * w["closest_inner"] + 48.0 * w["closest_tris"]) / c + 40, 2),
+            "bytes_per_shadow_ray": round((32.0 * w["shadow_nodes"] + 48.0 * w["shadow_tris"]) / s + 40, 2),
+            "closest_rays_per_path": round(c / (512 * 512 * samples), 4),
+            "shadow_rays_per_path": round(s / (512 * 512 * samples), 4),
+            "inner_nodes_per_closest_ray": round(w["closest_inner"] / c, 3),
+            "triangles_per_closest_ray": round(w["closest_tris"] / c, 3), "samples": samples}
+
+
 def main():
     path = os.path.join(HERE, "algorithmic_bytes.json")
     out = json.load(open(path)) if os.path.exists(path) else {}
     out["closest"] = closest_bytes()
-    try:
-        from tests.golden import make_render_fixtures  # noqa: F401
-    except ImportError:
-        pass
+    out["pt_box"] = box_scene_bytes()
     json.dump(out, open(path, "w"), indent=1, sort_keys=True)
     print(json.dumps(out, indent=1))
 

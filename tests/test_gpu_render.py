@@ -1,0 +1,94 @@
+"""GPU path tracer vs the oracle's restatement of trace.frag.
+
+Both sides draw each path's random numbers from the reference's per-pixel PCG
+stream in the reference's order and take triangle hits from the reference's
+binary64 intersector, so GPU and oracle follow the same paths; they differ
+only by binary32 rounding in shading (FMA, libm), which occasionally flips a
+Russian-roulette or lobe choice. The tests therefore bound (a) the share of
+pixels that agree to 1e-3 relative and (b) the image RMSE, and compare a
+converged image against the oracle's binary64 render.
+"""
+import numpy as np
+import pytest
+
+from oracle import render as OR
+from lucent_gb300 import workloads as W
+from lucent_gb300.renderer import Renderer
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu(scene, w, h, spp, seed=0, max_bounces=8, batches=1):
+    r = Renderer(w, h)
+    r.settings.max_bounces = max_bounces
+    r.load_scene(scene)
+    r.set_seed(seed)
+    for _ in range(batches):
+        r.trace_samples(spp // batches)
+    col, alb, nrm, hist = r.read()
+    st = r.stats()
+    r.dispose()
+    return col, alb, nrm, hist, st
+
+
+def _close_frac(a, b, rel=1e-3):
+    return (np.abs(a - b) <= rel * (np.abs(b) + 1e-3)).mean()
+
+
+def test_box_scene_matches_oracle_per_pixel():
+    sc = W.box_scene(0, 3)
+    w = h = 64
+    col, alb, nrm, hist, st = _gpu(sc, w, h, 4)
+    prep = OR.prepare(sc)
+    oc, oa, on, oh = OR.render(prep, w, h, 0, 4, max_bounces=8)
+    assert np.all(hist == 4) and np.array_equal(hist, oh)
+    assert not np.isnan(col).any()
+    frac = _close_frac(col[..., :3], oc[..., :3])
+    assert frac > 0.97, frac
+    rmse = np.sqrt(np.mean((col[..., :3] - oc[..., :3]) ** 2)) / np.mean(oc[..., :3])
+    assert rmse < 0.02, rmse
+    assert _close_frac(alb, oa, 2e-3) > 0.97
+    assert st["closest_rays"] > 0 and st["shadow_rays"] > 0
+
+
+def test_converged_image_matches_fp64_render():
+    sc = W.box_scene(1, 3)
+    w = h = 32
+    col, *_ = _gpu(sc, w, h, 256, seed=7, batches=4)
+    prep = OR.prepare(sc)
+    ref, *_ = OR.render(prep, w, h, 7, 256, max_bounces=8, precision=64)
+    rel_rmse = np.sqrt(np.mean((col[..., :3] - ref[..., :3]) ** 2)) / np.mean(ref[..., :3])
+    assert rel_rmse < 0.01, rel_rmse
+
+
+def test_white_furnace():
+    # A rough, IOR-1 sphere of albedo 1 under a uniform environment: the image
+    # must match the binary64 oracle and stay within the model's energy bounds.
+    sc = W.furnace_scene(albedo=1.0, roughness=1.0, ior=1.0, radiance=1.0)
+    w = h = 32
+    col, alb, *_ = _gpu(sc, w, h, 64, max_bounces=12)
+    prep = OR.prepare(sc)
+    ref, *_ = OR.render(prep, w, h, 0, 64, max_bounces=12, precision=64)
+    cov = alb[..., 3] == 1.0  # every sample hit the sphere
+    bg = alb[..., 3] == 0.0  # no sample did
+    g = col[..., :3][cov].mean()
+    o = ref[..., :3][cov].mean()
+    assert abs(g - o) / o < 0.01, (g, o)
+    assert 0.85 < g < 1.02, g
+    assert bg.any() and np.allclose(col[..., :3][bg], 1.0, atol=1e-5)  # background sees the environment
+
+
+def test_full_size_box_scene_crop():
+    # 512 x 512, 16 spp, depth 8 on the 81,956-triangle scene; a crop is
+    # checked against the oracle (the whole frame would take the CPU minutes).
+    sc = W.box_scene(0, 6)
+    col, alb, nrm, hist, st = _gpu(sc, 512, 512, 16)
+    assert np.all(hist == 16) and not np.isnan(col).any()
+    prep = OR.prepare(sc)
+    x0, y0 = 240, 200
+    oc, *_ = OR.render(prep, 512, 512, 0, 16, max_bounces=8, crop=(x0, y0, 48, 48))
+    g = col[y0:y0 + 48, x0:x0 + 48, :3]
+    frac = _close_frac(g, oc[..., :3])
+    assert frac > 0.9, frac
+    rmse = np.sqrt(np.mean((g - oc[..., :3]) ** 2)) / np.mean(oc[..., :3])
+    assert rmse < 0.05, rmse
