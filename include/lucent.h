@@ -106,6 +106,30 @@ lucent_status lucent_bvh_intersect_f64(lucent_bvh* bvh, const double* rays, uint
                                        double t_max, int32_t* prim_out, double* t_out, double* u_out,
                                        double* v_out, void* stream);
 
+/* Closest hit that allocates no device memory. It has no counterpart in the
+ * reference: it exists for callers that may not call cudaMalloc (a host whose
+ * own allocator owns the device's memory, a loop that must not take the
+ * allocator's implicit synchronisation, a plugin whose host owns every
+ * allocation). Inputs and outputs are the caller's device buffers:
+ *   nodes_d   node_count nodes of 8 floats: min.xyz, leftFirst, max.xyz, count,
+ *             with leftFirst and count stored as int32 bit patterns (the
+ *             reference's layout, bvh.ts:6-16, with integer fields);
+ *   tris_d    tri_count triangles in BVH leaf (slot) order, 12 floats each:
+ *             v0.xyz, source index as int32 bits, v1.xyz, 0, v2.xyz, 0;
+ *   rays_d    n rays of 6 floats; prim/t/u/v as in lucent_bvh_intersect.
+ * The kernels' scratch is a file-scope device array of 4 MiB + 256 B that
+ * every GPU loading the library keeps until exit, so n is limited to
+ * 1,048,576 rays per call (larger n fails with LUCENT_ERR_UNSUPPORTED). All
+ * calls share that array: calls that overlap on the GPU (other threads, other
+ * streams) race on it and must be serialised by the caller. The first call on
+ * each device looks up the array's device address with that device current.
+ * The call returns after the work completes (it synchronises `stream`) and
+ * reports kernel errors like lucent_bvh_check. */
+lucent_status lucent_bvh_intersect_noalloc(const float* nodes_d, uint32_t node_count, const float* tris_d,
+                                           uint32_t tri_count, const float* rays_d, uint32_t n, double t_min,
+                                           double t_max, int32_t* prim_d, float* t_d, float* u_d, float* v_d,
+                                           void* stream);
+
 /* ---------------------------------------------------------------------------
  * Renderer: the Renderer class of src/renderer.ts:171-871 without its WebGL
  * plumbing. Accumulation targets, scene data and the path state live on the
