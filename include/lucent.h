@@ -248,6 +248,35 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
  * lucent_render_stats.phase_ms after lucent_renderer_check. */
 lucent_status lucent_renderer_set_profiling(lucent_renderer* r, int32_t enabled);
 
+/* runDenoiser (renderer.ts:788-830; variance.frag, atrous.frag,
+ * denoise.glsl): per-pixel variance of the demodulated illumination, then
+ * `levels` (0..5) edge-avoiding a-trous iterations of spacing 1, 2, 4, 8, 16
+ * guided by the albedo/normal/depth targets and the uploaded camera. The
+ * reference passes levels = atrousLevels(frame) (renderer.ts:142) and sigma
+ * L/N/P = 4, 64, 1.5. Asynchronous on `stream`; the result stays on the
+ * device for lucent_renderer_display until the next reset or resize. */
+lucent_status lucent_renderer_denoise(lucent_renderer* r, uint32_t levels, float sigma_l, float sigma_n,
+                                      float sigma_p, void* stream);
+/* Copies the last denoised illumination (width*height*4 floats: RGB,
+ * variance) to the host; the filter targets the reference keeps in
+ * `filtered`. */
+lucent_status lucent_renderer_read_denoised(lucent_renderer* r, float* out4);
+/* The display pass (renderer.ts:573-591, display.frag) at render size ==
+ * view size: blend in the remodulated denoised image with `denoise_weight`
+ * (denoiseWeight(frame), renderer.ts:144; 0 = raw), exposure, tone map
+ * (0 ACES, 1 Reinhard, 2 none), sRGB, interleaved-gradient dither. Writes
+ * the RGBA8 canvas (rows bottom to top) and/or the RGB floats before
+ * quantization to host memory (either may be NULL); synchronous. */
+lucent_status lucent_renderer_display(lucent_renderer* r, float denoise_weight, int32_t tonemap, float exposure,
+                                      uint8_t* rgba8_out, float* rgb_out, void* stream);
+
+/* Diagnostic with no reference counterpart: evaluates the path tracer's
+ * BSDF code (the device restatement of bsdf.glsl evalOpaque :114-166,
+ * sampleOpaque :174-211, sampleDielectric :216-248) on `n` caller tuples of
+ * 32 floats, writing 24 floats each; the layout is documented in
+ * lucent_gb300/csrc/bsdf_tuples.cu. Host buffers; synchronous. */
+lucent_status lucent_bsdf_eval_tuples(const float* tuples, uint32_t n, float* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,8 +55,7 @@ def declare(L, sig):
     sig(L, "lucent_renderer_read", [VP, F32P, F32P, F32P, F32P])
     sig(L, "lucent_renderer_stats", [VP, P(RenderStats)])
     sig(L, "lucent_renderer_set_profiling", [VP, C.c_int32])
-    for name, args in (("lucent_renderer_denoise", [VP, C.c_uint32, C.c_float, C.c_float, C.c_float, VP]),
-                       ("lucent_renderer_display", [VP, C.c_float, C.c_int32, C.c_float, U8P, F32P, VP]),
-                       ("lucent_renderer_read_denoised", [VP, F32P])):
-        if hasattr(L, name):
-            sig(L, name, args)
+    sig(L, "lucent_renderer_denoise", [VP, C.c_uint32, C.c_float, C.c_float, C.c_float, VP])
+    sig(L, "lucent_renderer_display", [VP, C.c_float, C.c_int32, C.c_float, U8P, F32P, VP])
+    sig(L, "lucent_renderer_read_denoised", [VP, F32P])
+    sig(L, "lucent_bsdf_eval_tuples", [F32P, C.c_uint32, F32P])

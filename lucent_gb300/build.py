@@ -19,8 +19,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I" + os.path.join(ROOT, "include")]
 # Per-file extra flags. The BVH builder's binary64 arithmetic must match
-# JavaScript operation by operation, so no contraction into FMA there.
-EXTRA = {"bvh_build.cu": ["-fmad=false"]}
+# JavaScript operation by operation, so no contraction into FMA there; the
+# denoiser and display pass keep the shaders' separate multiply and add so
+# that variance differences (second moment minus squared mean) round the
+# same way as the unfused restatement they are tested against.
+EXTRA = {"bvh_build.cu": ["-fmad=false"], "denoise.cu": ["-fmad=false"]}
 
 
 def nvcc():

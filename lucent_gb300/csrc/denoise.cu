@@ -1,0 +1,211 @@
+// SVGF-style denoiser and display pass: the reference's variance.frag,
+// atrous.frag (driven as runDenoiser, src/renderer.ts:788-830) and
+// display.frag, as CUDA kernels over the accumulation targets.
+//
+// The a-trous taps need, per neighbour, the unit guide normal and the world
+// position reconstructed from the primary ray and depth (atrous.frag:92-126).
+// Both depend only on the pixel, so k_guides computes them once per denoise
+// (32 B per pixel) instead of once per tap; the values are the reference's
+// formulas evaluated the same way.
+#include <cuda_fp16.h>
+
+#include "internal.h"
+#include "render_internal.h"
+#include "shade.cuh"
+
+namespace lucent {
+
+using namespace sh;
+
+__device__ __forceinline__ float lum3(float r, float g, float b) { return r * 0.2126f + g * 0.7152f + b * 0.0722f; }
+
+__device__ __forceinline__ float3 unit_normal(float x, float y, float z) {  // denoise.glsl:21-24
+  const float l = sqrtf(x * x + y * y + z * z);
+  return l > 1e-6f ? make_float3(x / l, y / l, z / l) : make_float3(0.f, 0.f, 1.f);
+}
+
+__device__ __forceinline__ float4 h4(half4 v) {
+  return make_float4(__half2float(v.x), __half2float(v.y), __half2float(v.z), __half2float(v.w));
+}
+
+// variance.frag:15-55 -> (demodulated illumination, variance).
+__global__ void k_variance(AccumDev A, int W, int H, float4* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const size_t p = (size_t)y * W + x;
+  const float4 c = A.color[p];
+  const float4 a = h4(A.albedo[p]);
+  if (a.w < 0.5f) {
+    out[p] = make_float4(c.x, c.y, c.z, 0.f);
+    return;
+  }
+  const float3 illum = make_float3(c.x / fmaxf(a.x, 1e-3f), c.y / fmaxf(a.y, 1e-3f), c.z / fmaxf(a.z, 1e-3f));
+  const float samples = fmaxf(A.history[p], 1.f);
+  const float la = fmaxf(lum3(a.x, a.y, a.z), 1e-3f);
+  float variance;
+  if (samples >= 4.f) {
+    const float l = lum3(c.x, c.y, c.z);
+    variance = fmaxf(0.f, c.w - l * l) / (la * la) / samples;
+  } else {  // 7 x 7 spatial estimate for the first samples
+    const float4 np = h4(A.normal[p]);
+    const float3 n = unit_normal(np.x, np.y, np.z);
+    float s1 = 0.f, s2 = 0.f, ws = 0.f;
+    for (int dy = -3; dy <= 3; dy++)
+      for (int dx = -3; dx <= 3; dx++) {
+        const int qx = x + dx, qy = y + dy;
+        if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
+        const size_t q = (size_t)qy * W + qx;
+        const float4 aq = h4(A.albedo[q]);
+        if (aq.w < 0.5f) continue;
+        const float4 nq = h4(A.normal[q]);
+        const float3 un = unit_normal(nq.x, nq.y, nq.z);
+        const float st = (0.1f * np.w < fabsf(np.w - nq.w)) ? 0.f : 1.f;
+        const float w = powf(fmaxf(0.f, n.x * un.x + n.y * un.y + n.z * un.z), 32.f) * st;
+        const float4 cq = A.color[q];
+        const float l = lum3(cq.x / fmaxf(aq.x, 1e-3f), cq.y / fmaxf(aq.y, 1e-3f), cq.z / fmaxf(aq.z, 1e-3f));
+        s1 += w * l;
+        s2 += w * l * l;
+        ws += w;
+      }
+    const float m1 = s1 / fmaxf(ws, 1e-6f);
+    variance = fmaxf(0.f, s2 / fmaxf(ws, 1e-6f) - m1 * m1) / samples;
+  }
+  out[p] = make_float4(illum.x, illum.y, illum.z, variance);
+}
+
+// Per pixel: (unit normal, covered) and (world position, depth).
+__global__ void k_guides(AccumDev A, CameraDev cam, int W, int H, float4* __restrict__ g0, float4* __restrict__ g1) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const size_t p = (size_t)y * W + x;
+  const float4 np = h4(A.normal[p]);
+  const float cov = __half2float(A.albedo[p].w);
+  const float3 n = unit_normal(np.x, np.y, np.z);
+  // primaryDir (atrous.frag:77-81)
+  const float ux = ((float)x + 0.5f) / (float)W * 2.f - 1.f, uy = ((float)y + 0.5f) / (float)H * 2.f - 1.f;
+  const float aspect = (float)W / (float)H;
+  const float3 d = norm3(cam.forward + cam.right * (ux * aspect * cam.tan_half_fov) + cam.up * (uy * cam.tan_half_fov));
+  const float3 P = cam.pos + d * np.w;
+  g0[p] = make_float4(n.x, n.y, n.z, cov);
+  g1[p] = make_float4(P.x, P.y, P.z, np.w);
+}
+
+// One a-trous iteration (atrous.frag:85-137) at hole spacing `step`.
+__global__ void __launch_bounds__(256) k_atrous(const float4* __restrict__ in, const float4* __restrict__ g0,
+                                                const float4* __restrict__ g1, int W, int H, int step, float tan_half,
+                                                float sigma_l, float sigma_n, float sigma_p,
+                                                float4* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const size_t p = (size_t)y * W + x;
+  const float4 cp = __ldg(in + p);
+  const float4 gp = __ldg(g0 + p);
+  if (gp.w < 0.5f) {
+    out[p] = cp;
+    return;
+  }
+  const float4 Pp = __ldg(g1 + p);
+  const float footprint = 2.f * tan_half * Pp.w / (float)H;
+  float var = 0.f, wv = 0.f;
+#pragma unroll
+  for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+    for (int dx = -1; dx <= 1; dx++) {
+      const int qx = x + dx, qy = y + dy;
+      if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
+      const float k = (dx == 0 ? 0.5f : 0.25f) * (dy == 0 ? 0.5f : 0.25f);
+      var += __ldg(&in[(size_t)qy * W + qx].w) * k;
+      wv += k;
+    }
+  const float denom = sigma_l * sqrtf(fmaxf(var / wv, 0.f)) + 1e-6f;
+  const float lp = lum3(cp.x, cp.y, cp.z);
+  const float h[3] = {0.375f, 0.25f, 0.0625f};
+  float3 sum = make_float3(cp.x * (h[0] * h[0]), cp.y * (h[0] * h[0]), cp.z * (h[0] * h[0]));
+  float sumVar = cp.w * (h[0] * h[0]) * (h[0] * h[0]);
+  float wsum = h[0] * h[0];
+#pragma unroll
+  for (int dy = -2; dy <= 2; dy++)
+#pragma unroll
+    for (int dx = -2; dx <= 2; dx++) {
+      if (dx == 0 && dy == 0) continue;
+      const int qx = x + dx * step, qy = y + dy * step;
+      if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
+      const size_t q = (size_t)qy * W + qx;
+      const float4 gq = __ldg(g0 + q);
+      if (gq.w < 0.5f) continue;
+      const float4 cq = __ldg(in + q);
+      const float4 Q = __ldg(g1 + q);
+      const float k = h[dx < 0 ? -dx : dx] * h[dy < 0 ? -dy : dy];
+      const float wn = powf(fmaxf(0.f, gp.x * gq.x + gp.y * gq.y + gp.z * gq.z), sigma_n);
+      const float reach = sigma_p * footprint * (float)step * sqrtf((float)(dx * dx + dy * dy));
+      const float pd = gp.x * (Q.x - Pp.x) + gp.y * (Q.y - Pp.y) + gp.z * (Q.z - Pp.z);
+      const float wp = expf(-fabsf(pd) / (reach + 1e-6f));
+      const float wl = expf(-fabsf(lp - lum3(cq.x, cq.y, cq.z)) / denom);
+      const float w = k * wn * wp * wl;
+      sum = sum + make_float3(cq.x, cq.y, cq.z) * w;
+      sumVar += cq.w * w * w;
+      wsum += w;
+    }
+  out[p] = make_float4(sum.x / wsum, sum.y / wsum, sum.z / wsum, sumVar / (wsum * wsum));
+}
+
+// display.frag:42-67 (render size == view size): remodulate and blend the
+// denoised image, exposure, tone map, sRGB, IGN dither, RGBA8.
+__global__ void k_display(AccumDev A, const float4* __restrict__ den, int W, int H, float weight, float exposure,
+                          int tonemap, uchar4* __restrict__ rgba8, float* __restrict__ rgb) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const size_t p = (size_t)y * W + x;
+  const float4 raw = A.color[p];
+  float c[3] = {raw.x, raw.y, raw.z};
+  if (weight > 0.f && den) {
+    const float4 a = h4(A.albedo[p]);
+    if (a.w >= 0.5f) {
+      const float4 d = den[p];
+      const float dv[3] = {d.x * fmaxf(a.x, 1e-3f), d.y * fmaxf(a.y, 1e-3f), d.z * fmaxf(a.z, 1e-3f)};
+      for (int k = 0; k < 3; k++) c[k] = c[k] * (1.f - weight) + dv[k] * weight;
+    }
+  }
+  const float t = 0.06711056f * ((float)x + 0.5f) + 0.00583715f * ((float)y + 0.5f);
+  const float u = 52.9829189f * (t - floorf(t));
+  const float ign = u - floorf(u);
+  unsigned char q[3];
+  for (int k = 0; k < 3; k++) {
+    float v = c[k] * exposure;
+    if (tonemap == 0)
+      v = clampf((v * (2.51f * v + 0.03f)) / (v * (2.43f * v + 0.59f) + 0.14f), 0.f, 1.f);  // Narkowicz ACES
+    else if (tonemap == 1)
+      v = v / (1.f + v);
+    v = clampf(v, 0.f, 1.f);
+    v = v < 0.0031308f ? v * 12.92f : 1.055f * powf(v, 1.f / 2.4f) - 0.055f;
+    v += (ign - 0.5f) / 255.f;
+    if (rgb) rgb[3 * p + k] = v;
+    q[k] = (unsigned char)__float2int_rn(clampf(v, 0.f, 1.f) * 255.f);
+  }
+  if (rgba8) rgba8[p] = make_uchar4(q[0], q[1], q[2], 255);
+}
+
+// runDenoiser: variance, then `levels` a-trous steps (1, 2, 4, 8, 16),
+// ping-ponging; returns the buffer holding the result.
+float4* denoise_run(AccumDev A, const CameraDev& cam, int W, int H, int levels, float sigma_l, float sigma_n,
+                    float sigma_p, float4* fa, float4* fb, float4* g0, float4* g1, cudaStream_t s) {
+  const dim3 blk(16, 16), grd((W + 15) / 16, (H + 15) / 16);
+  k_variance<<<grd, blk, 0, s>>>(A, W, H, fa);
+  k_guides<<<grd, blk, 0, s>>>(A, cam, W, H, g0, g1);
+  float4 *rd = fa, *wr = fb;
+  for (int l = 0; l < levels; l++) {
+    k_atrous<<<grd, blk, 0, s>>>(rd, g0, g1, W, H, 1 << l, cam.tan_half_fov, sigma_l, sigma_n, sigma_p, wr);
+    float4* t = rd;
+    rd = wr;
+    wr = t;
+  }
+  return rd;
+}
+
+void display_run(AccumDev A, const float4* den, int W, int H, float weight, float exposure, int tonemap,
+                 uchar4* rgba8, float* rgb, cudaStream_t s) {
+  const dim3 blk(16, 16), grd((W + 15) / 16, (H + 15) / 16);
+  k_display<<<grd, blk, 0, s>>>(A, den, W, H, weight, exposure, tonemap, rgba8, rgb);
+}
+
+}  // namespace lucent

@@ -144,7 +144,7 @@ static bool env_sampler(const float* rgb, uint32_t w, uint32_t h, uint32_t max_w
 
 // sheenAlbedoLUT (src/scene/sheen.ts:13-60): 16 x 16, 96 quadrature steps,
 // then rounded to half precision like the reference's R16F upload.
-static void sheen_lut(float* out) {
+void sheen_lut_half(float* out) {
   const int size = 16, steps = 96;
   for (int y = 0; y < size; y++)
     for (int x = 0; x < size; x++) {
@@ -202,6 +202,9 @@ struct lucent_renderer {
   std::vector<int> ptag;
   int pn = 0;
   double phase_ms[kPhases] = {0, 0, 0, 0, 0, 0};
+  // denoiser ping-pong targets, guide buffers, display staging
+  DeviceBuffer den_a, den_b, guide0, guide1, disp;
+  const float4* denoised = nullptr;  // result of the last lucent_renderer_denoise, or null
 };
 
 static AccumDev accum_of(lucent_renderer* r) {
@@ -218,6 +221,7 @@ static lucent_status alloc_targets(lucent_renderer* r, uint32_t w, uint32_t h) {
   r->H = h;
   k_clear_accum<<<grid_for((uint32_t)n, 256), 256>>>(accum_of(r), (uint32_t)n);
   r->frame = 0;
+  r->denoised = nullptr;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "clear targets");
 }
@@ -281,7 +285,7 @@ lucent_status lucent_renderer_create(uint32_t width, uint32_t height, lucent_ren
   if (!st) st = r->sheen.reserve(256 * 4);
   if (!st) {
     float lut[256];
-    sheen_lut(lut);
+    sheen_lut_half(lut);
     cudaError_t e = cudaMemcpy(r->sheen.ptr, lut, sizeof lut, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaEventCreate(&r->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&r->ev1);
@@ -300,7 +304,7 @@ void lucent_renderer_destroy(lucent_renderer* r) {
   if (!r) return;
   for (DeviceBuffer* b : {&r->nodes, &r->geo, &r->attr, &r->mats, &r->spheres, &r->sph_mat, &r->sph_light,
                           &r->lights, &r->env_rgb, &r->env_alias, &r->sheen, &r->color, &r->albedo, &r->normal,
-                          &r->history, &r->paths, &r->ctr})
+                          &r->history, &r->paths, &r->ctr, &r->den_a, &r->den_b, &r->guide0, &r->guide1, &r->disp})
     b->release();
   if (r->ev0) cudaEventDestroy(r->ev0);
   if (r->ev1) cudaEventDestroy(r->ev1);
@@ -507,6 +511,7 @@ lucent_status lucent_renderer_reset(lucent_renderer* r) {
   const uint32_t n = r->W * r->H;
   k_clear_accum<<<grid_for(n, 256), 256>>>(accum_of(r), n);
   r->frame = 0;
+  r->denoised = nullptr;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "reset");
 }
@@ -618,6 +623,55 @@ lucent_status lucent_renderer_read(lucent_renderer* r, float* color4, float* alb
     tmp.release();
   }
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "read targets");
+}
+
+lucent_status lucent_renderer_denoise(lucent_renderer* r, uint32_t levels, float sigma_l, float sigma_n,
+                                      float sigma_p, void* stream) {
+  clear_error();
+  if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  if (levels > 5) return fail(LUCENT_ERR_INVALID, "at most 5 a-trous levels (steps 1, 2, 4, 8, 16)");
+  const size_t n = (size_t)r->W * r->H;
+  lucent_status st;
+  if ((st = r->den_a.reserve(n * 16)) || (st = r->den_b.reserve(n * 16)) || (st = r->guide0.reserve(n * 16)) ||
+      (st = r->guide1.reserve(n * 16)))
+    return st;
+  r->denoised = denoise_run(accum_of(r), r->cam, (int)r->W, (int)r->H, (int)levels, sigma_l, sigma_n, sigma_p,
+                            (float4*)r->den_a.ptr, (float4*)r->den_b.ptr, (float4*)r->guide0.ptr,
+                            (float4*)r->guide1.ptr, (cudaStream_t)stream);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "denoise launch");
+}
+
+lucent_status lucent_renderer_read_denoised(lucent_renderer* r, float* out4) {
+  lucent_status st = lucent_renderer_check(r, nullptr);
+  if (st) return st;
+  if (!out4) return fail(LUCENT_ERR_INVALID, "null output");
+  if (!r->denoised) return fail(LUCENT_ERR_INVALID, "no denoised image since the last reset");
+  cudaError_t e = cudaMemcpy(out4, r->denoised, (size_t)r->W * r->H * 16, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "read denoised");
+}
+
+lucent_status lucent_renderer_display(lucent_renderer* r, float denoise_weight, int32_t tonemap, float exposure,
+                                      uint8_t* rgba8_out, float* rgb_out, void* stream) {
+  clear_error();
+  if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  if (tonemap < 0 || tonemap > 2) return fail(LUCENT_ERR_INVALID, "tonemap must be 0 (ACES), 1 (Reinhard) or 2 (none)");
+  if (!(denoise_weight >= 0.f && denoise_weight <= 1.f)) return fail(LUCENT_ERR_INVALID, "denoise weight outside [0, 1]");
+  if (denoise_weight > 0.f && !r->denoised)
+    return fail(LUCENT_ERR_INVALID, "denoise weight > 0 with no denoised image since the last reset");
+  const size_t n = (size_t)r->W * r->H;
+  lucent_status st = r->disp.reserve(n * 16);
+  if (st) return st;
+  uchar4* d8 = (uchar4*)r->disp.ptr;
+  float* drgb = (float*)((char*)r->disp.ptr + n * 4);
+  cudaStream_t s = (cudaStream_t)stream;
+  display_run(accum_of(r), denoise_weight > 0.f ? r->denoised : nullptr, (int)r->W, (int)r->H, denoise_weight,
+              exposure, tonemap, rgba8_out ? d8 : nullptr, rgb_out ? drgb : nullptr, s);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && rgba8_out) e = cudaMemcpyAsync(rgba8_out, d8, n * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && rgb_out) e = cudaMemcpyAsync(rgb_out, drgb, n * 12, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "display");
 }
 
 lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out) {

@@ -84,4 +84,16 @@ struct PhaseEvents {
 
 void render_batch(const RenderLaunch& R, cudaStream_t s, PhaseEvents* pe);
 
+// sheenAlbedoLUT (16 x 16) rounded to half precision, as the reference uploads it.
+void sheen_lut_half(float* out);
+
+// Denoiser (variance + `levels` a-trous steps of spacing 1, 2, 4, ...): fa,
+// fb are W*H float4 ping-pong targets, g0, g1 W*H float4 guide buffers.
+// Returns fa or fb, whichever holds the result.
+float4* denoise_run(AccumDev A, const sh::CameraDev& cam, int W, int H, int levels, float sigma_l, float sigma_n,
+                    float sigma_p, float4* fa, float4* fb, float4* g0, float4* g1, cudaStream_t s);
+// Display pass: RGBA8 and/or the pre-quantization RGB floats (either may be null).
+void display_run(AccumDev A, const float4* den, int W, int H, float weight, float exposure, int tonemap,
+                 uchar4* rgba8, float* rgb, cudaStream_t s);
+
 }  // namespace lucent

@@ -36,6 +36,12 @@ class RenderSettings:
     tonemap: str = "aces"
     firefly_clamp: float = 8.0
     denoise: bool = True
+    samples_per_frame: int = 1
+    max_samples: int = 0
+
+
+TONEMAPS = {"aces": 0, "reinhard": 1, "none": 2}  # display.frag uTonemap
+SIGMA_L, SIGMA_N, SIGMA_P = 4.0, 64.0, 1.5  # runDenoiser uniforms (renderer.ts:815-817)
 
 
 def _f(a):
@@ -174,6 +180,51 @@ class Renderer:
     def set_profiling(self, enabled=True):
         N.check(N.lib().lucent_renderer_set_profiling(self._h, 1 if enabled else 0))
 
+    # --------------------------------------------------------- denoise/display
+    def samples(self):
+        """Samples behind the current average (the reference's `frame`)."""
+        return self.stats()["samples"]
+
+    def denoise(self, levels=None, sigma_l=SIGMA_L, sigma_n=SIGMA_N, sigma_p=SIGMA_P, stream=None):
+        """runDenoiser (renderer.ts:788-830): variance, then atrousLevels(frame) a-trous steps."""
+        if levels is None:
+            levels = atrous_levels(self.samples())
+        N.check(N.lib().lucent_renderer_denoise(self._h, levels, sigma_l, sigma_n, sigma_p, stream))
+
+    def read_denoised(self):
+        """Filtered illumination (rgb) and variance (a), [H, W, 4], row 0 = bottom."""
+        out = np.empty(self.width * self.height * 4, np.float32)
+        N.check(N.lib().lucent_renderer_read_denoised(self._h, _f(out)))
+        return out.reshape(self.height, self.width, 4)
+
+    def display(self, denoise_weight=0.0, exposure=None, tonemap=None, want_float=False, stream=None):
+        """The display pass (renderer.ts:573-591): RGBA8 canvas [H, W, 4], row 0 = bottom;
+        with want_float also the RGB values before quantization."""
+        exposure = self.settings.exposure if exposure is None else exposure
+        tm = TONEMAPS[self.settings.tonemap if tonemap is None else tonemap]
+        n = self.width * self.height
+        rgba = np.empty(n * 4, np.uint8)
+        rgb = np.empty(n * 3, np.float32) if want_float else None
+        N.check(N.lib().lucent_renderer_display(self._h, denoise_weight, tm, exposure, N.ptr(rgba, C.c_uint8),
+                                                _f(rgb), stream))
+        img = rgba.reshape(self.height, self.width, 4)
+        return (img, rgb.reshape(self.height, self.width, 3)) if want_float else img
+
+    def render(self):
+        """render() (renderer.ts:553-611) with a fixed samples_per_frame budget:
+        trace, filter when the denoiser is on, present. Returns the RGBA8 canvas."""
+        st = self.settings
+        frame = self.samples()
+        remaining = st.max_samples - frame if st.max_samples > 0 else st.samples_per_frame
+        n = max(0, min(st.samples_per_frame, remaining))
+        if n:
+            self.trace_samples(n)
+            frame += n
+        weight = denoise_weight(frame) if st.denoise and frame > 0 else 0.0
+        if weight > 0:
+            self.denoise(atrous_levels(frame))
+        return self.display(weight)
+
     def benchmark(self, samples):
         """benchmark(n) (renderer.ts:745-777): one warm-up sample, then `samples` timed."""
         self.reset()
@@ -185,3 +236,13 @@ class Renderer:
         trace_ms = (time.perf_counter() - t0) * 1e3
         return {"trace_ms": trace_ms, "mpaths_per_sec": samples * self.width * self.height / (trace_ms / 1e3) / 1e6,
                 "width": self.width, "height": self.height}
+
+
+def bsdf_eval_tuples(tuples):
+    """The renderer's BSDF code on [n, 32] float tuples -> [n, 24] float32
+    (layout in csrc/bsdf_tuples.cu: evalOpaque f, pdf; sampleOpaque dir,
+    weight, pdf; sampleDielectric ok, dir, weight, reflected)."""
+    t = np.ascontiguousarray(tuples, np.float32).reshape(-1, 32)
+    out = np.zeros((t.shape[0], 24), np.float32)
+    N.check(N.lib().lucent_bsdf_eval_tuples(_f(t), t.shape[0], _f(out)))
+    return out

@@ -1209,6 +1209,193 @@ int orc_render_work(const orc_scene* s, const orc_camera* cam, uint32_t max_boun
                      albedo4, normal4, history, threads, work_out, detailed != 0);
 }
 
+// ---------------------------------------------------------------------------
+// Denoiser: variance.frag :15-55, atrous.frag :77-137, denoise.glsl :10-25;
+// driven as runDenoiser (renderer.ts:788-830). Binary32 like the GLSL.
+// Buffers are W x H, row 0 = bottom; color4/out4 RGBA, albedo4/normal4 RGBA.
+// ---------------------------------------------------------------------------
+static inline float lumf(float r, float g, float b) { return r * 0.2126f + g * 0.7152f + b * 0.0722f; }
+
+static inline void unit_normal(const float* n, float* o) {  // denoise.glsl:21-24
+  const float l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  if (l > 1e-6f) {
+    o[0] = n[0] / l, o[1] = n[1] / l, o[2] = n[2] / l;
+  } else {
+    o[0] = 0.f, o[1] = 0.f, o[2] = 1.f;
+  }
+}
+
+int orc_denoise(const float* color4, const float* albedo4, const float* normal4, const float* history, uint32_t w,
+                uint32_t h, const orc_camera* cam, uint32_t levels, float sigma_l, float sigma_n, float sigma_p,
+                float* out4) {
+  const int W = (int)w, H = (int)h;
+  std::vector<float> a((size_t)W * H * 4), b((size_t)W * H * 4);
+  auto inside = [&](int x, int y) { return x >= 0 && y >= 0 && x < W && y < H; };
+  // variance.frag
+  for (int y = 0; y < H; y++)
+    for (int x = 0; x < W; x++) {
+      const size_t p = (size_t)y * W + x;
+      const float* c = color4 + 4 * p;
+      const float* al = albedo4 + 4 * p;
+      float* o = a.data() + 4 * p;
+      if (al[3] < 0.5f) {
+        o[0] = c[0], o[1] = c[1], o[2] = c[2], o[3] = 0.f;
+        continue;
+      }
+      const float illum[3] = {c[0] / std::max(al[0], 1e-3f), c[1] / std::max(al[1], 1e-3f), c[2] / std::max(al[2], 1e-3f)};
+      const float samples = std::max(history[p], 1.0f);
+      const float la = std::max(lumf(al[0], al[1], al[2]), 1e-3f);
+      float variance;
+      if (samples >= 4.0f) {
+        const float l = lumf(c[0], c[1], c[2]);
+        variance = std::max(0.0f, c[3] - l * l) / (la * la) / samples;
+      } else {
+        const float* np = normal4 + 4 * p;
+        float n[3];
+        unit_normal(np, n);
+        float s1 = 0, s2 = 0, ws = 0;
+        for (int dy = -3; dy <= 3; dy++)
+          for (int dx = -3; dx <= 3; dx++) {
+            const int qx = x + dx, qy = y + dy;
+            if (!inside(qx, qy)) continue;
+            const size_t q = (size_t)qy * W + qx;
+            const float* aq = albedo4 + 4 * q;
+            if (aq[3] < 0.5f) continue;
+            const float* nq = normal4 + 4 * q;
+            float un[3];
+            unit_normal(nq, un);
+            const float cosn = std::max(0.0f, n[0] * un[0] + n[1] * un[1] + n[2] * un[2]);
+            const float stepv = (0.1f * np[3] < std::fabs(np[3] - nq[3])) ? 0.0f : 1.0f;  // step(|dz|, 0.1 z)
+            const float wgt = std::pow(cosn, 32.0f) * stepv;
+            const float* cq = color4 + 4 * q;
+            const float l = lumf(cq[0] / std::max(aq[0], 1e-3f), cq[1] / std::max(aq[1], 1e-3f), cq[2] / std::max(aq[2], 1e-3f));
+            s1 += wgt * l;
+            s2 += wgt * l * l;
+            ws += wgt;
+          }
+        const float m1 = s1 / std::max(ws, 1e-6f);
+        variance = std::max(0.0f, s2 / std::max(ws, 1e-6f) - m1 * m1) / samples;
+      }
+      o[0] = illum[0], o[1] = illum[1], o[2] = illum[2], o[3] = variance;
+    }
+  // atrous.frag, steps 1, 2, 4, 8, 16 (renderer.ts:140)
+  const float F[3] = {cam->forward[0], cam->forward[1], cam->forward[2]};
+  const float Rt[3] = {cam->right[0], cam->right[1], cam->right[2]};
+  const float U[3] = {cam->up[0], cam->up[1], cam->up[2]};
+  const float CP[3] = {cam->pos[0], cam->pos[1], cam->pos[2]};
+  const float th = cam->tan_half_fov;
+  auto primary_dir = [&](int x, int y, float* d) {  // atrous.frag:77-81
+    const float ux = ((float)x + 0.5f) / (float)W * 2.0f - 1.0f, uy = ((float)y + 0.5f) / (float)H * 2.0f - 1.0f;
+    const float aspect = (float)W / (float)H;
+    float v[3];
+    for (int k = 0; k < 3; k++) v[k] = F[k] + Rt[k] * (ux * aspect * th) + U[k] * (uy * th);
+    const float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    for (int k = 0; k < 3; k++) d[k] = v[k] / l;
+  };
+  const float hk[3] = {0.375f, 0.25f, 0.0625f};
+  float* in = a.data();
+  float* outb = b.data();
+  for (uint32_t lv = 0; lv < levels; lv++) {
+    const int stepv = 1 << lv;
+    for (int y = 0; y < H; y++)
+      for (int x = 0; x < W; x++) {
+        const size_t p = (size_t)y * W + x;
+        const float* cp = in + 4 * p;
+        float* o = outb + 4 * p;
+        if (albedo4[4 * p + 3] < 0.5f) {
+          o[0] = cp[0], o[1] = cp[1], o[2] = cp[2], o[3] = cp[3];
+          continue;
+        }
+        const float* np = normal4 + 4 * p;
+        float n[3], dp[3], P[3];
+        unit_normal(np, n);
+        primary_dir(x, y, dp);
+        for (int k = 0; k < 3; k++) P[k] = CP[k] + dp[k] * np[3];
+        const float footprint = 2.0f * th * np[3] / (float)H;
+        float var = 0, wv = 0;
+        for (int dy = -1; dy <= 1; dy++)
+          for (int dx = -1; dx <= 1; dx++) {
+            const int qx = x + dx, qy = y + dy;
+            if (!inside(qx, qy)) continue;
+            const float k = (dx == 0 ? 0.5f : 0.25f) * (dy == 0 ? 0.5f : 0.25f);
+            var += in[4 * ((size_t)qy * W + qx) + 3] * k;
+            wv += k;
+          }
+        const float denom = sigma_l * std::sqrt(std::max(var / wv, 0.0f)) + 1e-6f;
+        const float lp = lumf(cp[0], cp[1], cp[2]);
+        float sum[3] = {cp[0] * (hk[0] * hk[0]), cp[1] * (hk[0] * hk[0]), cp[2] * (hk[0] * hk[0])};
+        float sumVar = cp[3] * (hk[0] * hk[0]) * (hk[0] * hk[0]);
+        float wsum = hk[0] * hk[0];
+        for (int dy = -2; dy <= 2; dy++)
+          for (int dx = -2; dx <= 2; dx++) {
+            if (dx == 0 && dy == 0) continue;
+            const int qx = x + dx * stepv, qy = y + dy * stepv;
+            if (!inside(qx, qy)) continue;
+            const size_t q = (size_t)qy * W + qx;
+            if (albedo4[4 * q + 3] < 0.5f) continue;
+            const float* cq = in + 4 * q;
+            const float* nq = normal4 + 4 * q;
+            const float k = hk[std::abs(dx)] * hk[std::abs(dy)];
+            float un[3], dq[3], Q[3];
+            unit_normal(nq, un);
+            const float wn = std::pow(std::max(0.0f, n[0] * un[0] + n[1] * un[1] + n[2] * un[2]), sigma_n);
+            primary_dir(qx, qy, dq);
+            for (int c = 0; c < 3; c++) Q[c] = CP[c] + dq[c] * nq[3];
+            const float reach = sigma_p * footprint * (float)stepv * std::sqrt((float)(dx * dx + dy * dy));
+            const float pd = n[0] * (Q[0] - P[0]) + n[1] * (Q[1] - P[1]) + n[2] * (Q[2] - P[2]);
+            const float wp = std::exp(-std::fabs(pd) / (reach + 1e-6f));
+            const float wl = std::exp(-std::fabs(lp - lumf(cq[0], cq[1], cq[2])) / denom);
+            const float wgt = k * wn * wp * wl;
+            for (int c = 0; c < 3; c++) sum[c] += cq[c] * wgt;
+            sumVar += cq[3] * wgt * wgt;
+            wsum += wgt;
+          }
+        o[0] = sum[0] / wsum, o[1] = sum[1] / wsum, o[2] = sum[2] / wsum, o[3] = sumVar / (wsum * wsum);
+      }
+    std::swap(in, outb);
+  }
+  std::memcpy(out4, in, (size_t)W * H * 16);
+  return 0;
+}
+
+// display.frag :42-67 with uRenderSize == uViewSize. out_rgb: the value
+// written to the RGBA8 target before quantization (dither included).
+int orc_display(const float* color4, const float* albedo4, const float* denoised4, uint32_t w, uint32_t h,
+                float denoise_weight, float exposure, int tonemap, float* out_rgb) {
+  for (uint32_t y = 0; y < h; y++)
+    for (uint32_t x = 0; x < w; x++) {
+      const size_t p = (size_t)y * w + x;
+      float c[3] = {color4[4 * p], color4[4 * p + 1], color4[4 * p + 2]};
+      if (denoise_weight > 0.0f) {
+        const float* a = albedo4 + 4 * p;
+        if (a[3] >= 0.5f)
+          for (int k = 0; k < 3; k++) {
+            const float dn = denoised4[4 * p + k] * std::max(a[k], 1e-3f);
+            c[k] = c[k] * (1.0f - denoise_weight) + dn * denoise_weight;
+          }
+      }
+      const float ign = [&]() {
+        const float fx = (float)x + 0.5f, fy = (float)y + 0.5f;
+        const float t = 0.06711056f * fx + 0.00583715f * fy;
+        const float f1 = t - std::floor(t);
+        const float u = 52.9829189f * f1;
+        return u - std::floor(u);
+      }();
+      for (int k = 0; k < 3; k++) {
+        float v = c[k] * exposure;
+        if (tonemap == 0)
+          v = std::min(std::max((v * (2.51f * v + 0.03f)) / (v * (2.43f * v + 0.59f) + 0.14f), 0.0f), 1.0f);
+        else if (tonemap == 1)
+          v = v / (1.0f + v);
+        v = std::min(std::max(v, 0.0f), 1.0f);
+        const float lo = v * 12.92f, hi = 1.055f * std::pow(v, 1.0f / 2.4f) - 0.055f;
+        v = v < 0.0031308f ? lo : hi;  // mix(lo, hi, step(0.0031308, c))
+        out_rgb[3 * p + k] = v + (ign - 0.5f) / 255.0f;
+      }
+    }
+  return 0;
+}
+
 // BSDF tuples. in: 32 floats per tuple
 //   0-2 albedo, 3 metallic, 4 roughness, 5 ior, 6 clearcoat, 7 clearcoatRoughness,
 //   8-10 sheenColor, 11 sheenRoughness, 12 thinWalled, 13-15 n, 16-18 nc,

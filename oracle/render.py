@@ -40,9 +40,8 @@ def declare(L):
                                   P(F), P(F), P(F), C.c_int, C.c_int, P(C.c_uint64)]
     L.orc_bsdf_tuples.argtypes = [P(F), C.c_uint64, C.c_int, P(D), C.c_int]
     L.orc_bsdf_set_lut.argtypes = [P(F)]
-    if hasattr(L, "orc_denoise"):
-        L.orc_denoise.argtypes = [P(F), P(F), P(F), P(F), U32, U32, P(OrcCamera), U32, F, F, F, P(F)]
-        L.orc_display.argtypes = [P(F), P(F), P(F), U32, U32, F, F, C.c_int, P(F)]
+    L.orc_denoise.argtypes = [P(F), P(F), P(F), P(F), U32, U32, P(OrcCamera), U32, F, F, F, P(F)]
+    L.orc_display.argtypes = [P(F), P(F), P(F), U32, U32, F, F, C.c_int, P(F)]
 
 
 def half_lut():
@@ -161,4 +160,31 @@ def bsdf_tuples(tuples, precision=64, threads=0):
     lib().orc_bsdf_set_lut(_p(lut, F))
     out = np.zeros((t.shape[0], 24), np.float64)
     lib().orc_bsdf_tuples(_p(t, F), t.shape[0], precision, _p(out, D), threads)
+    return out
+
+
+def _c32(a, shape):
+    return np.ascontiguousarray(np.asarray(a, np.float32).reshape(shape))
+
+
+def denoise(color4, albedo4, normal4, history, camera, levels, sigma_l=4.0, sigma_n=64.0, sigma_p=1.5):
+    """orc_denoise: variance + `levels` a-trous steps over [H, W, 4] targets
+    (albedo/normal as the RGBA16F values). `camera` is an OrcCamera.
+    Returns [H, W, 4] float32 (illumination rgb, variance)."""
+    h, w = color4.shape[:2]
+    c, a, n = (_c32(x, (h, w, 4)) for x in (color4, albedo4, normal4))
+    hi = _c32(history, (h, w))
+    out = np.zeros((h, w, 4), np.float32)
+    lib().orc_denoise(_p(c, F), _p(a, F), _p(n, F), _p(hi, F), w, h, C.byref(camera), levels, sigma_l, sigma_n,
+                      sigma_p, _p(out, F))
+    return out
+
+
+def display(color4, albedo4, denoised4, denoise_weight, exposure=1.0, tonemap=0):
+    """orc_display: [H, W, 3] float32 values written to the RGBA8 canvas before quantization."""
+    h, w = color4.shape[:2]
+    c, a = _c32(color4, (h, w, 4)), _c32(albedo4, (h, w, 4))
+    d = _c32(denoised4 if denoised4 is not None else np.zeros((h, w, 4)), (h, w, 4))
+    out = np.zeros((h, w, 3), np.float32)
+    lib().orc_display(_p(c, F), _p(a, F), _p(d, F), w, h, denoise_weight, exposure, tonemap, _p(out, F))
     return out
