@@ -247,6 +247,11 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
  * the reference's GPU timer queries, renderer.ts:668-700); results appear in
  * lucent_render_stats.phase_ms after lucent_renderer_check. */
 lucent_status lucent_renderer_set_profiling(lucent_renderer* r, int32_t enabled);
+/* Frees the path-state buffers (about 315 bytes per path of the largest
+ * wave traced so far); the next trace allocates them again. For hosts that
+ * keep many renderers alive but trace one at a time. No reference
+ * counterpart (WebGL owns the reference's render targets). */
+lucent_status lucent_renderer_trim(lucent_renderer* r);
 
 /* runDenoiser (renderer.ts:788-830; variance.frag, atrous.frag,
  * denoise.glsl): per-pixel variance of the demodulated illumination, then
@@ -269,6 +274,41 @@ lucent_status lucent_renderer_read_denoised(lucent_renderer* r, float* out4);
  * quantization to host memory (either may be NULL); synchronous. */
 lucent_status lucent_renderer_display(lucent_renderer* r, float denoise_weight, int32_t tonemap, float exposure,
                                       uint8_t* rgba8_out, float* rgb_out, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Multi-scene batches. No reference counterpart: the reference renders one
+ * scene per WebGL context. A batch traces the next `samples` samples of
+ * several renderers (each with its own scene, lighting, camera, settings and
+ * targets) as one wavefront: every kernel of a bounce covers the paths of all
+ * scenes, so small scenes and the short last bounces of each one share the
+ * GPU. The result equals lucent_renderer_trace(r, samples) on each renderer
+ * in turn, sample for sample and bit for bit (same kernels, same random
+ * streams, same per-pixel accumulation order).
+ * ------------------------------------------------------------------------- */
+typedef struct lucent_batch lucent_batch;
+typedef struct lucent_batch_options {
+  uint32_t samples_per_wave; /* samples of every pixel per wave; 0 = as many as max_wave_paths allows */
+  uint32_t max_wave_paths;   /* path-state budget of one wave (about 315 bytes of device memory per path) */
+  int32_t use_graph;         /* capture a full wave once as a CUDA graph and replay it */
+  uint32_t trace_blocks;     /* grid of the persistent traversal kernels; 0 = all resident blocks */
+  uint32_t shade_blocks;     /* grid of the shade / resolve kernels; 0 = all resident blocks */
+} lucent_batch_options;
+typedef struct lucent_batch_stats {
+  uint64_t closest_rays, shadow_rays; /* traced by this batch since creation */
+  uint32_t waves, graph_waves;        /* waves launched, of which replayed graphs */
+  uint32_t wave_paths;                /* path capacity of a wave */
+} lucent_batch_stats;
+/* The renderers must stay alive (and keep their scenes loaded) while the
+ * batch is used; they may be traced on their own in between. */
+lucent_status lucent_batch_create(lucent_renderer* const* renderers, uint32_t n, lucent_batch** out);
+void lucent_batch_destroy(lucent_batch* batch);
+/* Defaults: samples_per_wave 0, max_wave_paths 2^25, use_graph 1, trace_blocks 0, shade_blocks 0. */
+lucent_status lucent_batch_set_options(lucent_batch* batch, const lucent_batch_options* options);
+/* Asynchronous on `stream`. */
+lucent_status lucent_batch_trace(lucent_batch* batch, uint32_t samples, void* stream);
+/* Synchronises `stream`, reports the device error word and (if `stats` is
+ * non-NULL) the batch's counters. */
+lucent_status lucent_batch_check(lucent_batch* batch, void* stream, lucent_batch_stats* stats);
 
 /* Diagnostic with no reference counterpart: evaluates the path tracer's
  * BSDF code (the device restatement of bsdf.glsl evalOpaque :114-166,

@@ -62,6 +62,7 @@ def _declare(L):
     try:
         from . import _native_render
         _native_render.declare(L, _sig)
+        _native_render.declare_batch(L, _sig)
     except ImportError:
         pass
 

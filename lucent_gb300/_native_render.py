@@ -55,7 +55,26 @@ def declare(L, sig):
     sig(L, "lucent_renderer_read", [VP, F32P, F32P, F32P, F32P])
     sig(L, "lucent_renderer_stats", [VP, P(RenderStats)])
     sig(L, "lucent_renderer_set_profiling", [VP, C.c_int32])
+    sig(L, "lucent_renderer_trim", [VP])
     sig(L, "lucent_renderer_denoise", [VP, C.c_uint32, C.c_float, C.c_float, C.c_float, VP])
     sig(L, "lucent_renderer_display", [VP, C.c_float, C.c_int32, C.c_float, U8P, F32P, VP])
     sig(L, "lucent_renderer_read_denoised", [VP, F32P])
     sig(L, "lucent_bsdf_eval_tuples", [F32P, C.c_uint32, F32P])
+
+
+class BatchOptions(C.Structure):
+    _fields_ = [("samples_per_wave", C.c_uint32), ("max_wave_paths", C.c_uint32), ("use_graph", C.c_int32),
+                ("trace_blocks", C.c_uint32), ("shade_blocks", C.c_uint32)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("closest_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("waves", C.c_uint32),
+                ("graph_waves", C.c_uint32), ("wave_paths", C.c_uint32)]
+
+
+def declare_batch(L, sig):
+    sig(L, "lucent_batch_create", [P(VP), C.c_uint32, P(VP)])
+    sig(L, "lucent_batch_destroy", [VP], None)
+    sig(L, "lucent_batch_set_options", [VP, P(BatchOptions)])
+    sig(L, "lucent_batch_trace", [VP, C.c_uint32, VP])
+    sig(L, "lucent_batch_check", [VP, VP, P(BatchStats)])

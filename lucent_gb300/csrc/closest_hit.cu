@@ -24,7 +24,8 @@ struct ApiPolicy {
   __device__ uint32_t count() const { return n; }
   __device__ void ray(uint32_t k, float3& o, float3& d) const { load_ray6(rays, k, o, d); }
   __device__ uint32_t key(uint32_t) const { return 0; }
-  __device__ bool alpha(int, uint32_t) const { return true; }
+  static constexpr bool kMultiScene = false;
+  __device__ bool alpha(int, int, uint32_t) const { return true; }
   __device__ bool alpha_any() const { return false; }
   // intersectBVH's t, u, v are binary64 values: always confirmed in binary64.
   __device__ bool exact_output() const { return true; }
@@ -52,7 +53,7 @@ __global__ void k_closest_exact_d(TravArgs A, const double* __restrict__ rays, u
     const double* r = rays + (size_t)i * 6;
     int slot;
     double t = 0, u = 0, v = 0;
-    if (!trace_exact(A, P, {r[0], r[1], r[2]}, {r[3], r[4], r[5]}, 0, slot, t, u, v)) {
+    if (!trace_exact(A, P, bvh_of(A, P, i), {r[0], r[1], r[2]}, {r[3], r[4], r[5]}, 0, slot, t, u, v)) {
       prim[i] = -2;
     } else if (slot < 0) {
       prim[i] = -1;

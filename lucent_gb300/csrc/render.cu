@@ -45,8 +45,9 @@ struct PathClosest {
   }
   __device__ uint32_t key(uint32_t k) const { return rng[queue[k]]; }
   __device__ bool alpha_any() const { return any_alpha != 0; }
+  static constexpr bool kMultiScene = false;
   // alphaOpaque (scene.glsl:284-297) with constant alpha.
-  __device__ bool alpha(int slot, uint32_t key) const {
+  __device__ bool alpha(int, int slot, uint32_t key) const {
     if (__ldg(&geo[3 * (size_t)slot + 2].w) < 0.5f) return true;
     const int m = (int)__ldg(&geo[3 * (size_t)slot].w);
     const float alpha = __ldg(&mats[m * 10 + 2].w);
@@ -85,8 +86,85 @@ struct PathShadow {
   __device__ double tmax(uint32_t k) const { return (double)so[queue[k]].w; }
   __device__ uint32_t key(uint32_t k) const { return __float_as_uint(sd[queue[k]].w); }
   __device__ bool alpha_any() const { return any_alpha != 0; }
-  __device__ bool alpha(int slot, uint32_t key) const {
-    return PathClosest{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, geo, mats, any_alpha}.alpha(slot, key);
+  static constexpr bool kMultiScene = false;
+  __device__ bool alpha(int, int slot, uint32_t key) const {
+    return PathClosest{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, geo, mats, any_alpha}.alpha(0, slot, key);
+  }
+  __device__ void shadow(uint32_t k, bool occluded) const { occ[queue[k]] = occluded ? 1 : 0; }
+};
+
+// Policies for waves holding the paths of several scenes: a path's scene is
+// sid[path]; its BVH, triangles and materials come from the scene table.
+__device__ __forceinline__ bool alpha_opaque(const float4* geo, const float4* mats, int slot, uint32_t key) {
+  return PathClosest{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, geo, mats, 1}.alpha(0, slot, key);
+}
+
+struct PathClosestMulti {
+  const uint32_t* cnt;
+  const uint32_t* queue;
+  const float4* ro;
+  const float4* rd;
+  const uint32_t* rng;
+  float4* hits;
+  const SceneRec* recs;
+  const uint16_t* sid;
+  int any_alpha;
+  static constexpr bool kMultiScene = true;
+  __device__ uint32_t count() const { return *cnt; }
+  __device__ void ray(uint32_t k, float3& o, float3& d) const {
+    const uint32_t p = queue[k];
+    const float4 a = ro[p], b = rd[p];
+    o = make_float3(a.x, a.y, a.z);
+    d = make_float3(b.x, b.y, b.z);
+  }
+  __device__ BvhView bvh(uint32_t k) const {
+    const int sc = __ldg(sid + queue[k]);
+    const SceneDev& S = recs[sc].scene;
+    return {S.nodes, S.geo, S.node_count, sc};
+  }
+  __device__ uint32_t key(uint32_t k) const { return rng[queue[k]]; }
+  __device__ bool alpha_any() const { return any_alpha != 0; }
+  __device__ bool alpha(int sc, int slot, uint32_t key) const {
+    return alpha_opaque(recs[sc].scene.geo, recs[sc].scene.materials, slot, key);
+  }
+  __device__ bool exact_output() const { return false; }
+  __device__ void hit32(uint32_t k, int slot, float3 e) const {
+    hits[queue[k]] = make_float4(e.x, e.y, e.z, __int_as_float(slot));
+  }
+  __device__ void hit(uint32_t k, int slot, double t, double u, double v) const {
+    hits[queue[k]] = make_float4(__double2float_rn(t), __double2float_rn(u), __double2float_rn(v), __int_as_float(slot));
+  }
+  __device__ void miss(uint32_t k) const { hits[queue[k]] = make_float4(INF, 0.f, 0.f, __int_as_float(-1)); }
+  __device__ void fail(uint32_t k) const { miss(k); }
+};
+
+struct PathShadowMulti {
+  const uint32_t* cnt;
+  const uint32_t* queue;
+  const float4* so;
+  const float4* sd;
+  uint8_t* occ;
+  const SceneRec* recs;
+  const uint16_t* sid;
+  int any_alpha;
+  static constexpr bool kMultiScene = true;
+  __device__ uint32_t count() const { return *cnt; }
+  __device__ void ray(uint32_t k, float3& o, float3& d) const {
+    const uint32_t s = queue[k];
+    const float4 a = so[s], b = sd[s];
+    o = make_float3(a.x, a.y, a.z);
+    d = make_float3(b.x, b.y, b.z);
+  }
+  __device__ BvhView bvh(uint32_t k) const {
+    const int sc = __ldg(sid + queue[k] / 3);  // shadow slot 3 * path + j
+    const SceneDev& S = recs[sc].scene;
+    return {S.nodes, S.geo, S.node_count, sc};
+  }
+  __device__ double tmax(uint32_t k) const { return (double)so[queue[k]].w; }
+  __device__ uint32_t key(uint32_t k) const { return __float_as_uint(sd[queue[k]].w); }
+  __device__ bool alpha_any() const { return any_alpha != 0; }
+  __device__ bool alpha(int sc, int slot, uint32_t key) const {
+    return alpha_opaque(recs[sc].scene.geo, recs[sc].scene.materials, slot, key);
   }
   __device__ void shadow(uint32_t k, bool occluded) const { occ[queue[k]] = occluded ? 1 : 0; }
 };
@@ -94,33 +172,61 @@ struct PathShadow {
 // ------------------------------------------------------------ kernels
 constexpr unsigned kSpecular = 1u, kGuideDone = 2u;
 
+// cameraRay (trace.frag:53-62) and the path's initial state; sample s of
+// pixel `pixel` draws from the stream seeded with (pixel, seed0 + s).
+__device__ __forceinline__ void camera_path(const Paths& P, uint32_t p, uint32_t pixel, uint32_t s,
+                                            const CameraDev& cam, int W, int H, uint32_t seed0) {
+  const uint32_t x = pixel % W, y = pixel / W;
+  uint32_t st = pixel * 1973u + (seed0 + s) * 9277u + 26699u;  // trace.frag:327-328
+  pcg(st);
+  const float j0 = rnd(st), j1 = rnd(st);
+  const float ux = ((float)x + 0.5f + j0) / (float)W * 2.f - 1.f;
+  const float uy = ((float)y + 0.5f + j1) / (float)H * 2.f - 1.f;
+  const float aspect = (float)W / (float)H;
+  const float3 dir = norm3(cam.forward + cam.right * (ux * aspect * cam.tan_half_fov) + cam.up * (uy * cam.tan_half_fov));
+  const float3 focus = cam.pos + dir * (cam.focus / dot3(dir, cam.forward));
+  const float l0 = rnd(st), l1 = rnd(st);
+  const float2 lens = concentric_disk(l0, l1);
+  const float3 ro = cam.pos + cam.right * (lens.x * cam.aperture) + cam.up * (lens.y * cam.aperture);
+  const float3 rd = norm3(focus - ro);
+  P.ro[p] = make_float4(ro.x, ro.y, ro.z, 0.f);
+  P.rd[p] = make_float4(rd.x, rd.y, rd.z, 0.f);
+  P.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+  P.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+  P.tint[p] = make_float4(1.f, 1.f, 1.f, __uint_as_float(kSpecular));
+  P.galb[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+  P.gnrm[p] = make_float4(-rd.x, -rd.y, -rd.z, 1e4f);
+  P.rng[p] = st;
+  P.q[0][p] = p;
+}
+
 __global__ void k_camera(Paths P, CameraDev cam, int W, int H, int S, uint32_t seed0) {
   const uint32_t WH = (uint32_t)W * H, total = WH * S;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x)
+    camera_path(P, p, p % WH, p / WH, cam, W, H, seed0);
+  if (blockIdx.x == 0 && threadIdx.x == 0) P.ctr[kCtrQ0] = total;
+}
+
+// Index of the scene whose range [base[i], base[i + 1]) holds v (n scenes).
+__device__ __forceinline__ int find_scene(const uint32_t* __restrict__ base, int n, uint32_t v) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(base + mid) <= v) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Several scenes in one wave: scene i owns paths [path_base[i], path_base[i + 1]).
+__global__ void k_camera_multi(Paths P, const SceneRec* __restrict__ recs, const uint32_t* __restrict__ path_base,
+                               int n, uint16_t* __restrict__ sid, int S) {
+  const uint32_t total = __ldg(path_base + n);
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
-    const uint32_t pixel = p % WH, s = p / WH;
-    const uint32_t x = pixel % W, y = pixel / W;
-    uint32_t st = pixel * 1973u + (seed0 + s) * 9277u + 26699u;  // trace.frag:327-328
-    pcg(st);
-    // cameraRay (trace.frag:53-62)
-    const float j0 = rnd(st), j1 = rnd(st);
-    const float ux = ((float)x + 0.5f + j0) / (float)W * 2.f - 1.f;
-    const float uy = ((float)y + 0.5f + j1) / (float)H * 2.f - 1.f;
-    const float aspect = (float)W / (float)H;
-    const float3 dir = norm3(cam.forward + cam.right * (ux * aspect * cam.tan_half_fov) + cam.up * (uy * cam.tan_half_fov));
-    const float3 focus = cam.pos + dir * (cam.focus / dot3(dir, cam.forward));
-    const float l0 = rnd(st), l1 = rnd(st);
-    const float2 lens = concentric_disk(l0, l1);
-    const float3 ro = cam.pos + cam.right * (lens.x * cam.aperture) + cam.up * (lens.y * cam.aperture);
-    const float3 rd = norm3(focus - ro);
-    P.ro[p] = make_float4(ro.x, ro.y, ro.z, 0.f);
-    P.rd[p] = make_float4(rd.x, rd.y, rd.z, 0.f);
-    P.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
-    P.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-    P.tint[p] = make_float4(1.f, 1.f, 1.f, __uint_as_float(kSpecular));
-    P.galb[p] = make_float4(1.f, 1.f, 1.f, 0.f);
-    P.gnrm[p] = make_float4(-rd.x, -rd.y, -rd.z, 1e4f);
-    P.rng[p] = st;
-    P.q[0][p] = p;
+    const int sc = find_scene(path_base, n, p);
+    const SceneRec& R = recs[sc];
+    const uint32_t WH = (uint32_t)R.W * R.H, local = p - __ldg(path_base + sc);
+    camera_path(P, p, local % WH, local / WH, R.cam, R.W, R.H, R.seed0);
+    sid[p] = (uint16_t)sc;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) P.ctr[kCtrQ0] = total;
 }
@@ -147,13 +253,40 @@ __device__ __forceinline__ bool analytic_occluded(const SceneDev& S, float3 ro, 
   return hit_ground(S, ro, rd, tmax) < tmax;
 }
 
-__global__ void __launch_bounds__(128) k_shade(Paths P, SceneDev S, LightingDev L, int cur, int bounce,
-                                               int max_bounces, float uclamp) {
+// Where the shade kernel finds a path's scene, lighting and settings: one
+// scene per launch (kernel parameters) or a per-path scene index into a
+// table of SceneRec.
+struct OneScene {
+  SceneDev S;
+  LightingDev L;
+  int max_bounces;
+  float clamp;
+  __device__ const SceneDev& scene(uint32_t) const { return S; }
+  __device__ const LightingDev& light(uint32_t) const { return L; }
+  __device__ int bounces(uint32_t) const { return max_bounces; }
+  __device__ float uclamp(uint32_t) const { return clamp; }
+};
+struct SceneTable {
+  const SceneRec* recs;
+  const uint16_t* sid;
+  __device__ const SceneRec& rec(uint32_t p) const { return recs[__ldg(sid + p)]; }
+  __device__ const SceneDev& scene(uint32_t p) const { return rec(p).scene; }
+  __device__ const LightingDev& light(uint32_t p) const { return rec(p).light; }
+  __device__ int bounces(uint32_t p) const { return rec(p).max_bounces; }
+  __device__ float uclamp(uint32_t p) const { return rec(p).clamp; }
+};
+
+template <class Src>
+__global__ void __launch_bounds__(128) k_shade_t(Paths P, const __grid_constant__ Src src, int cur, int bounce) {
   const uint32_t n = P.ctr[kCtrQ0 + cur];
   const uint32_t* q = P.q[cur];
   uint32_t* qn = P.q[cur ^ 1];
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const uint32_t p = q[k];
+    const SceneDev& S = src.scene(p);
+    const LightingDev& L = src.light(p);
+    const int max_bounces = src.bounces(p);
+    const float uclamp = src.uclamp(p);
     float3 ro = f3(P.ro[p]), rd = f3(P.rd[p]);
     const float4 thr4 = P.thr[p], tint4 = P.tint[p];
     float3 thr = f3(thr4), rad = f3(P.rad[p]), tint = f3(tint4);
@@ -398,36 +531,58 @@ __global__ void k_resolve(Paths P, int cur) {
   }
 }
 
-// Running means (trace.frag:335-354), one thread per pixel, samples in order.
+// Running means (trace.frag:335-354) of one pixel over the batch's samples,
+// in order; sample s of the pixel is path path_base + s * W * H + px.
+__device__ __forceinline__ void accumulate_pixel(const Paths& P, const AccumDev& A, uint32_t WH, int S, uint32_t px,
+                                                 uint32_t path_base) {
+  float4 col = A.color[px];
+  float4 alb = make_float4(__half2float(A.albedo[px].x), __half2float(A.albedo[px].y), __half2float(A.albedo[px].z),
+                           __half2float(A.albedo[px].w));
+  float4 nrm = make_float4(__half2float(A.normal[px].x), __half2float(A.normal[px].y), __half2float(A.normal[px].z),
+                           __half2float(A.normal[px].w));
+  float n = A.history[px];
+  for (int s = 0; s < S; s++) {
+    const uint32_t p = path_base + (uint32_t)s * WH + px;
+    float4 c = P.rad[p];
+    if (isnan(c.x) || isnan(c.y) || isnan(c.z) || isinf(c.x) || isinf(c.y) || isinf(c.z)) c = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float l = lum(f3(c));
+    const float k = 1.f / (n + 1.f);
+    const float4 ga = P.galb[p], gn = P.gnrm[p];
+    col = make_float4(mixf(col.x, c.x, k), mixf(col.y, c.y, k), mixf(col.z, c.z, k), mixf(col.w, l * l, k));
+    // RGBA16F targets (renderer.ts:490): every store rounds to half.
+    alb = make_float4(__half2float(__float2half_rn(mixf(alb.x, ga.x, k))), __half2float(__float2half_rn(mixf(alb.y, ga.y, k))),
+                      __half2float(__float2half_rn(mixf(alb.z, ga.z, k))), __half2float(__float2half_rn(mixf(alb.w, ga.w, k))));
+    nrm = make_float4(__half2float(__float2half_rn(mixf(nrm.x, gn.x, k))), __half2float(__float2half_rn(mixf(nrm.y, gn.y, k))),
+                      __half2float(__float2half_rn(mixf(nrm.z, gn.z, k))), __half2float(__float2half_rn(mixf(nrm.w, gn.w, k))));
+    n = n + 1.f;
+  }
+  A.color[px] = col;
+  A.albedo[px] = make_half4(alb);
+  A.normal[px] = make_half4(nrm);
+  A.history[px] = n;
+}
+
 __global__ void k_accumulate(Paths P, AccumDev A, int W, int H, int S) {
   const uint32_t WH = (uint32_t)W * H;
-  for (uint32_t px = blockIdx.x * blockDim.x + threadIdx.x; px < WH; px += gridDim.x * blockDim.x) {
-    float4 col = A.color[px];
-    float4 alb = make_float4(__half2float(A.albedo[px].x), __half2float(A.albedo[px].y), __half2float(A.albedo[px].z),
-                             __half2float(A.albedo[px].w));
-    float4 nrm = make_float4(__half2float(A.normal[px].x), __half2float(A.normal[px].y), __half2float(A.normal[px].z),
-                             __half2float(A.normal[px].w));
-    float n = A.history[px];
-    for (int s = 0; s < S; s++) {
-      const uint32_t p = (uint32_t)s * WH + px;
-      float4 c = P.rad[p];
-      if (isnan(c.x) || isnan(c.y) || isnan(c.z) || isinf(c.x) || isinf(c.y) || isinf(c.z)) c = make_float4(0.f, 0.f, 0.f, 0.f);
-      const float l = lum(f3(c));
-      const float k = 1.f / (n + 1.f);
-      const float4 ga = P.galb[p], gn = P.gnrm[p];
-      col = make_float4(mixf(col.x, c.x, k), mixf(col.y, c.y, k), mixf(col.z, c.z, k), mixf(col.w, l * l, k));
-      // RGBA16F targets (renderer.ts:490): every store rounds to half.
-      alb = make_float4(__half2float(__float2half_rn(mixf(alb.x, ga.x, k))), __half2float(__float2half_rn(mixf(alb.y, ga.y, k))),
-                        __half2float(__float2half_rn(mixf(alb.z, ga.z, k))), __half2float(__float2half_rn(mixf(alb.w, ga.w, k))));
-      nrm = make_float4(__half2float(__float2half_rn(mixf(nrm.x, gn.x, k))), __half2float(__float2half_rn(mixf(nrm.y, gn.y, k))),
-                        __half2float(__float2half_rn(mixf(nrm.z, gn.z, k))), __half2float(__float2half_rn(mixf(nrm.w, gn.w, k))));
-      n = n + 1.f;
-    }
-    A.color[px] = col;
-    A.albedo[px] = make_half4(alb);
-    A.normal[px] = make_half4(nrm);
-    A.history[px] = n;
+  for (uint32_t px = blockIdx.x * blockDim.x + threadIdx.x; px < WH; px += gridDim.x * blockDim.x)
+    accumulate_pixel(P, A, WH, S, px, 0);
+}
+
+// Scene i owns batch pixels [pix_base[i], pix_base[i + 1]).
+__global__ void k_accumulate_multi(Paths P, const SceneRec* __restrict__ recs, const uint32_t* __restrict__ pix_base,
+                                   const uint32_t* __restrict__ path_base, int n, int S) {
+  const uint32_t total = __ldg(pix_base + n);
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    const int sc = find_scene(pix_base, n, g);
+    const SceneRec& R = recs[sc];
+    accumulate_pixel(P, R.accum, (uint32_t)R.W * R.H, S, g - __ldg(pix_base + sc), __ldg(path_base + sc));
   }
+}
+
+// Advances every scene's sample seed by the wave's S samples (on the device,
+// so a captured wave can be replayed unchanged).
+__global__ void k_advance_seeds(SceneRec* recs, int n, int S) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) recs[i].seed0 += (uint32_t)S;
 }
 
 __global__ void k_zero_counters(uint32_t* ctr, int nxt) {
@@ -461,7 +616,7 @@ void render_batch(const RenderLaunch& R, cudaStream_t s, PhaseEvents* pe) {
   static int closest_blocks = 0, shade_blocks = 0;
   if (!closest_blocks) {
     closest_blocks = persistent_blocks((const void*)k_closest_fast_t<PathClosest>, 256);
-    shade_blocks = persistent_blocks((const void*)k_shade, 128);
+    shade_blocks = persistent_blocks((const void*)k_shade_t<OneScene>, 128);
   }
   for (int b = 0; b <= R.max_bounces; b++) {
     const int cur = b & 1;
@@ -474,7 +629,7 @@ void render_batch(const RenderLaunch& R, cudaStream_t s, PhaseEvents* pe) {
     k_closest_fast_t<PathClosest><<<closest_blocks, 256, 0, s>>>(A, pc);
     k_closest_exact_t<PathClosest><<<64, 128, 0, s>>>(A, pc);
     E.mark(kPhClosest, s);
-    k_shade<<<shade_blocks, 128, 0, s>>>(P, R.scene, R.light, cur, b, R.max_bounces, R.clamp);
+    k_shade_t<OneScene><<<shade_blocks, 128, 0, s>>>(P, OneScene{R.scene, R.light, R.max_bounces, R.clamp}, cur, b);
     E.mark(kPhShade, s);
     PathShadow ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, R.scene.geo, R.scene.materials, R.scene.any_alpha};
     TravArgs B{R.scene.nodes, R.scene.node_count, R.scene.geo, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2,
@@ -488,6 +643,36 @@ void render_batch(const RenderLaunch& R, cudaStream_t s, PhaseEvents* pe) {
   E.mark(kPhResolve, s);
   k_accumulate<<<grid_for((uint32_t)R.W * R.H, 256), 256, 0, s>>>(P, R.accum, R.W, R.H, R.S);
   E.mark(kPhAccumulate, s);
+}
+
+// ------------------------------------------------------------ one multi-scene wave
+void render_wave_multi(const MultiLaunch& M, cudaStream_t s) {
+  const Paths& P = M.paths;
+  k_camera_multi<<<grid_for(M.total_paths, 256), 256, 0, s>>>(P, M.recs, M.path_base, M.n, M.sid, M.S);
+  static int max_closest = 0, max_shade = 0;
+  if (!max_closest) {
+    max_closest = persistent_blocks((const void*)k_closest_fast_t<PathClosestMulti>, 256);
+    max_shade = persistent_blocks((const void*)k_shade_t<SceneTable>, 128);
+  }
+  const int closest_blocks = M.trace_blocks > 0 ? M.trace_blocks : max_closest;
+  const int shade_blocks = M.shade_blocks > 0 ? M.shade_blocks : max_shade;
+  for (int b = 0; b <= M.max_bounces; b++) {
+    const int cur = b & 1;
+    k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
+    PathClosestMulti pc{P.ctr + kCtrQ0 + cur, P.q[cur], P.ro, P.rd, P.rng, P.hit, M.recs, M.sid, M.any_alpha};
+    TravArgs A{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr};
+    k_closest_fast_t<PathClosestMulti><<<closest_blocks, 256, 0, s>>>(A, pc);
+    k_closest_exact_t<PathClosestMulti><<<64, 128, 0, s>>>(A, pc);
+    k_shade_t<SceneTable><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b);
+    PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};
+    TravArgs B{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr};
+    k_anyhit_fast_t<PathShadowMulti><<<shade_blocks * 2, 256, 0, s>>>(B, ps);
+    k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, s>>>(B, ps);
+    k_resolve<<<shade_blocks, 128, 0, s>>>(P, cur);
+    k_count_rays<<<1, 32, 0, s>>>(P.ctr, cur);
+  }
+  k_accumulate_multi<<<grid_for(M.total_pixels, 256), 256, 0, s>>>(P, M.recs, M.pix_base, M.path_base, M.n, M.S);
+  k_advance_seeds<<<1, 64, 0, s>>>(M.recs, M.n, M.S);
 }
 
 }  // namespace lucent

@@ -228,23 +228,23 @@ static lucent_status alloc_targets(lucent_renderer* r, uint32_t w, uint32_t h) {
 
 // Path buffers for `cap` paths (bytes per path: 8 float4 + rng + 2 queue
 // entries + 3 shadow slots of 3 float4, a flag and a queue entry).
-static lucent_status alloc_paths(lucent_renderer* r, uint32_t cap) {
-  if (cap <= r->path_cap) return LUCENT_OK;
+static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, uint32_t& path_cap, Paths& P,
+                                        uint32_t cap) {
+  if (cap <= path_cap) return LUCENT_OK;
   // Per-path arrays in allocation order (bytes per path); each starts on a 256-byte boundary.
   static const size_t kPer[] = {16, 16, 16, 16, 16, 16, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12};
   size_t total = 0;
   for (size_t b : kPer) total += ((size_t)cap * b + 255) & ~(size_t)255;
-  lucent_status st = r->paths.reserve(total);
+  lucent_status st = paths.reserve(total);
   if (st) return st;
-  if ((st = r->ctr.reserve(kCtrWords * 4))) return st;
-  char* b = (char*)r->paths.ptr;
+  if ((st = ctr.reserve(kCtrWords * 4))) return st;
+  char* b = (char*)paths.ptr;
   size_t off = 0;
   auto take = [&](size_t bytes) {
     char* p = b + off;
     off += (bytes + 255) & ~(size_t)255;
     return (void*)p;
   };
-  Paths& P = r->P;
   P.ro = (float4*)take((size_t)cap * 16);
   P.rd = (float4*)take((size_t)cap * 16);
   P.thr = (float4*)take((size_t)cap * 16);
@@ -263,13 +263,17 @@ static lucent_status alloc_paths(lucent_renderer* r, uint32_t cap) {
   P.qs = (uint32_t*)take((size_t)cap * 12);
   P.slow = (uint32_t*)take((size_t)cap * 4);
   P.slow2 = (uint32_t*)take((size_t)cap * 12);
-  if (off > r->paths.cap) return fail(LUCENT_ERR_DEVICE, "path buffer layout overflow");
-  P.ctr = (uint32_t*)r->ctr.ptr;
+  if (off > paths.cap) return fail(LUCENT_ERR_DEVICE, "path buffer layout overflow");
+  P.ctr = (uint32_t*)ctr.ptr;
   cudaError_t e = cudaMemset(P.sh_c, 0, (size_t)cap * 48);
   if (e == cudaSuccess) e = cudaMemset(P.ctr, 0, kCtrWords * 4);
   if (e != cudaSuccess) return cuda_fail(e, "clear path buffers");
-  r->path_cap = cap;
+  path_cap = cap;
   return LUCENT_OK;
+}
+
+static lucent_status alloc_paths(lucent_renderer* r, uint32_t cap) {
+  return alloc_path_buffers(r->paths, r->ctr, r->path_cap, r->P, cap);
 }
 
 extern "C" {
@@ -563,6 +567,18 @@ lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* 
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "trace launch");
 }
 
+lucent_status lucent_renderer_trim(lucent_renderer* r) {
+  clear_error();
+  if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "synchronize");
+  r->paths.release();
+  r->path_cap = 0;
+  r->P = Paths{};
+  r->P.ctr = (uint32_t*)r->ctr.ptr;
+  return LUCENT_OK;
+}
+
 lucent_status lucent_renderer_set_profiling(lucent_renderer* r, int32_t enabled) {
   clear_error();
   if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
@@ -696,6 +712,219 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
   if (r->ctr.ptr) {
     cudaError_t e = cudaMemcpy(out->traversal, (uint32_t*)r->ctr.ptr + kCtrTrav, 40, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "read traversal counters");
+  }
+  return LUCENT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Multi-scene batches: one wavefront over the paths of several renderers.
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+struct lucent_batch {
+  std::vector<lucent_renderer*> rs;
+  lucent_batch_options opt{0, 1u << 25, 1, 0, 0};
+  DeviceBuffer recs, bases, tail_bases, sid, paths, ctr;
+  uint32_t path_cap = 0, sid_cap = 0;
+  Paths P{};
+  // captured full wave
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t graph_key[4] = {0, 0, 0, 0};
+  uint32_t waves = 0, graph_waves = 0;
+  cudaStream_t cap_stream = nullptr;  // capture happens here (the legacy stream cannot be captured)
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+};
+
+static SceneRec scene_rec(const lucent_renderer* r) {
+  SceneRec R{};
+  R.scene = {(const Node*)r->nodes.ptr, r->node_count, (const float4*)r->geo.ptr, (const float4*)r->attr.ptr,
+             (const float4*)r->mats.ptr, (const float4*)r->spheres.ptr, (const int*)r->sph_mat.ptr,
+             (const int*)r->sph_light.ptr, (int)r->sphere_count, (const float4*)r->lights.ptr, (int)r->light_count,
+             r->ground_enabled ? r->ground_material : -1, r->ground_height, r->any_alpha};
+  R.light = r->light;
+  R.cam = r->cam;
+  R.accum = {(float4*)r->color.ptr, (half4*)r->albedo.ptr, (half4*)r->normal.ptr, (float*)r->history.ptr};
+  R.W = (int)r->W;
+  R.H = (int)r->H;
+  R.max_bounces = (int)r->max_bounces;
+  R.clamp = r->clamp;
+  R.seed0 = r->seed;
+  return R;
+}
+
+extern "C" {
+
+lucent_status lucent_batch_create(lucent_renderer* const* renderers, uint32_t n, lucent_batch** out) {
+  clear_error();
+  if (!out || (!renderers && n)) return fail(LUCENT_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (n == 0 || n > 65535) return fail(LUCENT_ERR_INVALID, "a batch holds 1 to 65535 renderers, got %u", n);
+  for (uint32_t i = 0; i < n; i++) {
+    if (!renderers[i]) return fail(LUCENT_ERR_INVALID, "renderer %u is null", i);
+    for (uint32_t j = 0; j < i; j++)
+      if (renderers[j] == renderers[i]) return fail(LUCENT_ERR_INVALID, "renderer %u appears twice", i);
+  }
+  lucent_batch* b = new lucent_batch();
+  b->rs.assign(renderers, renderers + n);
+  *out = b;
+  return LUCENT_OK;
+}
+
+void lucent_batch_destroy(lucent_batch* b) {
+  if (!b) return;
+  b->drop_graph();
+  if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+  for (DeviceBuffer* d : {&b->recs, &b->bases, &b->tail_bases, &b->sid, &b->paths, &b->ctr}) d->release();
+  delete b;
+}
+
+lucent_status lucent_batch_set_options(lucent_batch* b, const lucent_batch_options* o) {
+  clear_error();
+  if (!b || !o) return fail(LUCENT_ERR_INVALID, "null argument");
+  if (o->max_wave_paths == 0) return fail(LUCENT_ERR_INVALID, "max_wave_paths must be positive");
+  b->opt = *o;
+  b->drop_graph();
+  return LUCENT_OK;
+}
+
+lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream) {
+  clear_error();
+  if (!b) return fail(LUCENT_ERR_INVALID, "null batch");
+  if (samples == 0) return LUCENT_OK;
+  const int n = (int)b->rs.size();
+  std::vector<SceneRec> recs(n);
+  uint64_t pixels = 0;
+  int max_bounces = 0, any_alpha = 0;
+  for (int i = 0; i < n; i++) {
+    const lucent_renderer* r = b->rs[i];
+    if (!r->has_scene || !r->has_lighting)
+      return fail(LUCENT_ERR_INVALID, "renderer %d: trace before load_scene / upload_lighting", i);
+    recs[i] = scene_rec(r);
+    pixels += (uint64_t)r->W * r->H;
+    max_bounces = std::max(max_bounces, (int)r->max_bounces);
+    any_alpha |= r->any_alpha;
+  }
+  // Samples per wave: as many as fit in max_wave_paths (at least one).
+  uint64_t S = b->opt.samples_per_wave ? b->opt.samples_per_wave : std::max<uint64_t>(1, b->opt.max_wave_paths / pixels);
+  S = std::min<uint64_t>(S, samples);
+  if (pixels * S * 3 >= (1ull << 32)) return fail(LUCENT_ERR_UNSUPPORTED, "wave of %llu paths exceeds the 32-bit path index",
+                                                  (unsigned long long)(pixels * S));
+  const uint32_t cap = (uint32_t)(pixels * S);
+  lucent_status st = alloc_path_buffers(b->paths, b->ctr, b->path_cap, b->P, cap);
+  if (st) return st;
+  if (cap > b->sid_cap) {
+    if ((st = b->sid.reserve((size_t)cap * 2))) return st;
+    if (cudaMemset(b->sid.ptr, 0, (size_t)cap * 2) != cudaSuccess) return cuda_fail(cudaGetLastError(), "clear sid");
+    b->sid_cap = cap;
+    b->drop_graph();
+  }
+  if ((st = b->recs.reserve(sizeof(SceneRec) * n)) || (st = b->bases.reserve(8 * (n + 1))) ||
+      (st = b->tail_bases.reserve(8 * (n + 1))))
+    return st;
+  auto make_bases = [&](uint32_t s_wave, std::vector<uint32_t>& hb) {
+    hb.assign(2 * (n + 1), 0);
+    for (int i = 0; i < n; i++) {
+      const uint32_t wh = (uint32_t)recs[i].W * recs[i].H;
+      hb[i + 1] = hb[i] + wh * s_wave;                   // path_base
+      hb[n + 1 + i + 1] = hb[n + 1 + i] + wh;            // pix_base
+    }
+  };
+  cudaStream_t s = (cudaStream_t)stream;
+  std::vector<uint32_t> hb, tb;
+  make_bases((uint32_t)S, hb);
+  cudaError_t e = cudaMemcpyAsync(b->recs.ptr, recs.data(), sizeof(SceneRec) * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b->bases.ptr, hb.data(), 4 * hb.size(), cudaMemcpyHostToDevice, s);
+  const uint32_t tail = samples % (uint32_t)S;
+  if (e == cudaSuccess && tail) {
+    make_bases(tail, tb);
+    e = cudaMemcpyAsync(b->tail_bases.ptr, tb.data(), 4 * tb.size(), cudaMemcpyHostToDevice, s);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "upload batch tables");
+  MultiLaunch M;
+  M.paths = b->P;
+  M.recs = (SceneRec*)b->recs.ptr;
+  M.sid = (uint16_t*)b->sid.ptr;
+  M.n = n;
+  M.max_bounces = max_bounces;
+  M.any_alpha = any_alpha;
+  M.total_pixels = (uint32_t)pixels;
+  M.trace_blocks = (int)b->opt.trace_blocks;
+  M.shade_blocks = (int)b->opt.shade_blocks;
+  auto setup = [&](uint32_t s_wave, const DeviceBuffer& base) {
+    M.S = (int)s_wave;
+    M.total_paths = (uint32_t)(pixels * s_wave);
+    M.path_base = (const uint32_t*)base.ptr;
+    M.pix_base = (const uint32_t*)base.ptr + (n + 1);
+  };
+  const uint64_t key[4] = {S | ((uint64_t)n << 32), pixels | ((uint64_t)b->opt.trace_blocks << 40),
+                           (uint64_t)(uintptr_t)b->P.ro ^ ((uint64_t)max_bounces << 48) ^ ((uint64_t)b->opt.shade_blocks << 56),
+                           (uint64_t)(uintptr_t)b->recs.ptr ^ ((uint64_t)any_alpha << 63)};
+  const uint32_t full = samples / (uint32_t)S;
+  for (uint32_t w = 0; w < full; w++) {
+    setup((uint32_t)S, b->bases);
+    if (b->opt.use_graph && b->waves > 0) {  // first wave ever runs uncaptured (one-time setup inside)
+      if (!b->exec || std::memcmp(key, b->graph_key, sizeof key) != 0) {
+        b->drop_graph();
+        if (!b->cap_stream && (e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking)) != cudaSuccess)
+          return cuda_fail(e, "capture stream");
+        e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_fail(e, "begin capture");
+        render_wave_multi(M, b->cap_stream);
+        e = cudaStreamEndCapture(b->cap_stream, &b->graph);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+        if (e != cudaSuccess) {
+          b->drop_graph();
+          return cuda_fail(e, "capture wave");
+        }
+        std::memcpy(b->graph_key, key, sizeof key);
+      }
+      e = cudaGraphLaunch(b->exec, s);
+      if (e != cudaSuccess) return cuda_fail(e, "launch wave graph");
+      b->graph_waves++;
+    } else {
+      render_wave_multi(M, s);
+    }
+    b->waves++;
+  }
+  if (tail) {
+    setup(tail, b->tail_bases);
+    render_wave_multi(M, s);
+    b->waves++;
+  }
+  for (lucent_renderer* r : b->rs) {
+    r->seed += samples;
+    r->frame += samples;
+  }
+  e = cudaGetLastError();
+  return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "batch trace launch");
+}
+
+lucent_status lucent_batch_check(lucent_batch* b, void* stream, lucent_batch_stats* out) {
+  clear_error();
+  if (!b) return fail(LUCENT_ERR_INVALID, "null batch");
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "synchronize");
+  if (out) std::memset(out, 0, sizeof *out);
+  if (!b->ctr.ptr) return LUCENT_OK;
+  uint32_t words[kCtrWords];
+  e = cudaMemcpy(words, b->ctr.ptr, sizeof words, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "read batch counters");
+  if (out) {
+    std::memcpy(&out->closest_rays, words + kCtrStatClosest, 8);
+    std::memcpy(&out->shadow_rays, words + kCtrStatShadow, 8);
+    out->waves = b->waves;
+    out->graph_waves = b->graph_waves;
+    out->wave_paths = b->path_cap;
+  }
+  if (words[kCtrErr]) {
+    cudaMemset((uint32_t*)b->ctr.ptr + kCtrErr, 0, 4);
+    return fail(LUCENT_ERR_DEVICE, "batch raised device error word 0x%x", words[kCtrErr]);
   }
   return LUCENT_OK;
 }

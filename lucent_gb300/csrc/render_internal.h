@@ -67,6 +67,29 @@ struct RenderLaunch {
   unsigned long long* trav_stats;  // closest-hit traversal counters or nullptr
 };
 
+// One scene of a multi-scene wave (device table, one entry per scene).
+struct SceneRec {
+  sh::SceneDev scene;
+  sh::LightingDev light;
+  sh::CameraDev cam;
+  AccumDev accum;
+  int W, H, max_bounces;
+  float clamp;
+  uint32_t seed0;  // sample seed (uSeed) of the wave's first sample; advanced on the device
+};
+
+struct MultiLaunch {
+  Paths paths;
+  SceneRec* recs;              // device, n entries
+  const uint32_t* path_base;   // device, n + 1 entries: scene i owns paths [path_base[i], path_base[i+1])
+  const uint32_t* pix_base;    // device, n + 1 entries: the same for pixels
+  uint16_t* sid;               // device, scene index per path
+  int n, S, max_bounces;       // max_bounces = the largest over the scenes
+  uint32_t total_paths, total_pixels;
+  int any_alpha;
+  int trace_blocks, shade_blocks;  // 0 = all resident blocks
+};
+
 // Optional per-phase timing: events recorded between launches, each tagged
 // with the phase of the interval that ends at it.
 enum Phase : int { kPhCamera = 0, kPhClosest, kPhShade, kPhShadow, kPhResolve, kPhAccumulate, kPhases };
@@ -83,6 +106,10 @@ struct PhaseEvents {
 };
 
 void render_batch(const RenderLaunch& R, cudaStream_t s, PhaseEvents* pe);
+
+// One wave of S samples for every scene of a multi-scene launch. Graph-safe:
+// no host synchronisation, every count stays on the device.
+void render_wave_multi(const MultiLaunch& M, cudaStream_t s);
 
 // sheenAlbedoLUT (16 x 16) rounded to half precision, as the reference uploads it.
 void sheen_lut_half(float* out);

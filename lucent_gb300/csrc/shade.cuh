@@ -9,6 +9,15 @@
 namespace lucent {
 namespace sh {
 
+// The BSDF evaluation is called from four places of the shade kernel (three
+// light samples and the BSDF sample); how it is compiled is set here.
+#ifndef LUCENT_EVAL_FN
+#define LUCENT_EVAL_FN LUCENT_DEV
+#endif
+#ifndef LUCENT_BSDF_FN
+#define LUCENT_BSDF_FN LUCENT_DEV
+#endif
+
 constexpr float PI = 3.14159265358979323846f;
 constexpr float INV_PI = 0.31830988618379067154f;
 constexpr float TWO_PI = 6.28318530717958647692f;
@@ -340,6 +349,60 @@ LUCENT_DEV float d_ggx(float NdotH, float a) {
   const float d = NdotH * NdotH * (a2 - 1.f) + 1.f;
   return a2 / (PI * d * d);
 }
+
+// Error-free transformations (Knuth TwoSum; the FMA product residual;
+// Kahan's difference of products), used where a binary32 formula cancels.
+LUCENT_DEV void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+LUCENT_DEV float diff_of_products(float a, float b, float c, float d) {  // a*b - c*d to ~1.5 ulp
+  const float w = c * d;
+  const float e = fmaf(-c, d, w);
+  return fmaf(a, b, -w) + e;
+}
+
+// The unnormalised half vector h = wo + wi as an exact pair (hs + he) and
+// the pieces of the GGX denominator that cancel near the lobe's peak.
+struct HalfVec {
+  float3 hs, he;
+  float hh;  // |h|^2
+};
+LUCENT_DEV HalfVec half_vec(float3 wo, float3 wi) {
+  HalfVec h;
+  two_sum(wo.x, wi.x, h.hs.x, h.he.x);
+  two_sum(wo.y, wi.y, h.hs.y, h.he.y);
+  two_sum(wo.z, wi.z, h.hs.z, h.he.z);
+  h.hh = dot3(h.hs, h.hs) + 2.f * dot3(h.hs, h.he);
+  return h;
+}
+// 1 - |n|^2 (a binary32 unit vector is unit only to ~1e-7).
+LUCENT_DEV float one_minus_norm2(float3 n) {
+  const float px = n.x * n.x, py = n.y * n.y, pz = n.z * n.z;
+  const float ex = fmaf(n.x, n.x, -px), ey = fmaf(n.y, n.y, -py), ez = fmaf(n.z, n.z, -pz);
+  float s, t1, t2;
+  two_sum(px, py, s, t1);
+  two_sum(s, pz, s, t2);
+  return (1.f - s) - (ex + ey + ez + t1 + t2);
+}
+// D_GGX (bsdf.glsl:28-32) for n and H = h / |h|. Near the peak the
+// shader's denominator NdotH^2 (a^2 - 1) + 1 cancels (a binary32 evaluation
+// keeps ~1e-7 of absolute accuracy); below 1/4 it is evaluated as the equal
+// sin^2 + (1 - |n|^2) + NdotH^2 a^2, sin^2 = |n x h|^2 / |h|^2 from exact
+// cross products, which keeps full relative accuracy at any sharpness.
+LUCENT_DEV float d_ggx_h(float3 n, float3 wo, float3 wi, float NdotH, float a) {
+  const float a2 = a * a;
+  const float d = NdotH * NdotH * (a2 - 1.f) + 1.f;
+  if (!(NdotH > 0.f && d < 0.25f)) return a2 / (PI * d * d);
+  const HalfVec h = half_vec(wo, wi);
+  const float3 c = f3(diff_of_products(n.y, h.hs.z, n.z, h.hs.y) + (n.y * h.he.z - n.z * h.he.y),
+                      diff_of_products(n.z, h.hs.x, n.x, h.hs.z) + (n.z * h.he.x - n.x * h.he.z),
+                      diff_of_products(n.x, h.hs.y, n.y, h.hs.x) + (n.x * h.he.y - n.y * h.he.x));
+  const float num = dot3(c, c) + h.hh * (one_minus_norm2(n) + NdotH * NdotH * a2);  // d |h|^2
+  const float hn = h.hh / num;
+  return a2 * hn * hn / PI;
+}
 LUCENT_DEV float g1_ggx(float NdotX, float a) {
   const float a2 = a * a;
   return 2.f * NdotX / (NdotX + sqrtf(a2 + (1.f - a2) * NdotX * NdotX));
@@ -357,19 +420,42 @@ LUCENT_DEV float dielectric_f0(float ior) {
 }
 LUCENT_DEV float alpha_of(float r) { return fmaxf(r * r, 1e-3f); }
 
-LUCENT_DEV float3 sample_vndf(float3 Ve, float a, float u0, float u1) {  // Heitz 2018 (bsdf.glsl:59-72)
-  const float3 Vh = norm3(f3(a * Ve.x, a * Ve.y, Ve.z));
+// sampleGGXVNDF (Heitz 2018; bsdf.glsl:59-72). Three differences of the
+// shader's form cancel in binary32 for sharp lobes (Vh.z -> 1) and samples
+// at the rim of the projected disk (u0 -> 1): 1 - s, sqrt(1 - t1^2) and
+// sqrt(1 - t1^2 - t2'^2). They are evaluated in rearranged forms with the
+// same value:
+//   1 - s = (1 - Vh.z) / 2,  1 - Vh.z = (v.x^2 + v.y^2) / (|v| (|v| + v.z))
+//   q^2 = 1 - t1^2 = (1 - u0) + u0 sin^2(phi)            (1 - u0 exact, u0 >= 0.5)
+//   1 - t1^2 - t2'^2 = s (q - t2)(q + t2'),  q^2 - t2^2 = 1 - u0, so
+//   q - t2 = (1 - u0) / (q + t2) (t2 > 0),  q + t2' = (1-s)(q - t2) + (1 - u0) / (q - t2) (t2 <= 0).
+LUCENT_BSDF_FN float3 sample_vndf(float3 Ve, float a, float u0, float u1) {
+  const float3 v = f3(a * Ve.x, a * Ve.y, Ve.z);
+  const float vl = len3(v);
+  const float3 Vh = v / vl;
   const float lensq = Vh.x * Vh.x + Vh.y * Vh.y;
-  const float3 T1 = lensq > 0.f ? f3(-Vh.y, Vh.x, 0.f) * rsqrtf(lensq) : f3(1.f, 0.f, 0.f);
+  const float3 T1 = lensq > 0.f ? f3(-Vh.y, Vh.x, 0.f) / sqrtf(lensq) : f3(1.f, 0.f, 0.f);
   const float3 T2 = cross3(Vh, T1);
   const float r = sqrtf(u0);
   float sp, cp;
   sincosf(TWO_PI * u1, &sp, &cp);
   const float t1 = r * cp;
-  float t2 = r * sp;
+  const float t2 = r * sp;
   const float s = 0.5f * (1.f + Vh.z);
-  t2 = (1.f - s) * sqrtf(fmaxf(0.f, 1.f - t1 * t1)) + s * t2;
-  const float3 Nh = t1 * T1 + t2 * T2 + sqrtf(fmaxf(0.f, 1.f - t1 * t1 - t2 * t2)) * Vh;
+  const float s1 = v.z > 0.f ? 0.5f * (v.x * v.x + v.y * v.y) / (vl * (vl + v.z)) : 1.f - s;
+  const float om = 1.f - u0;
+  const float q = sqrtf(fmaxf(0.f, om + u0 * sp * sp));
+  const float t2b = s1 * q + s * t2;
+  float qm, qp;  // q - t2 and q + t2'
+  if (t2 > 0.f) {
+    qm = om / (q + t2);
+    qp = (1.f + s1) * q + s * t2;
+  } else {
+    qm = q - t2;
+    qp = qm > 0.f ? s1 * qm + om / qm : 0.f;
+  }
+  const float z2 = s * qm * qp;
+  const float3 Nh = t1 * T1 + t2b * T2 + sqrtf(fmaxf(0.f, z2)) * Vh;
   return norm3(f3(a * Nh.x, a * Nh.y, fmaxf(0.f, Nh.z)));
 }
 
@@ -404,7 +490,7 @@ LUCENT_DEV float3 base_f0(const Surface& s) {
 }
 
 // evalOpaque (bsdf.glsl:114-166): f (not cosine-weighted) and the mixture pdf.
-LUCENT_DEV float3 eval_opaque(const LightingDev& L, const Surface& s, float3 wo, float3 wi, float& pdf) {
+LUCENT_EVAL_FN float3 eval_opaque(const LightingDev& L, const Surface& s, float3 wo, float3 wi, float& pdf) {
   const float3 n = s.n;
   const float NdotL = dot3(n, wi), NdotV = dot3(n, wo);
   pdf = 0.f;
@@ -414,7 +500,7 @@ LUCENT_DEV float3 eval_opaque(const LightingDev& L, const Surface& s, float3 wo,
   const float NdotH = fmaxf(dot3(n, H), 0.f), VdotH = fmaxf(dot3(wo, H), 0.f);
   const float3 F0 = base_f0(s);
   const float3 F = fresnel3(VdotH, F0);
-  const float D = d_ggx(NdotH, a);
+  const float D = d_ggx_h(n, wo, wi, NdotH, a);
   const float G1v = g1_ggx(NdotV, a);
   const float G = G1v * g1_ggx(NdotL, a);
   const float3 spec = (D * G) * F / fmaxf(4.f * NdotV * NdotL, 1e-6f);
@@ -436,7 +522,7 @@ LUCENT_DEV float3 eval_opaque(const LightingDev& L, const Surface& s, float3 wo,
     if (cV > 0.f && cL > 0.f) {
       const float ac = alpha_of(s.clearcoat_roughness);
       const float cH = fmaxf(dot3(s.nc, H), 0.f);
-      const float Dc = d_ggx(cH, ac), G1c = g1_ggx(cV, ac);
+      const float Dc = d_ggx_h(s.nc, wo, wi, cH, ac), G1c = g1_ggx(cV, ac);
       coat = Dc * G1c * g1_ggx(cL, ac) * fresnel1(VdotH, 0.04f) / (4.f * cV * cL);
       pdf_coat = G1c * Dc / (4.f * cV);
     }

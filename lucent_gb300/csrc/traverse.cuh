@@ -16,7 +16,9 @@
 //   uint32_t count() const                        rays in this launch
 //   void ray(uint32_t k, float3& o, float3& d)   k-th ray
 //   uint32_t key(uint32_t k) const                alpha any-hit key (RNG state)
-//   bool alpha(int slot, uint32_t key) const      true if a hit on `slot` counts
+//   bool alpha(int scene, int slot, uint32_t key) true if a hit on `slot` counts
+//   static constexpr bool kMultiScene             rays of several scenes in one launch:
+//   BvhView bvh(uint32_t k) const                 then the k-th ray's BVH (else TravArgs')
 //   bool alpha_any() const                        false: no alpha-tested triangles
 //   void hit(uint32_t k, int slot, double t, double u, double v)   (closest)
 //   void miss(uint32_t k); void fail(uint32_t k)
@@ -38,6 +40,23 @@ __device__ __forceinline__ D3 inv_exact(float3 d) {
   return {ddiv(1.0, (double)d.x), ddiv(1.0, (double)d.y), ddiv(1.0, (double)d.z)};
 }
 
+// Binary64 fallbacks of the fast closest-hit kernel, kept out of line: they
+// run for a few percent of rays, and inlined they raise the register
+// allocation (and the spills) of the binary32 loop around them. (The any-hit
+// kernel measured faster with them inline.)
+struct Tri64 {
+  double t, u, v;
+  bool hit;
+};
+static __device__ __noinline__ Tri64 tri_f64(float3 o, float3 d, float4 a, float4 b, float4 c, double tMin, double tMax) {
+  Tri64 r{0.0, 0.0, 0.0, false};
+  r.hit = ts_triangle({o.x, o.y, o.z}, {d.x, d.y, d.z}, d3f(a), d3f(b), d3f(c), tMin, tMax, r.t, r.u, r.v);
+  return r;
+}
+static __device__ __noinline__ bool slab_f64_culled(float4 mn, float4 mx, float3 o, float3 d, double tMax) {
+  return ts_slab_culled(mn, mx, {o.x, o.y, o.z}, inv_exact(d), tMax);
+}
+
 struct TravArgs {
   const Node* nodes;
   uint32_t node_limit;
@@ -56,6 +75,22 @@ __device__ __forceinline__ void count_stat(const TravArgs& A, int k) {
   if (A.stats) atomicAdd(A.stats + k, 1ull);
 }
 
+// The BVH one ray traverses: the launch's (TravArgs) or, for policies that
+// trace the rays of several scenes in one launch, its scene's.
+struct BvhView {
+  const Node* nodes;
+  const float4* tris;
+  uint32_t node_limit;
+  int scene;
+};
+template <class Pol>
+__device__ __forceinline__ BvhView bvh_of(const TravArgs& A, const Pol& P, uint32_t k) {
+  if constexpr (Pol::kMultiScene)
+    return P.bvh(k);
+  else
+    return {A.nodes, A.tris, A.node_limit, 0};
+}
+
 struct PendingNode {
   int node;
   float ehi;
@@ -64,8 +99,8 @@ struct PendingNode {
 // Entire reference algorithm in binary64 for one ray (slow path, f64 rays).
 // Returns false if the traversal was aborted (error word set).
 template <class Pol>
-__device__ bool trace_exact(const TravArgs& A, const Pol& P, D3 o, D3 d, uint32_t key, int& slot, double& t_out,
-                            double& u_out, double& v_out) {
+__device__ bool trace_exact(const TravArgs& A, const Pol& P, const BvhView& bv, D3 o, D3 d, uint32_t key, int& slot,
+                            double& t_out, double& u_out, double& v_out) {
   const D3 inv = {ddiv(1.0, d.x), ddiv(1.0, d.y), ddiv(1.0, d.z)};
   int stack[kTsStack];
   int sp = 0;
@@ -74,21 +109,21 @@ __device__ bool trace_exact(const TravArgs& A, const Pol& P, D3 o, D3 d, uint32_
   slot = -1;
   uint32_t iters = 0;
   while (sp > 0) {
-    if (++iters > A.node_limit) {
+    if (++iters > bv.node_limit) {
       atomicOr(A.err, kErrIterations);
       return false;
     }
     const int n = stack[--sp];
-    const Node nd = load_node(A.nodes, n);
+    const Node nd = load_node(bv.nodes, n);
     if (ts_slab_culled(nd.lo, nd.hi, o, inv, closest)) continue;
     const int cnt = node_count(nd), first = node_first(nd);
     if (cnt > 0) {
       for (int k = 0; k < cnt; k++) {
         const int s = first + k;
-        const float4 a = __ldg(A.tris + 3 * (size_t)s), b = __ldg(A.tris + 3 * (size_t)s + 1),
-                     c = __ldg(A.tris + 3 * (size_t)s + 2);
+        const float4 a = __ldg(bv.tris + 3 * (size_t)s), b = __ldg(bv.tris + 3 * (size_t)s + 1),
+                     c = __ldg(bv.tris + 3 * (size_t)s + 2);
         double t, u, v;
-        if (ts_triangle(o, d, d3f(a), d3f(b), d3f(c), A.tMin, closest, t, u, v) && P.alpha(s, key)) {
+        if (ts_triangle(o, d, d3f(a), d3f(b), d3f(c), A.tMin, closest, t, u, v) && P.alpha(bv.scene, s, key)) {
           closest = t;
           slot = s;
           t_out = t;
@@ -117,7 +152,7 @@ __global__ void k_closest_exact_t(TravArgs A, Pol P) {
     P.ray(k, o, d);
     int slot;
     double t = 0, u = 0, v = 0;
-    if (!trace_exact(A, P, {o.x, o.y, o.z}, {d.x, d.y, d.z}, P.key(k), slot, t, u, v))
+    if (!trace_exact(A, P, bvh_of(A, P, k), {o.x, o.y, o.z}, {d.x, d.y, d.z}, P.key(k), slot, t, u, v))
       P.fail(k);
     else if (slot < 0)
       P.miss(k);
@@ -151,6 +186,7 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
   double c64 = A.tMax, bu64 = 0, bv64 = 0;  // binary64 (t, u, v) of `best` when best_exact
   float3 best_est = make_float3(0.f, 0.f, 0.f);  // binary32 (t, u, v) of a certainly accepted `best`
   int best = -1, sp = 0;
+  BvhView bv{A.nodes, A.tris, A.node_limit, 0};  // multi-scene policies set it per ray below
   Node cur;
   PendingNode stack[kTsStack];
 
@@ -174,6 +210,7 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
           } else {
             r = make_ray32(o, d);
             key = P.key(ri);
+            if constexpr (Pol::kMultiScene) bv = P.bvh(ri);
             c_lo = cmax_lo;
             c_hi = cmax_hi;
             c64 = A.tMax;
@@ -183,11 +220,11 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
             sp = 0;
             iters = 0;
             count_stat(A, 0);
-            cur = load_node(A.nodes, 0);  // the reference pops the root first and tests its box
+            cur = load_node(bv.nodes, 0);  // the reference pops the root first and tests its box
             SlabClass cl = classify_slab(r, cur.lo, cur.hi, c_lo, c_hi);
             if (cl == kAmbiguous) {
               count_stat(A, 1);
-              cl = ts_slab_culled(cur.lo, cur.hi, {o.x, o.y, o.z}, inv_exact(d), c64) ? kCulled : kPass;
+              cl = slab_f64_culled(cur.lo, cur.hi, o, d, c64) ? kCulled : kPass;
             }
             have_cur = cl != kCulled;
             active = true;
@@ -201,24 +238,23 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
     auto exact_c = [&]() {  // the reference's binary64 `closest`, on demand
       if (!c_exact) {
         count_stat(A, 3);
-        const float4 a = __ldg(A.tris + 3 * (size_t)best), b = __ldg(A.tris + 3 * (size_t)best + 1),
-                     c = __ldg(A.tris + 3 * (size_t)best + 2);
-        double t, u, v;
-        ts_triangle({r.o.x, r.o.y, r.o.z}, {r.d.x, r.d.y, r.d.z}, d3f(a), d3f(b), d3f(c), A.tMin, INF64, t, u, v);
-        c64 = t;
-        bu64 = u;
-        bv64 = v;
+        const float4 a = __ldg(bv.tris + 3 * (size_t)best), b = __ldg(bv.tris + 3 * (size_t)best + 1),
+                     c = __ldg(bv.tris + 3 * (size_t)best + 2);
+        const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, INF64);
+        c64 = h.t;
+        bu64 = h.u;
+        bv64 = h.v;
         c_exact = true;
         best_exact = true;
-        c_lo = __double2float_rd(t);
-        c_hi = __double2float_ru(t);
+        c_lo = __double2float_rd(h.t);
+        c_hi = __double2float_ru(h.t);
       }
       return c64;
     };
     auto slab_decide = [&](const Node& nd, SlabClass cl) {
       if (cl != kAmbiguous) return cl;
       count_stat(A, 1);
-      return ts_slab_culled(nd.lo, nd.hi, {r.o.x, r.o.y, r.o.z}, inv_exact(r.d), exact_c()) ? kCulled : kPass;
+      return slab_f64_culled(nd.lo, nd.hi, r.o, r.d, exact_c()) ? kCulled : kPass;
     };
 
     if (!have_cur) {
@@ -229,11 +265,10 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
           P.hit(ri, best, c64, bu64, bv64);
         } else if (P.exact_output()) {  // the reference's binary64 t, u, v
           count_stat(A, 4);
-          const float4 a = __ldg(A.tris + 3 * (size_t)best), b = __ldg(A.tris + 3 * (size_t)best + 1),
-                       c = __ldg(A.tris + 3 * (size_t)best + 2);
-          double t = 0, u = 0, v = 0;
-          ts_triangle({r.o.x, r.o.y, r.o.z}, {r.d.x, r.d.y, r.d.z}, d3f(a), d3f(b), d3f(c), A.tMin, INF64, t, u, v);
-          P.hit(ri, best, t, u, v);
+          const float4 a = __ldg(bv.tris + 3 * (size_t)best), b = __ldg(bv.tris + 3 * (size_t)best + 1),
+                       c = __ldg(bv.tris + 3 * (size_t)best + 2);
+          const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, INF64);
+          P.hit(ri, best, h.t, h.u, h.v);
         } else {  // same triangle; binary32 t, u, v like the GLSL's own
           P.hit32(ri, best, best_est);
         }
@@ -241,12 +276,12 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
         continue;
       }
       const PendingNode e = stack[--sp];
-      const Node nd = load_node(A.nodes, e.node);
+      const Node nd = load_node(bv.nodes, e.node);
       if (e.ehi > c_lo && slab_decide(nd, classify_slab(r, nd.lo, nd.hi, c_lo, c_hi)) == kCulled) continue;
       cur = nd;
       have_cur = true;
     }
-    if (++iters > A.node_limit) {  // a valid BVH visits each node at most once per ray
+    if (++iters > bv.node_limit) {  // a valid BVH visits each node at most once per ray
       atomicOr(A.err, kErrIterations);
       P.fail(ri);
       active = false;
@@ -257,13 +292,13 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
     if (cnt > 0) {
       for (int k = 0; k < cnt; k++) {
         const int slot = first + k;
-        const float4 a = __ldg(A.tris + 3 * (size_t)slot), b = __ldg(A.tris + 3 * (size_t)slot + 1),
-                     c = __ldg(A.tris + 3 * (size_t)slot + 2);
+        const float4 a = __ldg(bv.tris + 3 * (size_t)slot), b = __ldg(bv.tris + 3 * (size_t)slot + 1),
+                     c = __ldg(bv.tris + 3 * (size_t)slot + 2);
         float tl, th;
         float3 est;
         const TriClass tc = mt_classify(r, a, b, c, tmin_lo, tmin_hi, c_lo, c_hi, tl, th, est);
         if (tc == kTriReject) continue;
-        if (use_alpha && !P.alpha(slot, key)) continue;  // alpha depends on (key, slot) only
+        if (use_alpha && !P.alpha(bv.scene, slot, key)) continue;  // alpha depends on (key, slot) only
         if (tc == kTriAccept) {
           best = slot;
           best_est = est;
@@ -274,22 +309,22 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
           continue;
         }
         count_stat(A, 2);
-        double t, u, v;
         const double cc = exact_c();
-        if (ts_triangle({r.o.x, r.o.y, r.o.z}, {r.d.x, r.d.y, r.d.z}, d3f(a), d3f(b), d3f(c), A.tMin, cc, t, u, v)) {
+        const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, cc);
+        if (h.hit) {
           best = slot;
-          c64 = t;
-          bu64 = u;
-          bv64 = v;
+          c64 = h.t;
+          bu64 = h.u;
+          bv64 = h.v;
           c_exact = true;
           best_exact = true;
-          c_lo = __double2float_rd(t);
-          c_hi = __double2float_ru(t);
+          c_lo = __double2float_rd(h.t);
+          c_hi = __double2float_ru(h.t);
         }
       }
       have_cur = false;
     } else {
-      const Node L = load_node(A.nodes, first), R = load_node(A.nodes, first + 1);  // one 64-byte pair
+      const Node L = load_node(bv.nodes, first), R = load_node(bv.nodes, first + 1);  // one 64-byte pair
       float ehl, ehr;
       const SlabClass cl = slab_decide(L, classify_slab_e(r, L.lo, L.hi, c_lo, c_hi, ehl));
       const SlabClass cr = slab_decide(R, classify_slab_e(r, R.lo, R.hi, c_lo, c_hi, ehr));
@@ -316,7 +351,8 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
 
 // Any hit in binary64 (slow path).
 template <class Pol>
-__device__ bool any_exact(const TravArgs& A, const Pol& P, D3 o, D3 d, uint32_t key, double tMax, bool& ok) {
+__device__ bool any_exact(const TravArgs& A, const Pol& P, const BvhView& bv, D3 o, D3 d, uint32_t key, double tMax,
+                          bool& ok) {
   const D3 inv = {ddiv(1.0, d.x), ddiv(1.0, d.y), ddiv(1.0, d.z)};
   int stack[kTsStack];
   int sp = 0;
@@ -324,22 +360,22 @@ __device__ bool any_exact(const TravArgs& A, const Pol& P, D3 o, D3 d, uint32_t 
   uint32_t iters = 0;
   ok = true;
   while (sp > 0) {
-    if (++iters > A.node_limit) {
+    if (++iters > bv.node_limit) {
       atomicOr(A.err, kErrIterations);
       ok = false;
       return false;
     }
     const int n = stack[--sp];
-    const Node nd = load_node(A.nodes, n);
+    const Node nd = load_node(bv.nodes, n);
     if (ts_slab_culled(nd.lo, nd.hi, o, inv, tMax)) continue;
     const int cnt = node_count(nd), first = node_first(nd);
     if (cnt > 0) {
       for (int k = 0; k < cnt; k++) {
         const int s = first + k;
-        const float4 a = __ldg(A.tris + 3 * (size_t)s), b = __ldg(A.tris + 3 * (size_t)s + 1),
-                     c = __ldg(A.tris + 3 * (size_t)s + 2);
+        const float4 a = __ldg(bv.tris + 3 * (size_t)s), b = __ldg(bv.tris + 3 * (size_t)s + 1),
+                     c = __ldg(bv.tris + 3 * (size_t)s + 2);
         double t, u, v;
-        if (ts_triangle(o, d, d3f(a), d3f(b), d3f(c), A.tMin, tMax, t, u, v) && P.alpha(s, key)) return true;
+        if (ts_triangle(o, d, d3f(a), d3f(b), d3f(c), A.tMin, tMax, t, u, v) && P.alpha(bv.scene, s, key)) return true;
       }
     } else if (sp + 2 <= kTsStack) {
       stack[sp++] = first + 1;
@@ -362,7 +398,7 @@ __global__ void k_anyhit_exact_t(TravArgs A, Pol P) {
     float3 o, d;
     P.ray(k, o, d);
     bool ok;
-    const bool occ = any_exact(A, P, {o.x, o.y, o.z}, {d.x, d.y, d.z}, P.key(k), P.tmax(k), ok);
+    const bool occ = any_exact(A, P, bvh_of(A, P, k), {o.x, o.y, o.z}, {d.x, d.y, d.z}, P.key(k), P.tmax(k), ok);
     P.shadow(k, ok ? occ : true);
   }
 }
@@ -385,6 +421,7 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
     const Ray32 r = make_ray32(o, d);
     const uint32_t key = P.key(k);
     const double tmax = P.tmax(k);
+    const BvhView bv = bvh_of(A, P, k);
     const float c_lo = __double2float_rd(tmax), c_hi = __double2float_ru(tmax);
     int stack[kTsStack];
     int sp = 0;
@@ -392,12 +429,12 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
     bool occ = false, ok = true;
     uint32_t iters = 0;
     while (sp > 0 && !occ) {
-      if (++iters > A.node_limit) {
+      if (++iters > bv.node_limit) {
         atomicOr(A.err, kErrIterations);
         ok = false;
         break;
       }
-      const Node nd = load_node(A.nodes, stack[--sp]);
+      const Node nd = load_node(bv.nodes, stack[--sp]);
       SlabClass cl = classify_slab(r, nd.lo, nd.hi, c_lo, c_hi);
       if (cl == kAmbiguous) cl = ts_slab_culled(nd.lo, nd.hi, {o.x, o.y, o.z}, inv_exact(d), tmax) ? kCulled : kPass;
       if (cl == kCulled) continue;
@@ -405,13 +442,13 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
       if (cnt > 0) {
         for (int q = 0; q < cnt && !occ; q++) {
           const int slot = first + q;
-          const float4 a = __ldg(A.tris + 3 * (size_t)slot), b = __ldg(A.tris + 3 * (size_t)slot + 1),
-                       c = __ldg(A.tris + 3 * (size_t)slot + 2);
+          const float4 a = __ldg(bv.tris + 3 * (size_t)slot), b = __ldg(bv.tris + 3 * (size_t)slot + 1),
+                       c = __ldg(bv.tris + 3 * (size_t)slot + 2);
           float tl, th;
           float3 est;
           const TriClass tc = mt_classify(r, a, b, c, tmin_lo, tmin_hi, c_lo, c_hi, tl, th, est);
           if (tc == kTriReject) continue;
-          if (use_alpha && !P.alpha(slot, key)) continue;
+          if (use_alpha && !P.alpha(bv.scene, slot, key)) continue;
           if (tc == kTriAccept) {
             occ = true;
           } else {

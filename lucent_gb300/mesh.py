@@ -183,12 +183,16 @@ def displace(mesh, amplitude, octaves=3, seed=0, base_cells=4.0):
     """
     p = mesh.positions.astype(np.float64).reshape(-1, 3)
     n = mesh.normals.astype(np.float64).reshape(-1, 3)
-    d = np.zeros(p.shape[0])
+    # The noise depends on the position only: evaluate it once per distinct vertex.
+    key = np.ascontiguousarray(mesh.positions.reshape(-1, 3)).view(np.dtype((np.void, 12))).reshape(-1)
+    uniq, first, inverse = np.unique(key, return_index=True, return_inverse=True)
+    pu = p[first]
+    du = np.zeros(pu.shape[0])
     amp, norm = 1.0, 0.0
     for o in range(octaves):
-        d += amp * _value_noise(p, seed + o, base_cells * (2 ** o))
+        du += amp * _value_noise(pu, seed + o, base_cells * (2 ** o))
         norm += amp
         amp *= 0.5
-    d *= amplitude / norm
+    d = du[inverse.reshape(-1)] * (amplitude / norm)
     pos = (p + n * d[:, None]).reshape(-1).astype(np.float32)
     return Mesh(pos, mesh.normals.copy(), mesh.uvs)

@@ -177,6 +177,10 @@ class Renderer:
                                     [int(x) for x in st.traversal]))
         return out
 
+    def trim(self):
+        """Frees the path-state buffers until the next trace (lucent_renderer_trim)."""
+        N.check(N.lib().lucent_renderer_trim(self._h))
+
     def set_profiling(self, enabled=True):
         N.check(N.lib().lucent_renderer_set_profiling(self._h, 1 if enabled else 0))
 
@@ -246,3 +250,100 @@ def bsdf_eval_tuples(tuples):
     out = np.zeros((t.shape[0], 24), np.float32)
     N.check(N.lib().lucent_bsdf_eval_tuples(_f(t), t.shape[0], _f(out)))
     return out
+
+
+class Batch:
+    """Several renderers traced as one wavefront (lucent_batch_*): the next
+    `samples` samples of every renderer, bit for bit what trace_samples on
+    each renderer alone would give. Options (lucent_batch_options):
+    samples_per_wave (0 = as many as max_wave_paths allows), max_wave_paths,
+    use_graph (replay a captured wave), trace_blocks / shade_blocks (grid
+    sizes, 0 = all resident blocks)."""
+
+    DEFAULTS = {"samples_per_wave": 0, "max_wave_paths": 1 << 25, "use_graph": True, "trace_blocks": 0,
+                "shade_blocks": 0}
+
+    def __init__(self, renderers, **options):
+        self.renderers = list(renderers)
+        arr = (C.c_void_p * len(self.renderers))(*[r.handle.value for r in self.renderers])
+        h = C.c_void_p()
+        N.check(N.lib().lucent_batch_create(arr, len(self.renderers), C.byref(h)))
+        self._h = h
+        self.options = dict(self.DEFAULTS)
+        self.set_options(**options)
+
+    def set_options(self, **options):
+        unknown = set(options) - set(self.DEFAULTS)
+        if unknown:
+            raise KeyError("unknown batch options: %s" % sorted(unknown))
+        self.options.update(options)
+        o = self.options
+        d = NR.BatchOptions(o["samples_per_wave"], o["max_wave_paths"], 1 if o["use_graph"] else 0,
+                            o["trace_blocks"], o["shade_blocks"])
+        N.check(N.lib().lucent_batch_set_options(self._h, C.byref(d)))
+
+    def trace_samples(self, count, stream=None):
+        N.check(N.lib().lucent_batch_trace(self._h, count, stream))
+
+    def check(self, stream=None):
+        st = NR.BatchStats()
+        N.check(N.lib().lucent_batch_check(self._h, stream, C.byref(st)))
+        return {k: int(getattr(st, k)) for k, _ in NR.BatchStats._fields_}
+
+    def signature(self):
+        """Workload key for the tuning cache: scene count, pixels, triangles, bounces."""
+        px = sum(r.width * r.height for r in self.renderers)
+        tris = sum(r.stats()["triangles"] for r in self.renderers)
+        mb = max(r.settings.max_bounces for r in self.renderers)
+        return "n%d_px%d_tri%d_b%d" % (len(self.renderers), px, tris, mb)
+
+    def autotune(self, samples=2, candidates=None, cache=None):
+        """Times `samples` samples under each candidate option set (wall clock
+        around trace + synchronise, so launch overhead counts) and keeps the
+        fastest. The samples are real: reset the renderers afterwards for a
+        fresh average. With `cache` (a JSON file path) a result for the same
+        signature() is reused, and new results are stored there.
+        Returns (chosen options, {candidate index: seconds})."""
+        import json
+        import os
+        key = self.signature()
+        if cache and os.path.exists(cache):
+            with open(cache) as f:
+                known = json.load(f)
+            if key in known:
+                self.set_options(**known[key])
+                return dict(self.options), {}
+        if candidates is None:
+            px = sum(r.width * r.height for r in self.renderers)
+            waves = [s for s in (1, 2, 4) if s * px <= 4 * self.DEFAULTS["max_wave_paths"]] or [1]
+            candidates = [{"samples_per_wave": s, "use_graph": g, "max_wave_paths": max(s * px, 1)}
+                          for s in waves for g in (True, False)]
+        base = dict(self.options)
+        times = {}
+        for i, c in enumerate(candidates):
+            self.set_options(**{**base, **c})
+            self.trace_samples(1)  # allocation and graph capture happen outside the timed call
+            self.check()
+            t0 = time.perf_counter()
+            self.trace_samples(samples)
+            self.check()
+            times[i] = time.perf_counter() - t0
+        best = min(times, key=times.get)
+        self.set_options(**{**base, **candidates[best]})
+        if cache:
+            known = {}
+            if os.path.exists(cache):
+                with open(cache) as f:
+                    known = json.load(f)
+            known[key] = {k: self.options[k] for k in candidates[best]}
+            os.makedirs(os.path.dirname(os.path.abspath(cache)), exist_ok=True)
+            with open(cache, "w") as f:
+                json.dump(known, f, indent=1, sort_keys=True)
+        return dict(self.options), times
+
+    def dispose(self):
+        if getattr(self, "_h", None):
+            N.lib().lucent_batch_destroy(self._h)
+            self._h = None
+
+    __del__ = dispose

@@ -208,3 +208,59 @@ def knot_scene(seed=0, tubular=5000, radial=200, env_width=1024):
     cam = S.Camera(position=(0.0, 0.4, 4.2), target=(0.0, 0.0, 0.0), fov=40.0, aperture=0.02,
                    focus_distance=4.22)
     return S.Scene(name="knot", camera=cam, env=env, meshes=meshes)
+
+
+def env_lognormal(rng, width, height):
+    """HDRI of lognormal(0, 1) luminance with per-texel tints U[0.8,1.2]^3
+    normalised to that luminance; draws luminance (H x W) then tints."""
+    from . import scene as S
+    lum = np.exp(rng.normal(0.0, 1.0, (height, width)))
+    tint = rng.uniform(0.8, 1.2, (height, width, 3))
+    tint /= (tint @ np.array([0.2126, 0.7152, 0.0722]))[..., None]
+    return S.HDRImage(width, height, (lum[..., None] * tint).astype(np.float32).reshape(-1))
+
+
+BATCH_RESOLUTIONS = (256, 512, 768, 1024)
+
+
+def batch_scene(seed, tri_lo=10_000, tri_hi=2_000_000):
+    """One scene of the batched workload: a displaced torus knot or
+    icosphere with a triangle count log-uniform in [tri_lo, tri_hi], four
+    layered materials, a 512 x 256 lognormal HDRI, a square resolution from
+    BATCH_RESOLUTIONS. Returns (scene, resolution).
+
+    Draw order from numpy.random.Generator(PCG64(seed)): log triangle count,
+    shape (knot if < 0.5), resolution index, knot radial segments in
+    [16, 64), then per material albedo (3), roughness, metallic, clearcoat,
+    sheen; then the HDRI.
+    """
+    from . import mesh as M
+    from . import scene as S
+    rng = np.random.Generator(np.random.PCG64(seed))
+    target = float(np.exp(rng.uniform(np.log(tri_lo), np.log(tri_hi))))
+    knot = rng.random() < 0.5
+    res = BATCH_RESOLUTIONS[int(rng.integers(0, len(BATCH_RESOLUTIONS)))]
+    radial = int(rng.integers(16, 64))
+    if knot:
+        tubular = max(8, int(round(target / (2 * radial))))
+        mesh = M.torus_knot(2, 3, 1.0, 0.32, tubular, radial)
+    else:
+        sub = int(np.clip(np.round(np.log(target / 20.0) / np.log(4.0)), 0, 9))
+        mesh = M.icosphere(sub, radius=1.2)
+    mesh = M.displace(mesh, 0.05, octaves=3, seed=seed)
+    mats = []
+    for _ in range(4):
+        alb = rng.uniform(0.2, 0.8, 3)
+        rough, metallic = rng.uniform(0.05, 1.0), float(rng.random() < 0.5)
+        coat, sheen = rng.uniform(0.0, 1.0), rng.uniform(0.0, 1.0)
+        mats.append(S.material(albedo=tuple(float(x) for x in alb), roughness=float(rough), metallic=metallic,
+                               clearcoat=float(coat), clearcoat_roughness=0.1, sheen_color=(float(sheen),) * 3,
+                               sheen_roughness=0.5))
+    n = mesh.triangle_count
+    band = (np.arange(n) * 4) // max(n, 1)
+    pos, nrm = mesh.positions.reshape(-1, 9), mesh.normals.reshape(-1, 9)
+    meshes = [S.MeshInstance(M.Mesh(pos[band == k].reshape(-1).copy(), nrm[band == k].reshape(-1).copy()), mats[k])
+              for k in range(4) if (band == k).any()]
+    env = S.Environment(map=env_lognormal(rng, 512, 256), name="lognormal", background=True)
+    cam = S.Camera(position=(0.0, 0.3, 4.0), target=(0.0, 0.0, 0.0), fov=45.0, focus_distance=4.0)
+    return S.Scene(name="batch%d" % seed, camera=cam, env=env, meshes=meshes), res
