@@ -8,6 +8,13 @@ Workloads:
            is closest-hit rays per second inside the renderer, with spp/s
   closest  random soup, 65,536 triangles, 10^6 rays, seed 0: one step = one
            closest-hit pass over all rays (the reference's intersectBVH)
+  adjoint  8 views of workloads.adjoint_scene at 512x512, 32 spp, depth 6:
+           one step = forward + path-replay backward of every view; value =
+           backward / forward time
+  batch    64 scenes of workloads.batch_scene (10^4..2*10^6 triangles,
+           256^2..1024^2 pixels), 64 spp, depth 8: one step renders every
+           scene as one batch; reports the one-renderer-after-another figure
+           beside it and whether both give identical images
 Under torchrun (N > 1) every rank runs an independent replica of the same
 workload on its own GPU (weak scaling: the work is rays, which need no
 exchange); the timed region is bracketed by barriers and the max over ranks
@@ -336,6 +343,263 @@ def cpu_pt(threads, reps=1, crop=512):
     return rays / dt / 1e6, "%dx%d centre crop of the 512x512 frame, 16 spp x %d reps" % (crop, crop, reps)
 
 
+# ----------------------------------------------------------------------------- batch workload
+BATCH_SPP, BATCH_DEPTH = 64, 8
+
+
+def _batch_setup(n):
+    from lucent_gb300 import workloads as W
+    from lucent_gb300.renderer import Renderer
+    rs = []
+    for seed in range(n):
+        sc, res = W.batch_scene(seed)
+        r = Renderer(res, res)
+        r.settings.max_bounces = BATCH_DEPTH
+        r.load_scene(sc)
+        rs.append(r)
+    return rs
+
+
+def _image_digest(r):
+    import hashlib
+    col, alb, nrm, hist = r.read()
+    h = hashlib.sha1()
+    for a in (col, alb, nrm, hist):
+        h.update(a.tobytes())
+    return h.hexdigest()
+
+
+def run_ours_batch(args, rank, world, local):
+    """Many scenes: `--batch-scenes` seeded scenes of workloads.batch_scene
+    (triangles log-uniform in [1e4, 2e6], resolutions from {256..1024}^2,
+    512x256 HDRIs), 64 spp each, depth 8. One step renders every scene once
+    (a) one renderer after another and (b) as one batch (autotuned wave size,
+    captured waves); value = batched Mpaths/s, with the sequential figure
+    and a check that both produce the same images bit for bit."""
+    import torch
+    from lucent_gb300.renderer import Batch
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    t_setup = time.perf_counter()
+    rs = _batch_setup(args.batch_scenes)
+    setup_s = time.perf_counter() - t_setup
+    px = sum(r.width * r.height for r in rs)
+    tris = sum(r.stats()["triangles"] for r in rs)
+    paths_per_step = px * BATCH_SPP
+
+    def seq_step(digests=None):
+        ms = 0.0
+        for i, r in enumerate(rs):
+            r.reset()
+            r.set_seed(1000)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r.trace_samples(BATCH_SPP, sp)
+            e1.record(stream)
+            r.check(sp)
+            ms += e0.elapsed_time(e1)
+            if digests is not None:
+                digests.append(_image_digest(r))
+            r.trim()
+        return ms
+
+    b = Batch(rs)
+    for r in rs:  # allocate each renderer's buffers once, outside the timed steps
+        r.trace_samples(1, sp)
+        r.check(sp)
+        r.trim()
+    tuned, trials = b.autotune(samples=2)
+    barrier(world)
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        seq_step()
+    seq_ms, digests = [], []
+    for k in range(args.steps):
+        seq_ms.append(seq_step(digests if k == 0 else None))
+
+    def batch_step():
+        for r in rs:
+            r.reset()
+            r.set_seed(1000)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.trace_samples(BATCH_SPP, sp)
+        e1.record(stream)
+        st = b.check(sp)
+        return e0.elapsed_time(e1), st
+
+    for _ in range(args.warmup):
+        batch_step()
+    with Clocks(local) as clk:
+        bat = [batch_step() for _ in range(args.steps)]
+    bat_ms = [m for m, _ in bat]
+    same = all(_image_digest(r) == d for r, d in zip(rs, digests))
+    # end to end: the batched call plus every image read back to host memory
+    t0 = time.perf_counter()
+    _, st = batch_step()
+    for r in rs:
+        r.read()
+    e2e_s = time.perf_counter() - t0
+    dev_b = max_over_ranks(sum(bat_ms) / 1000.0, world)
+    dev_s = max_over_ranks(sum(seq_ms) / 1000.0, world)
+    value = paths_per_step * args.steps * world / dev_b / 1e6
+    seq_value = paths_per_step * args.steps * world / dev_s / 1e6
+    return {
+        "metric": "batched path-tracing Mpaths/s: %d scenes (workloads.batch_scene seeds 0..%d), %d spp, depth %d"
+                  % (len(rs), len(rs) - 1, BATCH_SPP, BATCH_DEPTH),
+        "value": round(value, 2), "unit": "Mpaths/s", "ms_per_step": round(sum(bat_ms) / len(bat_ms), 3),
+        "e2e": {"value": round(paths_per_step * world / e2e_s / 1e6, 2), "unit": "Mpaths/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": px * 52},
+        "roofline": None, "clocks": clk.summary(), "gpu_launches": st["waves"] * (4 + 8 * (BATCH_DEPTH + 1)),
+        "dtype": "f32 (+f64 exact hit decisions)",
+        "config": {"workload": "batch: %d scenes, %d triangles, %d pixels, %d spp, depth %d" % (
+            len(rs), tris, px, BATCH_SPP, BATCH_DEPTH), "l2": "working set far above L2 (>10 GB of path state)"},
+        "extra": {"sequential_mpaths_per_s": round(seq_value, 2), "batched_over_sequential": round(dev_s / dev_b, 3),
+                  "identical_images": bool(same), "tuned_options": tuned,
+                  "autotune_trials_s": {str(k): round(v, 4) for k, v in trials.items()},
+                  "waves_per_step": st["waves"] // max(1, args.steps + args.warmup + 1), "setup_s": round(setup_s, 1)},
+    }
+
+
+def cpu_batch(threads, reps=1, crop=16):
+    """Oracle on a crop x crop window at the centre of the first 4 batch scenes, 64 spp."""
+    from lucent_gb300 import workloads as W
+    from oracle import render as R
+    paths, dt = 0, 0.0
+    for seed in range(4):
+        sc, res = W.batch_scene(seed)
+        prep = R.prepare(sc)
+        x0 = (res - crop) // 2
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            R.render(prep, res, res, 1000, BATCH_SPP, max_bounces=BATCH_DEPTH, crop=(x0, x0, crop, crop),
+                     threads=threads)
+        dt += time.perf_counter() - t0
+        paths += crop * crop * BATCH_SPP * reps
+    return paths / dt / 1e6, "%dx%d centre crops of batch scenes 0-3, %d spp" % (crop, crop, BATCH_SPP)
+
+
+# ----------------------------------------------------------------------------- adjoint workload
+ADJ_W, ADJ_SPP, ADJ_DEPTH, ADJ_VIEWS = 512, 32, 6, 8
+
+
+def run_ours_adjoint(args, rank, world, local):
+    """Inverse rendering: workloads.adjoint_scene (the box scene's geometry,
+    32 materials, 256x128 HDRI) seen from 8 views at 512x512, depth 6. One
+    step = one optimisation iteration: 32-spp forward renders of the 8 views
+    and the 32-spp path-replay backward of each (material and environment
+    gradients of an L2 image loss). value = backward / forward time ratio.
+    Also times the 8 forward views as one batch vs one by one, at 32 spp per
+    call and at 1 spp per call (progressive)."""
+    import torch
+    from lucent_gb300 import adjoint as AD
+    from lucent_gb300 import workloads as W
+    from lucent_gb300.renderer import Batch, Renderer
+    from lucent_gb300 import scene as S
+    torch.cuda.set_device(local)
+    sc = W.adjoint_scene(0, 6)
+    rs = []
+    for cam in W.adjoint_views(ADJ_VIEWS):
+        v = S.Scene(name=sc.name, camera=cam, env=sc.env, meshes=sc.meshes)
+        r = Renderer(ADJ_W, ADJ_W)
+        r.settings.max_bounces = ADJ_DEPTH
+        r.load_scene(v)
+        rs.append(r)
+    targets = [AD.forward(r, ADJ_SPP, 0) for r in rs]
+    rng = np.random.default_rng(0)
+    theta = np.clip(AD.get_params(rs[0].packed.materials) + rng.normal(0, 0.1, (rs[0].packed.material_count, 6)),
+                    0, 1).astype(np.float32)
+
+    def step():
+        tf = tb = 0.0
+        loss = 0.0
+        for r, tgt in zip(rs, targets):
+            t0 = time.perf_counter()
+            img = AD.forward(r, ADJ_SPP, 1, theta=theta)
+            tf += time.perf_counter() - t0
+            loss += float(((img - tgt) ** 2).sum())
+            t0 = time.perf_counter()
+            AD.backward(r, ADJ_SPP, 1, 2.0 * (img - tgt))
+            tb += time.perf_counter() - t0
+        return tf, tb, loss
+
+    for _ in range(args.warmup):
+        step()
+    with Clocks(local) as clk:
+        res = [step() for _ in range(args.steps)]
+    tf = sum(x[0] for x in res)
+    tb = sum(x[1] for x in res)
+    paths = ADJ_VIEWS * ADJ_W * ADJ_W * ADJ_SPP * args.steps
+
+    # forward of the 8 views: one batch vs one renderer after another
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    b = Batch(rs, use_graph=True)
+
+    def seq(spp, calls):
+        for _ in range(calls):
+            for r in rs:
+                r.trace_samples(spp)
+        for r in rs:
+            r.check()
+
+    def bat(spp, calls):
+        for _ in range(calls):
+            b.trace_samples(spp)
+        b.check()
+
+    modes = {}
+    for spp, calls in ((ADJ_SPP, 1), (1, ADJ_SPP)):
+        for r in rs:
+            r.reset()
+        seq(spp, 2)  # warm-up (allocations, graph capture)
+        bat(spp, 2)
+        for r in rs:
+            r.reset()
+        ts = timed(lambda: seq(spp, calls))
+        for r in rs:
+            r.reset()
+        tbt = timed(lambda: bat(spp, calls))
+        px = ADJ_VIEWS * ADJ_W * ADJ_W * spp * calls
+        modes["%d_spp_per_call" % spp] = {"sequential_mpaths_per_s": round(px / ts / 1e6, 2),
+                                          "batched_mpaths_per_s": round(px / tbt / 1e6, 2),
+                                          "batched_over_sequential": round(ts / tbt, 3)}
+    ratio = tb / tf
+    return {
+        "metric": "adjoint/forward time ratio: path-replay backward vs forward, 8 views 512x512, 32 spp, depth 6",
+        "value": round(ratio, 3), "unit": "x", "ms_per_step": round(1e3 * (tf + tb) / args.steps, 2),
+        "higher_is_better": False,
+        "e2e": {"value": round(ratio, 3), "unit": "x", "h2d_bytes_per_step": ADJ_VIEWS * ADJ_W * ADJ_W * 16,
+                "d2h_bytes_per_step": ADJ_VIEWS * ADJ_W * ADJ_W * 52},
+        "roofline": None, "clocks": clk.summary(), "gpu_launches": None, "dtype": "f32 (+f64 exact hit decisions)",
+        "config": {"workload": "adjoint: adjoint_scene(0, 6) (81,956 triangles, 33 materials, 256x128 HDRI), "
+                               "8 views 512x512, 32 spp forward / 32 replayed, depth 6"},
+        "extra": {"forward_ms_per_view": round(1e3 * tf / (ADJ_VIEWS * args.steps), 2),
+                  "backward_ms_per_view": round(1e3 * tb / (ADJ_VIEWS * args.steps), 2),
+                  "forward_mpaths_per_s": round(paths / tf / 1e6, 2), "loss_first_step": round(res[0][2], 3),
+                  "batched_forward": modes},
+    }
+
+
+def cpu_adjoint(threads, reps=1):
+    """Oracle forward on a 32x32 crop of view 0 at 32 spp (the backward has no CPU counterpart)."""
+    from lucent_gb300 import workloads as W
+    from oracle import render as R
+    sc = W.adjoint_scene(0, 6)
+    prep = R.prepare(sc)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        R.render(prep, ADJ_W, ADJ_W, 1, ADJ_SPP, max_bounces=ADJ_DEPTH, crop=(240, 240, 32, 32), threads=threads)
+    dt = time.perf_counter() - t0
+    return 32 * 32 * ADJ_SPP * reps / dt / 1e6, "32x32 crop of view 0, 32 spp, forward only (Mpaths/s)"
+
+
 # ----------------------------------------------------------------------------- plumbing
 _pg = None
 
@@ -365,19 +629,23 @@ def max_over_ranks(x, world):
     return float(t.item())
 
 
-WORKLOADS = {"closest": (run_ours_closest, cpu_closest, "Mrays/s"), "pt": (run_ours_pt, cpu_pt, "Mrays/s")}
+WORKLOADS = {"closest": (run_ours_closest, cpu_closest, "Mrays/s"), "pt": (run_ours_pt, cpu_pt, "Mrays/s"),
+             "batch": (run_ours_batch, cpu_batch, "Mpaths/s"), "adjoint": (run_ours_adjoint, cpu_adjoint, "Mpaths/s")}
 DEFAULT_WORKLOAD = "pt"
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None, help="default 20 (batch: 1)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-scenes", type=int, default=64, help="scenes of the batch workload")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = {"batch": 1, "adjoint": 3}.get(args.workload, 20)
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     rank, world, local = dist_env()
     run, cpu, unit = WORKLOADS[args.workload]
@@ -401,7 +669,8 @@ def main():
                                  "sample": sample + " (oracle: C++ restatement of the reference's TypeScript, "
                                                     "binary64, std::thread on all host cores; not V8)"},
                 "e2e": {"value": round(v, 3), "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        ours_metric = {"closest": "closest-hit Mrays/s (intersectBVH, 65,536-triangle soup, 1e6 rays)", "pt": PT_METRIC}
+        ours_metric = {"closest": "closest-hit Mrays/s (intersectBVH, 65,536-triangle soup, 1e6 rays)", "pt": PT_METRIC,
+                       "batch": "path-tracing Mpaths/s (batch scenes)"}
         line["metric"] = ours_metric.get(args.workload, args.workload)
         line["config"] = {"workload": args.workload}
         print(json.dumps(line), flush=True)
@@ -413,7 +682,8 @@ def main():
         return
     line = {"metric": res["metric"], "value": res["value"], "unit": res["unit"], "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms_per_step"],
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": res["dtype"],
+            "higher_is_better": res.get("higher_is_better", True), "scaling": "weak", "vs_baseline": None,
+            "dtype": res["dtype"],
             "data": "synthetic", "config": res["config"], "e2e": res["e2e"], "roofline": res["roofline"],
             "clocks": res["clocks"], "gpu_launches": res["gpu_launches"]}
     for k in ("spp_per_s", "extra"):
@@ -421,7 +691,7 @@ def main():
             line[k] = res[k]
     if world == 1 and not args.no_cpu_baseline:
         v, sample = cpu(cores)
-        line["cpu_baseline"] = {"value": round(v, 3), "unit": res["unit"], "cores": cores, "kind": "port",
+        line["cpu_baseline"] = {"value": round(v, 3), "unit": unit, "cores": cores, "kind": "port",
                                 "sample": sample + " (oracle C++ restatement, binary64, not V8)"}
     print(json.dumps(line), flush=True)
 

@@ -247,6 +247,29 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
  * the reference's GPU timer queries, renderer.ts:668-700); results appear in
  * lucent_render_stats.phase_ms after lucent_renderer_check. */
 lucent_status lucent_renderer_set_profiling(lucent_renderer* r, int32_t enabled);
+/* ---------------------------------------------------------------------------
+ * Differentiable rendering (path replay backpropagation). No reference
+ * counterpart: the reference renders forward only.
+ * ------------------------------------------------------------------------- */
+/* Replaces the packed materials (count * 40 floats, packMaterials layout,
+ * material.ts:121-149) of the loaded scene; count must equal the scene's
+ * material count. Resets the accumulation. */
+lucent_status lucent_renderer_set_materials(lucent_renderer* r, const float* materials, uint32_t count);
+/* Gradient of  sum over pixels of dl_dimage[px] . I[px]  where I is the mean
+ * of the `samples` samples starting at sample seed `seed` (what reset +
+ * set_seed(seed) + trace(samples) renders), with respect to every material's
+ * base colour (r, g, b), roughness, metallic and clearcoat (d_materials:
+ * material_count * 6 floats, in that order) and, if d_env is non-NULL, to the
+ * environment map's texels (env_width * env_height * 3 floats, rows top to
+ * bottom). Both outputs are host buffers and are ADDED to. dl_dimage: host,
+ * width * height * 4 floats (rgb used), rows bottom to top like the targets.
+ * The samples are replayed from their seeds (twice: primal radiance, then the
+ * adjoint), so memory is per wave, not per sample. Sampling is held fixed:
+ * directions, pdfs, MIS weights, lobe and Russian-roulette choices, and the
+ * firefly clamp's scale. The accumulation targets are left untouched.
+ * Synchronous. */
+lucent_status lucent_renderer_backward(lucent_renderer* r, uint32_t samples, uint32_t seed, const float* dl_dimage,
+                                       float* d_materials, float* d_env, void* stream);
 /* Frees the path-state buffers (about 315 bytes per path of the largest
  * wave traced so far); the next trace allocates them again. For hosts that
  * keep many renderers alive but trace one at a time. No reference
@@ -316,6 +339,9 @@ lucent_status lucent_batch_check(lucent_batch* batch, void* stream, lucent_batch
  * 32 floats, writing 24 floats each; the layout is documented in
  * lucent_gb300/csrc/bsdf_tuples.cu. Host buffers; synchronous. */
 lucent_status lucent_bsdf_eval_tuples(const float* tuples, uint32_t n, float* out);
+/* Same tuples through the adjoint's BSDF derivative: 24 floats each, f (3)
+ * then df/d(base colour r, g, b, roughness, metallic, clearcoat) (6 x 3). */
+lucent_status lucent_bsdf_grad_tuples(const float* tuples, uint32_t n, float* out);
 
 #ifdef __cplusplus
 }

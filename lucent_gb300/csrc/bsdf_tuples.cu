@@ -59,11 +59,42 @@ __global__ void k_bsdf_tuples(const float* __restrict__ in, uint32_t n, const fl
   }
 }
 
+// eval_opaque_grad on the same tuples: out 24 floats = f (3), then
+// df/d(albedo r, g, b, roughness, metallic, clearcoat) (6 x 3), then 3 zeros.
+__global__ void k_bsdf_grad_tuples(const float* __restrict__ in, uint32_t n, const float* __restrict__ lut,
+                                   float* __restrict__ out) {
+  LightingDev L{};
+  L.sheen_lut = lut;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float* t = in + (size_t)i * 32;
+    Surface s;
+    s.albedo = f3(t[0], t[1], t[2]);
+    s.metallic = t[3];
+    s.roughness = t[4];
+    s.ior = t[5];
+    s.transmission = 0.f;
+    s.clearcoat = t[6];
+    s.clearcoat_roughness = t[7];
+    s.sheen_color = f3(t[8], t[9], t[10]);
+    s.sheen_roughness = t[11];
+    s.thin = t[12] > 0.5f;
+    s.n = f3(t[13], t[14], t[15]);
+    s.nc = f3(t[16], t[17], t[18]);
+    s.absorption = f3(0.f, 0.f, 0.f);
+    float3 df[6];
+    const float3 f = eval_opaque_grad(L, s, f3(t[19], t[20], t[21]), f3(t[22], t[23], t[24]), df);
+    float* o = out + (size_t)i * 24;
+    o[0] = f.x, o[1] = f.y, o[2] = f.z;
+    for (int k = 0; k < 6; k++) o[3 + 3 * k] = df[k].x, o[4 + 3 * k] = df[k].y, o[5 + 3 * k] = df[k].z;
+    o[21] = o[22] = o[23] = 0.f;
+  }
+}
+
 }  // namespace lucent
 
 using namespace lucent;
 
-extern "C" lucent_status lucent_bsdf_eval_tuples(const float* tuples, uint32_t n, float* out) {
+static lucent_status run_tuples(const float* tuples, uint32_t n, float* out, bool grad) {
   clear_error();
   if (n == 0) return LUCENT_OK;
   if (!tuples || !out) return fail(LUCENT_ERR_INVALID, "null argument");
@@ -80,10 +111,21 @@ extern "C" lucent_status lucent_bsdf_eval_tuples(const float* tuples, uint32_t n
   cudaError_t e = cudaMemcpy(din, tuples, in_b, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dlut, lut, sizeof lut, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) {
-    k_bsdf_tuples<<<grid_for(n, 256), 256>>>(din, n, dlut, dout);
+    if (grad)
+      k_bsdf_grad_tuples<<<grid_for(n, 256), 256>>>(din, n, dlut, dout);
+    else
+      k_bsdf_tuples<<<grid_for(n, 256), 256>>>(din, n, dlut, dout);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpy(out, dout, out_b, cudaMemcpyDeviceToHost);
   d.release();
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "bsdf tuples");
+}
+
+extern "C" lucent_status lucent_bsdf_eval_tuples(const float* tuples, uint32_t n, float* out) {
+  return run_tuples(tuples, n, out, false);
+}
+
+extern "C" lucent_status lucent_bsdf_grad_tuples(const float* tuples, uint32_t n, float* out) {
+  return run_tuples(tuples, n, out, true);
 }

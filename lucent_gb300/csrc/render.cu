@@ -200,13 +200,6 @@ __device__ __forceinline__ void camera_path(const Paths& P, uint32_t p, uint32_t
   P.q[0][p] = p;
 }
 
-__global__ void k_camera(Paths P, CameraDev cam, int W, int H, int S, uint32_t seed0) {
-  const uint32_t WH = (uint32_t)W * H, total = WH * S;
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x)
-    camera_path(P, p, p % WH, p / WH, cam, W, H, seed0);
-  if (blockIdx.x == 0 && threadIdx.x == 0) P.ctr[kCtrQ0] = total;
-}
-
 // Index of the scene whose range [base[i], base[i + 1]) holds v (n scenes).
 __device__ __forceinline__ int find_scene(const uint32_t* __restrict__ base, int n, uint32_t v) {
   int lo = 0, hi = n - 1;
@@ -253,19 +246,85 @@ __device__ __forceinline__ bool analytic_occluded(const SceneDev& S, float3 ro, 
   return hit_ground(S, ro, rd, tmax) < tmax;
 }
 
-// Where the shade kernel finds a path's scene, lighting and settings: one
-// scene per launch (kernel parameters) or a per-path scene index into a
-// table of SceneRec.
-struct OneScene {
-  SceneDev S;
-  LightingDev L;
-  int max_bounces;
-  float clamp;
-  __device__ const SceneDev& scene(uint32_t) const { return S; }
-  __device__ const LightingDev& light(uint32_t) const { return L; }
-  __device__ int bounces(uint32_t) const { return max_bounces; }
-  __device__ float uclamp(uint32_t) const { return clamp; }
+// Path-replay adjoint state (used by the ADJ instantiation of k_shade_t).
+// Gradients are of sum_pixels dl[pixel] . (mean radiance of the replayed
+// samples) with respect to each material's base colour (3), roughness,
+// metallic and clearcoat (dmat, 6 floats per material) and to the
+// environment texels (denv, 3 floats per texel). Sampling (directions,
+// pdfs, MIS weights, lobe and Russian-roulette choices, the firefly clamp's
+// scale) is held fixed, as in path replay backpropagation.
+struct AdjointDev {
+  const float4* dl;  // per pixel: dL/dI (rgb) / samples
+  float4* lrem;      // per path: radiance still to come (primal total minus what is accounted for)
+  float4* gcont;     // per path, 5 float4: dl_c * df_c/dtheta_p / f_c at the BSDF-sampled direction (18), material
+  float4* gslot;     // per shadow slot, 2 float4: dl . c * df/f for its light direction (6), material
+  float4* genv;      // per path: environment sample uv and scale (rgb) of its env shadow slot
+  float* dmat;
+  float* denv;       // nullptr: no environment gradient
+  uint32_t WH;
+  int primal;        // 1: the primal replay (paths only, no adjoint work)
 };
+
+// Adds g[0..5] to dmat[mat * 6 ..], one atomic per distinct material per warp.
+__device__ __forceinline__ void add_material_grad(float* dmat, int mat, const float g[6]) {
+  const unsigned act = __activemask();
+  const unsigned peers = __match_any_sync(act, mat);
+  const int leader = __ffs(peers) - 1;
+  const int lane = threadIdx.x & 31;
+  float sum[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (unsigned b = peers; b; b &= b - 1) {
+    const int src = __ffs(b) - 1;
+#pragma unroll
+    for (int k = 0; k < 6; k++) sum[k] += __shfl_sync(peers, g[k], src);
+  }
+  if (lane == leader && mat >= 0)
+#pragma unroll
+    for (int k = 0; k < 6; k++)
+      if (sum[k] != 0.f) atomicAdd(dmat + (size_t)mat * 6 + k, sum[k]);
+}
+
+// Environment texel gradient: sv_c * bilinear weight into each of 4 texels.
+__device__ __forceinline__ void add_env_grad(const AdjointDev& A, const LightingDev& L, float2 uv, float3 dl, float3 sv) {
+  int idx[4];
+  float wt[4];
+  bilinear_taps(L.env_w, L.env_h, uv.x, uv.y, true, idx, wt);
+  const float g[3] = {dl.x * sv.x, dl.y * sv.y, dl.z * sv.z};
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+      if (g[c] * wt[k] != 0.f) atomicAdd(A.denv + (size_t)idx[k] * 3 + c, g[c] * wt[k]);
+}
+
+// The clamp_c scale factor (1 when unclamped).
+__device__ __forceinline__ float clamp_scale(float3 c, int bounce, float uclamp) {
+  if (bounce == 0 || uclamp <= 0.f) return 1.f;
+  const float l = lum(c);
+  return l > uclamp ? uclamp / l : 1.f;
+}
+
+// dl . (c (.) df_p / f) for p = 0..5 (zero where f is zero).
+__device__ __forceinline__ void contract_grad(float3 dl, float3 c, float3 f, const float3 df[6], float g[6]) {
+  const float w[3] = {f.x != 0.f ? dl.x * c.x / f.x : 0.f, f.y != 0.f ? dl.y * c.y / f.y : 0.f,
+                      f.z != 0.f ? dl.z * c.z / f.z : 0.f};
+#pragma unroll
+  for (int k = 0; k < 6; k++) g[k] = w[0] * df[k].x + w[1] * df[k].y + w[2] * df[k].z;
+}
+
+// Gradient of one next-event contribution c (light direction wi) with respect
+// to the vertex's material, stored in its shadow slot until occlusion is known.
+__device__ __forceinline__ void nee_grad(const AdjointDev& A, const LightingDev& L, const Surface& s, float3 wo,
+                                         float3 wi, float3 dl, float3 c, int material, uint32_t slot) {
+  float3 df[6];
+  const float3 fg = eval_opaque_grad(L, s, wo, wi, df);
+  float g[6];
+  contract_grad(dl, c, fg, df, g);
+  A.gslot[2 * (size_t)slot] = make_float4(g[0], g[1], g[2], g[3]);
+  A.gslot[2 * (size_t)slot + 1] = make_float4(g[4], g[5], __int_as_float(material), 0.f);
+}
+
+// Where the shade kernel finds a path's scene, lighting and settings: a
+// per-path scene index into a table of SceneRec.
 struct SceneTable {
   const SceneRec* recs;
   const uint16_t* sid;
@@ -276,8 +335,9 @@ struct SceneTable {
   __device__ float uclamp(uint32_t p) const { return rec(p).clamp; }
 };
 
-template <class Src>
-__global__ void __launch_bounds__(128) k_shade_t(Paths P, const __grid_constant__ Src src, int cur, int bounce) {
+template <class Src, bool ADJ = false>
+__global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_constant__ Src src, int cur, int bounce,
+                                                    const __grid_constant__ AdjointDev A = AdjointDev{}) {
   const uint32_t n = P.ctr[kCtrQ0 + cur];
   const uint32_t* q = P.q[cur];
   uint32_t* qn = P.q[cur ^ 1];
@@ -297,6 +357,14 @@ __global__ void __launch_bounds__(128) k_shade_t(Paths P, const __grid_constant_
     uint32_t st = P.rng[p];
     const float4 hv = P.hit[p];
     bool alive = false;
+    float3 dl = f3(0.f, 0.f, 0.f), lrem = f3(0.f, 0.f, 0.f);
+    int cont_mat = -1;
+    const bool adj = ADJ && !A.primal;
+    if (adj) {
+      const float4 l4 = A.lrem[p];
+      dl = l4.w == 0.f ? f3(A.dl[p % A.WH]) : f3(0.f, 0.f, 0.f);  // w != 0: the sample was dropped (NaN)
+      lrem = f3(l4);
+    }
 
     // traceScene (scene.glsl:192-333): spheres, ground, then the triangle hit.
     float closest = INF;
@@ -327,6 +395,13 @@ __global__ void __launch_bounds__(128) k_shade_t(Paths P, const __grid_constant_
       if (!tri && best_sphere < 0 && !ground) {  // miss (trace.frag:146-155)
         const float3 env = bounce == 0 && !L.env_background ? L.backdrop : environment(L, rd, spec, bsdf_pdf);
         rad = rad + clamp_c(thr * env, bounce, uclamp);
+        if (adj) {
+          if (A.denv && !(bounce == 0 && !L.env_background)) {
+            const float w = (!spec && L.env_sampling) ? mis(bsdf_pdf, env_pdf(L, rd)) : 1.f;
+            const float k = clamp_scale(thr * env, bounce, uclamp) * w * L.env_intensity;
+            add_env_grad(A, L, equirect_uv(env_to_local(L, rd)), dl, thr * k);
+          }
+        }
         if (!done) {
           galb = make_float4(tint.x, tint.y, tint.z, galb.w);
           gnrm = make_float4(-rd.x, -rd.y, -rd.z, gnrm.w);
@@ -411,6 +486,7 @@ __global__ void __launch_bounds__(128) k_shade_t(Paths P, const __grid_constant_
         float w = 1.f;
         if (!spec && light >= 0) w = mis(bsdf_pdf, light_pdf(S, light, ro, rd, closest) / (float)S.light_count);
         rad = rad + clamp_c(thr * emission * w, bounce, uclamp);
+        if (adj) lrem = lrem - clamp_c(thr * emission * w, bounce, uclamp);
         if (!done) {
           galb = make_float4(tint.x, tint.y, tint.z, galb.w);
           gnrm = make_float4(s.n.x, s.n.y, s.n.z, gnrm.w);
@@ -431,6 +507,14 @@ __global__ void __launch_bounds__(128) k_shade_t(Paths P, const __grid_constant_
         bool refl;
         if (!sample_dielectric(s, front, gn, wo, wi, weight, refl, U)) break;
         thr = thr * weight;
+        if (adj) {
+          if (!refl) {  // transmission weight = base colour: d/d albedo_c of what follows = lrem_c / albedo_c
+            const float g[6] = {s.albedo.x > 0.f ? dl.x * lrem.x / s.albedo.x : 0.f,
+                                s.albedo.y > 0.f ? dl.y * lrem.y / s.albedo.y : 0.f,
+                                s.albedo.z > 0.f ? dl.z * lrem.z / s.albedo.z : 0.f, 0.f, 0.f, 0.f};
+            add_material_grad(A.dmat, material, g);
+          }
+        }
         if (!done) tint = tint * weight;
         ro = offset_ray(pos, refl ? gn : -gn);
         rd = wi;
@@ -449,7 +533,9 @@ __global__ void __launch_bounds__(128) k_shade_t(Paths P, const __grid_constant_
             float pb;
             const float3 f = eval_opaque(L, s, wo, wi, pb);
             const float w = mis(L.sun_pdf, pb);
-            emit_shadow(P, p, 0, so, wi, INF, st, clamp_c(thr * f * NdotL * L.sun_radiance * (w / L.sun_pdf), bounce, uclamp));
+            const float3 c = clamp_c(thr * f * NdotL * L.sun_radiance * (w / L.sun_pdf), bounce, uclamp);
+            emit_shadow(P, p, 0, so, wi, INF, st, c);
+            if (adj) nee_grad(A, L, s, wo, wi, dl, c, material, 3 * p + 0);
           }
         }
         if (L.env_sampling) {  // :228-237
@@ -459,7 +545,15 @@ __global__ void __launch_bounds__(128) k_shade_t(Paths P, const __grid_constant_
             float pb;
             const float3 f = eval_opaque(L, s, wo, ls.dir, pb);
             const float w = mis(ls.pdf, pb);
-            emit_shadow(P, p, 1, so, ls.dir, INF, st, clamp_c(thr * f * NdotL * ls.radiance * (w / ls.pdf), bounce, uclamp));
+            const float3 cu = thr * f * NdotL * ls.radiance * (w / ls.pdf);
+            const float3 c = clamp_c(cu, bounce, uclamp);
+            emit_shadow(P, p, 1, so, ls.dir, INF, st, c);
+            if (adj) {
+              nee_grad(A, L, s, wo, ls.dir, dl, c, material, 3 * p + 1);
+              const float3 sv = thr * f * (clamp_scale(cu, bounce, uclamp) * NdotL * (w / ls.pdf) * L.env_intensity);
+              A.genv[2 * (size_t)p] = make_float4(ls.uv.x, ls.uv.y, sv.x, sv.y);
+              A.genv[2 * (size_t)p + 1] = make_float4(sv.z, 0.f, 0.f, 0.f);
+            }
           }
         }
         if (S.light_count > 0) {  // :240-252
@@ -473,11 +567,30 @@ __global__ void __launch_bounds__(128) k_shade_t(Paths P, const __grid_constant_
             float pb;
             const float3 f = eval_opaque(L, s, wo, ls.dir, pb);
             const float w = mis(pl, pb);
-            emit_shadow(P, p, 2, so, ls.dir, tmax, st, clamp_c(thr * f * NdotL * ls.radiance * (w / pl), bounce, uclamp));
+            const float3 c = clamp_c(thr * f * NdotL * ls.radiance * (w / pl), bounce, uclamp);
+            emit_shadow(P, p, 2, so, ls.dir, tmax, st, c);
+            if (adj) nee_grad(A, L, s, wo, ls.dir, dl, c, material, 3 * p + 2);
           }
         }
         const BsdfSample bs = sample_opaque(L, s, wo, U);  // :255-261
         if (bs.pdf <= 0.f || dot3(bs.dir, gn) <= 0.f) break;
+        if (adj) {
+          float3 df[6];
+          const float3 fg = eval_opaque_grad(L, s, wo, bs.dir, df);
+          const float w[3] = {fg.x != 0.f ? dl.x / fg.x : 0.f, fg.y != 0.f ? dl.y / fg.y : 0.f,
+                              fg.z != 0.f ? dl.z / fg.z : 0.f};
+          float gc[18];
+#pragma unroll
+          for (int k = 0; k < 6; k++) gc[3 * k] = w[0] * df[k].x, gc[3 * k + 1] = w[1] * df[k].y, gc[3 * k + 2] = w[2] * df[k].z;
+          float4* o = A.gcont + 5 * (size_t)p;
+          o[0] = make_float4(gc[0], gc[1], gc[2], gc[3]);
+          o[1] = make_float4(gc[4], gc[5], gc[6], gc[7]);
+          o[2] = make_float4(gc[8], gc[9], gc[10], gc[11]);
+          o[3] = make_float4(gc[12], gc[13], gc[14], gc[15]);
+          o[4].x = gc[16];
+          o[4].y = gc[17];
+          cont_mat = material;
+        }
         thr = thr * bs.weight;
         bsdf_pdf = bs.pdf;
         spec = false;
@@ -486,11 +599,19 @@ __global__ void __launch_bounds__(128) k_shade_t(Paths P, const __grid_constant_
       }
       if (bounce >= 2) {  // Russian roulette (:265-269)
         const float pr = fminf(0.95f, max3(thr));
-        if (rnd(st) >= pr) break;
+        if (rnd(st) >= pr) {
+          cont_mat = -1;
+          break;
+        }
         thr = thr / pr;
       }
       alive = bounce < max_bounces;
+      if (!alive) cont_mat = -1;
     } while (false);
+    if (adj) {
+      A.lrem[p].x = lrem.x, A.lrem[p].y = lrem.y, A.lrem[p].z = lrem.z;
+      A.gcont[5 * (size_t)p + 4].z = __int_as_float(cont_mat);
+    }
 
     P.rad[p] = make_float4(rad.x, rad.y, rad.z, 0.f);
     P.galb[p] = galb;
@@ -531,6 +652,67 @@ __global__ void k_resolve(Paths P, int cur) {
   }
 }
 
+// k_resolve for the adjoint replay: the unoccluded next-event contributions
+// leave the path's remaining radiance and add their material (and
+// environment) gradients; what remains is the radiance that followed the
+// BSDF-sampled direction, whose gradient is lrem (.) dl (.) df/f.
+__global__ void k_resolve_adjoint(Paths P, const __grid_constant__ AdjointDev A, const SceneRec* __restrict__ rec,
+                                  int cur) {
+  const LightingDev& L = rec->light;
+  const uint32_t n = P.ctr[kCtrQ0 + cur];
+  const uint32_t* q = P.q[cur];
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const uint32_t p = q[k];
+    float4 r = P.rad[p];
+    const float4 l4 = A.lrem[p];
+    float3 lrem = f3(l4);
+    const float3 dl = l4.w == 0.f ? f3(A.dl[p % A.WH]) : f3(0.f, 0.f, 0.f);
+    float g[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int mat = -1;
+    for (int j = 0; j < 3; j++) {
+      const uint32_t s = 3 * p + j;
+      const float4 c = P.sh_c[s];
+      if (c.w == 0.f) continue;
+      if (!P.sh_occ[s]) {
+        r.x += c.x;
+        r.y += c.y;
+        r.z += c.z;
+        lrem = lrem - f3(c);
+        const float4 a = A.gslot[2 * (size_t)s], b = A.gslot[2 * (size_t)s + 1];
+        g[0] += a.x, g[1] += a.y, g[2] += a.z, g[3] += a.w, g[4] += b.x, g[5] += b.y;
+        mat = __float_as_int(b.z);
+        if (j == 1 && A.denv) {
+          const float4 e0 = A.genv[2 * (size_t)p], e1 = A.genv[2 * (size_t)p + 1];
+          add_env_grad(A, L, make_float2(e0.x, e0.y), dl, f3(e0.z, e0.w, e1.x));
+        }
+      }
+      P.sh_c[s].w = 0.f;
+    }
+    const float4* gc = A.gcont + 5 * (size_t)p;
+    const int cm = __float_as_int(gc[4].z);
+    if (cm >= 0) {
+      mat = cm;
+      const float4 a = gc[0], b = gc[1], c = gc[2], d = gc[3], e = gc[4];
+      const float v[18] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w, d.x, d.y, d.z, d.w, e.x, e.y};
+#pragma unroll
+      for (int t = 0; t < 6; t++) g[t] += lrem.x * v[3 * t] + lrem.y * v[3 * t + 1] + lrem.z * v[3 * t + 2];
+    }
+    P.rad[p] = r;
+    A.lrem[p] = make_float4(lrem.x, lrem.y, lrem.z, l4.w);
+    add_material_grad(A.dmat, mat, g);
+  }
+}
+
+// Primal radiance of each replayed sample -> the adjoint replay's remaining
+// radiance (a dropped NaN/inf sample is flagged in w and contributes nothing).
+__global__ void k_seed_lrem(Paths P, AdjointDev A, uint32_t total) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+    const float4 c = P.rad[p];
+    const bool bad = isnan(c.x) || isnan(c.y) || isnan(c.z) || isinf(c.x) || isinf(c.y) || isinf(c.z);
+    A.lrem[p] = bad ? make_float4(0.f, 0.f, 0.f, 1.f) : make_float4(c.x, c.y, c.z, 0.f);
+  }
+}
+
 // Running means (trace.frag:335-354) of one pixel over the batch's samples,
 // in order; sample s of the pixel is path path_base + s * W * H + px.
 __device__ __forceinline__ void accumulate_pixel(const Paths& P, const AccumDev& A, uint32_t WH, int S, uint32_t px,
@@ -560,12 +742,6 @@ __device__ __forceinline__ void accumulate_pixel(const Paths& P, const AccumDev&
   A.albedo[px] = make_half4(alb);
   A.normal[px] = make_half4(nrm);
   A.history[px] = n;
-}
-
-__global__ void k_accumulate(Paths P, AccumDev A, int W, int H, int S) {
-  const uint32_t WH = (uint32_t)W * H;
-  for (uint32_t px = blockIdx.x * blockDim.x + threadIdx.x; px < WH; px += gridDim.x * blockDim.x)
-    accumulate_pixel(P, A, WH, S, px, 0);
 }
 
 // Scene i owns batch pixels [pix_base[i], pix_base[i + 1]).
@@ -603,52 +779,14 @@ __global__ void k_count_rays(uint32_t* ctr, int cur) {  // statistics: rays trac
   }
 }
 
-// ------------------------------------------------------------ one batch
-void render_batch(const RenderLaunch& R, cudaStream_t s, PhaseEvents* pe) {
-  const Paths& P = R.paths;
-  const uint32_t total = (uint32_t)R.W * R.H * R.S;
-  const int blocks = grid_for(total, 256);
+// ------------------------------------------------------------ one wave
+void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
+  const Paths& P = M.paths;
   PhaseEvents none{nullptr, nullptr, 0, 0};
   PhaseEvents& E = pe ? *pe : none;
   E.mark(-1, s);
-  k_camera<<<blocks, 256, 0, s>>>(P, R.cam, R.W, R.H, R.S, R.seed0);
-  E.mark(kPhCamera, s);
-  static int closest_blocks = 0, shade_blocks = 0;
-  if (!closest_blocks) {
-    closest_blocks = persistent_blocks((const void*)k_closest_fast_t<PathClosest>, 256);
-    shade_blocks = persistent_blocks((const void*)k_shade_t<OneScene>, 128);
-  }
-  for (int b = 0; b <= R.max_bounces; b++) {
-    const int cur = b & 1;
-    k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
-    E.mark(kPhResolve, s);
-    PathClosest pc{P.ctr + kCtrQ0 + cur, P.q[cur], P.ro, P.rd, P.rng, P.hit, R.scene.geo, R.scene.materials,
-                   R.scene.any_alpha};
-    TravArgs A{R.scene.nodes, R.scene.node_count, R.scene.geo, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow,
-               P.ctr + kCtrWork, P.ctr + kCtrErr, R.trav_stats};
-    k_closest_fast_t<PathClosest><<<closest_blocks, 256, 0, s>>>(A, pc);
-    k_closest_exact_t<PathClosest><<<64, 128, 0, s>>>(A, pc);
-    E.mark(kPhClosest, s);
-    k_shade_t<OneScene><<<shade_blocks, 128, 0, s>>>(P, OneScene{R.scene, R.light, R.max_bounces, R.clamp}, cur, b);
-    E.mark(kPhShade, s);
-    PathShadow ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, R.scene.geo, R.scene.materials, R.scene.any_alpha};
-    TravArgs B{R.scene.nodes, R.scene.node_count, R.scene.geo, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2,
-               P.ctr + kCtrWork2, P.ctr + kCtrErr};
-    k_anyhit_fast_t<PathShadow><<<shade_blocks * 2, 256, 0, s>>>(B, ps);
-    k_anyhit_exact_t<PathShadow><<<64, 128, 0, s>>>(B, ps);
-    E.mark(kPhShadow, s);
-    k_resolve<<<shade_blocks, 128, 0, s>>>(P, cur);
-    k_count_rays<<<1, 32, 0, s>>>(P.ctr, cur);
-  }
-  E.mark(kPhResolve, s);
-  k_accumulate<<<grid_for((uint32_t)R.W * R.H, 256), 256, 0, s>>>(P, R.accum, R.W, R.H, R.S);
-  E.mark(kPhAccumulate, s);
-}
-
-// ------------------------------------------------------------ one multi-scene wave
-void render_wave_multi(const MultiLaunch& M, cudaStream_t s) {
-  const Paths& P = M.paths;
   k_camera_multi<<<grid_for(M.total_paths, 256), 256, 0, s>>>(P, M.recs, M.path_base, M.n, M.sid, M.S);
+  E.mark(kPhCamera, s);
   static int max_closest = 0, max_shade = 0;
   if (!max_closest) {
     max_closest = persistent_blocks((const void*)k_closest_fast_t<PathClosestMulti>, 256);
@@ -659,20 +797,64 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s) {
   for (int b = 0; b <= M.max_bounces; b++) {
     const int cur = b & 1;
     k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
+    E.mark(kPhResolve, s);
     PathClosestMulti pc{P.ctr + kCtrQ0 + cur, P.q[cur], P.ro, P.rd, P.rng, P.hit, M.recs, M.sid, M.any_alpha};
-    TravArgs A{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr};
+    TravArgs A{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
+               M.trav_stats};
     k_closest_fast_t<PathClosestMulti><<<closest_blocks, 256, 0, s>>>(A, pc);
     k_closest_exact_t<PathClosestMulti><<<64, 128, 0, s>>>(A, pc);
+    E.mark(kPhClosest, s);
     k_shade_t<SceneTable><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b);
+    E.mark(kPhShade, s);
     PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};
     TravArgs B{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr};
     k_anyhit_fast_t<PathShadowMulti><<<shade_blocks * 2, 256, 0, s>>>(B, ps);
     k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, s>>>(B, ps);
+    E.mark(kPhShadow, s);
     k_resolve<<<shade_blocks, 128, 0, s>>>(P, cur);
     k_count_rays<<<1, 32, 0, s>>>(P.ctr, cur);
   }
+  E.mark(kPhResolve, s);
   k_accumulate_multi<<<grid_for(M.total_pixels, 256), 256, 0, s>>>(P, M.recs, M.pix_base, M.path_base, M.n, M.S);
   k_advance_seeds<<<1, 64, 0, s>>>(M.recs, M.n, M.S);
+  E.mark(kPhAccumulate, s);
+}
+
+// ------------------------------------------------------------ path replay backpropagation
+// Replays the wave's samples twice with the adjoint instantiation of the
+// shade kernel (one instantiation, so both replays make identical choices):
+// first with the adjoint work off to recover each sample's primal radiance,
+// then propagating dl through every vertex.
+void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t s) {
+  const Paths& P = M.paths;
+  const SceneRec* rec = M.recs;
+  static int closest_blocks = 0, shade_blocks = 0;
+  if (!closest_blocks) {
+    closest_blocks = persistent_blocks((const void*)k_closest_fast_t<PathClosestMulti>, 256);
+    shade_blocks = persistent_blocks((const void*)k_shade_t<SceneTable, true>, 128);
+  }
+  for (int pass = 0; pass < 2; pass++) {
+    const AdjointDev A{H.dl, H.lrem, H.gcont, H.gslot, H.genv, H.dmat, H.denv, M.total_pixels, pass == 0 ? 1 : 0};
+    k_camera_multi<<<grid_for(M.total_paths, 256), 256, 0, s>>>(P, M.recs, M.path_base, M.n, M.sid, M.S);
+    for (int b = 0; b <= M.max_bounces; b++) {
+      const int cur = b & 1;
+      k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
+      PathClosestMulti pc{P.ctr + kCtrQ0 + cur, P.q[cur], P.ro, P.rd, P.rng, P.hit, M.recs, M.sid, M.any_alpha};
+      TravArgs TA{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr};
+      k_closest_fast_t<PathClosestMulti><<<closest_blocks, 256, 0, s>>>(TA, pc);
+      k_closest_exact_t<PathClosestMulti><<<64, 128, 0, s>>>(TA, pc);
+      k_shade_t<SceneTable, true><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b, A);
+      PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};
+      TravArgs TB{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr};
+      k_anyhit_fast_t<PathShadowMulti><<<shade_blocks * 2, 256, 0, s>>>(TB, ps);
+      k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, s>>>(TB, ps);
+      if (pass == 0)
+        k_resolve<<<shade_blocks, 128, 0, s>>>(P, cur);
+      else
+        k_resolve_adjoint<<<shade_blocks, 128, 0, s>>>(P, A, rec, cur);
+    }
+    if (pass == 0) k_seed_lrem<<<grid_for(M.total_paths, 256), 256, 0, s>>>(P, A, M.total_paths);
+  }
 }
 
 }  // namespace lucent

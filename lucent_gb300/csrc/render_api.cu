@@ -204,6 +204,11 @@ struct lucent_renderer {
   double phase_ms[kPhases] = {0, 0, 0, 0, 0, 0};
   // denoiser ping-pong targets, guide buffers, display staging
   DeviceBuffer den_a, den_b, guide0, guide1, disp;
+  // path-replay backward pass
+  DeviceBuffer adj_dl, adj_path, adj_grad;
+  // a renderer traces as a launch of one scene: its SceneRec, path/pixel bases (full and last wave), scene index per path
+  DeviceBuffer rec1, base1, sid1;
+  uint32_t sid_cap = 0;
   const float4* denoised = nullptr;  // result of the last lucent_renderer_denoise, or null
 };
 
@@ -276,6 +281,67 @@ static lucent_status alloc_paths(lucent_renderer* r, uint32_t cap) {
   return alloc_path_buffers(r->paths, r->ctr, r->path_cap, r->P, cap);
 }
 
+static SceneRec scene_rec(const lucent_renderer* r) {
+  SceneRec R{};
+  R.scene = {(const Node*)r->nodes.ptr, r->node_count, (const float4*)r->geo.ptr, (const float4*)r->attr.ptr,
+             (const float4*)r->mats.ptr, (const float4*)r->spheres.ptr, (const int*)r->sph_mat.ptr,
+             (const int*)r->sph_light.ptr, (int)r->sphere_count, (const float4*)r->lights.ptr, (int)r->light_count,
+             r->ground_enabled ? r->ground_material : -1, r->ground_height, r->any_alpha};
+  R.light = r->light;
+  R.cam = r->cam;
+  R.accum = {(float4*)r->color.ptr, (half4*)r->albedo.ptr, (half4*)r->normal.ptr, (float*)r->history.ptr};
+  R.W = (int)r->W;
+  R.H = (int)r->H;
+  R.max_bounces = (int)r->max_bounces;
+  R.clamp = r->clamp;
+  R.seed0 = r->seed;
+  return R;
+}
+
+// The renderer as a launch of one scene: uploads its SceneRec (sample seed
+// `seed0`) and the path/pixel bases of a full wave of S samples and of a last
+// wave of `tail` samples; fills M for the full wave.
+static lucent_status single_launch(lucent_renderer* r, uint32_t S, uint32_t tail, uint32_t seed0, cudaStream_t s,
+                                   MultiLaunch& M) {
+  const uint32_t WH = r->W * r->H;
+  lucent_status st = alloc_paths(r, S * WH);
+  if (st) return st;
+  if (r->path_cap > r->sid_cap) {
+    if ((st = r->sid1.reserve((size_t)r->path_cap * 2))) return st;
+    if (cudaMemset(r->sid1.ptr, 0, (size_t)r->path_cap * 2) != cudaSuccess) return cuda_fail(cudaGetLastError(), "clear sid");
+    r->sid_cap = r->path_cap;
+  }
+  if ((st = r->rec1.reserve(sizeof(SceneRec))) || (st = r->base1.reserve(32))) return st;
+  SceneRec rec = scene_rec(r);
+  rec.seed0 = seed0;
+  const uint32_t bases[8] = {0, WH * S, 0, WH, 0, WH * tail, 0, WH};
+  // pageable host-to-device copies are staged before the call returns, so the locals may go
+  cudaError_t e = cudaMemcpyAsync(r->rec1.ptr, &rec, sizeof rec, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(r->base1.ptr, bases, sizeof bases, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "upload scene record");
+  M = MultiLaunch{};
+  M.paths = r->P;
+  M.recs = (SceneRec*)r->rec1.ptr;
+  M.path_base = (const uint32_t*)r->base1.ptr;
+  M.pix_base = M.path_base + 2;
+  M.sid = (uint16_t*)r->sid1.ptr;
+  M.n = 1;
+  M.S = (int)S;
+  M.max_bounces = (int)r->max_bounces;
+  M.total_paths = WH * S;
+  M.total_pixels = WH;
+  M.any_alpha = r->any_alpha;
+  return LUCENT_OK;
+}
+
+// Switches M to the last wave of `tail` samples.
+static void single_tail(lucent_renderer* r, uint32_t tail, MultiLaunch& M) {
+  M.S = (int)tail;
+  M.total_paths = r->W * r->H * tail;
+  M.path_base = (const uint32_t*)r->base1.ptr + 4;
+  M.pix_base = M.path_base + 2;
+}
+
 extern "C" {
 
 lucent_status lucent_renderer_create(uint32_t width, uint32_t height, lucent_renderer** out) {
@@ -308,7 +374,7 @@ void lucent_renderer_destroy(lucent_renderer* r) {
   if (!r) return;
   for (DeviceBuffer* b : {&r->nodes, &r->geo, &r->attr, &r->mats, &r->spheres, &r->sph_mat, &r->sph_light,
                           &r->lights, &r->env_rgb, &r->env_alias, &r->sheen, &r->color, &r->albedo, &r->normal,
-                          &r->history, &r->paths, &r->ctr, &r->den_a, &r->den_b, &r->guide0, &r->guide1, &r->disp})
+                          &r->history, &r->paths, &r->ctr, &r->den_a, &r->den_b, &r->guide0, &r->guide1, &r->disp, &r->adj_dl, &r->adj_path, &r->adj_grad, &r->rec1, &r->base1, &r->sid1})
     b->release();
   if (r->ev0) cudaEventDestroy(r->ev0);
   if (r->ev1) cudaEventDestroy(r->ev1);
@@ -535,36 +601,89 @@ lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* 
   cudaStream_t s = (cudaStream_t)stream;
   const uint32_t WH = r->W * r->H;
   const uint32_t max_paths = 1u << 23;
-  uint32_t batch = std::max(1u, std::min(samples, max_paths / std::max(1u, WH)));
-  lucent_status st = alloc_paths(r, batch * WH);
+  const uint32_t batch = std::max(1u, std::min(samples, max_paths / std::max(1u, WH)));
+  const uint32_t full = samples / batch, tail = samples % batch;
+  MultiLaunch M{};
+  lucent_status st = single_launch(r, batch, tail, r->seed, s, M);
   if (st) return st;
-  RenderLaunch R;
-  R.paths = r->P;
-  R.scene = {(const Node*)r->nodes.ptr, r->node_count, (const float4*)r->geo.ptr, (const float4*)r->attr.ptr,
-             (const float4*)r->mats.ptr, (const float4*)r->spheres.ptr, (const int*)r->sph_mat.ptr,
-             (const int*)r->sph_light.ptr, (int)r->sphere_count, (const float4*)r->lights.ptr, (int)r->light_count,
-             r->ground_enabled ? r->ground_material : -1, r->ground_height, r->any_alpha};
-  R.light = r->light;
-  R.cam = r->cam;
-  R.accum = accum_of(r);
-  R.W = (int)r->W;
-  R.H = (int)r->H;
-  R.max_bounces = (int)r->max_bounces;
-  R.clamp = r->clamp;
-  R.trav_stats = r->profiling ? (unsigned long long*)((uint32_t*)r->ctr.ptr + kCtrTrav) : nullptr;
+  M.trav_stats = r->profiling ? (unsigned long long*)((uint32_t*)r->ctr.ptr + kCtrTrav) : nullptr;
   cudaEventRecord(r->ev0, s);
   PhaseEvents pe{r->pev.data(), r->ptag.data(), (int)r->pev.size(), 0};
-  for (uint32_t done = 0; done < samples; done += batch) {
-    R.S = (int)std::min(batch, samples - done);
-    R.seed0 = r->seed;
-    render_batch(R, s, r->profiling ? &pe : nullptr);
-    r->seed += (uint32_t)R.S;
-    r->frame += (uint32_t)R.S;
+  for (uint32_t w = 0; w < full + (tail ? 1 : 0); w++) {
+    if (w == full) single_tail(r, tail, M);
+    render_wave_multi(M, s, r->profiling ? &pe : nullptr);  // seeds advance on the device
   }
+  r->seed += samples;
+  r->frame += samples;
   cudaEventRecord(r->ev1, s);
   r->pn = pe.n;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "trace launch");
+}
+
+lucent_status lucent_renderer_set_materials(lucent_renderer* r, const float* materials, uint32_t count) {
+  clear_error();
+  if (!r || !materials) return fail(LUCENT_ERR_INVALID, "null argument");
+  if (!r->has_scene) return fail(LUCENT_ERR_INVALID, "set_materials before load_scene");
+  if (count != r->material_count)
+    return fail(LUCENT_ERR_INVALID, "scene has %u materials, got %u", r->material_count, count);
+  for (size_t i = 0; i < (size_t)count * 40; i++)
+    if (!std::isfinite(materials[i])) return fail(LUCENT_ERR_INVALID, "material value %zu is not finite", i);
+  cudaError_t e = cudaMemcpy(r->mats.ptr, materials, (size_t)count * 160, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "upload materials");
+  return lucent_renderer_reset(r);
+}
+
+lucent_status lucent_renderer_backward(lucent_renderer* r, uint32_t samples, uint32_t seed, const float* dl_dimage,
+                                       float* d_materials, float* d_env, void* stream) {
+  clear_error();
+  if (!r || !dl_dimage || !d_materials) return fail(LUCENT_ERR_INVALID, "null argument");
+  if (!r->has_scene || !r->has_lighting) return fail(LUCENT_ERR_INVALID, "backward before load_scene / upload_lighting");
+  if (samples == 0) return LUCENT_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const uint32_t WH = r->W * r->H;
+  const uint32_t max_paths = 1u << 23;
+  const uint32_t batch = std::max(1u, std::min(samples, max_paths / std::max(1u, WH)));
+  lucent_status st = alloc_paths(r, batch * WH);
+  if (st) return st;
+  const size_t cap = r->path_cap;
+  const size_t nmat = (size_t)r->material_count * 6;
+  const size_t nenv = d_env ? (size_t)r->light.env_w * r->light.env_h * 3 : 0;
+  // per path: lrem 1 + gcont 5 + genv 2 float4; per shadow slot: gslot 2 float4 (3 slots per path)
+  if ((st = r->adj_dl.reserve((size_t)WH * 16)) || (st = r->adj_path.reserve(cap * 16 * (1 + 5 + 2 + 6))) ||
+      (st = r->adj_grad.reserve((nmat + nenv) * 4 + 16)))
+    return st;
+  std::vector<float> dl((size_t)WH * 4);
+  const float inv = 1.f / (float)samples;
+  for (size_t i = 0; i < dl.size(); i++) {
+    if (!std::isfinite(dl_dimage[i])) return fail(LUCENT_ERR_INVALID, "dl_dimage value %zu is not finite", i);
+    dl[i] = dl_dimage[i] * inv;
+  }
+  cudaError_t e = cudaMemcpyAsync(r->adj_dl.ptr, dl.data(), dl.size() * 4, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(r->adj_grad.ptr, 0, (nmat + nenv) * 4, s);
+  if (e != cudaSuccess) return cuda_fail(e, "backward setup");
+  float4* base = (float4*)r->adj_path.ptr;
+  AdjointDevHost H{(const float4*)r->adj_dl.ptr, base, base + cap, base + 6 * cap, base + 12 * cap,
+                   (float*)r->adj_grad.ptr, nenv ? (float*)r->adj_grad.ptr + nmat : nullptr};
+  for (uint32_t done = 0; done < samples; done += batch) {
+    const uint32_t S = std::min(batch, samples - done);
+    MultiLaunch M{};
+    if ((st = single_launch(r, S, 0, seed + done, s, M))) return st;
+    render_backward(M, H, s);
+  }
+  std::vector<float> g(nmat + nenv);
+  e = cudaMemcpyAsync(g.data(), r->adj_grad.ptr, g.size() * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "backward");
+  uint32_t word = 0;
+  cudaMemcpy(&word, (uint32_t*)r->ctr.ptr + kCtrErr, 4, cudaMemcpyDeviceToHost);
+  if (word) {
+    cudaMemset((uint32_t*)r->ctr.ptr + kCtrErr, 0, 4);
+    return fail(LUCENT_ERR_DEVICE, "backward raised device error word 0x%x", word);
+  }
+  for (size_t i = 0; i < nmat; i++) d_materials[i] += g[i];
+  for (size_t i = 0; i < nenv; i++) d_env[i] += g[nmat + i];
+  return LUCENT_OK;
 }
 
 lucent_status lucent_renderer_trim(lucent_renderer* r) {
@@ -741,22 +860,6 @@ struct lucent_batch {
   }
 };
 
-static SceneRec scene_rec(const lucent_renderer* r) {
-  SceneRec R{};
-  R.scene = {(const Node*)r->nodes.ptr, r->node_count, (const float4*)r->geo.ptr, (const float4*)r->attr.ptr,
-             (const float4*)r->mats.ptr, (const float4*)r->spheres.ptr, (const int*)r->sph_mat.ptr,
-             (const int*)r->sph_light.ptr, (int)r->sphere_count, (const float4*)r->lights.ptr, (int)r->light_count,
-             r->ground_enabled ? r->ground_material : -1, r->ground_height, r->any_alpha};
-  R.light = r->light;
-  R.cam = r->cam;
-  R.accum = {(float4*)r->color.ptr, (half4*)r->albedo.ptr, (half4*)r->normal.ptr, (float*)r->history.ptr};
-  R.W = (int)r->W;
-  R.H = (int)r->H;
-  R.max_bounces = (int)r->max_bounces;
-  R.clamp = r->clamp;
-  R.seed0 = r->seed;
-  return R;
-}
 
 extern "C" {
 
@@ -846,7 +949,7 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
     e = cudaMemcpyAsync(b->tail_bases.ptr, tb.data(), 4 * tb.size(), cudaMemcpyHostToDevice, s);
   }
   if (e != cudaSuccess) return cuda_fail(e, "upload batch tables");
-  MultiLaunch M;
+  MultiLaunch M{};
   M.paths = b->P;
   M.recs = (SceneRec*)b->recs.ptr;
   M.sid = (uint16_t*)b->sid.ptr;

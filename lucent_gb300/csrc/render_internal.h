@@ -55,18 +55,6 @@ struct AccumDev {
   float* history;
 };
 
-struct RenderLaunch {
-  Paths paths;
-  sh::SceneDev scene;
-  sh::LightingDev light;
-  sh::CameraDev cam;
-  AccumDev accum;
-  int W, H, S, max_bounces;
-  uint32_t seed0;
-  float clamp;
-  unsigned long long* trav_stats;  // closest-hit traversal counters or nullptr
-};
-
 // One scene of a multi-scene wave (device table, one entry per scene).
 struct SceneRec {
   sh::SceneDev scene;
@@ -88,6 +76,7 @@ struct MultiLaunch {
   uint32_t total_paths, total_pixels;
   int any_alpha;
   int trace_blocks, shade_blocks;  // 0 = all resident blocks
+  unsigned long long* trav_stats;  // closest-hit traversal counters (profiling) or nullptr
 };
 
 // Optional per-phase timing: events recorded between launches, each tagged
@@ -105,11 +94,24 @@ struct PhaseEvents {
   }
 };
 
-void render_batch(const RenderLaunch& R, cudaStream_t s, PhaseEvents* pe);
 
-// One wave of S samples for every scene of a multi-scene launch. Graph-safe:
-// no host synchronisation, every count stays on the device.
-void render_wave_multi(const MultiLaunch& M, cudaStream_t s);
+// One wave of S samples for every scene of a launch (a single renderer is a
+// launch of one scene: the same kernels, so a batch reproduces it bit for
+// bit). Graph-safe: no host synchronisation, every count stays on the device.
+void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe = nullptr);
+
+// Device buffers of a path-replay backward pass (per path: lrem 1, gcont 5,
+// genv 2 float4; per shadow slot: gslot 2 float4; dl per pixel).
+struct AdjointDevHost {
+  const float4* dl;
+  float4 *lrem, *gcont, *gslot, *genv;
+  float* dmat;
+  float* denv;
+};
+// Gradient of sum_px dl[px] . (mean of the wave's samples) with respect to
+// material parameters (6 per material) and environment texels, for a launch
+// of one scene (recs[0].seed0 = the wave's first sample seed).
+void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t s);
 
 // sheenAlbedoLUT (16 x 16) rounded to half precision, as the reference uploads it.
 void sheen_lut_half(float* out);

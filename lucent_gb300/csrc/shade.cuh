@@ -188,6 +188,27 @@ LUCENT_DEV void bilinear(const float* img, int w, int h, int ch, float u, float 
   }
 }
 
+// The four texels and weights bilinear() blends (same clamping and wrap).
+LUCENT_DEV void bilinear_taps(int w, int h, float u, float v, bool repeat_s, int idx[4], float wt[4]) {
+  const float x = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
+  const float fx = floorf(x), fy = floorf(y);
+  const float ax = x - fx, ay = y - fy;
+  int x0 = (int)fx, y0 = (int)fy, x1 = x0 + 1, y1 = y0 + 1;
+  if (repeat_s) {
+    x0 %= w;
+    x0 = x0 < 0 ? x0 + w : x0;
+    x1 %= w;
+    x1 = x1 < 0 ? x1 + w : x1;
+  } else {
+    x0 = min(max(x0, 0), w - 1);
+    x1 = min(max(x1, 0), w - 1);
+  }
+  y0 = min(max(y0, 0), h - 1);
+  y1 = min(max(y1, 0), h - 1);
+  idx[0] = y0 * w + x0, idx[1] = y0 * w + x1, idx[2] = y1 * w + x0, idx[3] = y1 * w + x1;
+  wt[0] = (1.f - ax) * (1.f - ay), wt[1] = ax * (1.f - ay), wt[2] = (1.f - ax) * ay, wt[3] = ax * ay;
+}
+
 // ------------------------------------------------------------ lights.glsl
 LUCENT_DEV float3 env_to_local(const LightingDev& L, float3 d) {
   return f3(L.env_cos * d.x - L.env_sin * d.z, d.y, L.env_sin * d.x + L.env_cos * d.z);
@@ -220,6 +241,7 @@ struct LightSample {
   float3 dir;
   float dist, pdf;
   float3 radiance;
+  float2 uv;  // environment samples: the texture coordinate of the radiance lookup
 };
 
 LUCENT_DEV LightSample sample_environment(const LightingDev& L, uint32_t& rng) {
@@ -244,6 +266,7 @@ LUCENT_DEV LightSample sample_environment(const LightingDev& L, uint32_t& rng) {
   ls.dist = INF;
   ls.pdf = st > 1e-6f ? pdfUV / (2.f * PI * PI * st) : 0.f;
   ls.radiance = env_tex(L, make_float2(u, v)) * L.env_intensity;
+  ls.uv = make_float2(u, v);
   return ls;
 }
 
@@ -529,6 +552,79 @@ LUCENT_EVAL_FN float3 eval_opaque(const LightingDev& L, const Surface& s, float3
     const float Fcv = fresnel1(fmaxf(cV, 0.f), 0.04f);
     f = f * (1.f - s.clearcoat * Fcv) + f3(coat, coat, coat) * s.clearcoat;
     pdf = mixf(pdf, pdf_coat, pcoat);
+  }
+  return f;
+}
+
+// Derivatives of evalOpaque's f with respect to the material parameters an
+// inverse renderer optimises: df[0..2] base colour r, g, b; df[3] roughness;
+// df[4] metallic; df[5] clearcoat (each an RGB vector). The pdf, the lobe
+// and coat probabilities and the sheen energy scale are sampling-side
+// quantities and held fixed. The clearcoat derivative is the one-sided one
+// at clearcoat = 0. Returns f as eval_opaque does.
+LUCENT_DEV float3 eval_opaque_grad(const LightingDev& L, const Surface& s, float3 wo, float3 wi, float3 df[6]) {
+  for (int k = 0; k < 6; k++) df[k] = f3(0.f, 0.f, 0.f);
+  const float3 n = s.n;
+  const float NdotL = dot3(n, wi), NdotV = dot3(n, wo);
+  if (NdotL <= 0.f || NdotV <= 0.f) return f3(0.f, 0.f, 0.f);
+  const float r = s.roughness, a = alpha_of(r), dadr = r * r > 1e-3f ? 2.f * r : 0.f;
+  const float3 H = norm3(wo + wi);
+  const float NdotH = fmaxf(dot3(n, H), 0.f), VdotH = fmaxf(dot3(wo, H), 0.f);
+  const float d0 = dielectric_f0(s.ior), m = s.metallic, W = schlick_w(VdotH);
+  const float3 F0 = base_f0(s);
+  const float3 F = fresnel3(VdotH, F0);
+  const float D = d_ggx_h(n, wo, wi, NdotH, a);
+  const float dd = NdotH * NdotH * (a * a - 1.f) + 1.f;
+  const float dDda = D * (2.f / a - 4.f * a * NdotH * NdotH / dd);
+  auto g1 = [&](float N, float& dg) {
+    const float q = sqrtf(a * a + (1.f - a * a) * N * N);
+    const float g = 2.f * N / (N + q);
+    dg = -2.f * N * (a * (1.f - N * N) / q) / ((N + q) * (N + q));
+    return g;
+  };
+  float dG1v, dG1l;
+  const float G1v = g1(NdotV, dG1v), G1l = g1(NdotL, dG1l);
+  const float G = G1v * G1l, dGda = dG1v * G1l + G1v * dG1l;
+  const float den = fmaxf(4.f * NdotV * NdotL, 1e-6f);
+  const float3 spec = (D * G) * F / den;
+  const float3 diff = (f3(1.f, 1.f, 1.f) - F) * s.albedo * (1.f - m) * INV_PI;
+  float3 f1 = diff + spec;
+  const float* Fp = &F.x;
+  const float* alb = &s.albedo.x;
+  float g_alb[3], g_r[3], g_m[3];
+  for (int c = 0; c < 3; c++) {
+    const float dFa = (1.f - W) * m, dFm = (1.f - W) * (alb[c] - d0);
+    g_alb[c] = (-dFa * alb[c] + (1.f - Fp[c])) * (1.f - m) * INV_PI + D * G * dFa / den;
+    g_r[c] = (dDda * G + D * dGda) * Fp[c] / den * dadr;
+    g_m[c] = (-dFm * alb[c] * (1.f - m) - (1.f - Fp[c]) * alb[c]) * INV_PI + D * G * dFm / den;
+  }
+  float scale = 1.f;
+  const float smax = max3(s.sheen_color);
+  if (smax > 0.f) {
+    const float sr = fmaxf(s.sheen_roughness, 0.07f);
+    const float3 sheen = s.sheen_color * d_charlie(sr * sr, NdotH) * v_neubelt(NdotL, NdotV);
+    scale = 1.f - smax * fmaxf(sheen_albedo(L, NdotV, sr), sheen_albedo(L, NdotL, sr));
+    f1 = sheen + f1 * scale;
+  }
+  const float cV = dot3(s.nc, wo), cL = dot3(s.nc, wi);
+  float coat = 0.f;
+  if (cV > 0.f && cL > 0.f) {
+    const float ac = alpha_of(s.clearcoat_roughness);
+    const float cH = fmaxf(dot3(s.nc, H), 0.f);
+    coat = d_ggx_h(s.nc, wo, wi, cH, ac) * g1_ggx(cV, ac) * g1_ggx(cL, ac) * fresnel1(VdotH, 0.04f) / (4.f * cV * cL);
+  }
+  const float Fcv = fresnel1(fmaxf(cV, 0.f), 0.04f);
+  const float cc = s.clearcoat > 0.f ? s.clearcoat : 0.f;
+  const float keep = 1.f - cc * Fcv;
+  float3 f = cc > 0.f ? f1 * keep + f3(coat, coat, coat) * cc : f1;
+  const float* f1p = &f1.x;
+  float* dfp[6] = {&df[0].x, &df[1].x, &df[2].x, &df[3].x, &df[4].x, &df[5].x};
+  for (int c = 0; c < 3; c++) {
+    const float k = scale * (cc > 0.f ? keep : 1.f);
+    dfp[c][c] = g_alb[c] * k;
+    dfp[3][c] = g_r[c] * k;
+    dfp[4][c] = g_m[c] * k;
+    dfp[5][c] = coat - f1p[c] * Fcv;
   }
   return f;
 }

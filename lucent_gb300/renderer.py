@@ -242,6 +242,15 @@ class Renderer:
                 "width": self.width, "height": self.height}
 
 
+def bsdf_grad_tuples(tuples):
+    """f and its derivatives in (albedo r, g, b, roughness, metallic,
+    clearcoat) on [n, 32] tuples -> [n, 24] float32 (f 3, then 6 x 3)."""
+    t = np.ascontiguousarray(tuples, np.float32).reshape(-1, 32)
+    out = np.zeros((t.shape[0], 24), np.float32)
+    N.check(N.lib().lucent_bsdf_grad_tuples(_f(t), t.shape[0], _f(out)))
+    return out
+
+
 def bsdf_eval_tuples(tuples):
     """The renderer's BSDF code on [n, 32] float tuples -> [n, 24] float32
     (layout in csrc/bsdf_tuples.cu: evalOpaque f, pdf; sampleOpaque dir,
@@ -298,12 +307,13 @@ class Batch:
         return "n%d_px%d_tri%d_b%d" % (len(self.renderers), px, tris, mb)
 
     def autotune(self, samples=2, candidates=None, cache=None):
-        """Times `samples` samples under each candidate option set (wall clock
-        around trace + synchronise, so launch overhead counts) and keeps the
-        fastest. The samples are real: reset the renderers afterwards for a
-        fresh average. With `cache` (a JSON file path) a result for the same
-        signature() is reused, and new results are stored there.
-        Returns (chosen options, {candidate index: seconds})."""
+        """Times at least `samples` samples (two full waves) under each
+        candidate option set (wall clock around trace + synchronise, so launch
+        overhead counts) and keeps the fastest per sample. The samples are
+        real: reset the renderers afterwards for a fresh average. With `cache`
+        (a JSON file path) a result for the same signature() is reused, and
+        new results are stored there.
+        Returns (chosen options, {candidate index: seconds per sample})."""
         import json
         import os
         key = self.signature()
@@ -313,21 +323,22 @@ class Batch:
             if key in known:
                 self.set_options(**known[key])
                 return dict(self.options), {}
-        if candidates is None:
+        if candidates is None:  # wave budgets of 2^23 .. 2^25 paths, with and without graph replay
             px = sum(r.width * r.height for r in self.renderers)
-            waves = [s for s in (1, 2, 4) if s * px <= 4 * self.DEFAULTS["max_wave_paths"]] or [1]
+            waves = sorted({max(1, (1 << k) // px) for k in (23, 24, 25)})
             candidates = [{"samples_per_wave": s, "use_graph": g, "max_wave_paths": max(s * px, 1)}
                           for s in waves for g in (True, False)]
         base = dict(self.options)
         times = {}
         for i, c in enumerate(candidates):
             self.set_options(**{**base, **c})
-            self.trace_samples(1)  # allocation and graph capture happen outside the timed call
+            n = max(samples, 2 * c.get("samples_per_wave", 1))  # at least two full waves
+            self.trace_samples(n)  # allocation and graph capture happen outside the timed call
             self.check()
             t0 = time.perf_counter()
-            self.trace_samples(samples)
+            self.trace_samples(n)
             self.check()
-            times[i] = time.perf_counter() - t0
+            times[i] = (time.perf_counter() - t0) / n  # seconds per sample
         best = min(times, key=times.get)
         self.set_options(**{**base, **candidates[best]})
         if cache:

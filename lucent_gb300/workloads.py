@@ -264,3 +264,45 @@ def batch_scene(seed, tri_lo=10_000, tri_hi=2_000_000):
     env = S.Environment(map=env_lognormal(rng, 512, 256), name="lognormal", background=True)
     cam = S.Camera(position=(0.0, 0.3, 4.0), target=(0.0, 0.0, 0.0), fov=45.0, focus_distance=4.0)
     return S.Scene(name="batch%d" % seed, camera=cam, env=env, meshes=meshes), res
+
+
+def adjoint_scene(seed=0, subdivisions=6, env_size=(256, 128)):
+    """The inverse-rendering workload: the box scene's geometry with 32
+    materials (5 walls, the lamp, 2 boxes and the icosphere split into 24
+    bands of its triangles, each a layered material with the box scene's
+    parameter ranges) under a lognormal env_size HDRI seen through the open
+    front. Draw order from numpy.random.Generator(PCG64(seed + 1000)): 24
+    band materials (albedo 3, roughness, metallic, clearcoat, sheen), then
+    the HDRI."""
+    from . import mesh as M
+    from . import scene as S
+    sc = box_scene(seed, subdivisions)
+    rng = np.random.Generator(np.random.PCG64(seed + 1000))
+    ball = sc.meshes[-1]
+    n = ball.mesh.triangle_count
+    band = (np.arange(n) * 24) // n
+    pos, nrm = ball.mesh.positions.reshape(-1, 9), ball.mesh.normals.reshape(-1, 9)
+    meshes = sc.meshes[:-1]
+    for k in range(24):
+        alb = rng.uniform(0.2, 0.8, 3)
+        rough, metallic = rng.uniform(0.05, 1.0), float(rng.random() < 0.5)
+        coat, sheen = rng.uniform(0.0, 1.0), rng.uniform(0.0, 1.0)
+        mat = S.material(albedo=tuple(float(x) for x in alb), roughness=float(rough), metallic=metallic,
+                         clearcoat=float(coat), clearcoat_roughness=0.2, sheen_color=(float(sheen),) * 3,
+                         sheen_roughness=0.5)
+        sel = band == k
+        meshes.append(S.MeshInstance(M.Mesh(pos[sel].reshape(-1).copy(), nrm[sel].reshape(-1).copy()), mat))
+    env = S.Environment(map=env_lognormal(rng, *env_size), name="lognormal", background=True)
+    return S.Scene(name="adjoint", camera=sc.camera, env=env, meshes=meshes)
+
+
+def adjoint_views(count=8):
+    """Camera positions of the multi-view inverse-rendering workload: a 2 x 4
+    grid in front of the box's open side, all aimed at the box centre."""
+    from . import scene as S
+    out = []
+    for i in range(count):
+        x = -0.6 + 1.2 * (i % 4) / 3.0
+        y = 0.7 + 0.6 * (i // 4)
+        out.append(S.Camera(position=(x, y, 3.4), target=(0.0, 1.0, 0.0), fov=40.0, focus_distance=3.4))
+    return out

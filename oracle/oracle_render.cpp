@@ -174,8 +174,8 @@ struct Material {  // scene.glsl:140-201 fetchMaterial
   bool thinWalled;
 };
 
-Material fetch_material(const orc_scene* s, int index) {
-  const float* t = s->materials + (size_t)index * 40;
+Material fetch_material_from(const float* mats, int index) {
+  const float* t = mats + (size_t)index * 40;
   Material m;
   for (int k = 0; k < 3; k++) {
     m.albedo[k] = t[k];
@@ -432,6 +432,11 @@ struct Tracer {
   uint32_t g_seed = 0;
   WorkCounts* wc = nullptr;  // when set, counts rays (and, if `detailed`, their GLSL traversal work)
   bool detailed = true;
+  // Detached evaluation (tracePathDetached): materials and environment texels
+  // whose values are used for every BSDF value and emitted radiance, while
+  // sampling keeps s's (nullptr: s's own).
+  const float* mev = nullptr;
+  const float* eev = nullptr;
 
   R rand() { return R(pcg(g_seed)) * (R(1) / R(4294967296.0)); }
   V2 rand2() {
@@ -636,6 +641,12 @@ struct Tracer {
     bilinear<R>(s->env_rgb, (int)s->env_width, (int)s->env_height, 3, uv.x, uv.y, true, out);
     return {out[0], out[1], out[2]};
   }
+  V envTexEv(Vec2<R> uv) const {
+    if (!eev) return envTex(uv);
+    R out[3];
+    bilinear<R>(eev, (int)s->env_width, (int)s->env_height, 3, uv.x, uv.y, true, out);
+    return {out[0], out[1], out[2]};
+  }
   V envRadiance(V d) const { return envTex(equirectUV(envToLocal(d))) * R(s->env_intensity); }
   const float* aliasTexel(int cx, int cy) const { return s->env_alias + ((size_t)cy * s->env_grid_w + cx) * 4; }
   R envPdf(V d) const {  // :50-56
@@ -651,6 +662,7 @@ struct Tracer {
     V dir;
     R dist, pdf;
     V radiance;
+    Vec2<R> uv;  // environment samples: texture coordinate of the radiance lookup
   };
   LightSample sampleEnvironment() {  // :59-79
     LightSample ls;
@@ -672,10 +684,20 @@ struct Tracer {
     ls.dist = C::INF;
     ls.pdf = sinTheta > R(1e-6) ? pdfUV / (R(2) * C::PI * C::PI * sinTheta) : R(0);
     ls.radiance = envTex(uv) * R(s->env_intensity);
+    ls.uv = uv;
     return ls;
   }
   V environment(V d, bool specularBounce, R bsdfPdf) const {  // :83-91
     V L = envRadiance(d);
+    if (!specularBounce && s->env_sampling != 0) L = L * misWeight(bsdfPdf, envPdf(d));
+    if (s->sun_enabled != 0 && dot(d, f3(s->sun_dir)) >= R(s->sun_cos_angle)) {
+      const R w = specularBounce ? R(1) : misWeight(bsdfPdf, R(s->sun_pdf));
+      L = L + f3(s->sun_radiance) * w;
+    }
+    return L;
+  }
+  V environmentEv(V d, bool specularBounce, R bsdfPdf) const {  // environment() with eev's radiance
+    V L = envTexEv(equirectUV(envToLocal(d))) * R(s->env_intensity);
     if (!specularBounce && s->env_sampling != 0) L = L * misWeight(bsdfPdf, envPdf(d));
     if (s->sun_enabled != 0 && dot(d, f3(s->sun_dir)) >= R(s->sun_cos_angle)) {
       const R w = specularBounce ? R(1) : misWeight(bsdfPdf, R(s->sun_pdf));
@@ -956,8 +978,9 @@ struct Tracer {
     const R l = luminance(c);
     return l > uClamp ? c * (uClamp / l) : c;
   }
-  Surface surfaceAt(const Hit& hit, V& emission) const {  // :72-124 (no texture maps)
-    const Material m = fetch_material(s, hit.material);
+  Surface surfaceAt(const Hit& hit, V& emission) const { return surfaceAtFrom(s->materials, hit, emission); }
+  Surface surfaceAtFrom(const float* mats, const Hit& hit, V& emission) const {  // :72-124 (no texture maps)
+    const Material m = fetch_material_from(mats, hit.material);
     Surface sf;
     sf.albedo = f3(m.albedo);
     if (m.checkerScale > 0.0f) {
@@ -1120,6 +1143,126 @@ struct Tracer {
     }
     return radiance;
   }
+
+  // tracePath with sampling detached from evaluation: every sampling
+  // decision, direction, pdf, MIS weight, Russian-roulette probability and
+  // firefly-clamp scale comes from s (the primal parameters); every BSDF value
+  // and emitted environment radiance comes from mev / eev. At mev = s's
+  // materials and eev = s's map this returns tracePath's radiance; its
+  // derivative in mev / eev is what path replay backpropagation computes.
+  R clampScale(V c, int bounce) const {
+    if (bounce == 0 || uClamp <= R(0)) return R(1);
+    const R l = luminance(c);
+    return l > uClamp ? uClamp / l : R(1);
+  }
+  V tracePathDetached(V ro, V rd) {
+    V radiance = {R(0), R(0), R(0)};
+    V thr = {R(1), R(1), R(1)};  // sampling (primal) throughput
+    V tev = {R(1), R(1), R(1)};  // evaluated throughput
+    bool specularBounce = true;
+    R bsdfPdf = R(0);
+    auto U = [this]() { return rand(); };
+    const float* mats = mev ? mev : s->materials;
+    for (int bounce = 0; bounce <= (int)maxBounces; bounce++) {
+      Hit hit;
+      if (!traceScene(ro, rd, hit)) {
+        const bool backdrop = bounce == 0 && s->env_background == 0;
+        const V env0 = backdrop ? f3(s->backdrop) : environment(rd, specularBounce, bsdfPdf);
+        const V enve = backdrop ? f3(s->backdrop) : environmentEv(rd, specularBounce, bsdfPdf);
+        radiance = radiance + tev * enve * clampScale(thr * env0, bounce);
+        break;
+      }
+      const V wo = -rd;
+      V emission, emission_e;
+      const Surface sf = surfaceAt(hit, emission);
+      const Surface se = surfaceAtFrom(mats, hit, emission_e);
+      const V ng = hit.geomNormal;
+      if (!hit.frontFace && !sf.thinWalled && sf.transmission > R(0)) {
+        thr = thr * vexp(-sf.absorption * hit.t);
+        tev = tev * vexp(-se.absorption * hit.t);
+      }
+      if (emission.x > R(0) || emission.y > R(0) || emission.z > R(0)) {
+        R w = R(1);
+        if (!specularBounce && hit.light >= 0) {
+          const R pl = lightPdf(hit.light, ro, rd, hit.t) / R(s->light_count);
+          w = misWeight(bsdfPdf, pl);
+        }
+        radiance = radiance + tev * emission * w * clampScale(thr * emission * w, bounce);
+        if (hit.light >= 0) break;
+      }
+      const bool glass = sf.transmission > R(0) && rand() < sf.transmission;
+      if (glass) {
+        V wi, weight;
+        bool reflected;
+        if (!sampleDielectric(sf, hit.frontFace, ng, wo, wi, weight, reflected, U)) break;
+        thr = thr * weight;
+        tev = reflected ? tev : tev * se.albedo;
+        ro = offsetRay(hit.position, reflected ? ng : -ng);
+        rd = wi;
+        specularBounce = true;
+      } else {
+        const V shadowOrigin = offsetRay(hit.position, ng);
+        const V n = sf.n;
+        if (s->sun_enabled != 0) {
+          const V wi = sampleSunDirection(rand2());
+          const R NdotL = dot(n, wi);
+          if (NdotL > R(0) && dot(ng, wi) > R(0) && !occluded(shadowOrigin, wi, C::INF)) {
+            R pb, pe;
+            const V f = evalOpaque(sf, wo, wi, pb);
+            const V fe = evalOpaque(se, wo, wi, pe);
+            const R w = misWeight(R(s->sun_pdf), pb);
+            const V le = f3(s->sun_radiance) * (NdotL * w / R(s->sun_pdf));
+            radiance = radiance + tev * fe * le * clampScale(thr * f * le, bounce);
+          }
+        }
+        if (s->env_sampling != 0) {
+          const LightSample ls = sampleEnvironment();
+          const R NdotL = dot(n, ls.dir);
+          if (ls.pdf > R(0) && NdotL > R(0) && dot(ng, ls.dir) > R(0) && !occluded(shadowOrigin, ls.dir, C::INF)) {
+            R pb, pe;
+            const V f = evalOpaque(sf, wo, ls.dir, pb);
+            const V fe = evalOpaque(se, wo, ls.dir, pe);
+            const R w = misWeight(ls.pdf, pb);
+            const R k = NdotL * w / ls.pdf;
+            const V le = envTexEv(ls.uv) * R(s->env_intensity);
+            radiance = radiance + tev * fe * le * k * clampScale(thr * f * ls.radiance * k, bounce);
+          }
+        }
+        if (s->light_count > 0) {
+          const int li = std::min((int)(rand() * R(s->light_count)), (int)s->light_count - 1);
+          const LightSample ls = sampleLight(li, hit.position, rand2());
+          const R NdotL = dot(n, ls.dir);
+          if (ls.pdf > R(0) && NdotL > R(0) && dot(ng, ls.dir) > R(0) &&
+              !occluded(shadowOrigin, ls.dir, ls.dist * (R(1) - R(1e-4)))) {
+            const R pl = ls.pdf / R(s->light_count);
+            R pb, pe;
+            const V f = evalOpaque(sf, wo, ls.dir, pb);
+            const V fe = evalOpaque(se, wo, ls.dir, pe);
+            const R w = misWeight(pl, pb);
+            const V le = ls.radiance * (NdotL * w / pl);
+            radiance = radiance + tev * fe * le * clampScale(thr * f * le, bounce);
+          }
+        }
+        const BSDFSample bs = sampleOpaque(sf, wo, U);
+        if (bs.pdf <= R(0) || dot(bs.dir, ng) <= R(0)) break;
+        R pe;
+        const V fe = evalOpaque(se, wo, bs.dir, pe);
+        thr = thr * bs.weight;
+        tev = tev * fe * (dot(n, bs.dir) / bs.pdf);
+        bsdfPdf = bs.pdf;
+        specularBounce = false;
+        ro = shadowOrigin;
+        rd = bs.dir;
+      }
+      if (bounce >= 2) {
+        const R p = std::min(R(0.95), max3(thr));
+        if (rand() >= p) break;
+        thr = thr / p;
+        tev = tev / p;
+      }
+    }
+    return radiance;
+  }
 };
 
 }  // namespace
@@ -1207,6 +1350,48 @@ int orc_render_work(const orc_scene* s, const orc_camera* cam, uint32_t max_boun
                     float* history, int threads, int detailed, uint64_t* work_out) {
   return render_impl(s, cam, max_bounces, clamp_lum, width, height, x0, y0, cw, ch, seed0, samples, 32, color4,
                      albedo4, normal4, history, threads, work_out, detailed != 0);
+}
+
+// sum over pixels and channels of dl4[px].rgb * (mean of the samples' detached
+// radiance), in binary64 with a fixed reduction order (finite-difference
+// reference for the adjoint). NaN/inf samples count as 0, like the
+// accumulation.
+double orc_detached_dot(const orc_scene* s, const orc_camera* cam, uint32_t max_bounces, float clamp_lum,
+                        uint32_t width, uint32_t height, uint32_t seed0, uint32_t samples, const float* materials_eval,
+                        const float* env_eval, const float* dl4, int threads) {
+  const uint64_t npx = (uint64_t)width * height;
+  const uint64_t chunk = 64;
+  std::vector<double> part((npx + chunk - 1) / chunk, 0.0);
+  par_for((npx + chunk - 1) / chunk, threads, [&](uint64_t b, uint64_t e) {
+    Tracer<double> tr{s, cam, width, height, max_bounces, double(clamp_lum)};
+    tr.mev = materials_eval;
+    tr.eev = env_eval;
+    for (uint64_t ci = b; ci < e; ci++) {
+      double acc = 0.0;
+      for (uint64_t q = ci * chunk; q < std::min(npx, (ci + 1) * chunk); q++) {
+        const uint32_t px = (uint32_t)(q % width), py = (uint32_t)(q / width);
+        const uint32_t pixelIndex = px + py * width;
+        double sum[3] = {0, 0, 0};
+        for (uint32_t k = 0; k < samples; k++) {
+          tr.g_seed = pixelIndex * 1973u + (seed0 + k) * 9277u + 26699u;
+          pcg(tr.g_seed);
+          Vec3<double> ro, rd;
+          tr.cameraRay({double(px) + 0.5, double(py) + 0.5}, ro, rd);
+          const Vec3<double> c = tr.tracePathDetached(ro, rd);
+          if (std::isnan(c.x) || std::isnan(c.y) || std::isnan(c.z) || std::isinf(c.x) || std::isinf(c.y) ||
+              std::isinf(c.z))
+            continue;
+          sum[0] += c.x, sum[1] += c.y, sum[2] += c.z;
+        }
+        const float* d = dl4 + q * 4;
+        acc += (d[0] * sum[0] + d[1] * sum[1] + d[2] * sum[2]) / samples;
+      }
+      part[ci] = acc;
+    }
+  });
+  double total = 0.0;
+  for (double v : part) total += v;
+  return total;
 }
 
 // ---------------------------------------------------------------------------

@@ -87,6 +87,14 @@ int orc_denoise(const float* color4, const float* albedo4, const float* normal4,
 int orc_display(const float* color4, const float* albedo4, const float* denoised4, uint32_t w, uint32_t h,
                 float denoise_weight, float exposure, int tonemap, float* out_rgb);
 
+/* Finite-difference reference of the adjoint: sum over pixels of dl4[px].rgb
+ * times the mean over samples [seed0, seed0 + samples) of the radiance traced
+ * with sampling from s and BSDF values / environment radiance from
+ * materials_eval / env_eval (NULL: s's own), in binary64. */
+double orc_detached_dot(const orc_scene* s, const orc_camera* cam, uint32_t max_bounces, float clamp_lum,
+                        uint32_t width, uint32_t height, uint32_t seed0, uint32_t samples, const float* materials_eval,
+                        const float* env_eval, const float* dl4, int threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -41,6 +41,8 @@ def declare(L):
     L.orc_bsdf_tuples.argtypes = [P(F), C.c_uint64, C.c_int, P(D), C.c_int]
     L.orc_bsdf_set_lut.argtypes = [P(F)]
     L.orc_denoise.argtypes = [P(F), P(F), P(F), P(F), U32, U32, P(OrcCamera), U32, F, F, F, P(F)]
+    L.orc_detached_dot.argtypes = [P(OrcScene), P(OrcCamera), U32, F, U32, U32, U32, U32, P(F), P(F), P(F), C.c_int]
+    L.orc_detached_dot.restype = C.c_double
     L.orc_display.argtypes = [P(F), P(F), P(F), U32, U32, F, F, C.c_int, P(F)]
 
 
@@ -58,6 +60,7 @@ class Prepared:
         keep = self.keep.append
         p = packed
         n = p.tri_count
+        self.packed = p
         bvh = build_bvh(p.positions)
         self.bvh = bvh
         src = bvh.tri_indices.astype(np.int64)
@@ -100,6 +103,7 @@ class Prepared:
         s.sun_cos_angle, s.sun_pdf = L.sun_cos_angle, L.sun_pdf
         env = np.ascontiguousarray(L.env.data, np.float32)
         keep(env)
+        self.env_data = env
         s.env_width, s.env_height, s.env_rgb = L.env.width, L.env.height, _p(env, F)
         gw, gh, table, total = build_env_sampler(env, L.env.width, L.env.height, 1024)
         keep(table)
@@ -188,3 +192,16 @@ def display(color4, albedo4, denoised4, denoise_weight, exposure=1.0, tonemap=0)
     out = np.zeros((h, w, 3), np.float32)
     lib().orc_display(_p(c, F), _p(a, F), _p(d, F), w, h, denoise_weight, exposure, tonemap, _p(out, F))
     return out
+
+
+def detached_dot(prep, width, height, seed0, samples, dl4, materials_eval=None, env_eval=None, max_bounces=6,
+                 clamp=8.0, threads=0):
+    """orc_detached_dot: sum_px dl4[px].rgb . mean radiance, sampling from
+    prep's scene, BSDF values / environment radiance from the given
+    materials (flat, 40 per material) and env map (flat RGB), binary64."""
+    d = np.ascontiguousarray(dl4, np.float32).reshape(-1)
+    m = np.ascontiguousarray(materials_eval, np.float32).reshape(-1) if materials_eval is not None else None
+    e = np.ascontiguousarray(env_eval, np.float32).reshape(-1) if env_eval is not None else None
+    return lib().orc_detached_dot(C.byref(prep.scene), C.byref(prep.camera), max_bounces, clamp, width, height, seed0,
+                                  samples, _p(m, F) if m is not None else None, _p(e, F) if e is not None else None,
+                                  _p(d, F), threads)

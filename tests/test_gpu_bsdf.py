@@ -126,3 +126,34 @@ def test_sample_dielectric(evaluated):
     _report("sampleDielectric dir (abs)", d)
     assert (d > 1e-5).mean() < 1e-4
     assert np.array_equal(g[ok, 15:18], r[ok, 15:18].astype(np.float32).astype(np.float64))
+
+
+def test_eval_gradient_matches_fp64_finite_differences():
+    """The adjoint's BSDF derivative (eval_opaque_grad) vs central
+    differences of the oracle's binary64 evalOpaque, step 1e-4 (one-sided at
+    a range end, e.g. clearcoat = 0 or metallic in {0, 1}, where the
+    one-sided difference's own truncation error is ~1e-4); tuples within two
+    steps of the roughness clamp (alpha = max(r^2, 1e-3)) are skipped. Bar:
+    1e-3 relative (floor 1e-3 of the component's largest value) on all but
+    1 in 10^3 tuples."""
+    from lucent_gb300.renderer import bsdf_grad_tuples
+    n = 100_000
+    t = make_tuples(n, seed=3)
+    g = bsdf_grad_tuples(t).astype(np.float64)
+    h = 1e-4
+    cols = {0: 0, 1: 1, 2: 2, 3: 4, 4: 3, 5: 6}  # adjoint parameter -> tuple column
+    keep = np.abs(t[:, 4] - np.sqrt(1e-3)) > 2 * h
+    for p, col in cols.items():
+        up, dn = t.copy(), t.copy()
+        lo_edge = t[:, col] - h < 0
+        hi_edge = t[:, col] + h > 1
+        up[:, col] = np.where(hi_edge, t[:, col], t[:, col] + h)
+        dn[:, col] = np.where(lo_edge, t[:, col], t[:, col] - h)
+        fp = OR.bsdf_tuples(up, 64)[:, 0:3]
+        fm = OR.bsdf_tuples(dn, 64)[:, 0:3]
+        fd = (fp - fm) / (up[:, col:col + 1] - dn[:, col:col + 1]).astype(np.float64)
+        gd = g[:, 3 + 3 * p:6 + 3 * p]
+        scale = np.abs(fd).max(axis=0, keepdims=True)  # channels a parameter does not touch have fd = gd = 0
+        err = (np.abs(gd - fd) / np.maximum(np.abs(fd), np.maximum(1e-3 * scale, 1e-12))).max(axis=1)[keep]
+        _report("d f / d %s" % ("r", "g", "b", "roughness", "metallic", "clearcoat")[p], err)
+        assert (err > 1e-3).mean() < 1e-3, (p, (err > 1e-3).mean())
