@@ -247,6 +247,10 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
  * the reference's GPU timer queries, renderer.ts:668-700); results appear in
  * lucent_render_stats.phase_ms after lucent_renderer_check. */
 lucent_status lucent_renderer_set_profiling(lucent_renderer* r, int32_t enabled);
+/* Between bounces, reorder the surviving rays by direction octant and origin
+ * cell (counting sort, default on). Paths are independent: images are the
+ * same either way; only the traversal's coherence changes. */
+lucent_status lucent_renderer_set_ray_sort(lucent_renderer* r, int32_t enabled);
 /* ---------------------------------------------------------------------------
  * Differentiable rendering (path replay backpropagation). No reference
  * counterpart: the reference renders forward only.
@@ -315,6 +319,7 @@ typedef struct lucent_batch_options {
   int32_t use_graph;         /* capture a full wave once as a CUDA graph and replay it */
   uint32_t trace_blocks;     /* grid of the persistent traversal kernels; 0 = all resident blocks */
   uint32_t shade_blocks;     /* grid of the shade / resolve kernels; 0 = all resident blocks */
+  int32_t sort_rays;         /* reorder each bounce's rays (see lucent_renderer_set_ray_sort) */
 } lucent_batch_options;
 typedef struct lucent_batch_stats {
   uint64_t closest_rays, shadow_rays; /* traced by this batch since creation */
@@ -325,7 +330,8 @@ typedef struct lucent_batch_stats {
  * batch is used; they may be traced on their own in between. */
 lucent_status lucent_batch_create(lucent_renderer* const* renderers, uint32_t n, lucent_batch** out);
 void lucent_batch_destroy(lucent_batch* batch);
-/* Defaults: samples_per_wave 0, max_wave_paths 2^25, use_graph 1, trace_blocks 0, shade_blocks 0. */
+/* Defaults: samples_per_wave 0, max_wave_paths 2^25, use_graph 1, trace_blocks 0, shade_blocks 0,
+ * sort_rays 1. */
 lucent_status lucent_batch_set_options(lucent_batch* batch, const lucent_batch_options* options);
 /* Asynchronous on `stream`. */
 lucent_status lucent_batch_trace(lucent_batch* batch, uint32_t samples, void* stream);

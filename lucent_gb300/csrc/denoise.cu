@@ -149,6 +149,88 @@ __global__ void __launch_bounds__(256) k_atrous(const float4* __restrict__ in, c
   out[p] = make_float4(sum.x / wsum, sum.y / wsum, sum.z / wsum, sumVar / (wsum * wsum));
 }
 
+// k_atrous for hole spacings 1, 2 and 4 with the block's 16 x 16 pixels and
+// their 2 * STEP halo staged in shared memory (illumination + variance, unit
+// normal + coverage, world position + depth: 48 B per pixel), so every tap
+// and the 3 x 3 variance blur read shared memory. Same arithmetic in the same
+// order as k_atrous (this file is compiled without FMA contraction), so the
+// two give identical results.
+template <int STEP>
+__global__ void __launch_bounds__(256) k_atrous_tiled(const float4* __restrict__ in, const float4* __restrict__ g0,
+                                                      const float4* __restrict__ g1, int W, int H, float tan_half,
+                                                      float sigma_l, float sigma_n, float sigma_p,
+                                                      float4* __restrict__ out) {
+  constexpr int T = 16 + 4 * STEP;
+  extern __shared__ float4 sm[];
+  float4* s_in = sm;
+  float4* s_g0 = sm + T * T;
+  float4* s_g1 = sm + 2 * T * T;
+  const int ox = (int)blockIdx.x * 16 - 2 * STEP, oy = (int)blockIdx.y * 16 - 2 * STEP;
+  for (int i = threadIdx.y * 16 + threadIdx.x; i < T * T; i += 256) {
+    const int gx = ox + i % T, gy = oy + i / T;
+    if (gx >= 0 && gy >= 0 && gx < W && gy < H) {
+      const size_t q = (size_t)gy * W + gx;
+      s_in[i] = __ldg(in + q);
+      s_g0[i] = __ldg(g0 + q);
+      s_g1[i] = __ldg(g1 + q);
+    }
+  }
+  __syncthreads();
+  const int x = (int)blockIdx.x * 16 + threadIdx.x, y = (int)blockIdx.y * 16 + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const int lx = threadIdx.x + 2 * STEP, ly = threadIdx.y + 2 * STEP;
+  const size_t p = (size_t)y * W + x;
+  const float4 cp = s_in[ly * T + lx];
+  const float4 gp = s_g0[ly * T + lx];
+  if (gp.w < 0.5f) {
+    out[p] = cp;
+    return;
+  }
+  const float4 Pp = s_g1[ly * T + lx];
+  const float footprint = 2.f * tan_half * Pp.w / (float)H;
+  float var = 0.f, wv = 0.f;
+#pragma unroll
+  for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+    for (int dx = -1; dx <= 1; dx++) {
+      const int qx = x + dx, qy = y + dy;
+      if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
+      const float k = (dx == 0 ? 0.5f : 0.25f) * (dy == 0 ? 0.5f : 0.25f);
+      var += s_in[(ly + dy) * T + lx + dx].w * k;
+      wv += k;
+    }
+  const float denom = sigma_l * sqrtf(fmaxf(var / wv, 0.f)) + 1e-6f;
+  const float lp = lum3(cp.x, cp.y, cp.z);
+  const float h[3] = {0.375f, 0.25f, 0.0625f};
+  float3 sum = make_float3(cp.x * (h[0] * h[0]), cp.y * (h[0] * h[0]), cp.z * (h[0] * h[0]));
+  float sumVar = cp.w * (h[0] * h[0]) * (h[0] * h[0]);
+  float wsum = h[0] * h[0];
+#pragma unroll
+  for (int dy = -2; dy <= 2; dy++)
+#pragma unroll
+    for (int dx = -2; dx <= 2; dx++) {
+      if (dx == 0 && dy == 0) continue;
+      const int qx = x + dx * STEP, qy = y + dy * STEP;
+      if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
+      const int t = (ly + dy * STEP) * T + lx + dx * STEP;
+      const float4 gq = s_g0[t];
+      if (gq.w < 0.5f) continue;
+      const float4 cq = s_in[t];
+      const float4 Q = s_g1[t];
+      const float k = h[dx < 0 ? -dx : dx] * h[dy < 0 ? -dy : dy];
+      const float wn = powf(fmaxf(0.f, gp.x * gq.x + gp.y * gq.y + gp.z * gq.z), sigma_n);
+      const float reach = sigma_p * footprint * (float)STEP * sqrtf((float)(dx * dx + dy * dy));
+      const float pd = gp.x * (Q.x - Pp.x) + gp.y * (Q.y - Pp.y) + gp.z * (Q.z - Pp.z);
+      const float wp = expf(-fabsf(pd) / (reach + 1e-6f));
+      const float wl = expf(-fabsf(lp - lum3(cq.x, cq.y, cq.z)) / denom);
+      const float w = k * wn * wp * wl;
+      sum = sum + make_float3(cq.x, cq.y, cq.z) * w;
+      sumVar += cq.w * w * w;
+      wsum += w;
+    }
+  out[p] = make_float4(sum.x / wsum, sum.y / wsum, sum.z / wsum, sumVar / (wsum * wsum));
+}
+
 // display.frag:42-67 (render size == view size): remodulate and blend the
 // denoised image, exposure, tone map, sRGB, IGN dither, RGBA8.
 __global__ void k_display(AccumDev A, const float4* __restrict__ den, int W, int H, float weight, float exposure,
@@ -194,7 +276,16 @@ float4* denoise_run(AccumDev A, const CameraDev& cam, int W, int H, int levels, 
   k_guides<<<grd, blk, 0, s>>>(A, cam, W, H, g0, g1);
   float4 *rd = fa, *wr = fb;
   for (int l = 0; l < levels; l++) {
-    k_atrous<<<grd, blk, 0, s>>>(rd, g0, g1, W, H, 1 << l, cam.tan_half_fov, sigma_l, sigma_n, sigma_p, wr);
+    const int step = 1 << l;
+    const float th = cam.tan_half_fov;
+    if (step == 1)
+      k_atrous_tiled<1><<<grd, blk, 3 * 20 * 20 * 16, s>>>(rd, g0, g1, W, H, th, sigma_l, sigma_n, sigma_p, wr);
+    else if (step == 2)
+      k_atrous_tiled<2><<<grd, blk, 3 * 24 * 24 * 16, s>>>(rd, g0, g1, W, H, th, sigma_l, sigma_n, sigma_p, wr);
+    else if (step == 4)
+      k_atrous_tiled<4><<<grd, blk, 3 * 32 * 32 * 16, s>>>(rd, g0, g1, W, H, th, sigma_l, sigma_n, sigma_p, wr);
+    else  // the 8 and 16 halos (4 and 8 KB rows) would not fit: taps through L1
+      k_atrous<<<grd, blk, 0, s>>>(rd, g0, g1, W, H, step, th, sigma_l, sigma_n, sigma_p, wr);
     float4* t = rd;
     rd = wr;
     wr = t;

@@ -779,9 +779,100 @@ __global__ void k_count_rays(uint32_t* ctr, int cur) {  // statistics: rays trac
   }
 }
 
+// ------------------------------------------------------------ ray reordering
+// Between bounces the queue of surviving paths is counting-sorted by a key
+// of (scene, direction octant, Morton code of the origin in a 16^3 grid over
+// its scene's bounds), so that a warp's rays start in similar places and head
+// the same way: fewer divergent traversal steps and more cache reuse. Paths
+// are independent, so the order changes no result.
+__device__ __forceinline__ uint32_t spread3(uint32_t x) {  // 4 bits -> every third bit
+  x &= 15u;
+  x = (x | (x << 4)) & 0x0C3u;
+  x = (x | (x << 2)) & 0x249u;
+  return x;
+}
+
+__global__ void k_sort_keys(Paths P, const SceneRec* __restrict__ recs, const uint16_t* __restrict__ sid, int n_scenes,
+                            int nxt) {
+  const uint32_t n = P.ctr[kCtrQ0 + nxt];
+  const uint32_t* q = P.q[nxt];
+  int sbits = 0;
+  while ((1 << sbits) < n_scenes) sbits++;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const uint32_t p = q[k];
+    const float4 o = P.ro[p], d = P.rd[p];
+    const int sc = n_scenes > 1 ? __ldg(sid + p) : 0;
+    const Node* nodes = recs[sc].scene.nodes;
+    const float4 lo = __ldg(reinterpret_cast<const float4*>(nodes)), hi = __ldg(reinterpret_cast<const float4*>(nodes) + 1);
+    auto cell = [](float v, float a, float b) {
+      const float t = (v - a) / fmaxf(b - a, 1e-20f);
+      return (uint32_t)fminf(fmaxf(t * 16.f, 0.f), 15.f);
+    };
+    const uint32_t m = spread3(cell(o.x, lo.x, hi.x)) | (spread3(cell(o.y, lo.y, hi.y)) << 1) |
+                       (spread3(cell(o.z, lo.z, hi.z)) << 2);
+    const uint32_t oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+    const uint32_t local = (oct << 12) | m;  // 15 bits
+    const uint32_t key = ((uint32_t)sc << (kSortBits - sbits)) | (local >> sbits);
+    P.sort_keys[k] = key;
+    const unsigned peers = __match_any_sync(__activemask(), key);  // one atomic per distinct key per warp
+    if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(P.sort_hist + key, (uint32_t)__popc(peers));
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_sort_scan(uint32_t* __restrict__ hist) {  // exclusive scan, one block
+  constexpr int kPer = kSortBins / 1024;
+  __shared__ uint32_t part[1024];
+  uint32_t v[kPer], sum = 0;
+  for (int i = 0; i < kPer; i++) {
+    v[i] = hist[threadIdx.x * kPer + i];
+    sum += v[i];
+  }
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const uint32_t t = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += t;
+    __syncthreads();
+  }
+  uint32_t run = part[threadIdx.x] - sum;
+  for (int i = 0; i < kPer; i++) {
+    hist[threadIdx.x * kPer + i] = run;
+    run += v[i];
+  }
+}
+
+__global__ void k_sort_scatter(Paths P, int nxt) {
+  const uint32_t n = P.ctr[kCtrQ0 + nxt];
+  const uint32_t* q = P.q[nxt];
+  const unsigned lane = threadIdx.x & 31;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const uint32_t key = P.sort_keys[k];
+    const unsigned peers = __match_any_sync(__activemask(), key);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(P.sort_hist + key, (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    P.sort_tmp[base + __popc(peers & ((1u << lane) - 1u))] = q[k];
+  }
+}
+
+// Sorts queue `nxt` into sort_tmp, then swaps the two buffers in P (the
+// caller's copy of the path state; every wave starts from the launch's own
+// pointers, so a captured wave replays the same sequence of swaps).
+static void sort_queue(const MultiLaunch& M, Paths& P, int nxt, int blocks, cudaStream_t s) {
+  cudaMemsetAsync(P.sort_hist, 0, (size_t)kSortBins * 4, s);
+  k_sort_keys<<<blocks, 256, 0, s>>>(P, M.recs, M.sid, M.n, nxt);
+  k_sort_scan<<<1, 1024, 0, s>>>(P.sort_hist);
+  k_sort_scatter<<<blocks, 256, 0, s>>>(P, nxt);
+  uint32_t* t = P.q[nxt];
+  P.q[nxt] = P.sort_tmp;
+  P.sort_tmp = t;
+}
+
 // ------------------------------------------------------------ one wave
 void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
-  const Paths& P = M.paths;
+  Paths P = M.paths;  // queue buffers may swap with the sort buffer below
   PhaseEvents none{nullptr, nullptr, 0, 0};
   PhaseEvents& E = pe ? *pe : none;
   E.mark(-1, s);
@@ -813,6 +904,7 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     E.mark(kPhShadow, s);
     k_resolve<<<shade_blocks, 128, 0, s>>>(P, cur);
     k_count_rays<<<1, 32, 0, s>>>(P.ctr, cur);
+    if (M.sort_rays && b < 2 && b < M.max_bounces) sort_queue(M, P, cur ^ 1, shade_blocks, s);  // the two largest queues
   }
   E.mark(kPhResolve, s);
   k_accumulate_multi<<<grid_for(M.total_pixels, 256), 256, 0, s>>>(P, M.recs, M.pix_base, M.path_base, M.n, M.S);

@@ -43,8 +43,13 @@ struct Paths {
   uint32_t* qs;
   uint32_t* slow;
   uint32_t* slow2;
+  uint32_t* sort_keys;  // per queued path: ray-sort key (scene, direction octant, origin cell)
+  uint32_t* sort_tmp;   // sorted queue before it is copied back
+  uint32_t* sort_hist;  // kSortBins counters
   uint32_t* ctr;
 };
+
+constexpr int kSortBits = 15, kSortBins = 1 << kSortBits;
 
 // Accumulation targets (renderer.ts:490): RGBA32F colour + lum^2, RGBA16F
 // albedo + coverage, RGBA16F normal + depth, R32F history.
@@ -77,6 +82,7 @@ struct MultiLaunch {
   int any_alpha;
   int trace_blocks, shade_blocks;  // 0 = all resident blocks
   unsigned long long* trav_stats;  // closest-hit traversal counters (profiling) or nullptr
+  int sort_rays;                   // reorder each bounce's queue by scene, direction octant and origin cell
 };
 
 // Optional per-phase timing: events recorded between launches, each tagged

@@ -177,6 +177,10 @@ class Renderer:
                                     [int(x) for x in st.traversal]))
         return out
 
+    def set_ray_sort(self, enabled=True):
+        """Reorder each bounce's rays by direction and origin (lucent_renderer_set_ray_sort)."""
+        N.check(N.lib().lucent_renderer_set_ray_sort(self._h, 1 if enabled else 0))
+
     def trim(self):
         """Frees the path-state buffers until the next trace (lucent_renderer_trim)."""
         N.check(N.lib().lucent_renderer_trim(self._h))
@@ -270,7 +274,7 @@ class Batch:
     sizes, 0 = all resident blocks)."""
 
     DEFAULTS = {"samples_per_wave": 0, "max_wave_paths": 1 << 25, "use_graph": True, "trace_blocks": 0,
-                "shade_blocks": 0}
+                "shade_blocks": 0, "sort_rays": True}
 
     def __init__(self, renderers, **options):
         self.renderers = list(renderers)
@@ -288,7 +292,7 @@ class Batch:
         self.options.update(options)
         o = self.options
         d = NR.BatchOptions(o["samples_per_wave"], o["max_wave_paths"], 1 if o["use_graph"] else 0,
-                            o["trace_blocks"], o["shade_blocks"])
+                            o["trace_blocks"], o["shade_blocks"], 1 if o["sort_rays"] else 0)
         N.check(N.lib().lucent_batch_set_options(self._h, C.byref(d)))
 
     def trace_samples(self, count, stream=None):

@@ -92,3 +92,20 @@ def test_full_size_box_scene_crop():
     assert frac > 0.9, frac
     rmse = np.sqrt(np.mean((g - oc[..., :3]) ** 2)) / np.mean(oc[..., :3])
     assert rmse < 0.05, rmse
+
+
+def test_ray_sort_changes_no_pixel():
+    # Reordering the rays between bounces changes the order paths are
+    # processed in, never a path: the images are identical bit for bit.
+    sc = W.box_scene(2, 3)
+    out = []
+    for sort in (True, False):
+        r = Renderer(64, 48)
+        r.settings.max_bounces = 8
+        r.load_scene(sc)
+        r.set_ray_sort(sort)
+        r.set_seed(11)
+        r.trace_samples(6)
+        out.append(r.read())
+        r.dispose()
+    assert all(np.array_equal(a, b) for a, b in zip(*out))
