@@ -306,7 +306,9 @@ def run_ours_pt(args, rank, world, local):
                 "peak_source": which, "kernel": "k_closest_fast_t<PathClosest> (+ slow path)",
                 "bytes_per_closest_ray": alg["bytes_per_closest_ray"],
                 "closest_ms_per_frame": round(ph["closest"], 3)}
-    launches_per_frame = 2 + 8 * (PT_DEPTH + 1)
+    # camera, accumulate, seed advance; 8 per bounce (counters, closest fast + exact, shade, any-hit fast +
+    # exact, resolve, ray count); 3 per ray sort (after bounces 0 and 1)
+    launches_per_frame = 3 + 8 * (PT_DEPTH + 1) + 3 * 2
     return {
         "metric": PT_METRIC, "value": round(value, 2), "unit": "Mrays/s", "ms_per_step": round(sum(ms) / len(ms), 4),
         "wall_s": round(wall, 3), "e2e": e2e, "roofline": roof, "clocks": clk.summary(),

@@ -193,10 +193,13 @@ typedef struct lucent_camera {
   float tan_half_fov, aperture, focus_distance;
 } lucent_camera;
 
-/* applySettings (renderer.ts:454-460): RenderSettings.maxBounces / fireflyClamp. */
+/* applySettings (renderer.ts:454-460): RenderSettings.maxBounces /
+ * fireflyClamp / temporal (reproject the history when the camera moves,
+ * renderer.ts:441-451; the reference's default is on). */
 typedef struct lucent_settings {
   uint32_t max_bounces;
   float firefly_clamp;
+  int32_t temporal;
 } lucent_settings;
 
 /* stats() (renderer.ts:832-854) plus ray counters. */
@@ -225,6 +228,9 @@ lucent_status lucent_renderer_load_scene(lucent_renderer* r, const lucent_scene_
 lucent_status lucent_renderer_upload_lighting(lucent_renderer* r, const lucent_lighting* lighting);
 /* uploadGround (renderer.ts:415-421). */
 lucent_status lucent_renderer_upload_ground(lucent_renderer* r, int32_t enabled, float height);
+/* With temporal on and samples accumulated, the history is kept and the
+ * first sample traced after the move reprojects it (trace.frag:275-322,
+ * at most HISTORY_CAP = 8 samples of it per pixel); otherwise a reset. */
 lucent_status lucent_renderer_upload_camera(lucent_renderer* r, const lucent_camera* camera);
 lucent_status lucent_renderer_apply_settings(lucent_renderer* r, const lucent_settings* settings);
 /* resize (renderer.ts:476-496): new accumulation targets, history cleared. */

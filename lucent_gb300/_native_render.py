@@ -29,7 +29,7 @@ class CameraDesc(C.Structure):
 
 
 class SettingsDesc(C.Structure):
-    _fields_ = [("max_bounces", C.c_uint32), ("firefly_clamp", C.c_float)]
+    _fields_ = [("max_bounces", C.c_uint32), ("firefly_clamp", C.c_float), ("temporal", C.c_int32)]
 
 
 class RenderStats(C.Structure):

@@ -196,6 +196,7 @@ __device__ __forceinline__ void camera_path(const Paths& P, uint32_t p, uint32_t
   P.tint[p] = make_float4(1.f, 1.f, 1.f, __uint_as_float(kSpecular));
   P.galb[p] = make_float4(1.f, 1.f, 1.f, 0.f);
   P.gnrm[p] = make_float4(-rd.x, -rd.y, -rd.z, 1e4f);
+  P.gpos[p] = make_float4(0.f, 0.f, 0.f, 1.f);
   P.rng[p] = st;
   P.q[0][p] = p;
 }
@@ -415,6 +416,7 @@ __global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_consta
       }
       // Hit record.
       const float3 pos = ro + rd * closest;
+      if (bounce == 0) P.gpos[p] = make_float4(pos.x, pos.y, pos.z, 1.f);
       float3 normal, gn;
       bool front;
       int material, light = -1;
@@ -495,6 +497,12 @@ __global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_consta
         if (light >= 0) break;
       }
       const bool glass = s.transmission > 0.f && rnd(st) < s.transmission;
+      if (bounce == 0) {  // trace.frag:187-193: reflections and refractions do not move with the surface
+        const float sharp = 1.f - smooth(0.1f, 0.7f, s.roughness);
+        float glossy = fmaxf(sharp * mixf(0.5f, 1.f, s.metallic), s.transmission);
+        glossy = fmaxf(glossy, s.clearcoat * 0.5f * (1.f - smooth(0.08f, 0.5f, s.clearcoat_roughness)));
+        P.gpos[p].w = 1.f - glossy;
+      }
       const bool mirror = !glass && s.metallic > 0.9f && s.roughness < 0.1f;
       if (!done && !((glass || mirror) && bounce < 3)) {
         galb = make_float4(tint.x * s.albedo.x, tint.y * s.albedo.y, tint.z * s.albedo.z, galb.w);
@@ -713,16 +721,76 @@ __global__ void k_seed_lrem(Paths P, AdjointDev A, uint32_t total) {
   }
 }
 
+__device__ __forceinline__ float4 h4f(half4 v) {
+  return make_float4(__half2float(v.x), __half2float(v.y), __half2float(v.z), __half2float(v.w));
+}
+
+// reprojectHistory (trace.frag:274-322): the previous view's averages at the
+// place this sample's primary surface (or sky direction) occupied there,
+// bilinear over the taps that saw the same surface. False: disoccluded.
+__device__ bool reproject_history(const SceneRec& R, float4 gp, float4 ga, float4 gn, float4& col, float4& alb,
+                                  float4& nrm, float& n) {
+  col = alb = nrm = make_float4(0.f, 0.f, 0.f, 0.f);
+  n = 0.f;
+  const bool surface = ga.w > 0.5f;
+  const CameraDev& C = R.prev_cam;
+  const float3 d = surface ? f3(gp) - C.pos : -f3(gn);  // a sky guide normal is -rd
+  const float z = dot3(d, C.forward);
+  if (z <= 1e-6f) return false;
+  const float pw = (float)R.prev_w, ph = (float)R.prev_h;
+  const float aspect = pw / ph;
+  const float px = (dot3(d, C.right) / (z * C.tan_half_fov * aspect) * 0.5f + 0.5f) * pw;
+  const float py = (dot3(d, C.up) / (z * C.tan_half_fov) * 0.5f + 0.5f) * ph;
+  if (!(px >= 0.f && py >= 0.f && px < pw && py < ph)) return false;
+  const float expected = len3(d);
+  const float fx = px - 0.5f, fy = py - 0.5f;
+  const int bx = (int)floorf(fx), by = (int)floorf(fy);
+  const float tx = fx - floorf(fx), ty = fy - floorf(fy);
+  const float3 g = f3(gn);
+  float wsum = 0.f;
+  for (int i = 0; i < 4; i++) {
+    const int ox = i & 1, oy = i >> 1;
+    const int qx = bx + ox, qy = by + oy;
+    if (qx < 0 || qy < 0 || qx >= R.prev_w || qy >= R.prev_h) continue;
+    const size_t q = (size_t)qy * R.prev_w + qx;
+    const float4 a = h4f(R.prev.albedo[q]), nq = h4f(R.prev.normal[q]);
+    const bool same = surface ? a.w > 0.5f && fabsf(nq.w - expected) < 0.02f * expected &&
+                                    dot3(norm3(f3(nq) + f3(1e-6f, 1e-6f, 1e-6f)), g) > 0.85f
+                              : a.w < 0.5f;
+    if (!same) continue;
+    const float w = (ox == 1 ? tx : 1.f - tx) * (oy == 1 ? ty : 1.f - ty);
+    const float4 c = R.prev.color[q];
+    col = make_float4(col.x + c.x * w, col.y + c.y * w, col.z + c.z * w, col.w + c.w * w);
+    alb = make_float4(alb.x + a.x * w, alb.y + a.y * w, alb.z + a.z * w, alb.w + a.w * w);
+    nrm = make_float4(nrm.x + nq.x * w, nrm.y + nq.y * w, nrm.z + nq.z * w, nrm.w + nq.w * w);
+    n += R.prev.history[q] * w;
+    wsum += w;
+  }
+  if (wsum < 1e-3f) return false;
+  col = make_float4(col.x / wsum, col.y / wsum, col.z / wsum, col.w / wsum);
+  alb = make_float4(alb.x / wsum, alb.y / wsum, alb.z / wsum, alb.w / wsum);
+  nrm = make_float4(nrm.x / wsum, nrm.y / wsum, nrm.z / wsum, nrm.w / wsum);
+  n = fminf(n / wsum, kHistoryCap * gp.w);
+  return true;
+}
+
 // Running means (trace.frag:335-354) of one pixel over the batch's samples,
-// in order; sample s of the pixel is path path_base + s * W * H + px.
-__device__ __forceinline__ void accumulate_pixel(const Paths& P, const AccumDev& A, uint32_t WH, int S, uint32_t px,
+// in order; sample s of the pixel is path path_base + s * W * H + px. With
+// R.reproject the first sample starts from the reprojected history.
+__device__ __forceinline__ void accumulate_pixel(const Paths& P, const SceneRec& R, uint32_t WH, int S, uint32_t px,
                                                  uint32_t path_base) {
-  float4 col = A.color[px];
-  float4 alb = make_float4(__half2float(A.albedo[px].x), __half2float(A.albedo[px].y), __half2float(A.albedo[px].z),
-                           __half2float(A.albedo[px].w));
-  float4 nrm = make_float4(__half2float(A.normal[px].x), __half2float(A.normal[px].y), __half2float(A.normal[px].z),
-                           __half2float(A.normal[px].w));
-  float n = A.history[px];
+  const AccumDev& A = R.accum;
+  float4 col, alb, nrm;
+  float n;
+  if (R.reproject) {
+    const uint32_t p0 = path_base + px;
+    if (!reproject_history(R, P.gpos[p0], P.galb[p0], P.gnrm[p0], col, alb, nrm, n)) n = 0.f;  // disoccluded
+  } else {
+    col = A.color[px];
+    alb = h4f(A.albedo[px]);
+    nrm = h4f(A.normal[px]);
+    n = A.history[px];
+  }
   for (int s = 0; s < S; s++) {
     const uint32_t p = path_base + (uint32_t)s * WH + px;
     float4 c = P.rad[p];
@@ -751,14 +819,17 @@ __global__ void k_accumulate_multi(Paths P, const SceneRec* __restrict__ recs, c
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
     const int sc = find_scene(pix_base, n, g);
     const SceneRec& R = recs[sc];
-    accumulate_pixel(P, R.accum, (uint32_t)R.W * R.H, S, g - __ldg(pix_base + sc), __ldg(path_base + sc));
+    accumulate_pixel(P, R, (uint32_t)R.W * R.H, S, g - __ldg(pix_base + sc), __ldg(path_base + sc));
   }
 }
 
 // Advances every scene's sample seed by the wave's S samples (on the device,
 // so a captured wave can be replayed unchanged).
 __global__ void k_advance_seeds(SceneRec* recs, int n, int S) {
-  for (int i = threadIdx.x; i < n; i += blockDim.x) recs[i].seed0 += (uint32_t)S;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    recs[i].seed0 += (uint32_t)S;
+    recs[i].reproject = 0;  // only a view's first sample reprojects
+  }
 }
 
 __global__ void k_zero_counters(uint32_t* ctr, int nxt) {

@@ -210,6 +210,12 @@ struct lucent_renderer {
   DeviceBuffer rec1, base1, sid1;
   uint32_t sid_cap = 0;
   int sort_rays = 1;  // reorder each bounce's rays (lucent_renderer_set_ray_sort)
+  // temporal reprojection (renderer.ts:441-451, 717-731): the view the accumulation was traced with
+  int temporal = 1;
+  bool has_history = false, reproject_pending = false;
+  sh::CameraDev hist_cam{};
+  uint32_t hist_w = 0, hist_h = 0;
+  DeviceBuffer prev;  // the targets as the previous view left them (36 B per pixel)
   const float4* denoised = nullptr;  // result of the last lucent_renderer_denoise, or null
 };
 
@@ -228,6 +234,7 @@ static lucent_status alloc_targets(lucent_renderer* r, uint32_t w, uint32_t h) {
   k_clear_accum<<<grid_for((uint32_t)n, 256), 256>>>(accum_of(r), (uint32_t)n);
   r->frame = 0;
   r->denoised = nullptr;
+  r->has_history = r->reproject_pending = false;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "clear targets");
 }
@@ -238,7 +245,7 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
                                         uint32_t cap) {
   if (cap <= path_cap) return LUCENT_OK;
   // Per-path arrays in allocation order (bytes per path); each starts on a 256-byte boundary.
-  static const size_t kPer[] = {16, 16, 16, 16, 16, 16, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12, 4, 4};
+  static const size_t kPer[] = {16, 16, 16, 16, 16, 16, 16, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12, 4, 4};
   size_t total = 0;
   for (size_t b : kPer) total += ((size_t)cap * b + 255) & ~(size_t)255;
   total += (size_t)kSortBins * 4;
@@ -260,6 +267,7 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
   P.galb = (float4*)take((size_t)cap * 16);
   P.gnrm = (float4*)take((size_t)cap * 16);
   P.hit = (float4*)take((size_t)cap * 16);
+  P.gpos = (float4*)take((size_t)cap * 16);
   P.sh_o = (float4*)take((size_t)cap * 48);
   P.sh_d = (float4*)take((size_t)cap * 48);
   P.sh_c = (float4*)take((size_t)cap * 48);
@@ -300,7 +308,45 @@ static SceneRec scene_rec(const lucent_renderer* r) {
   R.max_bounces = (int)r->max_bounces;
   R.clamp = r->clamp;
   R.seed0 = r->seed;
+  R.reproject = r->reproject_pending ? 1 : 0;
+  if (R.reproject) {
+    const size_t n = (size_t)r->hist_w * r->hist_h;
+    char* b = (char*)r->prev.ptr;
+    R.prev = {(float4*)b, (half4*)(b + n * 16), (half4*)(b + n * 24), (float*)(b + n * 32)};
+    R.prev_cam = r->hist_cam;
+    R.prev_w = (int)r->hist_w;
+    R.prev_h = (int)r->hist_h;
+  }
   return R;
+}
+
+// Before a trace that reprojects: copies the targets (the previous view's
+// averages) aside, since the first sample reads them around each pixel while
+// it writes the new averages in place.
+static lucent_status prepare_reprojection(lucent_renderer* r, cudaStream_t s) {
+  if (!r->reproject_pending) return LUCENT_OK;
+  const size_t n = (size_t)r->W * r->H;
+  if (r->hist_w != r->W || r->hist_h != r->H) {  // the targets were reallocated: nothing to reproject
+    r->reproject_pending = false;
+    return LUCENT_OK;
+  }
+  lucent_status st = r->prev.reserve(n * 36);
+  if (st) return st;
+  char* b = (char*)r->prev.ptr;
+  cudaError_t e = cudaMemcpyAsync(b, r->color.ptr, n * 16, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b + n * 16, r->albedo.ptr, n * 8, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b + n * 24, r->normal.ptr, n * 8, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b + n * 32, r->history.ptr, n * 4, cudaMemcpyDeviceToDevice, s);
+  return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "copy history");
+}
+
+// After a trace: the targets now hold this view's averages.
+static void record_history(lucent_renderer* r) {
+  r->has_history = true;
+  r->reproject_pending = false;
+  r->hist_cam = r->cam;
+  r->hist_w = r->W;
+  r->hist_h = r->H;
 }
 
 // The renderer as a launch of one scene: uploads its SceneRec (sample seed
@@ -380,7 +426,7 @@ void lucent_renderer_destroy(lucent_renderer* r) {
   if (!r) return;
   for (DeviceBuffer* b : {&r->nodes, &r->geo, &r->attr, &r->mats, &r->spheres, &r->sph_mat, &r->sph_light,
                           &r->lights, &r->env_rgb, &r->env_alias, &r->sheen, &r->color, &r->albedo, &r->normal,
-                          &r->history, &r->paths, &r->ctr, &r->den_a, &r->den_b, &r->guide0, &r->guide1, &r->disp, &r->adj_dl, &r->adj_path, &r->adj_grad, &r->rec1, &r->base1, &r->sid1})
+                          &r->history, &r->paths, &r->ctr, &r->den_a, &r->den_b, &r->guide0, &r->guide1, &r->disp, &r->adj_dl, &r->adj_path, &r->adj_grad, &r->rec1, &r->base1, &r->sid1, &r->prev})
     b->release();
   if (r->ev0) cudaEventDestroy(r->ev0);
   if (r->ev1) cudaEventDestroy(r->ev1);
@@ -563,7 +609,14 @@ lucent_status lucent_renderer_upload_camera(lucent_renderer* r, const lucent_cam
   r->cam.tan_half_fov = c->tan_half_fov;
   r->cam.aperture = c->aperture;
   r->cam.focus = c->focus_distance;
-  return lucent_renderer_reset(r);  // the view changed; no temporal reprojection here
+  // invalidateView (renderer.ts:441-451): keep the history for reprojection if allowed, else start over
+  if (r->temporal && r->has_history && r->frame > 0) {
+    r->reproject_pending = true;
+    r->frame = std::min(r->frame, (uint32_t)kHistoryCap);
+    r->denoised = nullptr;
+    return LUCENT_OK;
+  }
+  return lucent_renderer_reset(r);
 }
 
 lucent_status lucent_renderer_apply_settings(lucent_renderer* r, const lucent_settings* s) {
@@ -572,6 +625,7 @@ lucent_status lucent_renderer_apply_settings(lucent_renderer* r, const lucent_se
   if (s->max_bounces > 64) return fail(LUCENT_ERR_INVALID, "max_bounces %u", s->max_bounces);
   r->max_bounces = s->max_bounces;
   r->clamp = s->firefly_clamp;
+  r->temporal = s->temporal ? 1 : 0;
   return LUCENT_OK;
 }
 
@@ -588,6 +642,7 @@ lucent_status lucent_renderer_reset(lucent_renderer* r) {
   k_clear_accum<<<grid_for(n, 256), 256>>>(accum_of(r), n);
   r->frame = 0;
   r->denoised = nullptr;
+  r->has_history = r->reproject_pending = false;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "reset");
 }
@@ -610,7 +665,8 @@ lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* 
   const uint32_t batch = std::max(1u, std::min(samples, max_paths / std::max(1u, WH)));
   const uint32_t full = samples / batch, tail = samples % batch;
   MultiLaunch M{};
-  lucent_status st = single_launch(r, batch, tail, r->seed, s, M);
+  lucent_status st = prepare_reprojection(r, s);
+  if (!st) st = single_launch(r, batch, tail, r->seed, s, M);
   if (st) return st;
   M.trav_stats = r->profiling ? (unsigned long long*)((uint32_t*)r->ctr.ptr + kCtrTrav) : nullptr;
   cudaEventRecord(r->ev0, s);
@@ -621,6 +677,7 @@ lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* 
   }
   r->seed += samples;
   r->frame += samples;
+  record_history(r);
   cudaEventRecord(r->ev1, s);
   r->pn = pe.n;
   cudaError_t e = cudaGetLastError();
@@ -917,10 +974,13 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
   std::vector<SceneRec> recs(n);
   uint64_t pixels = 0;
   int max_bounces = 0, any_alpha = 0;
+  cudaStream_t s = (cudaStream_t)stream;
   for (int i = 0; i < n; i++) {
-    const lucent_renderer* r = b->rs[i];
+    lucent_renderer* r = b->rs[i];
     if (!r->has_scene || !r->has_lighting)
       return fail(LUCENT_ERR_INVALID, "renderer %d: trace before load_scene / upload_lighting", i);
+    lucent_status st = prepare_reprojection(r, s);
+    if (st) return st;
     recs[i] = scene_rec(r);
     pixels += (uint64_t)r->W * r->H;
     max_bounces = std::max(max_bounces, (int)r->max_bounces);
@@ -951,7 +1011,6 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
       hb[n + 1 + i + 1] = hb[n + 1 + i] + wh;            // pix_base
     }
   };
-  cudaStream_t s = (cudaStream_t)stream;
   std::vector<uint32_t> hb, tb;
   make_bases((uint32_t)S, hb);
   cudaError_t e = cudaMemcpyAsync(b->recs.ptr, recs.data(), sizeof(SceneRec) * n, cudaMemcpyHostToDevice, s);
@@ -1017,6 +1076,7 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
   for (lucent_renderer* r : b->rs) {
     r->seed += samples;
     r->frame += samples;
+    record_history(r);
   }
   e = cudaGetLastError();
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "batch trace launch");

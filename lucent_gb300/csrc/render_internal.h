@@ -36,6 +36,7 @@ __device__ __forceinline__ half4 make_half4(float4 v) {
 // Structure-of-arrays path state; shadow slots are 3 per path (sun, env, light).
 struct Paths {
   float4 *ro, *rd, *thr, *rad, *tint, *galb, *gnrm, *hit;
+  float4* gpos;  // guide: primary hit position (xyz) and how much history it may reuse (w)
   float4 *sh_o, *sh_d, *sh_c;
   uint32_t* rng;
   uint8_t* sh_occ;
@@ -69,7 +70,14 @@ struct SceneRec {
   int W, H, max_bounces;
   float clamp;
   uint32_t seed0;  // sample seed (uSeed) of the wave's first sample; advanced on the device
+  // temporal reprojection of the wave's first sample (trace.frag:275-322); cleared on the device after it
+  int reproject;
+  AccumDev prev;       // copy of the targets as the previous view left them
+  sh::CameraDev prev_cam;
+  int prev_w, prev_h;
 };
+
+constexpr float kHistoryCap = 8.f;  // HISTORY_CAP (renderer.ts:139)
 
 struct MultiLaunch {
   Paths paths;

@@ -36,6 +36,7 @@ class RenderSettings:
     tonemap: str = "aces"
     firefly_clamp: float = 8.0
     denoise: bool = True
+    temporal: bool = True
     samples_per_frame: int = 1
     max_samples: int = 0
 
@@ -136,7 +137,7 @@ class Renderer:
         N.check(N.lib().lucent_renderer_upload_camera(self._h, C.byref(d)))
 
     def apply_settings(self):
-        d = NR.SettingsDesc(self.settings.max_bounces, self.settings.firefly_clamp)
+        d = NR.SettingsDesc(self.settings.max_bounces, self.settings.firefly_clamp, 1 if self.settings.temporal else 0)
         N.check(N.lib().lucent_renderer_apply_settings(self._h, C.byref(d)))
 
     def reset(self):

@@ -1012,6 +1012,8 @@ struct Tracer {
     V albedo, normal;
     R depth, coverage;
     bool done;
+    V position;  // primary hit (trace.frag:131-132)
+    R reuse;
   };
 
   // cameraRay (:53-62).
@@ -1036,7 +1038,7 @@ struct Tracer {
     bool specularBounce = true;
     R bsdfPdf = R(0);
     V guideTint = {R(1), R(1), R(1)};
-    guide = {{R(1), R(1), R(1)}, -rd, R(1e4), R(0), false};
+    guide = {{R(1), R(1), R(1)}, -rd, R(1e4), R(0), false, {R(0), R(0), R(0)}, R(1)};
     auto U = [this]() { return rand(); };
     for (int bounce = 0; bounce <= (int)maxBounces; bounce++) {
       Hit hit;
@@ -1053,6 +1055,7 @@ struct Tracer {
       if (bounce == 0) {
         guide.depth = hit.t;
         guide.coverage = R(1);
+        guide.position = hit.position;
       }
       const V wo = -rd;
       V emission;
@@ -1075,6 +1078,12 @@ struct Tracer {
         if (hit.light >= 0) break;
       }
       const bool glass = sf.transmission > R(0) && rand() < sf.transmission;
+      if (bounce == 0) {  // :187-193
+        const R sharp = R(1) - smoothstep(R(0.1), R(0.7), sf.roughness);
+        R glossy = std::max(sharp * mixr<R>(R(0.5), R(1), sf.metallic), sf.transmission);
+        glossy = std::max(glossy, sf.clearcoat * R(0.5) * (R(1) - smoothstep(R(0.08), R(0.5), sf.clearcoatRoughness)));
+        guide.reuse = R(1) - glossy;
+      }
       const bool mirror = !glass && sf.metallic > R(0.9) && sf.roughness < R(0.1);
       if (!guide.done && !((glass || mirror) && bounce < 3)) {
         guide.albedo = guideTint * sf.albedo;
@@ -1269,10 +1278,68 @@ struct Tracer {
 
 extern "C" {
 
+}  // extern "C"
+
+// reprojectHistory + projectToPrevious (trace.frag:274-322): the previous
+// view's averages where this sample's primary surface (or sky direction) was
+// seen, bilinear over the taps that saw the same surface; false if none.
+template <class R>
+static bool reproject_history(const orc_history* h, const typename Tracer<R>::Guide& g, Vec3<R> rd, R out_c[4],
+                              R out_a[4], R out_n[4], R& n) {
+  using V = Vec3<R>;
+  auto f3 = [](const float* p) { return V{R(p[0]), R(p[1]), R(p[2])}; };
+  for (int c = 0; c < 4; c++) out_c[c] = out_a[c] = out_n[c] = R(0);
+  n = R(0);
+  const bool surface = g.coverage > R(0.5);
+  const V d = surface ? g.position - f3(h->cam->pos) : rd;
+  const R z = dot(d, f3(h->cam->forward));
+  if (z <= R(1e-6)) return false;
+  const R pw = R(h->w), ph = R(h->h), aspect = pw / ph, th = R(h->cam->tan_half_fov);
+  const R px = (dot(d, f3(h->cam->right)) / (z * th * aspect) * R(0.5) + R(0.5)) * pw;
+  const R py = (dot(d, f3(h->cam->up)) / (z * th) * R(0.5) + R(0.5)) * ph;
+  if (!(px >= R(0) && py >= R(0) && px < pw && py < ph)) return false;
+  const R expected = length(d);
+  const R fx = px - R(0.5), fy = py - R(0.5);
+  const int bx = (int)std::floor(fx), by = (int)std::floor(fy);
+  const R tx = fx - std::floor(fx), ty = fy - std::floor(fy);
+  R wsum = R(0);
+  for (int i = 0; i < 4; i++) {
+    const int ox = i & 1, oy = i >> 1, qx = bx + ox, qy = by + oy;
+    if (qx < 0 || qy < 0 || qx >= (int)h->w || qy >= (int)h->h) continue;
+    const size_t q = (size_t)qy * h->w + qx;
+    const float* a = h->albedo4 + q * 4;
+    const float* nq = h->normal4 + q * 4;
+    const V nn = normalize(V{R(nq[0]) + R(1e-6), R(nq[1]) + R(1e-6), R(nq[2]) + R(1e-6)});
+    const bool same = surface ? R(a[3]) > R(0.5) && std::fabs(R(nq[3]) - expected) < R(0.02) * expected &&
+                                    dot(nn, g.normal) > R(0.85)
+                              : R(a[3]) < R(0.5);
+    if (!same) continue;
+    const R w = (ox == 1 ? tx : R(1) - tx) * (oy == 1 ? ty : R(1) - ty);
+    for (int c = 0; c < 4; c++) {
+      out_c[c] += R(h->color4[q * 4 + c]) * w;
+      out_a[c] += R(a[c]) * w;
+      out_n[c] += R(nq[c]) * w;
+    }
+    n += R(h->history[q]) * w;
+    wsum += w;
+  }
+  if (wsum < R(1e-3)) return false;
+  for (int c = 0; c < 4; c++) {
+    out_c[c] /= wsum;
+    out_a[c] /= wsum;
+    out_n[c] /= wsum;
+  }
+  n = std::min(n / wsum, R(8) * g.reuse);  // uHistoryCap = HISTORY_CAP (renderer.ts:139, 250)
+  return true;
+}
+
+extern "C" {
+
 static int render_impl(const orc_scene* s, const orc_camera* cam, uint32_t max_bounces, float clamp_lum,
                        uint32_t width, uint32_t height, uint32_t x0, uint32_t y0, uint32_t cw, uint32_t ch,
                        uint32_t seed0, uint32_t samples, int precision, float* color4, float* albedo4,
-                       float* normal4, float* history, int threads, uint64_t* work_out, bool detailed) {
+                       float* normal4, float* history, int threads, uint64_t* work_out, bool detailed,
+                       const orc_history* hist = nullptr) {
   // One counter set per par_for chunk (chunks start at multiples of 16), so
   // no two threads ever share one.
   std::vector<WorkCounts> counts(work_out ? (size_t)cw * ch / 16 + 2 : 1);
@@ -1305,6 +1372,12 @@ static int render_impl(const orc_scene* s, const orc_camera* cam, uint32_t max_b
               std::isinf(color.y) || std::isinf(color.z))
             color = {R(0), R(0), R(0)};
           const R lum = luminance(color);
+          if (k == 0 && hist) {  // the first sample after a camera move starts from the reprojected history
+            R pc[4], pa[4], pn[4], n0;
+            reproject_history<R>(hist, guide, rd, pc, pa, pn, n0);  // zeros and 0 samples when disoccluded
+            for (int c = 0; c < 4; c++) col[c] = (float)pc[c], alb[c] = (float)pa[c], nrm[c] = (float)pn[c];
+            history[q] = (float)n0;
+          }
           const float n = history[q];
           const R kk = R(1) / (R(n) + R(1));
           const R nc[4] = {color.x, color.y, color.z, lum * lum};
@@ -1342,6 +1415,14 @@ int orc_render(const orc_scene* s, const orc_camera* cam, uint32_t max_bounces, 
                int threads) {
   return render_impl(s, cam, max_bounces, clamp_lum, width, height, x0, y0, cw, ch, seed0, samples, precision,
                      color4, albedo4, normal4, history, threads, nullptr, false);
+}
+
+int orc_render_reproject(const orc_scene* s, const orc_camera* cam, const orc_history* hist, uint32_t max_bounces,
+                         float clamp_lum, uint32_t width, uint32_t height, uint32_t x0, uint32_t y0, uint32_t cw,
+                         uint32_t ch, uint32_t seed0, uint32_t samples, int precision, float* color4, float* albedo4,
+                         float* normal4, float* history, int threads) {
+  return render_impl(s, cam, max_bounces, clamp_lum, width, height, x0, y0, cw, ch, seed0, samples, precision,
+                     color4, albedo4, normal4, history, threads, nullptr, false, hist);
 }
 
 int orc_render_work(const orc_scene* s, const orc_camera* cam, uint32_t max_bounces, float clamp_lum,

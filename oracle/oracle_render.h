@@ -87,6 +87,24 @@ int orc_denoise(const float* color4, const float* albedo4, const float* normal4,
 int orc_display(const float* color4, const float* albedo4, const float* denoised4, uint32_t w, uint32_t h,
                 float denoise_weight, float exposure, int tonemap, float* out_rgb);
 
+/* The previous view of a temporal reprojection: its camera, size and
+ * targets (w x h, albedo/normal as the RGBA16F values). */
+typedef struct orc_history {
+  const orc_camera* cam;
+  uint32_t w, h;
+  const float* color4;
+  const float* albedo4;
+  const float* normal4;
+  const float* history;
+} orc_history;
+
+/* orc_render whose first sample per pixel starts from the history
+ * reprojected from `hist` (trace.frag:310-322 with uReproject = 1). */
+int orc_render_reproject(const orc_scene* s, const orc_camera* cam, const orc_history* hist, uint32_t max_bounces,
+                         float clamp_lum, uint32_t width, uint32_t height, uint32_t x0, uint32_t y0, uint32_t cw,
+                         uint32_t ch, uint32_t seed0, uint32_t samples, int precision, float* color4, float* albedo4,
+                         float* normal4, float* history, int threads);
+
 /* Finite-difference reference of the adjoint: sum over pixels of dl4[px].rgb
  * times the mean over samples [seed0, seed0 + samples) of the radiance traced
  * with sampling from s and BSDF values / environment radiance from

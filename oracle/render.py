@@ -205,3 +205,42 @@ def detached_dot(prep, width, height, seed0, samples, dl4, materials_eval=None, 
     return lib().orc_detached_dot(C.byref(prep.scene), C.byref(prep.camera), max_bounces, clamp, width, height, seed0,
                                   samples, _p(m, F) if m is not None else None, _p(e, F) if e is not None else None,
                                   _p(d, F), threads)
+
+
+class OrcHistory(C.Structure):
+    _fields_ = [("cam", P(OrcCamera)), ("w", U32), ("h", U32), ("color4", P(F)), ("albedo4", P(F)),
+                ("normal4", P(F)), ("history", P(F))]
+
+
+def camera_of(camera):
+    """OrcCamera of a scene.Camera (the renderer's uploadCamera basis)."""
+    from lucent_gb300 import scene as S
+    f, r, u = S.camera_basis(camera)
+    c = OrcCamera()
+    c.pos[:] = camera.position
+    c.right[:], c.up[:], c.forward[:] = r, u, f
+    c.tan_half_fov = float(np.tan(camera.fov * np.pi / 360))
+    c.aperture, c.focus_dist = camera.aperture, camera.focus_distance
+    return c
+
+
+def render_reproject(prep, camera, width, height, seed0, samples, prev_camera, prev, max_bounces=6, clamp=8.0,
+                     precision=32, threads=0):
+    """orc_render_reproject of the full width x height image with the view
+    `camera` (OrcCamera), the first sample of each pixel starting from the
+    previous view's targets `prev` = (color4, albedo4, normal4, history) seen
+    from `prev_camera` (OrcCamera). Returns (color4, albedo4, normal4, history)."""
+    L = lib()
+    L.orc_render_reproject.argtypes = [P(OrcScene), P(OrcCamera), P(OrcHistory), U32, F, U32, U32, U32, U32, U32,
+                                       U32, U32, U32, C.c_int, P(F), P(F), P(F), P(F), C.c_int]
+    ph, pw = prev[3].shape
+    arrs = [np.ascontiguousarray(a, np.float32) for a in prev]
+    hist = OrcHistory(C.pointer(prev_camera), pw, ph, *[_p(a, F) for a in arrs])
+    out = [np.zeros(width * height * 4, np.float32) for _ in range(3)] + [np.zeros(width * height, np.float32)]
+    st = L.orc_render_reproject(C.byref(prep.scene), C.byref(camera), C.byref(hist), max_bounces, clamp, width,
+                                height, 0, 0, width, height, seed0, samples, precision, *[_p(b, F) for b in out],
+                                threads)
+    if st:
+        raise RuntimeError("orc_render_reproject failed")
+    return (out[0].reshape(height, width, 4), out[1].reshape(height, width, 4), out[2].reshape(height, width, 4),
+            out[3].reshape(height, width))
