@@ -81,10 +81,13 @@ lucent_status lucent_bvh_create(const float* nodes, uint32_t node_count, const u
 void lucent_bvh_destroy(lucent_bvh* bvh);
 /* Node and triangle counts of an uploaded BVH. */
 lucent_status lucent_bvh_info(const lucent_bvh* bvh, uint32_t* node_count, uint32_t* tri_count);
-/* Traversal mode: 0 = f32 bounded-error path with binary64 fallback (default),
- * 1 = every decision in binary64. Both return identical results. */
+/* Traversal mode: 0 = f32 bounded-error path with binary64 fallback and the
+ * top six BVH levels staged in shared memory (default), 1 = every decision in
+ * binary64, 2 = mode 0 reading every node from global memory. All return
+ * identical results. */
 #define LUCENT_TRAVERSE_FAST 0
 #define LUCENT_TRAVERSE_EXACT 1
+#define LUCENT_TRAVERSE_FAST_GLOBAL 2
 lucent_status lucent_bvh_set_mode(lucent_bvh* bvh, int32_t mode);
 
 /* n rays, 6 floats each (origin xyz, direction xyz), host buffers. t_min and
@@ -253,10 +256,15 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
  * the reference's GPU timer queries, renderer.ts:668-700); results appear in
  * lucent_render_stats.phase_ms after lucent_renderer_check. */
 lucent_status lucent_renderer_set_profiling(lucent_renderer* r, int32_t enabled);
-/* Between bounces, reorder the surviving rays by direction octant and origin
- * cell (counting sort, default on). Paths are independent: images are the
- * same either way; only the traversal's coherence changes. */
+/* After bounces 0 and 1, sort the surviving rays by direction octant and
+ * origin cell (counting sort into a ray stream the closest-hit traversal
+ * reads in order; default on). Paths are independent: images are the same
+ * either way; only the traversal's coherence changes. */
 lucent_status lucent_renderer_set_ray_sort(lucent_renderer* r, int32_t enabled);
+/* Stage the top six BVH levels (63 nodes) in each traversal block's shared
+ * memory (default on). Hits and images are the same either way; only where
+ * the traversal reads those nodes changes. */
+lucent_status lucent_renderer_set_top_levels(lucent_renderer* r, int32_t enabled);
 /* ---------------------------------------------------------------------------
  * Differentiable rendering (path replay backpropagation). No reference
  * counterpart: the reference renders forward only.
@@ -321,11 +329,12 @@ lucent_status lucent_renderer_display(lucent_renderer* r, float denoise_weight, 
 typedef struct lucent_batch lucent_batch;
 typedef struct lucent_batch_options {
   uint32_t samples_per_wave; /* samples of every pixel per wave; 0 = as many as max_wave_paths allows */
-  uint32_t max_wave_paths;   /* path-state budget of one wave (about 315 bytes of device memory per path) */
+  uint32_t max_wave_paths;   /* path-state budget of one wave (about 370 bytes of device memory per path) */
   int32_t use_graph;         /* capture a full wave once as a CUDA graph and replay it */
   uint32_t trace_blocks;     /* grid of the persistent traversal kernels; 0 = all resident blocks */
   uint32_t shade_blocks;     /* grid of the shade / resolve kernels; 0 = all resident blocks */
-  int32_t sort_rays;         /* reorder each bounce's rays (see lucent_renderer_set_ray_sort) */
+  int32_t sort_rays;         /* sort the rays of bounces 1 and 2 (see lucent_renderer_set_ray_sort) */
+  int32_t top_levels;        /* top BVH levels of the first 8 scenes in shared memory (lucent_renderer_set_top_levels) */
 } lucent_batch_options;
 typedef struct lucent_batch_stats {
   uint64_t closest_rays, shadow_rays; /* traced by this batch since creation */
@@ -337,7 +346,7 @@ typedef struct lucent_batch_stats {
 lucent_status lucent_batch_create(lucent_renderer* const* renderers, uint32_t n, lucent_batch** out);
 void lucent_batch_destroy(lucent_batch* batch);
 /* Defaults: samples_per_wave 0, max_wave_paths 2^25, use_graph 1, trace_blocks 0, shade_blocks 0,
- * sort_rays 1. */
+ * sort_rays 1, top_levels 1. */
 lucent_status lucent_batch_set_options(lucent_batch* batch, const lucent_batch_options* options);
 /* Asynchronous on `stream`. */
 lucent_status lucent_batch_trace(lucent_batch* batch, uint32_t samples, void* stream);

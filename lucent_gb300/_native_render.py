@@ -57,6 +57,7 @@ def declare(L, sig):
     sig(L, "lucent_renderer_set_profiling", [VP, C.c_int32])
     sig(L, "lucent_renderer_trim", [VP])
     sig(L, "lucent_renderer_set_ray_sort", [VP, C.c_int32])
+    sig(L, "lucent_renderer_set_top_levels", [VP, C.c_int32])
     sig(L, "lucent_renderer_set_materials", [VP, F32P, C.c_uint32])
     sig(L, "lucent_renderer_backward", [VP, C.c_uint32, C.c_uint32, F32P, F32P, F32P, VP])
     sig(L, "lucent_renderer_denoise", [VP, C.c_uint32, C.c_float, C.c_float, C.c_float, VP])
@@ -68,7 +69,8 @@ def declare(L, sig):
 
 class BatchOptions(C.Structure):
     _fields_ = [("samples_per_wave", C.c_uint32), ("max_wave_paths", C.c_uint32), ("use_graph", C.c_int32),
-                ("trace_blocks", C.c_uint32), ("shade_blocks", C.c_uint32), ("sort_rays", C.c_int32)]
+                ("trace_blocks", C.c_uint32), ("shade_blocks", C.c_uint32), ("sort_rays", C.c_int32),
+                ("top_levels", C.c_int32)]
 
 
 class BatchStats(C.Structure):

@@ -69,8 +69,11 @@ class DeviceBVH:
 
     __del__ = close
 
-    def set_mode(self, exact):
-        N.check(N.lib().lucent_bvh_set_mode(self._h, 1 if exact else 0))
+    def set_mode(self, exact, top_levels=True):
+        """lucent_bvh_set_mode: all-binary64 traversal (exact), else the
+        binary32 path with (top_levels) or without the shared-memory copy of
+        the top BVH levels. Results are identical in every mode."""
+        N.check(N.lib().lucent_bvh_set_mode(self._h, 1 if exact else 0 if top_levels else 2))
 
     def intersect(self, rays, t_min=1e-5, t_max=math.inf, stream=None):
         """Closest hits of float32 rays [n, 6] -> (prim int32 (-1 miss), t, u, v) float32."""

@@ -257,7 +257,8 @@ lucent_status lucent_bvh_download(const lucent_bvh* b, float* nodes_out, uint32_
 lucent_status lucent_bvh_set_mode(lucent_bvh* b, int32_t mode) {
   clear_error();
   if (!b) return fail(LUCENT_ERR_INVALID, "null bvh");
-  if (mode != LUCENT_TRAVERSE_FAST && mode != LUCENT_TRAVERSE_EXACT) return fail(LUCENT_ERR_INVALID, "bad mode %d", mode);
+  if (mode != LUCENT_TRAVERSE_FAST && mode != LUCENT_TRAVERSE_EXACT && mode != LUCENT_TRAVERSE_FAST_GLOBAL)
+    return fail(LUCENT_ERR_INVALID, "bad mode %d", mode);
   b->mode = mode;
   return LUCENT_OK;
 }
@@ -299,7 +300,8 @@ lucent_status lucent_bvh_intersect_device(lucent_bvh* b, const float* rays_d, ui
     return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "memset");
   }
   launch_closest((const Node*)b->nodes.ptr, b->node_count, (const float4*)b->tris.ptr, rays_d, n, t_min, t_max, prim_d, t_d, u_d,
-                 v_d, queue, qlen, work, err, b->mode == LUCENT_TRAVERSE_EXACT || b->depth + 2 > kTsStack, s);
+                 v_d, queue, qlen, work, err, b->mode == LUCENT_TRAVERSE_EXACT || b->depth + 2 > kTsStack,
+                 b->mode != LUCENT_TRAVERSE_FAST_GLOBAL, s);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "closest-hit launch");
 }

@@ -135,10 +135,11 @@ void launch_unpack(const Node* nodes, uint32_t count, const float4* tris, uint32
 
 void launch_closest(const Node* nodes, uint32_t node_count, const float4* tris, const float* rays_d, uint32_t n,
                     double tMin, double tMax, int32_t* prim, float* t, float* u, float* v, uint32_t* queue,
-                    uint32_t* queue_len, uint32_t* work, unsigned* err, bool exact_only, cudaStream_t s) {
+                    uint32_t* queue_len, uint32_t* work, unsigned* err, bool exact_only, bool top_levels,
+                    cudaStream_t s) {
   if (n == 0) return;
   const ApiPolicy P{rays_d, n, tris, prim, t, u, v};
-  TravArgs A{nodes, node_count, tris, tMin, tMax, queue, queue_len, work, err};
+  TravArgs A{nodes, node_count, tris, tMin, tMax, queue, queue_len, work, err, nullptr, top_levels ? 1 : 0};
   if (exact_only) {
     TravArgs E = A;
     E.queue = nullptr;
@@ -148,7 +149,7 @@ void launch_closest(const Node* nodes, uint32_t node_count, const float4* tris, 
   static int blocks = 0;
   if (!blocks) blocks = persistent_blocks((const void*)k_closest_fast_t<ApiPolicy>, 256);
   const int want = (int)((n + 255) / 256);
-  k_closest_fast_t<ApiPolicy><<<want < blocks ? want : blocks, 256, 0, s>>>(A, P);
+  k_closest_fast_t<ApiPolicy><<<want < blocks ? want : blocks, 256, top_smem_bytes(A.top_scenes), s>>>(A, P);
   // Slow path over the rays the fast kernel queued (length read on the device).
   k_closest_exact_t<ApiPolicy><<<grid_for(n < 4096 ? n : 4096, 128), 128, 0, s>>>(A, P);
 }

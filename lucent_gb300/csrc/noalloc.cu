@@ -76,7 +76,7 @@ extern "C" lucent_status lucent_bvh_intersect_noalloc(const float* nodes_d, uint
   cudaError_t e = cudaMemsetAsync(b, 0, 12, s);
   if (e != cudaSuccess) return cuda_fail(e, "clear no-allocation scratch");
   launch_closest((const Node*)nodes_d, node_count, (const float4*)tris_d, rays_d, n, t_min, t_max, prim_d, t_d, u_d,
-                 v_d, queue, qlen, work, err, false, s);
+                 v_d, queue, qlen, work, err, false, true, s);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   unsigned word = 0;

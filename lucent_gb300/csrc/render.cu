@@ -99,6 +99,11 @@ __device__ __forceinline__ bool alpha_opaque(const float4* geo, const float4* ma
   return PathClosest{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, geo, mats, 1}.alpha(0, slot, key);
 }
 
+// Closest-hit rays of a wave. Ray k is path queue[k], read from the path
+// state; after a ray sort the rays come instead from the sorted stream `sray`
+// (contiguous, in sort order, with the path id and scene beside them), so the
+// traversal reads its rays in order while the queue keeps path order for the
+// kernels that touch the rest of the path state.
 struct PathClosestMulti {
   const uint32_t* cnt;
   const uint32_t* queue;
@@ -109,32 +114,44 @@ struct PathClosestMulti {
   const SceneRec* recs;
   const uint16_t* sid;
   int any_alpha;
+  const float4* sray;  // null: no sort this bounce
   static constexpr bool kMultiScene = true;
   __device__ uint32_t count() const { return *cnt; }
+  __device__ uint32_t path(uint32_t k) const { return sray ? __float_as_uint(sray[2 * (size_t)k].w) : queue[k]; }
   __device__ void ray(uint32_t k, float3& o, float3& d) const {
-    const uint32_t p = queue[k];
-    const float4 a = ro[p], b = rd[p];
+    float4 a, b;
+    if (sray) {
+      a = sray[2 * (size_t)k];
+      b = sray[2 * (size_t)k + 1];
+    } else {
+      const uint32_t p = queue[k];
+      a = ro[p];
+      b = rd[p];
+    }
     o = make_float3(a.x, a.y, a.z);
     d = make_float3(b.x, b.y, b.z);
   }
   __device__ BvhView bvh(uint32_t k) const {
-    const int sc = __ldg(sid + queue[k]);
+    const int sc = sray ? __float_as_int(sray[2 * (size_t)k + 1].w) : (int)__ldg(sid + queue[k]);
+    return scene_bvh(sc);
+  }
+  __device__ BvhView scene_bvh(int sc) const {
     const SceneDev& S = recs[sc].scene;
     return {S.nodes, S.geo, S.node_count, sc};
   }
-  __device__ uint32_t key(uint32_t k) const { return rng[queue[k]]; }
+  __device__ uint32_t key(uint32_t k) const { return rng[path(k)]; }
   __device__ bool alpha_any() const { return any_alpha != 0; }
   __device__ bool alpha(int sc, int slot, uint32_t key) const {
     return alpha_opaque(recs[sc].scene.geo, recs[sc].scene.materials, slot, key);
   }
   __device__ bool exact_output() const { return false; }
   __device__ void hit32(uint32_t k, int slot, float3 e) const {
-    hits[queue[k]] = make_float4(e.x, e.y, e.z, __int_as_float(slot));
+    hits[path(k)] = make_float4(e.x, e.y, e.z, __int_as_float(slot));
   }
   __device__ void hit(uint32_t k, int slot, double t, double u, double v) const {
-    hits[queue[k]] = make_float4(__double2float_rn(t), __double2float_rn(u), __double2float_rn(v), __int_as_float(slot));
+    hits[path(k)] = make_float4(__double2float_rn(t), __double2float_rn(u), __double2float_rn(v), __int_as_float(slot));
   }
-  __device__ void miss(uint32_t k) const { hits[queue[k]] = make_float4(INF, 0.f, 0.f, __int_as_float(-1)); }
+  __device__ void miss(uint32_t k) const { hits[path(k)] = make_float4(INF, 0.f, 0.f, __int_as_float(-1)); }
   __device__ void fail(uint32_t k) const { miss(k); }
 };
 
@@ -155,8 +172,8 @@ struct PathShadowMulti {
     o = make_float3(a.x, a.y, a.z);
     d = make_float3(b.x, b.y, b.z);
   }
-  __device__ BvhView bvh(uint32_t k) const {
-    const int sc = __ldg(sid + queue[k] / 3);  // shadow slot 3 * path + j
+  __device__ BvhView bvh(uint32_t k) const { return scene_bvh(__ldg(sid + queue[k] / 3)); }  // slot 3 * path + j
+  __device__ BvhView scene_bvh(int sc) const {
     const SceneDev& S = recs[sc].scene;
     return {S.nodes, S.geo, S.node_count, sc};
   }
@@ -913,7 +930,9 @@ __global__ void __launch_bounds__(1024) k_sort_scan(uint32_t* __restrict__ hist)
   }
 }
 
-__global__ void k_sort_scatter(Paths P, int nxt) {
+// Writes each queued ray (read in queue order, so coalesced) to its sorted
+// position in the ray stream: origin + path id, direction + scene.
+__global__ void k_sort_scatter(Paths P, const uint16_t* __restrict__ sid, int n_scenes, int nxt) {
   const uint32_t n = P.ctr[kCtrQ0 + nxt];
   const uint32_t* q = P.q[nxt];
   const unsigned lane = threadIdx.x & 31;
@@ -924,26 +943,27 @@ __global__ void k_sort_scatter(Paths P, int nxt) {
     uint32_t base = 0;
     if ((int)lane == leader) base = atomicAdd(P.sort_hist + key, (uint32_t)__popc(peers));
     base = __shfl_sync(peers, base, leader);
-    P.sort_tmp[base + __popc(peers & ((1u << lane) - 1u))] = q[k];
+    const uint32_t p = q[k];
+    const size_t at = 2 * (size_t)(base + __popc(peers & ((1u << lane) - 1u)));
+    const float4 o = P.ro[p], d = P.rd[p];
+    const int sc = n_scenes > 1 ? __ldg(sid + p) : 0;
+    P.sray[at] = make_float4(o.x, o.y, o.z, __uint_as_float(p));
+    P.sray[at + 1] = make_float4(d.x, d.y, d.z, __int_as_float(sc));
   }
 }
 
-// Sorts queue `nxt` into sort_tmp, then swaps the two buffers in P (the
-// caller's copy of the path state; every wave starts from the launch's own
-// pointers, so a captured wave replays the same sequence of swaps).
-static void sort_queue(const MultiLaunch& M, Paths& P, int nxt, int blocks, cudaStream_t s) {
+// Sorts the rays of queue `nxt` into the ray stream (the queue itself keeps
+// its order).
+static void sort_rays(const MultiLaunch& M, const Paths& P, int nxt, int blocks, cudaStream_t s) {
   cudaMemsetAsync(P.sort_hist, 0, (size_t)kSortBins * 4, s);
   k_sort_keys<<<blocks, 256, 0, s>>>(P, M.recs, M.sid, M.n, nxt);
   k_sort_scan<<<1, 1024, 0, s>>>(P.sort_hist);
-  k_sort_scatter<<<blocks, 256, 0, s>>>(P, nxt);
-  uint32_t* t = P.q[nxt];
-  P.q[nxt] = P.sort_tmp;
-  P.sort_tmp = t;
+  k_sort_scatter<<<blocks, 256, 0, s>>>(P, M.sid, M.n, nxt);
 }
 
 // ------------------------------------------------------------ one wave
 void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
-  Paths P = M.paths;  // queue buffers may swap with the sort buffer below
+  const Paths& P = M.paths;
   PhaseEvents none{nullptr, nullptr, 0, 0};
   PhaseEvents& E = pe ? *pe : none;
   E.mark(-1, s);
@@ -956,26 +976,31 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
   }
   const int closest_blocks = M.trace_blocks > 0 ? M.trace_blocks : max_closest;
   const int shade_blocks = M.shade_blocks > 0 ? M.shade_blocks : max_shade;
+  const int top = M.top_levels ? (M.n < kTopMaxScenes ? M.n : kTopMaxScenes) : 0;
+  bool sorted = false;  // the rays of this bounce are in the sorted stream
   for (int b = 0; b <= M.max_bounces; b++) {
     const int cur = b & 1;
     k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
     E.mark(kPhResolve, s);
-    PathClosestMulti pc{P.ctr + kCtrQ0 + cur, P.q[cur], P.ro, P.rd, P.rng, P.hit, M.recs, M.sid, M.any_alpha};
+    PathClosestMulti pc{P.ctr + kCtrQ0 + cur, P.q[cur], P.ro, P.rd, P.rng, P.hit,
+                        M.recs, M.sid, M.any_alpha, sorted ? P.sray : nullptr};
     TravArgs A{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
-               M.trav_stats};
-    k_closest_fast_t<PathClosestMulti><<<closest_blocks, 256, 0, s>>>(A, pc);
+               M.trav_stats, top};
+    k_closest_fast_t<PathClosestMulti><<<closest_blocks, 256, top_smem_bytes(top), s>>>(A, pc);
     k_closest_exact_t<PathClosestMulti><<<64, 128, 0, s>>>(A, pc);
     E.mark(kPhClosest, s);
     k_shade_t<SceneTable><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b);
     E.mark(kPhShade, s);
     PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};
-    TravArgs B{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr};
-    k_anyhit_fast_t<PathShadowMulti><<<shade_blocks * 2, 256, 0, s>>>(B, ps);
+    TravArgs B{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr,
+               nullptr, top};
+    k_anyhit_fast_t<PathShadowMulti><<<shade_blocks * 2, 256, top_smem_bytes(top), s>>>(B, ps);
     k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, s>>>(B, ps);
     E.mark(kPhShadow, s);
     k_resolve<<<shade_blocks, 128, 0, s>>>(P, cur);
     k_count_rays<<<1, 32, 0, s>>>(P.ctr, cur);
-    if (M.sort_rays && b < 2 && b < M.max_bounces) sort_queue(M, P, cur ^ 1, shade_blocks, s);  // the two largest queues
+    sorted = M.sort_rays && b < 2 && b < M.max_bounces;  // the two largest queues
+    if (sorted) sort_rays(M, P, cur ^ 1, shade_blocks, s);
   }
   E.mark(kPhResolve, s);
   k_accumulate_multi<<<grid_for(M.total_pixels, 256), 256, 0, s>>>(P, M.recs, M.pix_base, M.path_base, M.n, M.S);
@@ -996,20 +1021,23 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
     closest_blocks = persistent_blocks((const void*)k_closest_fast_t<PathClosestMulti>, 256);
     shade_blocks = persistent_blocks((const void*)k_shade_t<SceneTable, true>, 128);
   }
+  const int top = M.top_levels ? (M.n < kTopMaxScenes ? M.n : kTopMaxScenes) : 0;
   for (int pass = 0; pass < 2; pass++) {
     const AdjointDev A{H.dl, H.lrem, H.gcont, H.gslot, H.genv, H.dmat, H.denv, M.total_pixels, pass == 0 ? 1 : 0};
     k_camera_multi<<<grid_for(M.total_paths, 256), 256, 0, s>>>(P, M.recs, M.path_base, M.n, M.sid, M.S);
     for (int b = 0; b <= M.max_bounces; b++) {
       const int cur = b & 1;
       k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
-      PathClosestMulti pc{P.ctr + kCtrQ0 + cur, P.q[cur], P.ro, P.rd, P.rng, P.hit, M.recs, M.sid, M.any_alpha};
-      TravArgs TA{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr};
-      k_closest_fast_t<PathClosestMulti><<<closest_blocks, 256, 0, s>>>(TA, pc);
+      PathClosestMulti pc{P.ctr + kCtrQ0 + cur, P.q[cur], P.ro, P.rd, P.rng, P.hit, M.recs, M.sid, M.any_alpha, nullptr};
+      TravArgs TA{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
+                  nullptr, top};
+      k_closest_fast_t<PathClosestMulti><<<closest_blocks, 256, top_smem_bytes(top), s>>>(TA, pc);
       k_closest_exact_t<PathClosestMulti><<<64, 128, 0, s>>>(TA, pc);
       k_shade_t<SceneTable, true><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b, A);
       PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};
-      TravArgs TB{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr};
-      k_anyhit_fast_t<PathShadowMulti><<<shade_blocks * 2, 256, 0, s>>>(TB, ps);
+      TravArgs TB{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr,
+                  nullptr, top};
+      k_anyhit_fast_t<PathShadowMulti><<<shade_blocks * 2, 256, top_smem_bytes(top), s>>>(TB, ps);
       k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, s>>>(TB, ps);
       if (pass == 0)
         k_resolve<<<shade_blocks, 128, 0, s>>>(P, cur);

@@ -209,7 +209,8 @@ struct lucent_renderer {
   // a renderer traces as a launch of one scene: its SceneRec, path/pixel bases (full and last wave), scene index per path
   DeviceBuffer rec1, base1, sid1;
   uint32_t sid_cap = 0;
-  int sort_rays = 1;  // reorder each bounce's rays (lucent_renderer_set_ray_sort)
+  int sort_rays = 1;   // sort the rays of bounces 1 and 2 (lucent_renderer_set_ray_sort)
+  int top_levels = 1;  // top BVH levels in shared memory (lucent_renderer_set_top_levels)
   // temporal reprojection (renderer.ts:441-451, 717-731): the view the accumulation was traced with
   int temporal = 1;
   bool has_history = false, reproject_pending = false;
@@ -245,7 +246,7 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
                                         uint32_t cap) {
   if (cap <= path_cap) return LUCENT_OK;
   // Per-path arrays in allocation order (bytes per path); each starts on a 256-byte boundary.
-  static const size_t kPer[] = {16, 16, 16, 16, 16, 16, 16, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12, 4, 4};
+  static const size_t kPer[] = {16, 16, 16, 16, 16, 16, 16, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12, 4, 32};
   size_t total = 0;
   for (size_t b : kPer) total += ((size_t)cap * b + 255) & ~(size_t)255;
   total += (size_t)kSortBins * 4;
@@ -279,7 +280,7 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
   P.slow = (uint32_t*)take((size_t)cap * 4);
   P.slow2 = (uint32_t*)take((size_t)cap * 12);
   P.sort_keys = (uint32_t*)take((size_t)cap * 4);
-  P.sort_tmp = (uint32_t*)take((size_t)cap * 4);
+  P.sray = (float4*)take((size_t)cap * 32);
   P.sort_hist = (uint32_t*)take((size_t)kSortBins * 4);
   if (off > paths.cap) return fail(LUCENT_ERR_DEVICE, "path buffer layout overflow");
   P.ctr = (uint32_t*)ctr.ptr;
@@ -383,6 +384,7 @@ static lucent_status single_launch(lucent_renderer* r, uint32_t S, uint32_t tail
   M.total_pixels = WH;
   M.any_alpha = r->any_alpha;
   M.sort_rays = r->sort_rays;
+  M.top_levels = r->top_levels;
   return LUCENT_OK;
 }
 
@@ -756,6 +758,13 @@ lucent_status lucent_renderer_set_ray_sort(lucent_renderer* r, int32_t enabled) 
   return LUCENT_OK;
 }
 
+lucent_status lucent_renderer_set_top_levels(lucent_renderer* r, int32_t enabled) {
+  clear_error();
+  if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  r->top_levels = enabled ? 1 : 0;
+  return LUCENT_OK;
+}
+
 lucent_status lucent_renderer_trim(lucent_renderer* r) {
   clear_error();
   if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
@@ -912,7 +921,7 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
 
 struct lucent_batch {
   std::vector<lucent_renderer*> rs;
-  lucent_batch_options opt{0, 1u << 25, 1, 0, 0, 1};
+  lucent_batch_options opt{0, 1u << 25, 1, 0, 0, 1, 1};
   DeviceBuffer recs, bases, tail_bases, sid, paths, ctr;
   uint32_t path_cap = 0, sid_cap = 0;
   Paths P{};
@@ -1032,6 +1041,7 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
   M.trace_blocks = (int)b->opt.trace_blocks;
   M.shade_blocks = (int)b->opt.shade_blocks;
   M.sort_rays = b->opt.sort_rays;
+  M.top_levels = b->opt.top_levels;
   auto setup = [&](uint32_t s_wave, const DeviceBuffer& base) {
     M.S = (int)s_wave;
     M.total_paths = (uint32_t)(pixels * s_wave);

@@ -45,7 +45,7 @@ struct Paths {
   uint32_t* slow;
   uint32_t* slow2;
   uint32_t* sort_keys;  // per queued path: ray-sort key (scene, direction octant, origin cell)
-  uint32_t* sort_tmp;   // sorted queue before it is copied back
+  float4* sray;         // sorted ray stream: 2 float4 per queued ray (origin + path id, direction + scene)
   uint32_t* sort_hist;  // kSortBins counters
   uint32_t* ctr;
 };
@@ -90,7 +90,8 @@ struct MultiLaunch {
   int any_alpha;
   int trace_blocks, shade_blocks;  // 0 = all resident blocks
   unsigned long long* trav_stats;  // closest-hit traversal counters (profiling) or nullptr
-  int sort_rays;                   // reorder each bounce's queue by scene, direction octant and origin cell
+  int sort_rays;                   // after bounces 0 and 1, sort the rays by scene, direction octant and origin cell
+  int top_levels;                  // stage the top BVH levels of (up to 8) scenes in shared memory
 };
 
 // Optional per-phase timing: events recorded between launches, each tagged

@@ -18,7 +18,8 @@
 //   uint32_t key(uint32_t k) const                alpha any-hit key (RNG state)
 //   bool alpha(int scene, int slot, uint32_t key) true if a hit on `slot` counts
 //   static constexpr bool kMultiScene             rays of several scenes in one launch:
-//   BvhView bvh(uint32_t k) const                 then the k-th ray's BVH (else TravArgs')
+//   BvhView bvh(uint32_t k) const                 then the k-th ray's BVH (else TravArgs'),
+//   BvhView scene_bvh(int s) const                and scene s's BVH
 //   bool alpha_any() const                        false: no alpha-tested triangles
 //   void hit(uint32_t k, int slot, double t, double u, double v)   (closest)
 //   void miss(uint32_t k); void fail(uint32_t k)
@@ -69,7 +70,11 @@ struct TravArgs {
   // Optional counters (nullptr = off): rays, binary64 slab decisions,
   // binary64 triangle decisions, binary64 closest values, binary64 final hits.
   unsigned long long* stats = nullptr;
+  // Scenes (0, 1, ... top_scenes - 1) whose top BVH levels each block stages
+  // in shared memory (0 = off); the launch passes top_smem_bytes(top_scenes).
+  int top_scenes = 0;
 };
+
 
 __device__ __forceinline__ void count_stat(const TravArgs& A, int k) {
   if (A.stats) atomicAdd(A.stats + k, 1ull);
@@ -89,6 +94,52 @@ __device__ __forceinline__ BvhView bvh_of(const TravArgs& A, const Pol& P, uint3
     return P.bvh(k);
   else
     return {A.nodes, A.tris, A.node_limit, 0};
+}
+
+// Top BVH levels in shared memory. The top kTopDepth + 1 levels of a tree
+// (63 nodes, 2016 bytes) are copied at block start in breadth-first order,
+// 1-based: treelet node b has children 2b and 2b + 1, stored side by side.
+// Nodes are numbered depth-first in memory, so the treelet is a second copy,
+// reached by carrying each node's treelet index beside it (a stack entry
+// holds -b for treelet node b). Only where the nodes are read changes: the
+// decisions and their order do not.
+constexpr int kTopDepth = 5, kTopNodes = (1 << (kTopDepth + 1)) - 1, kTopMaxScenes = 8;
+inline size_t top_smem_bytes(int scenes) { return (size_t)scenes * kTopNodes * sizeof(Node); }
+
+// Treelet node b (1-based) of a tree: the path from the root follows the bits
+// of b below its leading one (0 = left child). Nodes under a leaf, or past
+// the node array, are absent: an inverted box, never read by a traversal of
+// a valid tree.
+__device__ __forceinline__ Node top_node(const Node* nodes, uint32_t limit, int b) {
+  const float inf = __int_as_float(0x7f800000);
+  const Node absent{make_float4(inf, inf, inf, 0.f), make_float4(-inf, -inf, -inf, 0.f)};
+  if (limit == 0) return absent;
+  int n = 0;
+  for (int d = 30 - __clz(b); d >= 0; d--) {
+    const Node nd = load_node(nodes, n);
+    const int f = node_first(nd);
+    if (node_count(nd) > 0 || f < 0 || (uint32_t)f + 1 >= limit) return absent;
+    n = f + ((b >> d) & 1);
+  }
+  return load_node(nodes, n);
+}
+
+template <class Pol>
+__device__ __forceinline__ BvhView scene_bvh_of(const TravArgs& A, const Pol& P, int s) {
+  if constexpr (Pol::kMultiScene)
+    return P.scene_bvh(s);
+  else
+    return {A.nodes, A.tris, A.node_limit, 0};
+}
+
+// Fills the block's treelets (all threads of the block must call it).
+template <class Pol>
+__device__ __forceinline__ void stage_top(const TravArgs& A, const Pol& P, Node* s_top) {
+  for (int i = threadIdx.x; i < A.top_scenes * kTopNodes; i += blockDim.x) {
+    const BvhView v = scene_bvh_of(A, P, i / kTopNodes);
+    s_top[i] = top_node(v.nodes, v.node_limit, i % kTopNodes + 1);
+  }
+  __syncthreads();
 }
 
 struct PendingNode {
@@ -189,6 +240,11 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
   BvhView bv{A.nodes, A.tris, A.node_limit, 0};  // multi-scene policies set it per ray below
   Node cur;
   PendingNode stack[kTsStack];
+  extern __shared__ float4 s_top4[];
+  Node* const s_top = reinterpret_cast<Node*>(s_top4);
+  stage_top(A, P, s_top);
+  const Node* sb = nullptr;  // this ray's treelet (null: its scene has none staged)
+  int ctb = 0;               // treelet index of `cur` (0: not in the treelet)
 
   while (true) {
     const bool need = !active && !exhausted;
@@ -220,7 +276,9 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
             sp = 0;
             iters = 0;
             count_stat(A, 0);
-            cur = load_node(bv.nodes, 0);  // the reference pops the root first and tests its box
+            sb = bv.scene < A.top_scenes ? s_top + bv.scene * kTopNodes : nullptr;
+            ctb = sb ? 1 : 0;
+            cur = sb ? sb[0] : load_node(bv.nodes, 0);  // the reference pops the root first and tests its box
             SlabClass cl = classify_slab(r, cur.lo, cur.hi, c_lo, c_hi);
             if (cl == kAmbiguous) {
               count_stat(A, 1);
@@ -276,9 +334,10 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
         continue;
       }
       const PendingNode e = stack[--sp];
-      const Node nd = load_node(bv.nodes, e.node);
+      const Node nd = e.node < 0 ? sb[-e.node - 1] : load_node(bv.nodes, e.node);
       if (e.ehi > c_lo && slab_decide(nd, classify_slab(r, nd.lo, nd.hi, c_lo, c_hi)) == kCulled) continue;
       cur = nd;
+      ctb = e.node < 0 ? -e.node : 0;
       have_cur = true;
     }
     if (++iters > bv.node_limit) {  // a valid BVH visits each node at most once per ray
@@ -324,7 +383,11 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
       }
       have_cur = false;
     } else {
-      const Node L = load_node(bv.nodes, first), R = load_node(bv.nodes, first + 1);  // one 64-byte pair
+      // One 64-byte pair, from the treelet while its children are in it.
+      const bool in_top = ctb > 0 && 2 * ctb + 1 <= kTopNodes;
+      const Node L = in_top ? sb[2 * ctb - 1] : load_node(bv.nodes, first);
+      const Node R = in_top ? sb[2 * ctb] : load_node(bv.nodes, first + 1);
+      const int ltb = in_top ? 2 * ctb : 0;
       float ehl, ehr;
       const SlabClass cl = slab_decide(L, classify_slab_e(r, L.lo, L.hi, c_lo, c_hi, ehl));
       const SlabClass cr = slab_decide(R, classify_slab_e(r, R.lo, R.hi, c_lo, c_hi, ehr));
@@ -337,11 +400,13 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
             have_cur = false;
             continue;
           }
-          stack[sp++] = {first + 1, ehr};
+          stack[sp++] = {ltb ? -(ltb + 1) : first + 1, ehr};
         }
         cur = L;
+        ctb = ltb;
       } else if (cr == kPass) {
         cur = R;
+        ctb = ltb ? ltb + 1 : 0;
       } else {
         have_cur = false;
       }
@@ -411,6 +476,9 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
   const float tmin_lo = __double2float_rd(A.tMin), tmin_hi = __double2float_ru(A.tMin);
   const uint32_t n = P.count();
   const bool use_alpha = P.alpha_any();
+  extern __shared__ float4 s_top4[];
+  Node* const s_top = reinterpret_cast<Node*>(s_top4);
+  stage_top(A, P, s_top);
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     float3 o, d;
     P.ray(k, o, d);
@@ -423,9 +491,10 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
     const double tmax = P.tmax(k);
     const BvhView bv = bvh_of(A, P, k);
     const float c_lo = __double2float_rd(tmax), c_hi = __double2float_ru(tmax);
-    int stack[kTsStack];
+    const Node* sb = bv.scene < A.top_scenes ? s_top + bv.scene * kTopNodes : nullptr;
+    int stack[kTsStack];  // node index, or -b for treelet node b
     int sp = 0;
-    stack[sp++] = 0;
+    stack[sp++] = sb ? -1 : 0;
     bool occ = false, ok = true;
     uint32_t iters = 0;
     while (sp > 0 && !occ) {
@@ -434,7 +503,8 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
         ok = false;
         break;
       }
-      const Node nd = load_node(bv.nodes, stack[--sp]);
+      const int e = stack[--sp];
+      const Node nd = e < 0 ? sb[-e - 1] : load_node(bv.nodes, e);
       SlabClass cl = classify_slab(r, nd.lo, nd.hi, c_lo, c_hi);
       if (cl == kAmbiguous) cl = ts_slab_culled(nd.lo, nd.hi, {o.x, o.y, o.z}, inv_exact(d), tmax) ? kCulled : kPass;
       if (cl == kCulled) continue;
@@ -462,8 +532,9 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
           ok = false;
           break;
         }
-        stack[sp++] = first + 1;
-        stack[sp++] = first;
+        const bool in_top = e < 0 && 2 * (-e) + 1 <= kTopNodes;
+        stack[sp++] = in_top ? 2 * e - 1 : first + 1;  // -(2b + 1)
+        stack[sp++] = in_top ? 2 * e : first;          // -(2b)
       }
     }
     P.shadow(k, ok ? occ : true);

@@ -179,8 +179,12 @@ class Renderer:
         return out
 
     def set_ray_sort(self, enabled=True):
-        """Reorder each bounce's rays by direction and origin (lucent_renderer_set_ray_sort)."""
+        """Sort the rays of bounces 1 and 2 by direction and origin (lucent_renderer_set_ray_sort)."""
         N.check(N.lib().lucent_renderer_set_ray_sort(self._h, 1 if enabled else 0))
+
+    def set_top_levels(self, enabled=True):
+        """Stage the top BVH levels in shared memory (lucent_renderer_set_top_levels)."""
+        N.check(N.lib().lucent_renderer_set_top_levels(self._h, 1 if enabled else 0))
 
     def trim(self):
         """Frees the path-state buffers until the next trace (lucent_renderer_trim)."""
@@ -272,10 +276,11 @@ class Batch:
     each renderer alone would give. Options (lucent_batch_options):
     samples_per_wave (0 = as many as max_wave_paths allows), max_wave_paths,
     use_graph (replay a captured wave), trace_blocks / shade_blocks (grid
-    sizes, 0 = all resident blocks)."""
+    sizes, 0 = all resident blocks), sort_rays, top_levels (as the
+    renderer's set_ray_sort / set_top_levels)."""
 
     DEFAULTS = {"samples_per_wave": 0, "max_wave_paths": 1 << 25, "use_graph": True, "trace_blocks": 0,
-                "shade_blocks": 0, "sort_rays": True}
+                "shade_blocks": 0, "sort_rays": True, "top_levels": True}
 
     def __init__(self, renderers, **options):
         self.renderers = list(renderers)
@@ -293,7 +298,8 @@ class Batch:
         self.options.update(options)
         o = self.options
         d = NR.BatchOptions(o["samples_per_wave"], o["max_wave_paths"], 1 if o["use_graph"] else 0,
-                            o["trace_blocks"], o["shade_blocks"], 1 if o["sort_rays"] else 0)
+                            o["trace_blocks"], o["shade_blocks"], 1 if o["sort_rays"] else 0,
+                            1 if o["top_levels"] else 0)
         N.check(N.lib().lucent_batch_set_options(self._h, C.byref(d)))
 
     def trace_samples(self, count, stream=None):

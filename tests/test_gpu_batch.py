@@ -58,7 +58,8 @@ def solo(specs):
 
 
 @pytest.mark.parametrize("opts", [{}, {"samples_per_wave": 2}, {"samples_per_wave": 1, "use_graph": False},
-                                  {"max_wave_paths": 5000}, {"samples_per_wave": 3}])
+                                  {"max_wave_paths": 5000}, {"samples_per_wave": 3},
+                                  {"sort_rays": False, "top_levels": False}])
 def test_batch_equals_renderers_alone(specs, solo, opts):
     rs = _renderers(specs)
     b = Batch(rs, **opts)
@@ -73,6 +74,27 @@ def test_batch_equals_renderers_alone(specs, solo, opts):
         assert not np.isnan(got[0]).any()
         assert np.all(got[3] == 5)
         assert _same(got, ref)
+    b.dispose()
+    for r in rs:
+        r.dispose()
+
+
+def test_batch_beyond_the_staged_top_levels(specs):
+    # Shared memory holds the top BVH levels of the first 8 scenes; the rays
+    # of later scenes read every node from global memory.
+    specs10 = (specs * 2)[:10]
+    rs = _renderers(specs10)
+    for r in rs:
+        r.trace_samples(2)
+    ref = [r.read() for r in rs]
+    for r in rs:
+        r.dispose()
+    rs = _renderers(specs10)
+    b = Batch(rs)
+    b.trace_samples(2)
+    b.check()
+    for r, want in zip(rs, ref):
+        assert _same(r.read(), want)
     b.dispose()
     for r in rs:
         r.dispose()

@@ -94,16 +94,18 @@ def test_full_size_box_scene_crop():
     assert rmse < 0.05, rmse
 
 
-def test_ray_sort_changes_no_pixel():
-    # Reordering the rays between bounces changes the order paths are
-    # processed in, never a path: the images are identical bit for bit.
+@pytest.mark.parametrize("option", ["ray_sort", "top_levels"])
+def test_traversal_options_change_no_pixel(option):
+    # Sorting the rays changes the order paths are traced in, never a path;
+    # the shared-memory copy of the top BVH levels changes where nodes are
+    # read from, never a decision: the images are identical bit for bit.
     sc = W.box_scene(2, 3)
     out = []
-    for sort in (True, False):
+    for on in (True, False):
         r = Renderer(64, 48)
         r.settings.max_bounces = 8
         r.load_scene(sc)
-        r.set_ray_sort(sort)
+        getattr(r, "set_" + option)(on)
         r.set_seed(11)
         r.trace_samples(6)
         out.append(r.read())
