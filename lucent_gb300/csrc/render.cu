@@ -907,27 +907,43 @@ __global__ void k_sort_keys(Paths P, const SceneRec* __restrict__ recs, const ui
   }
 }
 
-__global__ void __launch_bounds__(1024) k_sort_scan(uint32_t* __restrict__ hist) {  // exclusive scan, one block
-  constexpr int kPer = kSortBins / 1024;
-  __shared__ uint32_t part[1024];
-  uint32_t v[kPer], sum = 0;
-  for (int i = 0; i < kPer; i++) {
-    v[i] = hist[threadIdx.x * kPer + i];
-    sum += v[i];
+// Exclusive scan of the kSortBins counters, one block of 32 warps: warp w
+// owns bins [w * 1024, (w + 1) * 1024), read 32 at a time (coalesced) and
+// scanned with shuffles; then the warp totals are scanned.
+__global__ void __launch_bounds__(1024) k_sort_scan(uint32_t* __restrict__ hist) {
+  constexpr int kPerWarp = kSortBins / 32, kSteps = kPerWarp / 32;
+  __shared__ uint32_t warp_total[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t* seg = hist + w * kPerWarp;
+  uint32_t v[kSteps], carry = 0;
+#pragma unroll
+  for (int j = 0; j < kSteps; j++) {
+    const uint32_t x = seg[j * 32 + lane];
+    uint32_t incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    v[j] = carry + incl - x;
+    carry += __shfl_sync(0xffffffffu, incl, 31);
   }
-  part[threadIdx.x] = sum;
+  if (lane == 0) warp_total[w] = carry;
   __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {
-    const uint32_t t = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0u;
-    __syncthreads();
-    part[threadIdx.x] += t;
-    __syncthreads();
+  if (w == 0) {
+    const uint32_t x = warp_total[lane];
+    uint32_t incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    warp_total[lane] = incl - x;
   }
-  uint32_t run = part[threadIdx.x] - sum;
-  for (int i = 0; i < kPer; i++) {
-    hist[threadIdx.x * kPer + i] = run;
-    run += v[i];
-  }
+  __syncthreads();
+  const uint32_t base = warp_total[w];
+#pragma unroll
+  for (int j = 0; j < kSteps; j++) seg[j * 32 + lane] = base + v[j];
 }
 
 // Writes each queued ray (read in queue order, so coalesced) to its sorted
@@ -944,26 +960,32 @@ __global__ void k_sort_scatter(Paths P, const uint16_t* __restrict__ sid, int n_
     if ((int)lane == leader) base = atomicAdd(P.sort_hist + key, (uint32_t)__popc(peers));
     base = __shfl_sync(peers, base, leader);
     const uint32_t p = q[k];
-    const size_t at = 2 * (size_t)(base + __popc(peers & ((1u << lane) - 1u)));
+    const uint32_t pos = base + __popc(peers & ((1u << lane) - 1u));
     const float4 o = P.ro[p], d = P.rd[p];
     const int sc = n_scenes > 1 ? __ldg(sid + p) : 0;
-    P.sray[at] = make_float4(o.x, o.y, o.z, __uint_as_float(p));
-    P.sray[at + 1] = make_float4(d.x, d.y, d.z, __int_as_float(sc));
+    P.sray[2 * (size_t)pos] = make_float4(o.x, o.y, o.z, __uint_as_float(p));
+    P.sray[2 * (size_t)pos + 1] = make_float4(d.x, d.y, d.z, __int_as_float(sc));
+    P.sort_tmp[pos] = p;
   }
 }
 
-// Sorts the rays of queue `nxt` into the ray stream (the queue itself keeps
-// its order).
-static void sort_rays(const MultiLaunch& M, const Paths& P, int nxt, int blocks, cudaStream_t s) {
+// Sorts the rays of queue `nxt` into the ray stream and the queue into
+// sort_tmp, then swaps the two queue buffers in P (the caller's copy of the
+// path state; every wave starts from the launch's own pointers, so a
+// captured wave replays the same sequence of swaps).
+static void sort_rays(const MultiLaunch& M, Paths& P, int nxt, int blocks, cudaStream_t s) {
   cudaMemsetAsync(P.sort_hist, 0, (size_t)kSortBins * 4, s);
   k_sort_keys<<<blocks, 256, 0, s>>>(P, M.recs, M.sid, M.n, nxt);
   k_sort_scan<<<1, 1024, 0, s>>>(P.sort_hist);
   k_sort_scatter<<<blocks, 256, 0, s>>>(P, M.sid, M.n, nxt);
+  uint32_t* t = P.q[nxt];
+  P.q[nxt] = P.sort_tmp;
+  P.sort_tmp = t;
 }
 
 // ------------------------------------------------------------ one wave
 void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
-  const Paths& P = M.paths;
+  Paths P = M.paths;  // queue buffers swap with the sort buffer below
   PhaseEvents none{nullptr, nullptr, 0, 0};
   PhaseEvents& E = pe ? *pe : none;
   E.mark(-1, s);
@@ -997,7 +1019,11 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     k_anyhit_fast_t<PathShadowMulti><<<shade_blocks * 2, 256, top_smem_bytes(top), s>>>(B, ps);
     k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, s>>>(B, ps);
     E.mark(kPhShadow, s);
-    k_resolve<<<shade_blocks, 128, 0, s>>>(P, cur);
+    // Resolve is per path: it walks the queue as it was before the sort (still
+    // intact in sort_tmp), in path order, so its reads stay coalesced.
+    Paths Pr = P;
+    if (sorted) Pr.q[cur] = P.sort_tmp;
+    k_resolve<<<shade_blocks, 128, 0, s>>>(Pr, cur);
     k_count_rays<<<1, 32, 0, s>>>(P.ctr, cur);
     sorted = M.sort_rays && b < 2 && b < M.max_bounces;  // the two largest queues
     if (sorted) sort_rays(M, P, cur ^ 1, shade_blocks, s);

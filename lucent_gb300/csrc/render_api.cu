@@ -246,7 +246,7 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
                                         uint32_t cap) {
   if (cap <= path_cap) return LUCENT_OK;
   // Per-path arrays in allocation order (bytes per path); each starts on a 256-byte boundary.
-  static const size_t kPer[] = {16, 16, 16, 16, 16, 16, 16, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12, 4, 32};
+  static const size_t kPer[] = {16, 16, 16, 16, 16, 16, 16, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12, 4, 32, 4};
   size_t total = 0;
   for (size_t b : kPer) total += ((size_t)cap * b + 255) & ~(size_t)255;
   total += (size_t)kSortBins * 4;
@@ -281,6 +281,7 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
   P.slow2 = (uint32_t*)take((size_t)cap * 12);
   P.sort_keys = (uint32_t*)take((size_t)cap * 4);
   P.sray = (float4*)take((size_t)cap * 32);
+  P.sort_tmp = (uint32_t*)take((size_t)cap * 4);
   P.sort_hist = (uint32_t*)take((size_t)kSortBins * 4);
   if (off > paths.cap) return fail(LUCENT_ERR_DEVICE, "path buffer layout overflow");
   P.ctr = (uint32_t*)ctr.ptr;
