@@ -364,6 +364,15 @@ lucent_status lucent_bsdf_eval_tuples(const float* tuples, uint32_t n, float* ou
  * then df/d(base colour r, g, b, roughness, metallic, clearcoat) (6 x 3). */
 lucent_status lucent_bsdf_grad_tuples(const float* tuples, uint32_t n, float* out);
 
+/* ---------------------------------------------------------------------------
+ * Model ingestion helper. The reference leaves image decoding to the browser
+ * (createImageBitmap, src/loaders/model.ts:43-72); this build decodes PNG
+ * itself: the caller parses the chunks and inflates the data, this reverses
+ * the per-scanline filters (PNG specification 9.2). `in` holds `rows` rows of
+ * a filter-type byte plus `row_bytes` bytes; `bpp` is the bytes per complete
+ * pixel (at least 1). Writes rows * row_bytes bytes; synchronous, host only. */
+lucent_status lucent_png_unfilter(const uint8_t* in, uint32_t rows, uint32_t row_bytes, uint32_t bpp, uint8_t* out);
+
 #ifdef __cplusplus
 }
 #endif

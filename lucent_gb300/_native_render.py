@@ -65,6 +65,7 @@ def declare(L, sig):
     sig(L, "lucent_renderer_read_denoised", [VP, F32P])
     sig(L, "lucent_bsdf_eval_tuples", [F32P, C.c_uint32, F32P])
     sig(L, "lucent_bsdf_grad_tuples", [F32P, C.c_uint32, F32P])
+    sig(L, "lucent_png_unfilter", [U8P, C.c_uint32, C.c_uint32, C.c_uint32, U8P])
 
 
 class BatchOptions(C.Structure):

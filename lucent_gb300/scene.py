@@ -164,8 +164,17 @@ class MeshInstance:
 
 
 @dataclass
+class Texture:
+    """SceneTexture (scene.ts:58-62): a decoded image, 8-bit RGBA [h, w, 4],
+    row 0 = top (v = 0), unpremultiplied; resampled on upload to the shared
+    texture-array size."""
+    image: np.ndarray
+    name: str = "texture"
+
+
+@dataclass
 class Scene:
-    """scene.ts:64-77 (textures are not supported by this build)."""
+    """scene.ts:64-77."""
     name: str = "scene"
     camera: Camera = field(default_factory=Camera)
     sun: Sun = field(default_factory=Sun)
@@ -175,6 +184,7 @@ class Scene:
     spheres: List[Sphere] = field(default_factory=list)
     meshes: List[MeshInstance] = field(default_factory=list)
     exposure: float = 1.0
+    textures: List[Texture] = field(default_factory=list)
 
 
 def quad_from_mesh(m):
@@ -208,10 +218,28 @@ class PackedScene:
     lights: np.ndarray
     light_count: int
     ground_material: int
+    # scene texture index in each layer of the sRGB (colour) and linear (data) arrays (scene.ts:124-126)
+    color_layers: List[int] = field(default_factory=list)
+    data_layers: List[int] = field(default_factory=list)
 
     @property
     def tri_count(self):
         return self.positions.size // 9
+
+
+def _layer_map():
+    """layerMap (scene.ts:136-154): one layer per referenced texture, in first-use order."""
+    layers, index = [], {}
+
+    def layer(tex):
+        if tex < 0:
+            return -1
+        if tex not in index:
+            index[tex] = len(layers)
+            layers.append(tex)
+        return index[tex]
+
+    return layers, layer
 
 
 def pack_scene(scene: Scene) -> PackedScene:
@@ -262,16 +290,22 @@ def pack_scene(scene: Scene) -> PackedScene:
         if is_emissive(s.material):
             sph_light[i] = add_light(("sphere", s.center, s.radius, (0, 0, 0), (0, 0, 0), s.material.emission))
     ground_material = mindex(scene.ground.material)  # always packed (scene.ts:259-260)
-    for m in mats:
-        if max(m.base_color_map, m.metal_rough_map, m.normal_map, m.emissive_map) >= 0:
-            raise ValueError("texture maps are not supported by this build")
+    # sRGB maps (base colour, emissive) and linear maps (metal-rough, normal) get separate arrays (scene.ts:271-283)
+    color_layers, color = _layer_map()
+    data_layers, data = _layer_map()
+    layered = [replace(m, base_color_map=color(m.base_color_map), emissive_map=color(m.emissive_map),
+                       metal_rough_map=data(m.metal_rough_map), normal_map=data(m.normal_map)) for m in mats]
+    for t in color_layers + data_layers:
+        if t >= len(scene.textures):
+            raise ValueError("material references texture %d, scene has %d" % (t, len(scene.textures)))
     lt = np.zeros((MAX_LIGHTS, 16), np.float32)
     for i, (kind, pos, radius, e1, e2, rad) in enumerate(lights):  # scene.ts:262-269
         lt[i] = [*pos, 0.0 if kind == "sphere" else 1.0, *e1, radius, *e2, 0.0, *rad, 0.0]
     return PackedScene(merged.positions, merged.normals, merged.uvs, tri_mat, tri_light, tri_alpha,
-                       pack_materials(mats), len(mats), spheres.reshape(-1)[: 4 * len(scene.spheres)].copy(),
+                       pack_materials(layered), len(mats), spheres.reshape(-1)[: 4 * len(scene.spheres)].copy(),
                        sph_mat[: len(scene.spheres)].copy(), sph_light[: len(scene.spheres)].copy(),
-                       lt.reshape(-1)[: 16 * len(lights)].copy(), len(lights), ground_material)
+                       lt.reshape(-1)[: 16 * len(lights)].copy(), len(lights), ground_material,
+                       color_layers, data_layers)
 
 
 def from_spherical(elevation, azimuth):
