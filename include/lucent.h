@@ -170,6 +170,21 @@ typedef struct lucent_scene_desc {
   const float* lights;
   uint32_t light_count;
   int32_t ground_material;
+  /* Texture maps (SceneTexture, scene.ts:58-62; buildTextureArrays,
+   * renderer.ts:314-333). texture_count decoded images of 8-bit RGBA, rows
+   * top to bottom (texture_rgba8[i] holds texture_width[i] *
+   * texture_height[i] * 4 bytes). color_layers / data_layers: the scene
+   * texture index of each layer of the sRGB (base colour, emissive) and
+   * linear (metal-rough, normal) arrays; the material map fields (texel 4)
+   * hold layer indices (packScene, scene.ts:271-283). All may be 0 / NULL. */
+  uint32_t texture_count;
+  const uint8_t* const* texture_rgba8;
+  const uint32_t* texture_width;
+  const uint32_t* texture_height;
+  const int32_t* color_layers;
+  uint32_t color_layer_count;
+  const int32_t* data_layers;
+  uint32_t data_layer_count;
 } lucent_scene_desc;
 
 /* uploadLighting (renderer.ts:355-413): the analytic sun and an equirect
@@ -256,6 +271,11 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
  * the reference's GPU timer queries, renderer.ts:668-700); results appear in
  * lucent_render_stats.phase_ms after lucent_renderer_check. */
 lucent_status lucent_renderer_set_profiling(lucent_renderer* r, int32_t enabled);
+/* The texture arrays the scene's maps are sampled from (buildTextureArrays,
+ * renderer.ts:314-333): *size = the layer size (0: no textures); color_out
+ * and data_out (either may be NULL) receive color/data layer count x size x
+ * size x 4 bytes (sRGB codes / linear codes), layers in packScene's order. */
+lucent_status lucent_renderer_read_textures(lucent_renderer* r, uint32_t* size, uint8_t* color_out, uint8_t* data_out);
 /* After bounces 0 and 1, sort the surviving rays by direction octant and
  * origin cell (counting sort into a ray stream the closest-hit traversal
  * reads in order; default on). Paths are independent: images are the same

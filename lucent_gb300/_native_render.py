@@ -11,7 +11,9 @@ class SceneDesc(C.Structure):
                 ("bvh_node_count", C.c_uint32), ("bvh_tri_indices", U32P), ("materials", F32P),
                 ("material_count", C.c_uint32), ("spheres", F32P), ("sphere_materials", I32P),
                 ("sphere_lights", I32P), ("sphere_count", C.c_uint32), ("lights", F32P), ("light_count", C.c_uint32),
-                ("ground_material", C.c_int32)]
+                ("ground_material", C.c_int32), ("texture_count", C.c_uint32), ("texture_rgba8", P(U8P)),
+                ("texture_width", U32P), ("texture_height", U32P), ("color_layers", I32P),
+                ("color_layer_count", C.c_uint32), ("data_layers", I32P), ("data_layer_count", C.c_uint32)]
 
 
 class LightingDesc(C.Structure):
@@ -58,6 +60,7 @@ def declare(L, sig):
     sig(L, "lucent_renderer_trim", [VP])
     sig(L, "lucent_renderer_set_ray_sort", [VP, C.c_int32])
     sig(L, "lucent_renderer_set_top_levels", [VP, C.c_int32])
+    sig(L, "lucent_renderer_read_textures", [VP, U32P, U8P, U8P])
     sig(L, "lucent_renderer_set_materials", [VP, F32P, C.c_uint32])
     sig(L, "lucent_renderer_backward", [VP, C.c_uint32, C.c_uint32, F32P, F32P, F32P, VP])
     sig(L, "lucent_renderer_denoise", [VP, C.c_uint32, C.c_float, C.c_float, C.c_float, VP])

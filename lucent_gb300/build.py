@@ -23,7 +23,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
 # denoiser and display pass keep the shaders' separate multiply and add so
 # that variance differences (second moment minus squared mean) round the
 # same way as the unfused restatement they are tested against.
-EXTRA = {"bvh_build.cu": ["-fmad=false"], "denoise.cu": ["-fmad=false"]}
+EXTRA = {"bvh_build.cu": ["-fmad=false"], "denoise.cu": ["-fmad=false"], "texture.cu": ["-fmad=false"]}
 
 
 def nvcc():

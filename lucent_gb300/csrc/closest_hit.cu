@@ -25,7 +25,8 @@ struct ApiPolicy {
   __device__ void ray(uint32_t k, float3& o, float3& d) const { load_ray6(rays, k, o, d); }
   __device__ uint32_t key(uint32_t) const { return 0; }
   static constexpr bool kMultiScene = false;
-  __device__ bool alpha(int, int, uint32_t) const { return true; }
+  __device__ bool alpha(int, int, uint32_t, float, float) const { return true; }
+  __device__ AlphaAnswer alpha_fast(int, int, uint32_t) const { return kAlphaBlock; }
   __device__ bool alpha_any() const { return false; }
   // intersectBVH's t, u, v are binary64 values: always confirmed in binary64.
   __device__ bool exact_output() const { return true; }

@@ -93,6 +93,10 @@ LUCENT_DEV int node_count(const Node& n) { return __float_as_int(n.hi.w); }
 
 constexpr int kTsStack = 64;  // the reference's Int32Array(64) (bvh.ts:276)
 
+// Alpha test answers of the binary32 traversal kernels: the hit counts, it
+// passes through, or it needs a texture lookup done by the binary64 kernel.
+enum AlphaAnswer { kAlphaPass = 0, kAlphaBlock = 1, kAlphaDefer = 2 };
+
 // Device error word bits (read by the host after a launch).
 enum : unsigned {
   kErrStack = 1u,       // a traversal needed more than the reference's 64 stack entries

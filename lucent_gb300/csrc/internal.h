@@ -24,6 +24,15 @@ void launch_closest_d(const Node* nodes, uint32_t node_count, const float4* tris
                       double tMax, int32_t* prim, double* t, double* u, double* v, unsigned* err, cudaStream_t s);
 
 struct DeviceBuffer;
+// Texture arrays (texture.cu): decode tables (512: sRGB byte -> linear, then
+// byte / 255) and sRGB code-value midpoints (255), the shared layer size
+// (renderer.ts:316-322), and the resampling of each referenced image into its
+// layer of a size x size RGBA8 array.
+void texel_tables(float lut[512], float mid[255]);
+int texture_array_size(const uint32_t* w, const uint32_t* h, const int32_t* layers, uint32_t n_layers);
+lucent_status build_texture_layers(const uint8_t* const* images, const uint32_t* w, const uint32_t* h,
+                                   const int32_t* layers, uint32_t n_layers, int size, bool srgb, const float* lut_d,
+                                   const float* mid_d, uint8_t* out_d, cudaStream_t s);
 lucent_status gpu_build_bvh(const float* pos_d, uint32_t n, int max_leaf, int bins, cudaStream_t s,
                             std::vector<float>& nodes_ref, std::vector<uint32_t>& tri_out, double bounds[6],
                             DeviceBuffer* nodes_dev, DeviceBuffer* tris_dev);

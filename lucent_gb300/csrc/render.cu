@@ -26,78 +26,8 @@ namespace lucent {
 using namespace sh;
 
 // ------------------------------------------------------------ traversal policies
-struct PathClosest {
-  const uint32_t* cnt;
-  const uint32_t* queue;
-  const float4* ro;
-  const float4* rd;
-  const uint32_t* rng;
-  float4* hits;
-  const float4* geo;
-  const float4* mats;
-  int any_alpha;
-  __device__ uint32_t count() const { return *cnt; }
-  __device__ void ray(uint32_t k, float3& o, float3& d) const {
-    const uint32_t p = queue[k];
-    const float4 a = ro[p], b = rd[p];
-    o = make_float3(a.x, a.y, a.z);
-    d = make_float3(b.x, b.y, b.z);
-  }
-  __device__ uint32_t key(uint32_t k) const { return rng[queue[k]]; }
-  __device__ bool alpha_any() const { return any_alpha != 0; }
-  static constexpr bool kMultiScene = false;
-  // alphaOpaque (scene.glsl:284-297) with constant alpha.
-  __device__ bool alpha(int, int slot, uint32_t key) const {
-    if (__ldg(&geo[3 * (size_t)slot + 2].w) < 0.5f) return true;
-    const int m = (int)__ldg(&geo[3 * (size_t)slot].w);
-    const float alpha = __ldg(&mats[m * 10 + 2].w);
-    if ((int)__ldg(&mats[m * 10 + 3].w) == 1) return alpha >= __ldg(&mats[m * 10 + 5].w);
-    return alpha_rand(key, (uint32_t)slot) < alpha;
-  }
-  // Shading uses binary32 t and barycentrics (as the GLSL does); only the
-  // choice of triangle must be the reference's.
-  __device__ bool exact_output() const { return false; }
-  __device__ void hit32(uint32_t k, int slot, float3 e) const {
-    hits[queue[k]] = make_float4(e.x, e.y, e.z, __int_as_float(slot));
-  }
-  __device__ void hit(uint32_t k, int slot, double t, double u, double v) const {
-    hits[queue[k]] = make_float4(__double2float_rn(t), __double2float_rn(u), __double2float_rn(v), __int_as_float(slot));
-  }
-  __device__ void miss(uint32_t k) const { hits[queue[k]] = make_float4(INF, 0.f, 0.f, __int_as_float(-1)); }
-  __device__ void fail(uint32_t k) const { miss(k); }
-};
-
-struct PathShadow {
-  const uint32_t* cnt;
-  const uint32_t* queue;
-  const float4* so;  // origin xyz, tmax
-  const float4* sd;  // dir xyz, alpha key bits
-  uint8_t* occ;
-  const float4* geo;
-  const float4* mats;
-  int any_alpha;
-  __device__ uint32_t count() const { return *cnt; }
-  __device__ void ray(uint32_t k, float3& o, float3& d) const {
-    const uint32_t s = queue[k];
-    const float4 a = so[s], b = sd[s];
-    o = make_float3(a.x, a.y, a.z);
-    d = make_float3(b.x, b.y, b.z);
-  }
-  __device__ double tmax(uint32_t k) const { return (double)so[queue[k]].w; }
-  __device__ uint32_t key(uint32_t k) const { return __float_as_uint(sd[queue[k]].w); }
-  __device__ bool alpha_any() const { return any_alpha != 0; }
-  static constexpr bool kMultiScene = false;
-  __device__ bool alpha(int, int slot, uint32_t key) const {
-    return PathClosest{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, geo, mats, any_alpha}.alpha(0, slot, key);
-  }
-  __device__ void shadow(uint32_t k, bool occluded) const { occ[queue[k]] = occluded ? 1 : 0; }
-};
-
 // Policies for waves holding the paths of several scenes: a path's scene is
 // sid[path]; its BVH, triangles and materials come from the scene table.
-__device__ __forceinline__ bool alpha_opaque(const float4* geo, const float4* mats, int slot, uint32_t key) {
-  return PathClosest{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, geo, mats, 1}.alpha(0, slot, key);
-}
 
 // Closest-hit rays of a wave. Ray k is path queue[k], read from the path
 // state; after a ray sort the rays come instead from the sorted stream `sray`
@@ -141,8 +71,11 @@ struct PathClosestMulti {
   }
   __device__ uint32_t key(uint32_t k) const { return rng[path(k)]; }
   __device__ bool alpha_any() const { return any_alpha != 0; }
-  __device__ bool alpha(int sc, int slot, uint32_t key) const {
-    return alpha_opaque(recs[sc].scene.geo, recs[sc].scene.materials, slot, key);
+  __device__ bool alpha(int sc, int slot, uint32_t key, float bu, float bv) const {
+    return alpha_opaque(recs[sc].scene, slot, key, bu, bv);
+  }
+  __device__ AlphaAnswer alpha_fast(int sc, int slot, uint32_t key) const {
+    return sh::alpha_fast(recs[sc].scene, slot, key);
   }
   __device__ bool exact_output() const { return false; }
   __device__ void hit32(uint32_t k, int slot, float3 e) const {
@@ -180,8 +113,11 @@ struct PathShadowMulti {
   __device__ double tmax(uint32_t k) const { return (double)so[queue[k]].w; }
   __device__ uint32_t key(uint32_t k) const { return __float_as_uint(sd[queue[k]].w); }
   __device__ bool alpha_any() const { return any_alpha != 0; }
-  __device__ bool alpha(int sc, int slot, uint32_t key) const {
-    return alpha_opaque(recs[sc].scene.geo, recs[sc].scene.materials, slot, key);
+  __device__ bool alpha(int sc, int slot, uint32_t key, float bu, float bv) const {
+    return alpha_opaque(recs[sc].scene, slot, key, bu, bv);
+  }
+  __device__ AlphaAnswer alpha_fast(int sc, int slot, uint32_t key) const {
+    return sh::alpha_fast(recs[sc].scene, slot, key);
   }
   __device__ void shadow(uint32_t k, bool occluded) const { occ[queue[k]] = occluded ? 1 : 0; }
 };
@@ -353,11 +289,81 @@ struct SceneTable {
   __device__ float uclamp(uint32_t p) const { return rec(p).clamp; }
 };
 
-template <class Src, bool ADJ = false>
+// The texture-map part of surfaceAt (trace.frag:72-110): multipliers of the
+// base colour, roughness, metallic and emission, and the normal-mapped
+// shading normal. Only the TEX instantiation of the shade kernel contains
+// it. `slot`: the triangle, -1 for the ground plane, -2 for a sphere.
+struct MapSample {
+  float3 albedo, emission, n;
+  float roughness, metallic;
+  bool mapped;
+};
+static __device__ __forceinline__ MapSample sample_maps(const SceneDev& S, const float4* M, float4 maps, int slot,
+                                                     const float4* hit, float3 pos, float3 rd, float3 normal,
+                                                     float3 gn, bool front) {
+  MapSample out{f3(1.f, 1.f, 1.f), f3(1.f, 1.f, 1.f), normal, 1.f, 1.f, false};
+  // hit.uv and the surface derivatives (scene.glsl:274-320)
+  float2 huv = make_float2(0.f, 0.f);
+  float3 dpdu = f3(0.f, 0.f, 0.f), dpdv = f3(0.f, 0.f, 0.f);
+  if (slot == -1) {
+    huv = make_float2(pos.x, pos.z);
+  } else if (slot >= 0) {
+    const float4 h = *hit;
+    const float4* a = S.attr + 4 * (size_t)slot;
+    const float4* g = S.geo + 3 * (size_t)slot;
+    const float4 a3 = __ldg(a + 3), p0 = __ldg(g), p1 = __ldg(g + 1), p2 = __ldg(g + 2);
+    const float2 uv0 = make_float2(__ldg(&a[0].w), a3.x), uv1 = make_float2(__ldg(&a[1].w), a3.y),
+                 uv2 = make_float2(__ldg(&a[2].w), a3.z);
+    const float hw = 1.f - h.y - h.z;
+    huv = make_float2(uv0.x * hw + uv1.x * h.y + uv2.x * h.z, uv0.y * hw + uv1.y * h.y + uv2.y * h.z);
+    const float2 d1 = make_float2(uv1.x - uv0.x, uv1.y - uv0.y), d2 = make_float2(uv2.x - uv0.x, uv2.y - uv0.y);
+    const float det = d1.x * d2.y - d1.y * d2.x;
+    if (fabsf(det) > 1e-12f) {
+      const float r = 1.f / det;
+      const float3 e1 = f3(p1) - f3(p0), e2 = f3(p2) - f3(p0);
+      dpdu = (e1 * d2.y - e2 * d1.y) * r;
+      dpdv = (e2 * d1.x - e1 * d2.x) * r;
+    }
+  }
+  const float2 tuv = transform_uv(huv, __ldg(M + 8), __ldg(M + 9));
+  if (maps.x >= 0.f) out.albedo = f3(sample_layer(S, S.color_maps, (int)maps.x, tuv, true));
+  if (maps.y >= 0.f) {
+    const float4 mr = sample_layer(S, S.data_maps, (int)maps.y, tuv, false);
+    out.roughness = mr.y;
+    out.metallic = mr.z;
+  }
+  if (maps.w >= 0.f) out.emission = f3(sample_layer(S, S.color_maps, (int)maps.w, tuv, true));
+  if (maps.z >= 0.f && dot3(dpdu, dpdu) > 0.f) {
+    // Tangent frame from the UV derivatives on the outward normal, so back
+    // faces see the mirrored perturbation; glTF's +Y points to decreasing v.
+    const float3 N = front ? normal : -normal;
+    const float3 T = norm3(dpdu - N * dot3(N, dpdu));
+    float3 B = cross3(N, T);
+    if (dot3(B, -dpdv) < 0.f) B = -B;
+    const float4 t4 = sample_layer(S, S.data_maps, (int)maps.z, tuv, false);
+    const float scale = __ldg(&M[5].x);
+    const float tx = (t4.x * 2.f - 1.f) * scale, ty = (t4.y * 2.f - 1.f) * scale, tz = t4.z * 2.f - 1.f;
+    float3 mapped = norm3(T * tx + B * ty + N * fmaxf(tz, 1e-3f));
+    mapped = front ? mapped : -mapped;
+    if (dot3(mapped, -rd) > 1e-3f && dot3(mapped, gn) > 0.f) {
+      out.n = mapped;
+      out.mapped = true;
+    }
+  }
+  return out;
+}
+
+// One bounce of every path in queue `cur`. Hits on texture-mapped materials
+// are shaded by a second instantiation, TEX: the first appends them to the
+// textured-hit queue untouched, so untextured shading carries none of the
+// texture code; the TEX launch then shades exactly those paths. Which
+// instantiation shades a hit depends on the hit alone, never on the launch,
+// so a scene renders the same alone and in a batch.
+template <class Src, bool ADJ = false, bool TEX = false>
 __global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_constant__ Src src, int cur, int bounce,
                                                     const __grid_constant__ AdjointDev A = AdjointDev{}) {
-  const uint32_t n = P.ctr[kCtrQ0 + cur];
-  const uint32_t* q = P.q[cur];
+  const uint32_t n = TEX ? P.ctr[kCtrTex] : P.ctr[kCtrQ0 + cur];
+  const uint32_t* q = TEX ? P.qtex : P.q[cur];
   uint32_t* qn = P.q[cur ^ 1];
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const uint32_t p = q[k];
@@ -374,7 +380,7 @@ __global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_consta
     float4 galb = P.galb[p], gnrm = P.gnrm[p];
     uint32_t st = P.rng[p];
     const float4 hv = P.hit[p];
-    bool alive = false;
+    bool alive = false, deferred = false;
     float3 dl = f3(0.f, 0.f, 0.f), lrem = f3(0.f, 0.f, 0.f);
     int cont_mat = -1;
     const bool adj = ADJ && !A.primal;
@@ -470,7 +476,7 @@ __global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_consta
         material = (int)g0.w;
         light = (int)g1.w;
       }
-      // surfaceAt (trace.frag:72-124), no texture maps.
+      // surfaceAt (trace.frag:72-124).
       const float4* M = S.materials + (size_t)material * 10;
       const float4 m0 = __ldg(M), m1 = __ldg(M + 1), m2 = __ldg(M + 2), m3 = __ldg(M + 3), m5 = __ldg(M + 5),
                    m6 = __ldg(M + 6), m7 = __ldg(M + 7), m8 = __ldg(M + 8);
@@ -483,9 +489,24 @@ __global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_consta
       }
       s.metallic = m0.w;
       s.roughness = m1.x;
-      const float3 emission = f3(m2);
+      float3 emission = f3(m2);
       s.nc = normal;
       s.n = normal;
+      const float4 m4 = __ldg(M + 4);
+      if (S.tex_size > 0 && fmaxf(fmaxf(m4.x, m4.y), fmaxf(m4.z, m4.w)) >= 0.f) {
+        if constexpr (!TEX) {  // nothing of this path has been written yet
+          deferred = true;
+          break;
+        } else {
+          const MapSample ms =
+              sample_maps(S, M, m4, ground ? -1 : (tri ? slot : -2), P.hit + p, pos, rd, normal, gn, front);
+          s.albedo = s.albedo * ms.albedo;
+          s.roughness *= ms.roughness;
+          s.metallic *= ms.metallic;
+          emission = emission * ms.emission;
+          if (ms.mapped) s.n = ms.n;
+        }
+      }
       s.ior = m1.y;
       s.transmission = m1.z * (1.f - s.metallic);
       s.clearcoat = m5.y;
@@ -633,6 +654,10 @@ __global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_consta
       alive = bounce < max_bounces;
       if (!alive) cont_mat = -1;
     } while (false);
+    if (deferred) {
+      P.qtex[atomicAdd(&P.ctr[kCtrTex], 1u)] = p;
+      continue;
+    }
     if (adj) {
       A.lrem[p].x = lrem.x, A.lrem[p].y = lrem.y, A.lrem[p].z = lrem.z;
       A.gcont[5 * (size_t)p + 4].z = __int_as_float(cont_mat);
@@ -857,6 +882,7 @@ __global__ void k_zero_counters(uint32_t* ctr, int nxt) {
     ctr[kCtrSlow] = 0;
     ctr[kCtrWork2] = 0;
     ctr[kCtrSlow2] = 0;
+    ctr[kCtrTex] = 0;
   }
 }
 
@@ -1012,6 +1038,7 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     k_closest_exact_t<PathClosestMulti><<<64, 128, 0, s>>>(A, pc);
     E.mark(kPhClosest, s);
     k_shade_t<SceneTable><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b);
+    if (M.any_tex) k_shade_t<SceneTable, false, true><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b);
     E.mark(kPhShade, s);
     PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};
     TravArgs B{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr,

@@ -177,6 +177,10 @@ struct lucent_renderer {
   uint32_t W = 1, H = 1;
   // scene
   DeviceBuffer nodes, geo, attr, mats, spheres, sph_mat, sph_light, lights;
+  // texture arrays (sRGB colour layers, linear data layers), decode tables, layer size (0: none)
+  DeviceBuffer color_maps, data_maps, texel_lut;
+  int tex_size = 0;
+  uint32_t color_layers = 0, data_layers = 0;
   uint32_t node_count = 0, tri_count = 0, material_count = 0, sphere_count = 0, light_count = 0;
   int32_t ground_material = -1, ground_enabled = 0, any_alpha = 0;
   float ground_height = 0;
@@ -246,7 +250,7 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
                                         uint32_t cap) {
   if (cap <= path_cap) return LUCENT_OK;
   // Per-path arrays in allocation order (bytes per path); each starts on a 256-byte boundary.
-  static const size_t kPer[] = {16, 16, 16, 16, 16, 16, 16, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12, 4, 32, 4};
+  static const size_t kPer[] = {16, 16, 16, 16, 16, 16, 16, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12, 4, 32, 4, 4};
   size_t total = 0;
   for (size_t b : kPer) total += ((size_t)cap * b + 255) & ~(size_t)255;
   total += (size_t)kSortBins * 4;
@@ -282,6 +286,7 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
   P.sort_keys = (uint32_t*)take((size_t)cap * 4);
   P.sray = (float4*)take((size_t)cap * 32);
   P.sort_tmp = (uint32_t*)take((size_t)cap * 4);
+  P.qtex = (uint32_t*)take((size_t)cap * 4);
   P.sort_hist = (uint32_t*)take((size_t)kSortBins * 4);
   if (off > paths.cap) return fail(LUCENT_ERR_DEVICE, "path buffer layout overflow");
   P.ctr = (uint32_t*)ctr.ptr;
@@ -296,12 +301,47 @@ static lucent_status alloc_paths(lucent_renderer* r, uint32_t cap) {
   return alloc_path_buffers(r->paths, r->ctr, r->path_cap, r->P, cap);
 }
 
+// buildTextureArrays (renderer.ts:314-333): every referenced image resampled
+// into its layer of the sRGB or linear array, at one shared size.
+static lucent_status load_textures(lucent_renderer* r, const lucent_scene_desc* d, cudaStream_t s) {
+  r->tex_size = 0;
+  r->color_layers = r->data_layers = 0;
+  const uint32_t nc = d->color_layer_count, nd = d->data_layer_count;
+  if (nc + nd == 0) return LUCENT_OK;
+  std::vector<int32_t> used(d->color_layers, d->color_layers + nc);
+  used.insert(used.end(), d->data_layers, d->data_layers + nd);
+  const int size = texture_array_size(d->texture_width, d->texture_height, used.data(), (uint32_t)used.size());
+  float lut[512], mid[255];
+  texel_tables(lut, mid);
+  std::vector<float> tables(lut, lut + 512);
+  tables.insert(tables.end(), mid, mid + 255);
+  const size_t layer_bytes = (size_t)size * size * 4;
+  lucent_status st;
+  if ((st = r->texel_lut.reserve(tables.size() * 4)) || (st = r->color_maps.reserve((nc ? nc : 1) * layer_bytes)) ||
+      (st = r->data_maps.reserve((nd ? nd : 1) * layer_bytes)))
+    return st;
+  cudaError_t e = cudaMemcpy(r->texel_lut.ptr, tables.data(), tables.size() * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "texel tables");
+  const float* lut_d = (const float*)r->texel_lut.ptr;
+  if ((st = build_texture_layers(d->texture_rgba8, d->texture_width, d->texture_height, d->color_layers, nc, size, true,
+                                 lut_d, lut_d + 512, (uint8_t*)r->color_maps.ptr, s)) ||
+      (st = build_texture_layers(d->texture_rgba8, d->texture_width, d->texture_height, d->data_layers, nd, size, false,
+                                 lut_d, lut_d + 512, (uint8_t*)r->data_maps.ptr, s)))
+    return st;
+  r->tex_size = size;
+  r->color_layers = nc;
+  r->data_layers = nd;
+  return LUCENT_OK;
+}
+
 static SceneRec scene_rec(const lucent_renderer* r) {
   SceneRec R{};
   R.scene = {(const Node*)r->nodes.ptr, r->node_count, (const float4*)r->geo.ptr, (const float4*)r->attr.ptr,
              (const float4*)r->mats.ptr, (const float4*)r->spheres.ptr, (const int*)r->sph_mat.ptr,
              (const int*)r->sph_light.ptr, (int)r->sphere_count, (const float4*)r->lights.ptr, (int)r->light_count,
-             r->ground_enabled ? r->ground_material : -1, r->ground_height, r->any_alpha};
+             r->ground_enabled ? r->ground_material : -1, r->ground_height, r->any_alpha,
+             (const uchar4*)r->color_maps.ptr, (const uchar4*)r->data_maps.ptr, (const float*)r->texel_lut.ptr,
+             r->tex_size};
   R.light = r->light;
   R.cam = r->cam;
   R.accum = {(float4*)r->color.ptr, (half4*)r->albedo.ptr, (half4*)r->normal.ptr, (float*)r->history.ptr};
@@ -386,6 +426,7 @@ static lucent_status single_launch(lucent_renderer* r, uint32_t S, uint32_t tail
   M.any_alpha = r->any_alpha;
   M.sort_rays = r->sort_rays;
   M.top_levels = r->top_levels;
+  M.any_tex = r->tex_size > 0;
   return LUCENT_OK;
 }
 
@@ -429,7 +470,8 @@ void lucent_renderer_destroy(lucent_renderer* r) {
   if (!r) return;
   for (DeviceBuffer* b : {&r->nodes, &r->geo, &r->attr, &r->mats, &r->spheres, &r->sph_mat, &r->sph_light,
                           &r->lights, &r->env_rgb, &r->env_alias, &r->sheen, &r->color, &r->albedo, &r->normal,
-                          &r->history, &r->paths, &r->ctr, &r->den_a, &r->den_b, &r->guide0, &r->guide1, &r->disp, &r->adj_dl, &r->adj_path, &r->adj_grad, &r->rec1, &r->base1, &r->sid1, &r->prev})
+                          &r->history, &r->paths, &r->ctr, &r->den_a, &r->den_b, &r->guide0, &r->guide1, &r->disp, &r->adj_dl, &r->adj_path, &r->adj_grad, &r->rec1, &r->base1, &r->sid1, &r->prev,
+                          &r->color_maps, &r->data_maps, &r->texel_lut})
     b->release();
   if (r->ev0) cudaEventDestroy(r->ev0);
   if (r->ev1) cudaEventDestroy(r->ev1);
@@ -456,10 +498,32 @@ lucent_status lucent_renderer_load_scene(lucent_renderer* r, const lucent_scene_
   if (d->light_count > 8) return fail(LUCENT_ERR_INVALID, "scene has %u lights; max is 8", d->light_count);
   if (d->material_count == 0 || !d->materials) return fail(LUCENT_ERR_INVALID, "scene has no materials");
   const uint32_t M = d->material_count;
+  // Map fields hold layer indices: base colour and emissive into the colour
+  // array, metal-rough and normal into the data array (scene.ts:271-283).
   for (uint32_t m = 0; m < M; m++)
-    for (int k = 16; k < 20; k++)
-      if (d->materials[m * 40 + k] >= 0)
-        return fail(LUCENT_ERR_UNSUPPORTED, "material %u uses a texture map; texture layers are not supported", m);
+    for (int k = 16; k < 20; k++) {
+      const float v = d->materials[m * 40 + k];
+      const uint32_t layers = (k == 16 || k == 19) ? d->color_layer_count : d->data_layer_count;
+      if (v >= 0 && !(v < (float)layers && v == std::floor(v)))
+        return fail(LUCENT_ERR_INVALID, "material %u map %d is layer %g of %u", m, k - 16, v, layers);
+    }
+  if (d->color_layer_count + d->data_layer_count > 0) {
+    if (!d->texture_rgba8 || !d->texture_width || !d->texture_height)
+      return fail(LUCENT_ERR_INVALID, "texture layers without textures");
+    for (int a = 0; a < 2; a++) {
+      const int32_t* L = a ? d->data_layers : d->color_layers;
+      const uint32_t n_l = a ? d->data_layer_count : d->color_layer_count;
+      if (n_l && !L) return fail(LUCENT_ERR_INVALID, "null layer list");
+      for (uint32_t i = 0; i < n_l; i++) {
+        const int32_t t = L[i];
+        if (t < 0 || (uint32_t)t >= d->texture_count)  // scene.ts:281-283
+          return fail(LUCENT_ERR_INVALID, "material references texture %d, scene has %u", t, d->texture_count);
+        if (!d->texture_rgba8[t] || d->texture_width[t] == 0 || d->texture_height[t] == 0 ||
+            (uint64_t)d->texture_width[t] * d->texture_height[t] > (1ull << 28))
+          return fail(LUCENT_ERR_INVALID, "texture %d is empty or too large", t);
+      }
+    }
+  }
   for (uint32_t i = 0; i < n; i++) {
     if (d->tri_material[i] < 0 || (uint32_t)d->tri_material[i] >= M)
       return fail(LUCENT_ERR_INVALID, "triangle %u has material %d", i, d->tri_material[i]);
@@ -543,6 +607,7 @@ lucent_status lucent_renderer_load_scene(lucent_renderer* r, const lucent_scene_
   cudaError_t e = cudaStreamSynchronize(s);
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) return cleanup(cuda_fail(e, "scene upload"));
+  if ((st = load_textures(r, d, s))) return cleanup(st);
   r->node_count = nc;
   r->tri_count = n;
   r->material_count = M;
@@ -705,6 +770,8 @@ lucent_status lucent_renderer_backward(lucent_renderer* r, uint32_t samples, uin
   clear_error();
   if (!r || !dl_dimage || !d_materials) return fail(LUCENT_ERR_INVALID, "null argument");
   if (!r->has_scene || !r->has_lighting) return fail(LUCENT_ERR_INVALID, "backward before load_scene / upload_lighting");
+  // The parameters are the material factors; with maps the BSDF sees factor x texel.
+  if (r->tex_size > 0) return fail(LUCENT_ERR_UNSUPPORTED, "backward through texture-mapped materials");
   if (samples == 0) return LUCENT_OK;
   cudaStream_t s = (cudaStream_t)stream;
   const uint32_t WH = r->W * r->H;
@@ -757,6 +824,18 @@ lucent_status lucent_renderer_set_ray_sort(lucent_renderer* r, int32_t enabled) 
   if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
   r->sort_rays = enabled ? 1 : 0;
   return LUCENT_OK;
+}
+
+lucent_status lucent_renderer_read_textures(lucent_renderer* r, uint32_t* size, uint8_t* color_out, uint8_t* data_out) {
+  clear_error();
+  if (!r || !size) return fail(LUCENT_ERR_INVALID, "null argument");
+  *size = (uint32_t)r->tex_size;
+  const size_t layer = (size_t)r->tex_size * r->tex_size * 4;
+  cudaError_t e = cudaSuccess;
+  if (color_out && r->color_layers) e = cudaMemcpy(color_out, r->color_maps.ptr, r->color_layers * layer, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && data_out && r->data_layers)
+    e = cudaMemcpy(data_out, r->data_maps.ptr, r->data_layers * layer, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "read textures");
 }
 
 lucent_status lucent_renderer_set_top_levels(lucent_renderer* r, int32_t enabled) {
@@ -1043,6 +1122,7 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
   M.shade_blocks = (int)b->opt.shade_blocks;
   M.sort_rays = b->opt.sort_rays;
   M.top_levels = b->opt.top_levels;
+  for (lucent_renderer* rr : b->rs) M.any_tex |= rr->tex_size > 0;
   auto setup = [&](uint32_t s_wave, const DeviceBuffer& base) {
     M.S = (int)s_wave;
     M.total_paths = (uint32_t)(pixels * s_wave);

@@ -15,6 +15,7 @@ enum : int {
   kCtrWork2 = 5,        // any-hit work counter (unused by the grid-stride kernel)
   kCtrSlow2 = 6,        // any-hit slow-path queue length
   kCtrErr = 7,          // device error word
+  kCtrTex = 12,         // textured-hit queue length (paths left to the TEX shade instantiation)
   kCtrStatClosest = 8,  // u64: closest-hit rays traced (words 8-9)
   kCtrStatShadow = 10,  // u64: shadow rays traced (words 10-11)
   kCtrTrav = 16,        // 5 x u64 closest-hit traversal counters (words 16-25), profiling only
@@ -47,6 +48,7 @@ struct Paths {
   uint32_t* sort_keys;  // per queued path: ray-sort key (scene, direction octant, origin cell)
   float4* sray;         // sorted ray stream: 2 float4 per queued ray (origin + path id, direction + scene)
   uint32_t* sort_tmp;   // the sorted queue, swapped with the queue it sorts
+  uint32_t* qtex;       // paths whose hit material is texture-mapped (shaded by the TEX instantiation)
   uint32_t* sort_hist;  // kSortBins counters
   uint32_t* ctr;
 };
@@ -93,6 +95,7 @@ struct MultiLaunch {
   unsigned long long* trav_stats;  // closest-hit traversal counters (profiling) or nullptr
   int sort_rays;                   // after bounces 0 and 1, sort the rays by scene, direction octant and origin cell
   int top_levels;                  // stage the top BVH levels of (up to 8) scenes in shared memory
+  int any_tex;                     // some scene has texture maps: launch the TEX shade instantiation
 };
 
 // Optional per-phase timing: events recorded between launches, each tagged

@@ -141,7 +141,88 @@ struct SceneDev {
   int ground_material;      // -1: no ground plane
   float ground_height;
   int any_alpha;
+  // Texture arrays (scene.glsl:17-18): tex_size^2 RGBA8 texels per layer,
+  // row 0 at v = 0; colour layers hold sRGB codes. texel_lut: 512 floats,
+  // sRGB code -> linear, then code / 255. tex_size 0: no textures.
+  const uchar4* color_maps;
+  const uchar4* data_maps;
+  const float* texel_lut;
+  int tex_size;
 };
+
+// transformUV (scene.glsl:95-97): rows of a 2x3 affine map.
+LUCENT_DEV float2 transform_uv(float2 uv, float4 row0, float4 row1) {
+  return make_float2(row0.x * uv.x + row0.y * uv.y + row0.z, row1.x * uv.x + row1.y * uv.y + row1.z);
+}
+
+// textureLod(array, vec3(uv, layer), 0.0) with LINEAR filtering and REPEAT
+// wrapping (context.ts:241-244); sRGB layers decode before filtering, alpha
+// is linear.
+LUCENT_DEV float4 sample_layer(const SceneDev& S, const uchar4* tex, int layer, float2 uv, bool srgb) {
+  const int n = S.tex_size;
+  float u = uv.x - floorf(uv.x), v = uv.y - floorf(uv.y);  // REPEAT
+  if (!(u >= 0.f && u < 1.f)) u = 0.f;                     // NaN or infinite coordinates
+  if (!(v >= 0.f && v < 1.f)) v = 0.f;
+  const float x = u * (float)n - 0.5f, y = v * (float)n - 0.5f;
+  const float x0 = floorf(x), y0 = floorf(y);
+  const float fx = x - x0, fy = y - y0;
+  const int ix = (int)x0, iy = (int)y0;
+  const int xa = ix < 0 ? n - 1 : ix, xb = ix + 1 >= n ? 0 : ix + 1;
+  const int ya = iy < 0 ? n - 1 : iy, yb = iy + 1 >= n ? 0 : iy + 1;
+  const uchar4* L = tex + (size_t)layer * n * n;
+  const uchar4 t00 = __ldg(L + (size_t)ya * n + xa), t10 = __ldg(L + (size_t)ya * n + xb);
+  const uchar4 t01 = __ldg(L + (size_t)yb * n + xa), t11 = __ldg(L + (size_t)yb * n + xb);
+  const float* rgb = S.texel_lut + (srgb ? 0 : 256);
+  const float* lin = S.texel_lut + 256;
+  auto mix4 = [&](float a, float b, float c, float d) {
+    return (a * (1.f - fx) + b * fx) * (1.f - fy) + (c * (1.f - fx) + d * fx) * fy;
+  };
+  return make_float4(mix4(__ldg(rgb + t00.x), __ldg(rgb + t10.x), __ldg(rgb + t01.x), __ldg(rgb + t11.x)),
+                     mix4(__ldg(rgb + t00.y), __ldg(rgb + t10.y), __ldg(rgb + t01.y), __ldg(rgb + t11.y)),
+                     mix4(__ldg(rgb + t00.z), __ldg(rgb + t10.z), __ldg(rgb + t01.z), __ldg(rgb + t11.z)),
+                     mix4(__ldg(lin + t00.w), __ldg(lin + t10.w), __ldg(lin + t01.w), __ldg(lin + t11.w)));
+}
+
+// triangleUV (scene.glsl:163-173): the slot's texture coordinates at barycentrics (bu, bv).
+LUCENT_DEV float2 triangle_uv(const SceneDev& S, int slot, float bu, float bv) {
+  const float4* a = S.attr + 4 * (size_t)slot;
+  const float u0 = __ldg(&a[0].w), u1 = __ldg(&a[1].w), u2 = __ldg(&a[2].w);
+  const float4 a3 = __ldg(&a[3]);
+  const float w = 1.f - bu - bv;
+  return make_float2(u0 * w + u1 * bu + u2 * bv, a3.x * w + a3.y * bu + a3.z * bv);
+}
+
+// alphaOpaque (scene.glsl:176-189): does a hit at barycentrics (bu, bv) on an
+// alpha-tested slot block the ray? Constant alpha times the base colour map's
+// alpha at the hit; mask mode compares with the cutoff, blend mode draws a
+// uniform from (key, slot).
+LUCENT_DEV bool alpha_opaque(const SceneDev& S, int slot, uint32_t key, float bu, float bv) {
+  if (__ldg(&S.geo[3 * (size_t)slot + 2].w) < 0.5f) return true;
+  const int m = (int)__ldg(&S.geo[3 * (size_t)slot].w);
+  const float4* M = S.materials + (size_t)m * 10;
+  float alpha = __ldg(&M[2].w);
+  const int map = (int)__ldg(&M[4].x);
+  if (map >= 0 && S.tex_size > 0) {
+    const float2 tuv = transform_uv(triangle_uv(S, slot, bu, bv), __ldg(&M[8]), __ldg(&M[9]));
+    alpha *= sample_layer(S, S.color_maps, map, tuv, true).w;
+  }
+  if ((int)__ldg(&M[3].w) == 1) return alpha >= __ldg(&M[5].w);
+  return alpha_rand(key, (uint32_t)slot) < alpha;
+}
+
+// The alpha test without texture lookups, for the binary32 traversal
+// kernels: kAlphaBlock or kAlphaPass as alpha_opaque decides, or kAlphaDefer
+// when the answer needs the base colour map (the ray is then traced by the
+// binary64 kernel, which samples it).
+LUCENT_DEV AlphaAnswer alpha_fast(const SceneDev& S, int slot, uint32_t key) {
+  if (__ldg(&S.geo[3 * (size_t)slot + 2].w) < 0.5f) return kAlphaBlock;
+  const int m = (int)__ldg(&S.geo[3 * (size_t)slot].w);
+  const float4* M = S.materials + (size_t)m * 10;
+  if ((int)__ldg(&M[4].x) >= 0 && S.tex_size > 0) return kAlphaDefer;
+  const float alpha = __ldg(&M[2].w);
+  if ((int)__ldg(&M[3].w) == 1) return alpha >= __ldg(&M[5].w) ? kAlphaBlock : kAlphaPass;
+  return alpha_rand(key, (uint32_t)slot) < alpha ? kAlphaBlock : kAlphaPass;
+}
 
 struct LightingDev {
   int sun_enabled;

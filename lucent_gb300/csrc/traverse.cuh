@@ -16,7 +16,10 @@
 //   uint32_t count() const                        rays in this launch
 //   void ray(uint32_t k, float3& o, float3& d)   k-th ray
 //   uint32_t key(uint32_t k) const                alpha any-hit key (RNG state)
-//   bool alpha(int scene, int slot, uint32_t key) true if a hit on `slot` counts
+//   bool alpha(int scene, int slot, uint32_t key, float bu, float bv)
+//                                                 true if a hit on `slot` at barycentrics (bu, bv) counts
+//   AlphaAnswer alpha_fast(int scene, int slot, uint32_t key)
+//                                                 the same without texture lookups (kAlphaDefer: ask alpha)
 //   static constexpr bool kMultiScene             rays of several scenes in one launch:
 //   BvhView bvh(uint32_t k) const                 then the k-th ray's BVH (else TravArgs'),
 //   BvhView scene_bvh(int s) const                and scene s's BVH
@@ -174,7 +177,8 @@ __device__ bool trace_exact(const TravArgs& A, const Pol& P, const BvhView& bv, 
         const float4 a = __ldg(bv.tris + 3 * (size_t)s), b = __ldg(bv.tris + 3 * (size_t)s + 1),
                      c = __ldg(bv.tris + 3 * (size_t)s + 2);
         double t, u, v;
-        if (ts_triangle(o, d, d3f(a), d3f(b), d3f(c), A.tMin, closest, t, u, v) && P.alpha(bv.scene, s, key)) {
+        if (ts_triangle(o, d, d3f(a), d3f(b), d3f(c), A.tMin, closest, t, u, v) &&
+            P.alpha(bv.scene, s, key, (float)u, (float)v)) {
           closest = t;
           slot = s;
           t_out = t;
@@ -349,6 +353,7 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
     }
     const int cnt = node_count(cur), first = node_first(cur);
     if (cnt > 0) {
+      bool defer = false;
       for (int k = 0; k < cnt; k++) {
         const int slot = first + k;
         const float4 a = __ldg(bv.tris + 3 * (size_t)slot), b = __ldg(bv.tris + 3 * (size_t)slot + 1),
@@ -357,7 +362,14 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
         float3 est;
         const TriClass tc = mt_classify(r, a, b, c, tmin_lo, tmin_hi, c_lo, c_hi, tl, th, est);
         if (tc == kTriReject) continue;
-        if (use_alpha && !P.alpha(bv.scene, slot, key)) continue;  // alpha depends on (key, slot) only
+        if (use_alpha) {  // depends on (key, slot) only, unless a texture must be sampled
+          const AlphaAnswer aa = P.alpha_fast(bv.scene, slot, key);
+          if (aa == kAlphaDefer) {
+            defer = true;
+            break;
+          }
+          if (aa == kAlphaPass) continue;
+        }
         if (tc == kTriAccept) {
           best = slot;
           best_est = est;
@@ -382,6 +394,11 @@ __global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
         }
       }
       have_cur = false;
+      if (defer) {  // a textured alpha test: the binary64 kernel traces this ray
+        A.queue[atomicAdd(A.queue_len, 1u)] = ri;
+        active = false;
+        continue;
+      }
     } else {
       // One 64-byte pair, from the treelet while its children are in it.
       const bool in_top = ctb > 0 && 2 * ctb + 1 <= kTopNodes;
@@ -440,7 +457,9 @@ __device__ bool any_exact(const TravArgs& A, const Pol& P, const BvhView& bv, D3
         const float4 a = __ldg(bv.tris + 3 * (size_t)s), b = __ldg(bv.tris + 3 * (size_t)s + 1),
                      c = __ldg(bv.tris + 3 * (size_t)s + 2);
         double t, u, v;
-        if (ts_triangle(o, d, d3f(a), d3f(b), d3f(c), A.tMin, tMax, t, u, v) && P.alpha(bv.scene, s, key)) return true;
+        if (ts_triangle(o, d, d3f(a), d3f(b), d3f(c), A.tMin, tMax, t, u, v) &&
+            P.alpha(bv.scene, s, key, (float)u, (float)v))
+          return true;
       }
     } else if (sp + 2 <= kTsStack) {
       stack[sp++] = first + 1;
@@ -495,9 +514,9 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
     int stack[kTsStack];  // node index, or -b for treelet node b
     int sp = 0;
     stack[sp++] = sb ? -1 : 0;
-    bool occ = false, ok = true;
+    bool occ = false, ok = true, defer = false;
     uint32_t iters = 0;
-    while (sp > 0 && !occ) {
+    while (sp > 0 && !occ && !defer) {
       if (++iters > bv.node_limit) {
         atomicOr(A.err, kErrIterations);
         ok = false;
@@ -510,7 +529,7 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
       if (cl == kCulled) continue;
       const int cnt = node_count(nd), first = node_first(nd);
       if (cnt > 0) {
-        for (int q = 0; q < cnt && !occ; q++) {
+        for (int q = 0; q < cnt && !occ && !defer; q++) {
           const int slot = first + q;
           const float4 a = __ldg(bv.tris + 3 * (size_t)slot), b = __ldg(bv.tris + 3 * (size_t)slot + 1),
                        c = __ldg(bv.tris + 3 * (size_t)slot + 2);
@@ -518,7 +537,14 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
           float3 est;
           const TriClass tc = mt_classify(r, a, b, c, tmin_lo, tmin_hi, c_lo, c_hi, tl, th, est);
           if (tc == kTriReject) continue;
-          if (use_alpha && !P.alpha(bv.scene, slot, key)) continue;
+          if (use_alpha) {
+            const AlphaAnswer aa = P.alpha_fast(bv.scene, slot, key);
+            if (aa == kAlphaDefer) {
+              defer = true;
+              continue;
+            }
+            if (aa == kAlphaPass) continue;
+          }
           if (tc == kTriAccept) {
             occ = true;
           } else {
@@ -536,6 +562,10 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
         stack[sp++] = in_top ? 2 * e - 1 : first + 1;  // -(2b + 1)
         stack[sp++] = in_top ? 2 * e : first;          // -(2b)
       }
+    }
+    if (defer && ok) {  // a textured alpha test: the binary64 kernel answers this ray
+      A.queue[atomicAdd(A.queue_len, 1u)] = k;
+      continue;
     }
     P.shadow(k, ok ? occ : true);
   }

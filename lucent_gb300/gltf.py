@@ -516,3 +516,15 @@ def load_gltf(source, resolve: Optional[Resolver] = None) -> GLTFAsset:
         raise GLTFError("the file contains no triangle meshes")
     bounds = (tuple(float(v) for v in lo), tuple(float(v) for v in hi))
     return GLTFAsset(meshes, materials, images, bounds, count[0], warnings)
+
+
+def write_glb(doc, bin_bytes=None) -> bytes:
+    """A GLB container (glTF 2.0 binary): the JSON chunk padded with spaces,
+    the BIN chunk padded with zeros (the layout parse_glb reads)."""
+    js = _json.dumps(doc, separators=(",", ":")).encode("utf-8")
+    js += b" " * (-len(js) % 4)
+    body = struct.pack("<II", len(js), CHUNK_JSON) + js
+    if bin_bytes is not None:
+        b = bytes(bin_bytes) + b"\0" * (-len(bin_bytes) % 4)
+        body += struct.pack("<II", len(b), CHUNK_BIN) + b
+    return struct.pack("<III", GLB_MAGIC, 2, 12 + len(body)) + body

@@ -98,6 +98,21 @@ class Renderer:
         d.sphere_lights = N.ptr(p.sphere_lights, C.c_int32)
         d.lights, d.light_count = _f(p.lights), p.light_count
         d.ground_material = p.ground_material
+        if p.color_layers or p.data_layers:  # texture maps (buildTextureArrays, renderer.ts:314-333)
+            imgs = [np.ascontiguousarray(t.image, np.uint8) for t in scene.textures]
+            for i, im in enumerate(imgs):
+                if im.ndim != 3 or im.shape[2] != 4:
+                    raise ValueError("texture %d is not an RGBA8 [h, w, 4] image" % i)
+            ptrs = (NR.U8P * len(imgs))(*[N.ptr(im, C.c_uint8) for im in imgs])
+            ws = np.array([im.shape[1] for im in imgs], np.uint32)
+            hs = np.array([im.shape[0] for im in imgs], np.uint32)
+            cl = np.array(p.color_layers, np.int32)
+            dl = np.array(p.data_layers, np.int32)
+            keep += [imgs, ptrs, ws, hs, cl, dl]
+            d.texture_count, d.texture_rgba8 = len(imgs), ptrs
+            d.texture_width, d.texture_height = N.ptr(ws, C.c_uint32), N.ptr(hs, C.c_uint32)
+            d.color_layers, d.color_layer_count = N.ptr(cl, C.c_int32), len(cl)
+            d.data_layers, d.data_layer_count = N.ptr(dl, C.c_int32), len(dl)
         N.check(N.lib().lucent_renderer_load_scene(self._h, C.byref(d)))
         self.scene = scene
         self.upload_ground(scene.ground)
@@ -181,6 +196,18 @@ class Renderer:
     def set_ray_sort(self, enabled=True):
         """Sort the rays of bounces 1 and 2 by direction and origin (lucent_renderer_set_ray_sort)."""
         N.check(N.lib().lucent_renderer_set_ray_sort(self._h, 1 if enabled else 0))
+
+    def read_texture_arrays(self):
+        """(colour layers, data layers) as uint8 [layers, size, size, 4] (lucent_renderer_read_textures)."""
+        size = C.c_uint32()
+        N.check(N.lib().lucent_renderer_read_textures(self._h, C.byref(size), None, None))
+        n = size.value
+        p = self.packed
+        col = np.zeros((len(p.color_layers), n, n, 4), np.uint8)
+        dat = np.zeros((len(p.data_layers), n, n, 4), np.uint8)
+        N.check(N.lib().lucent_renderer_read_textures(self._h, C.byref(size), N.ptr(col, C.c_uint8),
+                                                      N.ptr(dat, C.c_uint8)))
+        return col, dat
 
     def set_top_levels(self, enabled=True):
         """Stage the top BVH levels in shared memory (lucent_renderer_set_top_levels)."""

@@ -306,3 +306,127 @@ def adjoint_views(count=8):
         y = 0.7 + 0.6 * (i // 4)
         out.append(S.Camera(position=(x, y, 3.4), target=(0.0, 1.0, 0.0), fov=40.0, focus_distance=3.4))
     return out
+
+
+# ------------------------------------------------------------------ textured model
+def _noise_rgb(rng, n, cells, lo, hi):
+    """Smooth value noise (bilinear over a cells x cells grid, wrapping) in [lo, hi]^3, [n, n, 3] floats."""
+    grid = rng.uniform(lo, hi, (cells, cells, 3))
+    x = (np.arange(n) + 0.5) / n * cells - 0.5
+    i0 = np.floor(x).astype(int)
+    f = x - i0
+    i0 %= cells
+    i1 = (i0 + 1) % cells
+    a = grid[i0][:, i0] * (1 - f)[None, :, None] + grid[i0][:, i1] * f[None, :, None]
+    b = grid[i1][:, i0] * (1 - f)[None, :, None] + grid[i1][:, i1] * f[None, :, None]
+    return a * (1 - f)[:, None, None] + b * f[:, None, None]
+
+
+def textured_model_glb(seed=0, tex=256):
+    """A GLB exercising every map of the layered material: a slab with tiled
+    (texture-transformed) base colour, metal-rough and normal maps; an
+    icosphere with spherical texture coordinates, base colour and normal maps
+    and a clearcoat; an alpha-masked cut-out quad; an emissive panel with an
+    emissive map. Textures are seeded value noise encoded as PNG."""
+    from . import gltf as G
+    from . import images as I
+    from . import mesh as M
+    rng = np.random.default_rng(seed)
+    u8 = lambda x: np.clip(np.rint(x * 255), 0, 255).astype(np.uint8)
+
+    def rgba(rgb, a=None):
+        out = np.empty(rgb.shape[:2] + (4,), np.uint8)
+        out[..., :3] = u8(rgb)
+        out[..., 3] = 255 if a is None else u8(a)
+        return out
+
+    base = _noise_rgb(rng, tex, 8, 0.1, 0.9)
+    checker = ((np.arange(tex)[:, None] // (tex // 8) + np.arange(tex)[None, :] // (tex // 8)) % 2)[..., None]
+    base = base * (0.55 + 0.45 * checker)
+    mr = _noise_rgb(rng, tex, 6, 0.0, 1.0)
+    mr[..., 0] = 1.0
+    mr[..., 1] = 0.15 + 0.85 * mr[..., 1]           # roughness in G
+    mr[..., 2] = (mr[..., 2] > 0.55).astype(float)  # metal in B
+    height = _noise_rgb(rng, tex, 16, 0.0, 1.0)[..., 0]
+    gy, gx = np.gradient(height * 6.0)
+    nrm = np.stack([-gx, -gy, np.ones_like(gx)], -1)
+    nrm /= np.linalg.norm(nrm, axis=-1, keepdims=True)
+    cut = _noise_rgb(rng, tex, 5, 0.0, 1.0)[..., 0]
+    glow = _noise_rgb(rng, tex, 4, 0.2, 1.0)
+    images = [rgba(base), rgba(np.clip(mr, 0, 1)), rgba(nrm * 0.5 + 0.5),
+              rgba(_noise_rgb(rng, tex, 6, 0.3, 1.0), (cut > 0.45).astype(float)), rgba(glow)]
+
+    def spherical_uv(m, center):
+        p = m.positions.reshape(-1, 3).astype(np.float64) - np.array(center)
+        p = p / np.linalg.norm(p, axis=1, keepdims=True)
+        u = 0.5 + np.arctan2(p[:, 2], p[:, 0]) / (2 * np.pi)
+        v = np.arccos(np.clip(p[:, 1], -1, 1)) / np.pi
+        return np.stack([u, v], 1).astype(np.float32).reshape(-1)
+
+    def quad_uv(m, reps):
+        return (np.array([0, 0, 1, 0, 1, 1, 0, 0, 1, 1, 0, 1], np.float32) * reps)
+
+    slab = M.quad([-2, 0, 2], [2, 0, 2], [2, 0, -2], [-2, 0, -2])
+    sphere = M.icosphere(3, 0.7, (0.0, 0.7, 0.0))
+    cutout = M.quad([-1.8, 0, -1.2], [-0.4, 0, -1.2], [-0.4, 1.4, -1.2], [-1.8, 1.4, -1.2])
+    panel = M.quad([0.6, 0.1, -1.6], [1.8, 0.1, -1.6], [1.8, 1.1, -1.6], [0.6, 1.1, -1.6])
+    meshes = [(slab, quad_uv(slab, 3.0), 0), (sphere, spherical_uv(sphere, (0.0, 0.7, 0.0)), 1), (cutout, quad_uv(cutout, 1.0), 2),
+              (panel, quad_uv(panel, 1.0), 3)]
+    blob = b""
+    views, accessors, prims = [], [], []
+
+    def add(data, **extra):
+        nonlocal blob
+        raw = np.ascontiguousarray(data).tobytes()
+        views.append({"buffer": 0, "byteOffset": len(blob), "byteLength": len(raw), **extra})
+        blob += raw + b"\0" * (-len(raw) % 4)
+        return len(views) - 1
+
+    for mesh, uv, mat in meshes:
+        n = mesh.positions.size // 3
+        pos = mesh.positions.reshape(-1, 3)
+        ids = []
+        for arr, typ in ((pos, "VEC3"), (mesh.normals.reshape(-1, 3), "VEC3"), (uv.reshape(-1, 2), "VEC2")):
+            acc = {"bufferView": add(arr.astype(np.float32)), "componentType": 5126, "count": n, "type": typ}
+            if typ == "VEC3" and len(ids) == 0:
+                acc["min"], acc["max"] = pos.min(0).tolist(), pos.max(0).tolist()
+            accessors.append(acc)
+            ids.append(len(accessors) - 1)
+        prims.append({"attributes": {"POSITION": ids[0], "NORMAL": ids[1], "TEXCOORD_0": ids[2]}, "material": mat})
+    image_views = [add(np.frombuffer(I.encode_png(im), np.uint8)) for im in images]
+    doc = {
+        "asset": {"version": "2.0", "generator": "lucent_gb300.workloads"},
+        "scene": 0, "scenes": [{"nodes": [0]}], "nodes": [{"mesh": 0}],
+        "meshes": [{"primitives": prims}],
+        "materials": [
+            {"pbrMetallicRoughness": {"baseColorTexture": {"index": 0, "extensions": {"KHR_texture_transform": {
+                "offset": [0.1, 0.2], "rotation": 0.3, "scale": [1.5, 1.5]}}},
+                "metallicRoughnessTexture": {"index": 1}, "metallicFactor": 1.0, "roughnessFactor": 1.0},
+             "normalTexture": {"index": 2, "scale": 0.8}},
+            {"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}, "metallicFactor": 0.0,
+                                      "roughnessFactor": 0.45},
+             "normalTexture": {"index": 2}, "extensions": {"KHR_materials_clearcoat": {"clearcoatFactor": 0.6}}},
+            {"pbrMetallicRoughness": {"baseColorTexture": {"index": 3}, "metallicFactor": 0.0,
+                                      "roughnessFactor": 0.7},
+             "alphaMode": "MASK", "alphaCutoff": 0.5, "doubleSided": True},
+            {"pbrMetallicRoughness": {"baseColorFactor": [0.05, 0.05, 0.05, 1], "metallicFactor": 0.0},
+             "emissiveTexture": {"index": 4}, "emissiveFactor": [1, 0.9, 0.8],
+             "extensions": {"KHR_materials_emissive_strength": {"emissiveStrength": 6.0}}},
+        ],
+        "textures": [{"source": i} for i in range(len(images))],
+        "images": [{"bufferView": v, "mimeType": "image/png", "name": "tex%d" % i} for i, v in enumerate(image_views)],
+        "accessors": accessors, "bufferViews": views, "buffers": [{"byteLength": len(blob)}],
+    }
+    return G.write_glb(doc, blob)
+
+
+def textured_scene(seed=0, tex=256, env_width=256):
+    """textured_model_glb through the model path (load_gltf, decode_images,
+    scene_from_model) under a lognormal HDRI."""
+    from . import gltf as G
+    from . import model as MD
+    from . import scene as S
+    rng = np.random.default_rng(seed + 1000)
+    env = S.Environment(map=env_lognormal(rng, env_width, env_width // 2), name="lognormal")
+    model = MD.model_from_asset("textured", G.load_gltf(textured_model_glb(seed, tex)))
+    return MD.scene_from_model(model, env)

@@ -204,11 +204,69 @@ Material fetch_material_from(const float* mats, int index) {
   return m;
 }
 
-// alphaOpaque (scene.glsl:284-297) with constant alpha (maps unsupported).
-bool alpha_opaque(const orc_scene* s, int slot, uint32_t key) {
+// ------------------------------------------------------------------ textures
+// Decode tables of the texture arrays: sRGB code -> linear (IEC 61966-2-1,
+// binary64 rounded to binary32), code / 255, and the linear values of the
+// code-value midpoints (the sRGB encoder's thresholds).
+struct TexelTables {
+  float srgb[256], unorm[256], mid[255];
+  TexelTables() {
+    auto eotf = [](double c) { return c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4); };
+    for (int v = 0; v < 256; v++) {
+      srgb[v] = (float)eotf(v / 255.0);
+      unorm[v] = (float)v / 255.f;
+    }
+    for (int k = 0; k < 255; k++) mid[k] = (float)eotf((k + 0.5) / 255.0);
+  }
+};
+const TexelTables& texel_tables() {
+  static const TexelTables t;
+  return t;
+}
+
+// textureLod(array, vec3(uv, layer), 0) with LINEAR filtering and REPEAT
+// wrapping; sRGB layers decode before filtering, alpha is linear.
+template <class R>
+void sample_layer(const orc_scene* s, const uint8_t* tex, int layer, R u_in, R v_in, bool srgb, R out[4]) {
+  const TexelTables& T = texel_tables();
+  const int n = (int)s->tex_size;
+  R u = u_in - std::floor(u_in), v = v_in - std::floor(v_in);
+  if (!(u >= R(0) && u < R(1))) u = R(0);
+  if (!(v >= R(0) && v < R(1))) v = R(0);
+  const R x = u * R(n) - R(0.5), y = v * R(n) - R(0.5);
+  const R x0 = std::floor(x), y0 = std::floor(y);
+  const R fx = x - x0, fy = y - y0;
+  const int ix = (int)x0, iy = (int)y0;
+  const int xa = ix < 0 ? n - 1 : ix, xb = ix + 1 >= n ? 0 : ix + 1;
+  const int ya = iy < 0 ? n - 1 : iy, yb = iy + 1 >= n ? 0 : iy + 1;
+  const uint8_t* L = tex + (size_t)layer * n * n * 4;
+  const uint8_t* t00 = L + ((size_t)ya * n + xa) * 4;
+  const uint8_t* t10 = L + ((size_t)ya * n + xb) * 4;
+  const uint8_t* t01 = L + ((size_t)yb * n + xa) * 4;
+  const uint8_t* t11 = L + ((size_t)yb * n + xb) * 4;
+  for (int c = 0; c < 4; c++) {
+    const float* d = (srgb && c < 3) ? T.srgb : T.unorm;
+    const R a = R(d[t00[c]]), b = R(d[t10[c]]), e = R(d[t01[c]]), f = R(d[t11[c]]);
+    out[c] = (a * (R(1) - fx) + b * fx) * (R(1) - fy) + (e * (R(1) - fx) + f * fx) * fy;
+  }
+}
+
+// alphaOpaque (scene.glsl:176-189): constant alpha times the base colour
+// map's alpha at the hit's texture coordinates (barycentrics bu, bv).
+bool alpha_opaque(const orc_scene* s, int slot, uint32_t key, float bu, float bv) {
   const float* g = s->geo + (size_t)slot * 12;
   const float* t = s->materials + (size_t)(int)g[3] * 40;
-  const float alpha = t[11];
+  float alpha = t[11];
+  const int map = (int)t[16];
+  if (map >= 0 && s->tex_size > 0) {
+    const float* a = s->attr + (size_t)slot * 16;
+    const float w = 1.f - bu - bv;
+    const float u = a[3] * w + a[7] * bu + a[11] * bv, v = a[12] * w + a[13] * bu + a[14] * bv;
+    const float tu = t[32] * u + t[33] * v + t[34], tv = t[36] * u + t[37] * v + t[38];
+    float c[4];
+    sample_layer<float>(s, s->color_maps, map, tu, tv, true, c);
+    alpha *= c[3];
+  }
   const int mode = (int)t[15];
   if (mode == 1) return alpha >= t[23];
   return alpha_rand(key, (uint32_t)slot) < alpha;
@@ -243,7 +301,7 @@ bool closest_tri(const orc_scene* s, orc::V3 o, orc::V3 d, double tMin, double t
         double th, uh, vh;
         if (!tri_hit(o, d, {g[0], g[1], g[2]}, {g[4], g[5], g[6]}, {g[8], g[9], g[10]}, tMin, closest, th, uh, vh))
           continue;
-        if (g[11] >= 0.5f && !alpha_opaque(s, slot, key)) continue;
+        if (g[11] >= 0.5f && !alpha_opaque(s, slot, key, (float)uh, (float)vh)) continue;
         closest = th;
         h = {slot, th, uh, vh};
       }
@@ -278,7 +336,7 @@ bool any_tri(const orc_scene* s, orc::V3 o, orc::V3 d, double tMin, double tMax,
         double th, uh, vh;
         if (!tri_hit(o, d, {g[0], g[1], g[2]}, {g[4], g[5], g[6]}, {g[8], g[9], g[10]}, tMin, tMax, th, uh, vh))
           continue;
-        if (g[11] >= 0.5f && !alpha_opaque(s, slot, key)) continue;
+        if (g[11] >= 0.5f && !alpha_opaque(s, slot, key, (float)uh, (float)vh)) continue;
         return true;
       }
     } else if (sp + 2 <= 64) {
@@ -525,6 +583,7 @@ struct Tracer {
     bool frontFace;
     int material, light;
     Vec2<R> uv;
+    V dpdu, dpdv;  // zero without texture coordinates (scene.glsl:108-109)
   };
 
   // traceScene (:192-333), triangle part replaced by the binary64 closest hit.
@@ -567,6 +626,7 @@ struct Tracer {
     hit.t = closest;
     hit.position = ro + rd * closest;
     hit.uv = {R(0), R(0)};
+    hit.dpdu = hit.dpdv = {R(0), R(0), R(0)};
     hit.light = -1;
     if (ground) {
       hit.frontFace = rd.y < R(0);
@@ -594,6 +654,13 @@ struct Tracer {
     const R w = R(1) - bary.x - bary.y;
     hit.uv = {uv0.x * w + uv1.x * bary.x + uv2.x * bary.y, uv0.y * w + uv1.y * bary.x + uv2.y * bary.y};
     const V e1 = p1 - p0, e2 = p2 - p0;
+    const Vec2<R> d1 = {uv1.x - uv0.x, uv1.y - uv0.y}, d2 = {uv2.x - uv0.x, uv2.y - uv0.y};
+    const R det = d1.x * d2.y - d1.y * d2.x;
+    if (std::fabs(det) > R(1e-12)) {  // scene.glsl:314-319
+      const R r = R(1) / det;
+      hit.dpdu = (e1 * d2.y - e2 * d1.y) * r;
+      hit.dpdv = (e2 * d1.x - e1 * d2.x) * r;
+    }
     V ng = normalize(cross(e1, e2));
     V ns = normalize(n0 * w + n1 * bary.x + n2 * bary.y);
     hit.frontFace = dot(rd, ng) < R(0);
@@ -978,8 +1045,8 @@ struct Tracer {
     const R l = luminance(c);
     return l > uClamp ? c * (uClamp / l) : c;
   }
-  Surface surfaceAt(const Hit& hit, V& emission) const { return surfaceAtFrom(s->materials, hit, emission); }
-  Surface surfaceAtFrom(const float* mats, const Hit& hit, V& emission) const {  // :72-124 (no texture maps)
+  Surface surfaceAt(const Hit& hit, V wo, V& emission) const { return surfaceAtFrom(s->materials, hit, wo, emission); }
+  Surface surfaceAtFrom(const float* mats, const Hit& hit, V wo, V& emission) const {  // :72-124
     const Material m = fetch_material_from(mats, hit.material);
     Surface sf;
     sf.albedo = f3(m.albedo);
@@ -996,6 +1063,36 @@ struct Tracer {
     emission = f3(m.emission);
     sf.nc = hit.normal;
     sf.n = hit.normal;
+    if (s->tex_size > 0 && std::max(std::max(m.maps[0], m.maps[1]), std::max(m.maps[2], m.maps[3])) >= 0) {
+      const R tu = R(m.uv0[0]) * hit.uv.x + R(m.uv0[1]) * hit.uv.y + R(m.uv0[2]);
+      const R tv = R(m.uv1[0]) * hit.uv.x + R(m.uv1[1]) * hit.uv.y + R(m.uv1[2]);
+      R c[4];
+      if (m.maps[0] >= 0) {
+        sample_layer<R>(s, s->color_maps, m.maps[0], tu, tv, true, c);
+        sf.albedo = sf.albedo * V{c[0], c[1], c[2]};
+      }
+      if (m.maps[1] >= 0) {
+        sample_layer<R>(s, s->data_maps, m.maps[1], tu, tv, false, c);
+        sf.roughness = sf.roughness * c[1];
+        sf.metallic = sf.metallic * c[2];
+      }
+      if (m.maps[3] >= 0) {
+        sample_layer<R>(s, s->color_maps, m.maps[3], tu, tv, true, c);
+        emission = emission * V{c[0], c[1], c[2]};
+      }
+      if (m.maps[2] >= 0 && dot(hit.dpdu, hit.dpdu) > R(0)) {  // :98-110
+        const V N = hit.frontFace ? hit.normal : -hit.normal;
+        const V T = normalize(hit.dpdu - N * dot(N, hit.dpdu));
+        V B = cross(N, T);
+        if (dot(B, -hit.dpdv) < R(0)) B = -B;
+        sample_layer<R>(s, s->data_maps, m.maps[2], tu, tv, false, c);
+        const R tx = (c[0] * R(2) - R(1)) * R(m.normalScale), ty = (c[1] * R(2) - R(1)) * R(m.normalScale);
+        const R tz = c[2] * R(2) - R(1);
+        V mapped = normalize(T * tx + B * ty + N * std::max(tz, R(1e-3)));
+        mapped = hit.frontFace ? mapped : -mapped;
+        if (dot(mapped, wo) > R(1e-3) && dot(mapped, hit.geomNormal) > R(0)) sf.n = mapped;
+      }
+    }
     sf.ior = R(m.ior);
     sf.transmission = R(m.transmission) * (R(1) - sf.metallic);
     sf.emission = emission;
@@ -1059,7 +1156,7 @@ struct Tracer {
       }
       const V wo = -rd;
       V emission;
-      const Surface sf = surfaceAt(hit, emission);
+      const Surface sf = surfaceAt(hit, wo, emission);
       const V ng = hit.geomNormal;
       if (!hit.frontFace && !sf.thinWalled && sf.transmission > R(0))
         throughput = throughput * vexp(-sf.absorption * hit.t);
@@ -1183,8 +1280,8 @@ struct Tracer {
       }
       const V wo = -rd;
       V emission, emission_e;
-      const Surface sf = surfaceAt(hit, emission);
-      const Surface se = surfaceAtFrom(mats, hit, emission_e);
+      const Surface sf = surfaceAt(hit, wo, emission);
+      const Surface se = surfaceAtFrom(mats, hit, wo, emission_e);
       const V ng = hit.geomNormal;
       if (!hit.frontFace && !sf.thinWalled && sf.transmission > R(0)) {
         thr = thr * vexp(-sf.absorption * hit.t);
@@ -1724,6 +1821,108 @@ int orc_bsdf_tuples(const float* in, uint64_t n, int precision, double* out, int
     run(double(0));
   else
     run(float(0));
+  return 0;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ texture arrays
+// buildTextureArrays (renderer.ts:314-333) as the product defines its
+// resampling: box mip chain (2x2 averages, edges clamped, each level stored as
+// 8-bit codes), level of detail log2(max(w, h) / size) in binary64, bilinear
+// taps with edge clamping at ((x + 0.5) / size, (y + 0.5) / size), sRGB
+// decoded before filtering and encoded by the code-value midpoints.
+namespace {
+
+struct TexLevel {
+  std::vector<uint8_t> texels;
+  int w, h;
+};
+
+float tex_decode(uint8_t v, int ch, bool srgb) {
+  const TexelTables& T = texel_tables();
+  return (srgb && ch < 3) ? T.srgb[v] : T.unorm[v];
+}
+
+uint8_t tex_encode(float c, int ch, bool srgb) {
+  if (!(c > 0.f)) return 0;
+  if (srgb && ch < 3) {
+    const float* mid = texel_tables().mid;  // number of midpoints <= c (increasing table)
+    return (uint8_t)(std::upper_bound(mid, mid + 255, c) - mid);
+  }
+  const float v = c * 255.f + 0.5f;
+  return v >= 255.f ? 255 : (uint8_t)v;
+}
+
+float tex_fetch(const TexLevel& L, int x, int y, int ch, bool srgb) {
+  x = x < 0 ? 0 : (x >= L.w ? L.w - 1 : x);
+  y = y < 0 ? 0 : (y >= L.h ? L.h - 1 : y);
+  return tex_decode(L.texels[((size_t)y * L.w + x) * 4 + ch], ch, srgb);
+}
+
+float tex_bilinear(const TexLevel& L, float u, float v, int ch, bool srgb) {
+  const float x = u * (float)L.w - 0.5f, y = v * (float)L.h - 0.5f;
+  const float x0 = std::floor(x), y0 = std::floor(y);
+  const float fx = x - x0, fy = y - y0;
+  const int ix = (int)x0, iy = (int)y0;
+  const float a = tex_fetch(L, ix, iy, ch, srgb), b = tex_fetch(L, ix + 1, iy, ch, srgb);
+  const float c = tex_fetch(L, ix, iy + 1, ch, srgb), d = tex_fetch(L, ix + 1, iy + 1, ch, srgb);
+  const float top = a * (1.f - fx) + b * fx, bottom = c * (1.f - fx) + d * fx;
+  return top * (1.f - fy) + bottom * fy;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t orc_texture_size(const uint32_t* w, const uint32_t* h, uint32_t n) {
+  if (n == 0) return 0;
+  uint32_t largest = 1;
+  for (uint32_t i = 0; i < n; i++) largest = std::max(largest, std::max(w[i], h[i]));
+  uint32_t size = 1;
+  while (size < largest) size <<= 1;
+  size = std::min<uint32_t>(size, 2048);
+  while (size > 256 && (uint64_t)n * size * size * 4 > (256ull << 20)) size /= 2;
+  return size;
+}
+
+int orc_resample_layer(const uint8_t* rgba, uint32_t w, uint32_t h, uint32_t size, int srgb, uint8_t* out) {
+  if (!rgba || !out || !w || !h || !size) return 1;
+  const bool sr = srgb != 0;
+  const double rho = (double)std::max(w, h) / size;
+  const double lambda = rho > 1.0 ? std::log2(rho) : 0.0;
+  const int d1 = (int)std::floor(lambda);
+  std::vector<TexLevel> L(1);
+  L[0].texels.assign(rgba, rgba + (size_t)w * h * 4);
+  L[0].w = (int)w;
+  L[0].h = (int)h;
+  for (int k = 1; k <= d1 + 1; k++) {
+    const TexLevel& src = L[k - 1];
+    if (src.w == 1 && src.h == 1) break;
+    TexLevel dst;
+    dst.w = src.w > 1 ? src.w / 2 : 1;
+    dst.h = src.h > 1 ? src.h / 2 : 1;
+    dst.texels.resize((size_t)dst.w * dst.h * 4);
+    for (int y = 0; y < dst.h; y++)
+      for (int x = 0; x < dst.w; x++)
+        for (int ch = 0; ch < 4; ch++) {
+          const float s4 = tex_fetch(src, 2 * x, 2 * y, ch, sr) + tex_fetch(src, 2 * x + 1, 2 * y, ch, sr) +
+                           tex_fetch(src, 2 * x, 2 * y + 1, ch, sr) + tex_fetch(src, 2 * x + 1, 2 * y + 1, ch, sr);
+          dst.texels[((size_t)y * dst.w + x) * 4 + ch] = tex_encode(s4 * 0.25f, ch, sr);
+        }
+    L.push_back(std::move(dst));
+  }
+  const int nlev = (int)L.size();
+  const int a = std::min(d1, nlev - 1), b = std::min(a + 1, nlev - 1);
+  const float blend = b > a ? (float)(lambda - d1) : 0.f;
+  for (uint32_t i = 0; i < size * size; i++) {
+    const float u = ((float)(i % size) + 0.5f) / (float)size, v = ((float)(i / size) + 0.5f) / (float)size;
+    for (int ch = 0; ch < 4; ch++) {
+      float c = tex_bilinear(L[a], u, v, ch, sr);
+      if (blend > 0.f) c = c * (1.f - blend) + tex_bilinear(L[b], u, v, ch, sr) * blend;
+      out[(size_t)i * 4 + ch] = tex_encode(c, ch, sr);
+    }
+  }
   return 0;
 }
 

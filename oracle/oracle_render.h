@@ -46,6 +46,11 @@ typedef struct orc_scene {
   int32_t env_sampling, env_background;
   float backdrop[3];
   const float* sheen_lut;     /* 16x16, already rounded to half precision */
+  /* texture arrays (scene.glsl:17-18): tex_size^2 RGBA8 texels per layer, row 0 at v = 0;
+   * colour layers hold sRGB codes. tex_size 0: no textures. */
+  const uint8_t* color_maps;
+  const uint8_t* data_maps;
+  uint32_t tex_size;
 } orc_scene;
 
 typedef struct orc_camera {
@@ -72,6 +77,15 @@ int orc_render_work(const orc_scene* s, const orc_camera* cam, uint32_t max_boun
                     uint32_t width, uint32_t height, uint32_t x0, uint32_t y0, uint32_t cw, uint32_t ch,
                     uint32_t seed0, uint32_t samples, float* color4, float* albedo4, float* normal4,
                     float* history, int threads, int detailed, uint64_t* work_out);
+
+/* One texture-array layer from a decoded RGBA8 image (rows top to bottom):
+ * the resampling of buildTextureArrays (renderer.ts:314-333, resample.frag)
+ * as the product defines it (box mip chain, level of detail log2(max(w, h) /
+ * size) in binary64, bilinear with edge clamping, sRGB decoded before
+ * filtering and re-encoded by code-value midpoints when srgb != 0). */
+int orc_resample_layer(const uint8_t* rgba, uint32_t w, uint32_t h, uint32_t size, int srgb, uint8_t* out);
+/* The shared layer size of buildTextureArrays for these image sizes. */
+uint32_t orc_texture_size(const uint32_t* w, const uint32_t* h, uint32_t n);
 
 /* BSDF tuples (bsdf.glsl): for each tuple evaluates evalOpaque, and
  * sampleOpaque / sampleDielectric driven by the given uniforms instead of the

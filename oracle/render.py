@@ -25,7 +25,8 @@ class OrcScene(C.Structure):
                 ("sun_cos_angle", F), ("sun_pdf", F), ("env_width", U32), ("env_height", U32),
                 ("env_rgb", P(F)), ("env_grid_w", U32), ("env_grid_h", U32), ("env_alias", P(F)),
                 ("env_rot_cos", F), ("env_rot_sin", F), ("env_intensity", F), ("env_sampling", I32),
-                ("env_background", I32), ("backdrop", F * 3), ("sheen_lut", P(F))]
+                ("env_background", I32), ("backdrop", F * 3), ("sheen_lut", P(F)), ("color_maps", P(C.c_uint8)),
+                ("data_maps", P(C.c_uint8)), ("tex_size", U32)]
 
 
 class OrcCamera(C.Structure):
@@ -44,6 +45,9 @@ def declare(L):
     L.orc_detached_dot.argtypes = [P(OrcScene), P(OrcCamera), U32, F, U32, U32, U32, U32, P(F), P(F), P(F), C.c_int]
     L.orc_detached_dot.restype = C.c_double
     L.orc_display.argtypes = [P(F), P(F), P(F), U32, U32, F, F, C.c_int, P(F)]
+    L.orc_resample_layer.argtypes = [P(C.c_uint8), U32, U32, U32, C.c_int, P(C.c_uint8)]
+    L.orc_texture_size.argtypes = [P(U32), P(U32), U32]
+    L.orc_texture_size.restype = U32
 
 
 def half_lut():
@@ -54,7 +58,7 @@ def half_lut():
 class Prepared:
     """A packed scene + lighting ready for orc_render (arrays kept alive here)."""
 
-    def __init__(self, packed, lighting, camera, ground=None):
+    def __init__(self, packed, lighting, camera, ground=None, textures=()):
         from lucent_gb300 import scene as S
         self.keep = []
         keep = self.keep.append
@@ -116,6 +120,12 @@ class Prepared:
         lut = half_lut()
         keep(lut)
         s.sheen_lut = _p(lut, F)
+        self.color_maps, self.data_maps, self.tex_size = texture_arrays(textures, p.color_layers, p.data_layers)
+        keep(self.color_maps)
+        keep(self.data_maps)
+        s.color_maps = _p(self.color_maps, C.c_uint8)
+        s.data_maps = _p(self.data_maps, C.c_uint8)
+        s.tex_size = self.tex_size
         self.scene = s
         f, r, u = S.camera_basis(camera)
         cam = OrcCamera()
@@ -126,9 +136,36 @@ class Prepared:
         self.camera = cam
 
 
+def resample_layer(rgba, size, srgb):
+    """orc_resample_layer: one texture-array layer [size, size, 4] uint8 from an RGBA8 image."""
+    img = np.ascontiguousarray(rgba, np.uint8)
+    out = np.zeros((size, size, 4), np.uint8)
+    if lib().orc_resample_layer(_p(img, C.c_uint8), img.shape[1], img.shape[0], size, 1 if srgb else 0,
+                                _p(out, C.c_uint8)):
+        raise RuntimeError("orc_resample_layer failed")
+    return out
+
+
+def texture_arrays(textures, color_layers, data_layers):
+    """(colour array, data array, size) of buildTextureArrays (renderer.ts:314-333)."""
+    used = list(color_layers) + list(data_layers)
+    if not used:
+        return np.zeros(4, np.uint8), np.zeros(4, np.uint8), 0
+    w = np.array([textures[t].image.shape[1] for t in used], np.uint32)
+    h = np.array([textures[t].image.shape[0] for t in used], np.uint32)
+    size = int(lib().orc_texture_size(_p(w, U32), _p(h, U32), len(used)))
+    arrays = []
+    for layers, srgb in ((color_layers, True), (data_layers, False)):
+        arr = np.zeros((max(1, len(layers)), size, size, 4), np.uint8)
+        for i, t in enumerate(layers):
+            arr[i] = resample_layer(textures[t].image, size, srgb)
+        arrays.append(arr)
+    return arrays[0], arrays[1], size
+
+
 def prepare(scene):
     from lucent_gb300 import scene as S
-    return Prepared(S.pack_scene(scene), S.lighting(scene), scene.camera, scene.ground)
+    return Prepared(S.pack_scene(scene), S.lighting(scene), scene.camera, scene.ground, scene.textures)
 
 
 def render(prep, width, height, seed0, samples, max_bounces=6, clamp=8.0, precision=32, crop=None, threads=0):
