@@ -25,6 +25,7 @@ struct ApiPolicy {
   __device__ void ray(uint32_t k, float3& o, float3& d) const { load_ray6(rays, k, o, d); }
   __device__ uint32_t key(uint32_t) const { return 0; }
   static constexpr bool kMultiScene = false;
+  static constexpr int kThreads = 128, kMinBlocks = 7;  // closest-hit block shape
   __device__ bool alpha(int, int, uint32_t, float, float) const { return true; }
   __device__ AlphaAnswer alpha_fast(int, int, uint32_t) const { return kAlphaBlock; }
   __device__ bool alpha_any() const { return false; }
@@ -148,9 +149,9 @@ void launch_closest(const Node* nodes, uint32_t node_count, const float4* tris, 
     return;
   }
   static int blocks = 0;
-  if (!blocks) blocks = persistent_blocks((const void*)k_closest_fast_t<ApiPolicy>, 256);
-  const int want = (int)((n + 255) / 256);
-  k_closest_fast_t<ApiPolicy><<<want < blocks ? want : blocks, 256, top_smem_bytes(A.top_scenes), s>>>(A, P);
+  if (!blocks) blocks = persistent_blocks((const void*)k_closest_fast_t<ApiPolicy>, ApiPolicy::kThreads);
+  const int want = (int)((n + ApiPolicy::kThreads - 1) / ApiPolicy::kThreads);
+  k_closest_fast_t<ApiPolicy><<<want < blocks ? want : blocks, ApiPolicy::kThreads, top_smem_bytes(A.top_scenes), s>>>(A, P);
   // Slow path over the rays the fast kernel queued (length read on the device).
   k_closest_exact_t<ApiPolicy><<<grid_for(n < 4096 ? n : 4096, 128), 128, 0, s>>>(A, P);
 }

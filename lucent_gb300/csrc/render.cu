@@ -31,9 +31,9 @@ using namespace sh;
 
 // Closest-hit rays of a wave. Ray k is path queue[k], read from the path
 // state; after a ray sort the rays come instead from the sorted stream `sray`
-// (contiguous, in sort order, with the path id and scene beside them), so the
-// traversal reads its rays in order while the queue keeps path order for the
-// kernels that touch the rest of the path state.
+// (contiguous, in the sorted queue's order, with the path id and scene
+// beside them). The hit of ray k is written to hits[k]: the shade kernel
+// walks the same queue and reads it at the same position, both in order.
 struct PathClosestMulti {
   const uint32_t* cnt;
   const uint32_t* queue;
@@ -46,6 +46,7 @@ struct PathClosestMulti {
   int any_alpha;
   const float4* sray;  // null: no sort this bounce
   static constexpr bool kMultiScene = true;
+  static constexpr int kThreads = 256, kMinBlocks = 3;  // closest-hit block shape
   __device__ uint32_t count() const { return *cnt; }
   __device__ uint32_t path(uint32_t k) const { return sray ? __float_as_uint(sray[2 * (size_t)k].w) : queue[k]; }
   __device__ void ray(uint32_t k, float3& o, float3& d) const {
@@ -79,12 +80,12 @@ struct PathClosestMulti {
   }
   __device__ bool exact_output() const { return false; }
   __device__ void hit32(uint32_t k, int slot, float3 e) const {
-    hits[path(k)] = make_float4(e.x, e.y, e.z, __int_as_float(slot));
+    hits[k] = make_float4(e.x, e.y, e.z, __int_as_float(slot));
   }
   __device__ void hit(uint32_t k, int slot, double t, double u, double v) const {
-    hits[path(k)] = make_float4(__double2float_rn(t), __double2float_rn(u), __double2float_rn(v), __int_as_float(slot));
+    hits[k] = make_float4(__double2float_rn(t), __double2float_rn(u), __double2float_rn(v), __int_as_float(slot));
   }
-  __device__ void miss(uint32_t k) const { hits[path(k)] = make_float4(INF, 0.f, 0.f, __int_as_float(-1)); }
+  __device__ void miss(uint32_t k) const { hits[k] = make_float4(INF, 0.f, 0.f, __int_as_float(-1)); }
   __device__ void fail(uint32_t k) const { miss(k); }
 };
 
@@ -299,8 +300,8 @@ struct MapSample {
   bool mapped;
 };
 static __device__ __forceinline__ MapSample sample_maps(const SceneDev& S, const float4* M, float4 maps, int slot,
-                                                     const float4* hit, float3 pos, float3 rd, float3 normal,
-                                                     float3 gn, bool front) {
+                                                        float4 hit, float3 pos, float3 rd, float3 normal, float3 gn,
+                                                        bool front) {
   MapSample out{f3(1.f, 1.f, 1.f), f3(1.f, 1.f, 1.f), normal, 1.f, 1.f, false};
   // hit.uv and the surface derivatives (scene.glsl:274-320)
   float2 huv = make_float2(0.f, 0.f);
@@ -308,7 +309,7 @@ static __device__ __forceinline__ MapSample sample_maps(const SceneDev& S, const
   if (slot == -1) {
     huv = make_float2(pos.x, pos.z);
   } else if (slot >= 0) {
-    const float4 h = *hit;
+    const float4 h = hit;
     const float4* a = S.attr + 4 * (size_t)slot;
     const float4* g = S.geo + 3 * (size_t)slot;
     const float4 a3 = __ldg(a + 3), p0 = __ldg(g), p1 = __ldg(g + 1), p2 = __ldg(g + 2);
@@ -363,10 +364,11 @@ template <class Src, bool ADJ = false, bool TEX = false>
 __global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_constant__ Src src, int cur, int bounce,
                                                     const __grid_constant__ AdjointDev A = AdjointDev{}) {
   const uint32_t n = TEX ? P.ctr[kCtrTex] : P.ctr[kCtrQ0 + cur];
-  const uint32_t* q = TEX ? P.qtex : P.q[cur];
+  const uint32_t* q = P.q[cur];
   uint32_t* qn = P.q[cur ^ 1];
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const uint32_t p = q[k];
+    const uint32_t kq = TEX ? P.qtex[k] : k;  // position in queue `cur`, which also indexes the hits
+    const uint32_t p = q[kq];
     const SceneDev& S = src.scene(p);
     const LightingDev& L = src.light(p);
     const int max_bounces = src.bounces(p);
@@ -379,7 +381,7 @@ __global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_consta
     bool spec = flags & kSpecular, done = flags & kGuideDone;
     float4 galb = P.galb[p], gnrm = P.gnrm[p];
     uint32_t st = P.rng[p];
-    const float4 hv = P.hit[p];
+    const float4 hv = P.hit[kq];
     bool alive = false, deferred = false;
     float3 dl = f3(0.f, 0.f, 0.f), lrem = f3(0.f, 0.f, 0.f);
     int cont_mat = -1;
@@ -499,7 +501,7 @@ __global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_consta
           break;
         } else {
           const MapSample ms =
-              sample_maps(S, M, m4, ground ? -1 : (tri ? slot : -2), P.hit + p, pos, rd, normal, gn, front);
+              sample_maps(S, M, m4, ground ? -1 : (tri ? slot : -2), hv, pos, rd, normal, gn, front);
           s.albedo = s.albedo * ms.albedo;
           s.roughness *= ms.roughness;
           s.metallic *= ms.metallic;
@@ -655,7 +657,7 @@ __global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_consta
       if (!alive) cont_mat = -1;
     } while (false);
     if (deferred) {
-      P.qtex[atomicAdd(&P.ctr[kCtrTex], 1u)] = p;
+      P.qtex[atomicAdd(&P.ctr[kCtrTex], 1u)] = kq;
       continue;
     }
     if (adj) {
@@ -1019,7 +1021,7 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
   E.mark(kPhCamera, s);
   static int max_closest = 0, max_shade = 0;
   if (!max_closest) {
-    max_closest = persistent_blocks((const void*)k_closest_fast_t<PathClosestMulti>, 256);
+    max_closest = persistent_blocks((const void*)k_closest_fast_t<PathClosestMulti>, PathClosestMulti::kThreads);
     max_shade = persistent_blocks((const void*)k_shade_t<SceneTable>, 128);
   }
   const int closest_blocks = M.trace_blocks > 0 ? M.trace_blocks : max_closest;
@@ -1034,7 +1036,7 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
                         M.recs, M.sid, M.any_alpha, sorted ? P.sray : nullptr};
     TravArgs A{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
                M.trav_stats, top};
-    k_closest_fast_t<PathClosestMulti><<<closest_blocks, 256, top_smem_bytes(top), s>>>(A, pc);
+    k_closest_fast_t<PathClosestMulti><<<closest_blocks, PathClosestMulti::kThreads, top_smem_bytes(top), s>>>(A, pc);
     k_closest_exact_t<PathClosestMulti><<<64, 128, 0, s>>>(A, pc);
     E.mark(kPhClosest, s);
     k_shade_t<SceneTable><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b);
@@ -1071,7 +1073,7 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
   const SceneRec* rec = M.recs;
   static int closest_blocks = 0, shade_blocks = 0;
   if (!closest_blocks) {
-    closest_blocks = persistent_blocks((const void*)k_closest_fast_t<PathClosestMulti>, 256);
+    closest_blocks = persistent_blocks((const void*)k_closest_fast_t<PathClosestMulti>, PathClosestMulti::kThreads);
     shade_blocks = persistent_blocks((const void*)k_shade_t<SceneTable, true>, 128);
   }
   const int top = M.top_levels ? (M.n < kTopMaxScenes ? M.n : kTopMaxScenes) : 0;
@@ -1084,7 +1086,7 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
       PathClosestMulti pc{P.ctr + kCtrQ0 + cur, P.q[cur], P.ro, P.rd, P.rng, P.hit, M.recs, M.sid, M.any_alpha, nullptr};
       TravArgs TA{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
                   nullptr, top};
-      k_closest_fast_t<PathClosestMulti><<<closest_blocks, 256, top_smem_bytes(top), s>>>(TA, pc);
+      k_closest_fast_t<PathClosestMulti><<<closest_blocks, PathClosestMulti::kThreads, top_smem_bytes(top), s>>>(TA, pc);
       k_closest_exact_t<PathClosestMulti><<<64, 128, 0, s>>>(TA, pc);
       k_shade_t<SceneTable, true><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b, A);
       PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};

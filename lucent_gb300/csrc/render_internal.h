@@ -48,7 +48,7 @@ struct Paths {
   uint32_t* sort_keys;  // per queued path: ray-sort key (scene, direction octant, origin cell)
   float4* sray;         // sorted ray stream: 2 float4 per queued ray (origin + path id, direction + scene)
   uint32_t* sort_tmp;   // the sorted queue, swapped with the queue it sorts
-  uint32_t* qtex;       // paths whose hit material is texture-mapped (shaded by the TEX instantiation)
+  uint32_t* qtex;       // queue positions of hits on texture-mapped materials (shaded by the TEX instantiation)
   uint32_t* sort_hist;  // kSortBins counters
   uint32_t* ctr;
 };

@@ -223,8 +223,13 @@ __global__ void k_closest_exact_t(TravArgs A, Pol P) {
 // an upper bound on its entry distance and re-tested on pop only if `c` has
 // dropped below it (the cull test is monotone in `c`). `c` is carried as
 // binary32 bounds [c_lo, c_hi] of the reference's binary64 value.
+// Block shape of the fast closest-hit kernel, per policy (Pol::kThreads,
+// Pol::kMinBlocks): the register budget 65,536 / (threads x blocks) per
+// thread sets the resident warps per SM. Deep traversals of long rays (the
+// BVH API) gain from 28 warps at 72 registers; the renderer's short rays
+// lose more to the extra spills and keep 24 warps at 80 (measured).
 template <class Pol>
-__global__ void __launch_bounds__(256, 3) k_closest_fast_t(TravArgs A, Pol P) {
+__global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_fast_t(TravArgs A, Pol P) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
