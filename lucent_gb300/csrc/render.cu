@@ -37,8 +37,8 @@ using namespace sh;
 struct PathClosestMulti {
   const uint32_t* cnt;
   const uint32_t* queue;
-  const float4* ro;
-  const float4* rd;
+  PathField ro;
+  PathField rd;
   const uint32_t* rng;
   float4* hits;
   const SceneRec* recs;

@@ -244,13 +244,14 @@ static lucent_status alloc_targets(lucent_renderer* r, uint32_t w, uint32_t h) {
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "clear targets");
 }
 
-// Path buffers for `cap` paths (bytes per path: 8 float4 + rng + 2 queue
-// entries + 3 shadow slots of 3 float4, a flag and a queue entry).
+// Path buffers for `cap` paths (bytes per path: the 128-byte path record, the
+// radiance, the hit, 3 shadow slots of 3 float4, rng, occlusion flags, queues, slow-path
+// queues, the sort key, the sorted ray stream, the sorted and textured-hit queues).
 static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, uint32_t& path_cap, Paths& P,
                                         uint32_t cap) {
   if (cap <= path_cap) return LUCENT_OK;
   // Per-path arrays in allocation order (bytes per path); each starts on a 256-byte boundary.
-  static const size_t kPer[] = {16, 16, 16, 16, 16, 16, 16, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12, 4, 32, 4, 4};
+  static const size_t kPer[] = {16 * kPathRecord, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12, 4, 32, 4, 4};
   size_t total = 0;
   for (size_t b : kPer) total += ((size_t)cap * b + 255) & ~(size_t)255;
   total += (size_t)kSortBins * 4;
@@ -264,15 +265,16 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
     off += (bytes + 255) & ~(size_t)255;
     return (void*)p;
   };
-  P.ro = (float4*)take((size_t)cap * 16);
-  P.rd = (float4*)take((size_t)cap * 16);
-  P.thr = (float4*)take((size_t)cap * 16);
+  P.rec = (float4*)take((size_t)cap * 16 * kPathRecord);
+  P.ro = {P.rec};
+  P.rd = {P.rec + 1};
+  P.thr = {P.rec + 2};
+  P.tint = {P.rec + 3};
+  P.galb = {P.rec + 4};
+  P.gnrm = {P.rec + 5};
+  P.gpos = {P.rec + 6};
   P.rad = (float4*)take((size_t)cap * 16);
-  P.tint = (float4*)take((size_t)cap * 16);
-  P.galb = (float4*)take((size_t)cap * 16);
-  P.gnrm = (float4*)take((size_t)cap * 16);
   P.hit = (float4*)take((size_t)cap * 16);
-  P.gpos = (float4*)take((size_t)cap * 16);
   P.sh_o = (float4*)take((size_t)cap * 48);
   P.sh_d = (float4*)take((size_t)cap * 48);
   P.sh_c = (float4*)take((size_t)cap * 48);
@@ -1130,7 +1132,7 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
     M.pix_base = (const uint32_t*)base.ptr + (n + 1);
   };
   const uint64_t key[4] = {S | ((uint64_t)n << 32), pixels | ((uint64_t)b->opt.trace_blocks << 40),
-                           (uint64_t)(uintptr_t)b->P.ro ^ ((uint64_t)max_bounces << 48) ^ ((uint64_t)b->opt.shade_blocks << 56),
+                           (uint64_t)(uintptr_t)b->P.rec ^ ((uint64_t)max_bounces << 48) ^ ((uint64_t)b->opt.shade_blocks << 56),
                            (uint64_t)(uintptr_t)b->recs.ptr ^ ((uint64_t)any_alpha << 63)};
   const uint32_t full = samples / (uint32_t)S;
   for (uint32_t w = 0; w < full; w++) {

@@ -35,9 +35,25 @@ __device__ __forceinline__ half4 make_half4(float4 v) {
 }
 
 // Structure-of-arrays path state; shadow slots are 3 per path (sun, env, light).
+// Path state lives in one 128-byte record per path (8 float4: origin,
+// direction, throughput + bsdf pdf, guide tint + flags, guide albedo, guide
+// normal + depth, guide position + reuse, unused); field f of path p is
+// float4 number f of record p. A kernel that walks paths in sorted (not path)
+// order then touches one DRAM line per path instead of one per field. The
+// radiance has its own array: the resolve kernel, which touches nothing
+// else, reads and writes it in path order.
+constexpr int kPathRecord = 8;
+struct PathField {
+  float4* base;  // the field in record 0
+  __host__ __device__ float4& operator[](size_t p) const { return base[p * kPathRecord]; }
+};
+
 struct Paths {
-  float4 *ro, *rd, *thr, *rad, *tint, *galb, *gnrm, *hit;
-  float4* gpos;  // guide: primary hit position (xyz) and how much history it may reuse (w)
+  float4* rec;  // path records
+  PathField ro, rd, thr, tint, galb, gnrm;
+  PathField gpos;  // guide: primary hit position (xyz) and how much history it may reuse (w)
+  float4* rad;     // radiance per path
+  float4* hit;     // closest hit per position of the bounce's queue
   float4 *sh_o, *sh_d, *sh_c;
   uint32_t* rng;
   uint8_t* sh_occ;
