@@ -17,6 +17,9 @@ namespace sh {
 #ifndef LUCENT_BSDF_FN
 #define LUCENT_BSDF_FN LUCENT_DEV
 #endif
+#ifndef LUCENT_SAMPLE_FN
+#define LUCENT_SAMPLE_FN LUCENT_DEV
+#endif
 
 constexpr float PI = 3.14159265358979323846f;
 constexpr float INV_PI = 0.31830988618379067154f;
@@ -717,7 +720,7 @@ struct BsdfSample {
 
 // sampleOpaque (bsdf.glsl:174-211); `U` draws the uniforms in the GLSL order.
 template <class UF>
-LUCENT_DEV BsdfSample sample_opaque(const LightingDev& L, const Surface& s, float3 wo, UF&& U) {
+LUCENT_SAMPLE_FN BsdfSample sample_opaque(const LightingDev& L, const Surface& s, float3 wo, UF&& U) {
   BsdfSample bs;
   bs.pdf = 0.f;
   bs.weight = f3(0.f, 0.f, 0.f);
