@@ -100,9 +100,8 @@ struct PathShadowMulti {
   int any_alpha;
   static constexpr bool kMultiScene = true;
   __device__ uint32_t count() const { return *cnt; }
-  __device__ void ray(uint32_t k, float3& o, float3& d) const {
-    const uint32_t s = queue[k];
-    const float4 a = so[s], b = sd[s];
+  __device__ void ray(uint32_t k, float3& o, float3& d) const {  // rays are stored in queue order
+    const float4 a = so[k], b = sd[k];
     o = make_float3(a.x, a.y, a.z);
     d = make_float3(b.x, b.y, b.z);
   }
@@ -111,8 +110,8 @@ struct PathShadowMulti {
     const SceneDev& S = recs[sc].scene;
     return {S.nodes, S.geo, S.node_count, sc};
   }
-  __device__ double tmax(uint32_t k) const { return (double)so[queue[k]].w; }
-  __device__ uint32_t key(uint32_t k) const { return __float_as_uint(sd[queue[k]].w); }
+  __device__ double tmax(uint32_t k) const { return (double)so[k].w; }
+  __device__ uint32_t key(uint32_t k) const { return __float_as_uint(sd[k].w); }
   __device__ bool alpha_any() const { return any_alpha != 0; }
   __device__ bool alpha(int sc, int slot, uint32_t key, float bu, float bv) const {
     return alpha_opaque(recs[sc].scene, slot, key, bu, bv);
@@ -185,14 +184,19 @@ __device__ __forceinline__ float3 clamp_c(float3 c, int bounce, float uclamp) { 
   return l > uclamp ? c * (uclamp / l) : c;
 }
 
-// Shadow slot: origin + tmax, direction + alpha key, contribution + pending.
+// Shadow ray j of path p: its slot s = 3p + j holds the contribution +
+// pending flag (and, after the any-hit launch, the occlusion flag), read by
+// resolve per path; the ray itself (origin + tmax, direction + alpha key) is
+// stored at its position in the shadow queue, so the any-hit kernel reads
+// the rays in order.
 __device__ __forceinline__ void emit_shadow(const Paths& P, uint32_t p, int j, float3 o, float3 d, float tmax,
                                             uint32_t key, float3 c) {
   const uint32_t s = 3 * p + j;
-  P.sh_o[s] = make_float4(o.x, o.y, o.z, tmax);
-  P.sh_d[s] = make_float4(d.x, d.y, d.z, __uint_as_float(key));
   P.sh_c[s] = make_float4(c.x, c.y, c.z, 1.f);
-  P.qs[atomicAdd(&P.ctr[kCtrShadow], 1u)] = s;
+  const uint32_t pos = atomicAdd(&P.ctr[kCtrShadow], 1u);
+  P.sh_o[pos] = make_float4(o.x, o.y, o.z, tmax);
+  P.sh_d[pos] = make_float4(d.x, d.y, d.z, __uint_as_float(key));
+  P.qs[pos] = s;
 }
 
 __device__ __forceinline__ bool analytic_occluded(const SceneDev& S, float3 ro, float3 rd, float tmax) {
