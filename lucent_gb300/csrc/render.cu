@@ -29,43 +29,28 @@ using namespace sh;
 // Policies for waves holding the paths of several scenes: a path's scene is
 // sid[path]; its BVH, triangles and materials come from the scene table.
 
-// Closest-hit rays of a wave. Ray k is path queue[k], read from the path
-// state; after a ray sort the rays come instead from the sorted stream `sray`
-// (contiguous, in the sorted queue's order, with the path id and scene
-// beside them). The hit of ray k is written to hits[k]: the shade kernel
-// walks the same queue and reads it at the same position, both in order.
+// Closest-hit rays of a wave, read in order from a ray stream: ray k of the
+// bounce's queue (origin + path id, direction + scene), written by the
+// camera or shade kernel at the path's queue position (`nray`), or by the
+// ray sort in sorted order (`sray`). The hit of ray k is written to hits[k]:
+// the shade kernel walks the same queue and reads it at the same position.
 struct PathClosestMulti {
   const uint32_t* cnt;
-  const uint32_t* queue;
-  PathField ro;
-  PathField rd;
+  const float4* rays;  // 2 float4 per ray: origin + path id, direction + scene
   const uint32_t* rng;
   float4* hits;
   const SceneRec* recs;
-  const uint16_t* sid;
   int any_alpha;
-  const float4* sray;  // null: no sort this bounce
   static constexpr bool kMultiScene = true;
   static constexpr int kThreads = 256, kMinBlocks = 3;  // closest-hit block shape
   __device__ uint32_t count() const { return *cnt; }
-  __device__ uint32_t path(uint32_t k) const { return sray ? __float_as_uint(sray[2 * (size_t)k].w) : queue[k]; }
+  __device__ uint32_t path(uint32_t k) const { return __float_as_uint(rays[2 * (size_t)k].w); }
   __device__ void ray(uint32_t k, float3& o, float3& d) const {
-    float4 a, b;
-    if (sray) {
-      a = sray[2 * (size_t)k];
-      b = sray[2 * (size_t)k + 1];
-    } else {
-      const uint32_t p = queue[k];
-      a = ro[p];
-      b = rd[p];
-    }
+    const float4 a = rays[2 * (size_t)k], b = rays[2 * (size_t)k + 1];
     o = make_float3(a.x, a.y, a.z);
     d = make_float3(b.x, b.y, b.z);
   }
-  __device__ BvhView bvh(uint32_t k) const {
-    const int sc = sray ? __float_as_int(sray[2 * (size_t)k + 1].w) : (int)__ldg(sid + queue[k]);
-    return scene_bvh(sc);
-  }
+  __device__ BvhView bvh(uint32_t k) const { return scene_bvh(__float_as_int(rays[2 * (size_t)k + 1].w)); }
   __device__ BvhView scene_bvh(int sc) const {
     const SceneDev& S = recs[sc].scene;
     return {S.nodes, S.geo, S.node_count, sc};
@@ -128,7 +113,7 @@ constexpr unsigned kSpecular = 1u, kGuideDone = 2u;
 // cameraRay (trace.frag:53-62) and the path's initial state; sample s of
 // pixel `pixel` draws from the stream seeded with (pixel, seed0 + s).
 __device__ __forceinline__ void camera_path(const Paths& P, uint32_t p, uint32_t pixel, uint32_t s,
-                                            const CameraDev& cam, int W, int H, uint32_t seed0) {
+                                            const CameraDev& cam, int W, int H, uint32_t seed0, int scene) {
   const uint32_t x = pixel % W, y = pixel / W;
   uint32_t st = pixel * 1973u + (seed0 + s) * 9277u + 26699u;  // trace.frag:327-328
   pcg(st);
@@ -152,6 +137,8 @@ __device__ __forceinline__ void camera_path(const Paths& P, uint32_t p, uint32_t
   P.gpos[p] = make_float4(0.f, 0.f, 0.f, 1.f);
   P.rng[p] = st;
   P.q[0][p] = p;
+  P.nray[2 * (size_t)p] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(p));
+  P.nray[2 * (size_t)p + 1] = make_float4(rd.x, rd.y, rd.z, __int_as_float(scene));
 }
 
 // Index of the scene whose range [base[i], base[i + 1]) holds v (n scenes).
@@ -172,7 +159,7 @@ __global__ void k_camera_multi(Paths P, const SceneRec* __restrict__ recs, const
     const int sc = find_scene(path_base, n, p);
     const SceneRec& R = recs[sc];
     const uint32_t WH = (uint32_t)R.W * R.H, local = p - __ldg(path_base + sc);
-    camera_path(P, p, local % WH, local / WH, R.cam, R.W, R.H, R.seed0);
+    camera_path(P, p, local % WH, local / WH, R.cam, R.W, R.H, R.seed0, sc);
     sid[p] = (uint16_t)sc;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) P.ctr[kCtrQ0] = total;
@@ -287,7 +274,8 @@ __device__ __forceinline__ void nee_grad(const AdjointDev& A, const LightingDev&
 struct SceneTable {
   const SceneRec* recs;
   const uint16_t* sid;
-  __device__ const SceneRec& rec(uint32_t p) const { return recs[__ldg(sid + p)]; }
+  __device__ int index(uint32_t p) const { return __ldg(sid + p); }
+  __device__ const SceneRec& rec(uint32_t p) const { return recs[index(p)]; }
   __device__ const SceneDev& scene(uint32_t p) const { return rec(p).scene; }
   __device__ const LightingDev& light(uint32_t p) const { return rec(p).light; }
   __device__ int bounces(uint32_t p) const { return rec(p).max_bounces; }
@@ -678,7 +666,10 @@ __global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_consta
       P.rd[p] = make_float4(rd.x, rd.y, rd.z, 0.f);
       P.thr[p] = make_float4(thr.x, thr.y, thr.z, bsdf_pdf);
       P.tint[p] = make_float4(tint.x, tint.y, tint.z, __uint_as_float((spec ? kSpecular : 0u) | (done ? kGuideDone : 0u)));
-      qn[atomicAdd(&P.ctr[kCtrQ0 + (cur ^ 1)], 1u)] = p;
+      const uint32_t pos = atomicAdd(&P.ctr[kCtrQ0 + (cur ^ 1)], 1u);
+      qn[pos] = p;
+      P.nray[2 * (size_t)pos] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(p));
+      P.nray[2 * (size_t)pos + 1] = make_float4(rd.x, rd.y, rd.z, __int_as_float(src.index(p)));
     }
   }
 }
@@ -912,16 +903,13 @@ __device__ __forceinline__ uint32_t spread3(uint32_t x) {  // 4 bits -> every th
   return x;
 }
 
-__global__ void k_sort_keys(Paths P, const SceneRec* __restrict__ recs, const uint16_t* __restrict__ sid, int n_scenes,
-                            int nxt) {
+__global__ void k_sort_keys(Paths P, const SceneRec* __restrict__ recs, int n_scenes, int nxt) {
   const uint32_t n = P.ctr[kCtrQ0 + nxt];
-  const uint32_t* q = P.q[nxt];
   int sbits = 0;
   while ((1 << sbits) < n_scenes) sbits++;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const uint32_t p = q[k];
-    const float4 o = P.ro[p], d = P.rd[p];
-    const int sc = n_scenes > 1 ? __ldg(sid + p) : 0;
+    const float4 o = P.nray[2 * (size_t)k], d = P.nray[2 * (size_t)k + 1];  // the queue's rays, in order
+    const int sc = __float_as_int(d.w);
     const Node* nodes = recs[sc].scene.nodes;
     const float4 lo = __ldg(reinterpret_cast<const float4*>(nodes)), hi = __ldg(reinterpret_cast<const float4*>(nodes) + 1);
     auto cell = [](float v, float a, float b) {
@@ -978,9 +966,9 @@ __global__ void __launch_bounds__(1024) k_sort_scan(uint32_t* __restrict__ hist)
   for (int j = 0; j < kSteps; j++) seg[j * 32 + lane] = base + v[j];
 }
 
-// Writes each queued ray (read in queue order, so coalesced) to its sorted
-// position in the ray stream: origin + path id, direction + scene.
-__global__ void k_sort_scatter(Paths P, const uint16_t* __restrict__ sid, int n_scenes, int nxt) {
+// Copies each queued ray (read in queue order from the unsorted stream) to
+// its sorted position in the sorted stream, and the path to the sorted queue.
+__global__ void k_sort_scatter(Paths P, int nxt) {
   const uint32_t n = P.ctr[kCtrQ0 + nxt];
   const uint32_t* q = P.q[nxt];
   const unsigned lane = threadIdx.x & 31;
@@ -991,13 +979,10 @@ __global__ void k_sort_scatter(Paths P, const uint16_t* __restrict__ sid, int n_
     uint32_t base = 0;
     if ((int)lane == leader) base = atomicAdd(P.sort_hist + key, (uint32_t)__popc(peers));
     base = __shfl_sync(peers, base, leader);
-    const uint32_t p = q[k];
     const uint32_t pos = base + __popc(peers & ((1u << lane) - 1u));
-    const float4 o = P.ro[p], d = P.rd[p];
-    const int sc = n_scenes > 1 ? __ldg(sid + p) : 0;
-    P.sray[2 * (size_t)pos] = make_float4(o.x, o.y, o.z, __uint_as_float(p));
-    P.sray[2 * (size_t)pos + 1] = make_float4(d.x, d.y, d.z, __int_as_float(sc));
-    P.sort_tmp[pos] = p;
+    P.sray[2 * (size_t)pos] = P.nray[2 * (size_t)k];  // origin + path id
+    P.sray[2 * (size_t)pos + 1] = P.nray[2 * (size_t)k + 1];  // direction + scene
+    P.sort_tmp[pos] = q[k];
   }
 }
 
@@ -1007,9 +992,9 @@ __global__ void k_sort_scatter(Paths P, const uint16_t* __restrict__ sid, int n_
 // captured wave replays the same sequence of swaps).
 static void sort_rays(const MultiLaunch& M, Paths& P, int nxt, int blocks, cudaStream_t s) {
   cudaMemsetAsync(P.sort_hist, 0, (size_t)kSortBins * 4, s);
-  k_sort_keys<<<blocks, 256, 0, s>>>(P, M.recs, M.sid, M.n, nxt);
+  k_sort_keys<<<blocks, 256, 0, s>>>(P, M.recs, M.n, nxt);
   k_sort_scan<<<1, 1024, 0, s>>>(P.sort_hist);
-  k_sort_scatter<<<blocks, 256, 0, s>>>(P, M.sid, M.n, nxt);
+  k_sort_scatter<<<blocks, 256, 0, s>>>(P, nxt);
   uint32_t* t = P.q[nxt];
   P.q[nxt] = P.sort_tmp;
   P.sort_tmp = t;
@@ -1036,8 +1021,7 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     const int cur = b & 1;
     k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
     E.mark(kPhResolve, s);
-    PathClosestMulti pc{P.ctr + kCtrQ0 + cur, P.q[cur], P.ro, P.rd, P.rng, P.hit,
-                        M.recs, M.sid, M.any_alpha, sorted ? P.sray : nullptr};
+    PathClosestMulti pc{P.ctr + kCtrQ0 + cur, sorted ? P.sray : P.nray, P.rng, P.hit, M.recs, M.any_alpha};
     TravArgs A{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
                M.trav_stats, top};
     k_closest_fast_t<PathClosestMulti><<<closest_blocks, PathClosestMulti::kThreads, top_smem_bytes(top), s>>>(A, pc);
@@ -1087,7 +1071,7 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
     for (int b = 0; b <= M.max_bounces; b++) {
       const int cur = b & 1;
       k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
-      PathClosestMulti pc{P.ctr + kCtrQ0 + cur, P.q[cur], P.ro, P.rd, P.rng, P.hit, M.recs, M.sid, M.any_alpha, nullptr};
+      PathClosestMulti pc{P.ctr + kCtrQ0 + cur, P.nray, P.rng, P.hit, M.recs, M.any_alpha};
       TravArgs TA{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
                   nullptr, top};
       k_closest_fast_t<PathClosestMulti><<<closest_blocks, PathClosestMulti::kThreads, top_smem_bytes(top), s>>>(TA, pc);

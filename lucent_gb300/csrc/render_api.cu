@@ -246,12 +246,12 @@ static lucent_status alloc_targets(lucent_renderer* r, uint32_t w, uint32_t h) {
 
 // Path buffers for `cap` paths (bytes per path: the 128-byte path record, the
 // radiance, the hit, 3 shadow slots of 3 float4, rng, occlusion flags, queues, slow-path
-// queues, the sort key, the sorted ray stream, the sorted and textured-hit queues).
+// queues, the sort key, the ray streams, the sorted and textured-hit queues).
 static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, uint32_t& path_cap, Paths& P,
                                         uint32_t cap) {
   if (cap <= path_cap) return LUCENT_OK;
   // Per-path arrays in allocation order (bytes per path); each starts on a 256-byte boundary.
-  static const size_t kPer[] = {16 * kPathRecord, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12, 4, 32, 4, 4};
+  static const size_t kPer[] = {16 * kPathRecord, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12, 4, 32, 32, 4, 4};
   size_t total = 0;
   for (size_t b : kPer) total += ((size_t)cap * b + 255) & ~(size_t)255;
   total += (size_t)kSortBins * 4;
@@ -286,6 +286,7 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
   P.slow = (uint32_t*)take((size_t)cap * 4);
   P.slow2 = (uint32_t*)take((size_t)cap * 12);
   P.sort_keys = (uint32_t*)take((size_t)cap * 4);
+  P.nray = (float4*)take((size_t)cap * 32);
   P.sray = (float4*)take((size_t)cap * 32);
   P.sort_tmp = (uint32_t*)take((size_t)cap * 4);
   P.qtex = (uint32_t*)take((size_t)cap * 4);

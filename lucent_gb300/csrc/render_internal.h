@@ -62,7 +62,8 @@ struct Paths {
   uint32_t* slow;
   uint32_t* slow2;
   uint32_t* sort_keys;  // per queued path: ray-sort key (scene, direction octant, origin cell)
-  float4* sray;         // sorted ray stream: 2 float4 per queued ray (origin + path id, direction + scene)
+  float4* nray;         // the bounce's rays in queue order: 2 float4 each (origin + path id, direction + scene)
+  float4* sray;         // the same sorted (after a ray sort)
   uint32_t* sort_tmp;   // the sorted queue, swapped with the queue it sorts
   uint32_t* qtex;       // queue positions of hits on texture-mapped materials (shaded by the TEX instantiation)
   uint32_t* sort_hist;  // kSortBins counters
