@@ -349,7 +349,7 @@ lucent_status lucent_renderer_display(lucent_renderer* r, float denoise_weight, 
 typedef struct lucent_batch lucent_batch;
 typedef struct lucent_batch_options {
   uint32_t samples_per_wave; /* samples of every pixel per wave; 0 = as many as max_wave_paths allows */
-  uint32_t max_wave_paths;   /* path-state budget of one wave (about 370 bytes of device memory per path) */
+  uint32_t max_wave_paths;   /* path-state budget of one wave (about 430 bytes of device memory per path) */
   int32_t use_graph;         /* capture a full wave once as a CUDA graph and replay it */
   uint32_t trace_blocks;     /* grid of the persistent traversal kernels; 0 = all resident blocks */
   uint32_t shade_blocks;     /* grid of the shade / resolve kernels; 0 = all resident blocks */

@@ -173,6 +173,58 @@ void sheen_lut_half(float* out) {
 
 }  // namespace lucent
 
+// One full wave captured as a CUDA graph on a private stream (the legacy
+// stream cannot be captured) and replayed while the launch parameters it
+// bakes in (`key`: sizes, options, buffer addresses) are unchanged. Saves the
+// launch gaps between the wave's ~80 dependent kernels.
+struct WaveGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t key[4] = {0, 0, 0, 0};
+  cudaStream_t cap = nullptr;
+  void drop() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+  void destroy() {
+    drop();
+    if (cap) cudaStreamDestroy(cap);
+    cap = nullptr;
+  }
+  lucent_status run(const MultiLaunch& M, const uint64_t k[4], cudaStream_t s) {
+    cudaError_t e;
+    if (!exec || std::memcmp(k, key, sizeof key) != 0) {
+      drop();
+      if (!cap && (e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_fail(e, "capture stream");
+      if ((e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return cuda_fail(e, "begin capture");
+      render_wave_multi(M, cap);
+      e = cudaStreamEndCapture(cap, &graph);
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+      if (e != cudaSuccess) {
+        drop();
+        return cuda_fail(e, "capture wave");
+      }
+      std::memcpy(key, k, sizeof key);
+    }
+    e = cudaGraphLaunch(exec, s);
+    return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "launch wave graph");
+  }
+};
+
+// Everything a captured wave bakes in besides the buffer contents.
+static void wave_key(const MultiLaunch& M, uint64_t key[4]) {
+  key[0] = (uint64_t)(uint32_t)M.S | ((uint64_t)(uint32_t)M.n << 32);
+  key[1] = (uint64_t)M.total_pixels | ((uint64_t)(uint32_t)M.trace_blocks << 32);
+  key[2] = ((uint64_t)(uintptr_t)M.paths.rec) ^ ((uint64_t)M.max_bounces << 48) ^ ((uint64_t)M.shade_blocks << 56);
+  key[3] = ((uint64_t)(uintptr_t)M.recs) ^ ((uint64_t)(uintptr_t)M.path_base << 20) ^ ((uint64_t)M.any_alpha << 59) ^
+           ((uint64_t)M.any_tex << 60) ^ ((uint64_t)M.sort_rays << 61) ^ ((uint64_t)M.top_levels << 62) ^
+           ((uint64_t)(M.trav_stats != nullptr) << 63);
+}
+
 struct lucent_renderer {
   uint32_t W = 1, H = 1;
   // scene
@@ -213,6 +265,8 @@ struct lucent_renderer {
   // a renderer traces as a launch of one scene: its SceneRec, path/pixel bases (full and last wave), scene index per path
   DeviceBuffer rec1, base1, sid1;
   uint32_t sid_cap = 0;
+  WaveGraph wave_graph;  // full waves of a trace replay a captured graph (not while profiling)
+  uint32_t waves = 0;
   int sort_rays = 1;   // sort the rays of bounces 1 and 2 (lucent_renderer_set_ray_sort)
   int top_levels = 1;  // top BVH levels in shared memory (lucent_renderer_set_top_levels)
   // temporal reprojection (renderer.ts:441-451, 717-731): the view the accumulation was traced with
@@ -476,6 +530,7 @@ void lucent_renderer_destroy(lucent_renderer* r) {
                           &r->history, &r->paths, &r->ctr, &r->den_a, &r->den_b, &r->guide0, &r->guide1, &r->disp, &r->adj_dl, &r->adj_path, &r->adj_grad, &r->rec1, &r->base1, &r->sid1, &r->prev,
                           &r->color_maps, &r->data_maps, &r->texel_lut})
     b->release();
+  r->wave_graph.destroy();
   if (r->ev0) cudaEventDestroy(r->ev0);
   if (r->ev1) cudaEventDestroy(r->ev1);
   for (cudaEvent_t e : r->pev) cudaEventDestroy(e);
@@ -742,9 +797,16 @@ lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* 
   M.trav_stats = r->profiling ? (unsigned long long*)((uint32_t*)r->ctr.ptr + kCtrTrav) : nullptr;
   cudaEventRecord(r->ev0, s);
   PhaseEvents pe{r->pev.data(), r->ptag.data(), (int)r->pev.size(), 0};
+  uint64_t key[4];
+  wave_key(M, key);
   for (uint32_t w = 0; w < full + (tail ? 1 : 0); w++) {
     if (w == full) single_tail(r, tail, M);
-    render_wave_multi(M, s, r->profiling ? &pe : nullptr);  // seeds advance on the device
+    if (w < full && !r->profiling && r->waves > 0) {  // the first wave ever runs uncaptured (one-time setup)
+      if ((st = r->wave_graph.run(M, key, s))) return st;
+    } else {
+      render_wave_multi(M, s, r->profiling ? &pe : nullptr);  // seeds advance on the device
+    }
+    r->waves++;
   }
   r->seed += samples;
   r->frame += samples;
@@ -1008,18 +1070,9 @@ struct lucent_batch {
   DeviceBuffer recs, bases, tail_bases, sid, paths, ctr;
   uint32_t path_cap = 0, sid_cap = 0;
   Paths P{};
-  // captured full wave
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  uint64_t graph_key[4] = {0, 0, 0, 0};
+  WaveGraph wave_graph;  // captured full wave
   uint32_t waves = 0, graph_waves = 0;
-  cudaStream_t cap_stream = nullptr;  // capture happens here (the legacy stream cannot be captured)
-  void drop_graph() {
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
-    exec = nullptr;
-    graph = nullptr;
-  }
+  void drop_graph() { wave_graph.drop(); }
 };
 
 
@@ -1043,8 +1096,7 @@ lucent_status lucent_batch_create(lucent_renderer* const* renderers, uint32_t n,
 
 void lucent_batch_destroy(lucent_batch* b) {
   if (!b) return;
-  b->drop_graph();
-  if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+  b->wave_graph.destroy();
   for (DeviceBuffer* d : {&b->recs, &b->bases, &b->tail_bases, &b->sid, &b->paths, &b->ctr}) d->release();
   delete b;
 }
@@ -1132,30 +1184,14 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
     M.path_base = (const uint32_t*)base.ptr;
     M.pix_base = (const uint32_t*)base.ptr + (n + 1);
   };
-  const uint64_t key[4] = {S | ((uint64_t)n << 32), pixels | ((uint64_t)b->opt.trace_blocks << 40),
-                           (uint64_t)(uintptr_t)b->P.rec ^ ((uint64_t)max_bounces << 48) ^ ((uint64_t)b->opt.shade_blocks << 56),
-                           (uint64_t)(uintptr_t)b->recs.ptr ^ ((uint64_t)any_alpha << 63)};
   const uint32_t full = samples / (uint32_t)S;
   for (uint32_t w = 0; w < full; w++) {
     setup((uint32_t)S, b->bases);
+    uint64_t key[4];
+    wave_key(M, key);
     if (b->opt.use_graph && b->waves > 0) {  // first wave ever runs uncaptured (one-time setup inside)
-      if (!b->exec || std::memcmp(key, b->graph_key, sizeof key) != 0) {
-        b->drop_graph();
-        if (!b->cap_stream && (e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking)) != cudaSuccess)
-          return cuda_fail(e, "capture stream");
-        e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal);
-        if (e != cudaSuccess) return cuda_fail(e, "begin capture");
-        render_wave_multi(M, b->cap_stream);
-        e = cudaStreamEndCapture(b->cap_stream, &b->graph);
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
-        if (e != cudaSuccess) {
-          b->drop_graph();
-          return cuda_fail(e, "capture wave");
-        }
-        std::memcpy(b->graph_key, key, sizeof key);
-      }
-      e = cudaGraphLaunch(b->exec, s);
-      if (e != cudaSuccess) return cuda_fail(e, "launch wave graph");
+      const lucent_status gst = b->wave_graph.run(M, key, s);
+      if (gst) return gst;
       b->graph_waves++;
     } else {
       render_wave_multi(M, s);

@@ -111,3 +111,24 @@ def test_traversal_options_change_no_pixel(option):
         out.append(r.read())
         r.dispose()
     assert all(np.array_equal(a, b) for a, b in zip(*out))
+
+
+def test_graph_replay_changes_no_pixel():
+    # Full waves after a renderer's first replay a captured CUDA graph;
+    # profiling mode launches every kernel directly. Same images either way,
+    # including after an option change (a new graph).
+    sc = W.box_scene(3, 3)
+    out = []
+    for profiling in (False, True):
+        r = Renderer(48, 40)
+        r.settings.max_bounces = 6
+        r.load_scene(sc)
+        r.set_profiling(profiling)
+        r.set_seed(5)
+        for i in range(4):
+            if i == 2:
+                r.set_ray_sort(False)
+            r.trace_samples(2)
+        out.append(r.read())
+        r.dispose()
+    assert all(np.array_equal(a, b) for a, b in zip(*out))
