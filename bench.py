@@ -208,6 +208,7 @@ def cpu_closest(threads, sample_rays=1_000_000, reps=3):
 
 # ----------------------------------------------------------------------------- path-tracing workload
 PT_W, PT_H, PT_SPP, PT_DEPTH = 512, 512, 16, 8
+CPU_BASELINE_SECONDS = 10.0
 # dram__bytes_read.sum + dram__bytes_write.sum from ncu captures of the same
 # workloads (profiles/closest_pt_box512_16spp.md, closest_fast_soup65k_1Mrays.md).
 NCU_DRAM_BYTES_PT_FRAME = 1_478_600_000
@@ -692,7 +693,13 @@ def main():
         if k in res:
             line[k] = res[k]
     if world == 1 and not args.no_cpu_baseline:
-        v, sample = cpu(cores)
+        # a bounded sample of the same workload, repeated to about CPU_BASELINE_SECONDS of CPU work
+        t0, vals = time.perf_counter(), []
+        while not vals or time.perf_counter() - t0 < CPU_BASELINE_SECONDS:
+            v, sample = cpu(cores)
+            vals.append(v)
+        v = float(np.mean(vals))
+        sample += ", %d runs in %.1f s" % (len(vals), time.perf_counter() - t0)
         line["cpu_baseline"] = {"value": round(v, 3), "unit": unit, "cores": cores, "kind": "port",
                                 "sample": sample + " (oracle C++ restatement, binary64, not V8)"}
     print(json.dumps(line), flush=True)
