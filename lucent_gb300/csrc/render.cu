@@ -1057,7 +1057,6 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
 // first with the adjoint work off to recover each sample's primal radiance,
 // then propagating dl through every vertex.
 void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t s) {
-  const Paths& P = M.paths;
   const SceneRec* rec = M.recs;
   static int closest_blocks = 0, shade_blocks = 0;
   if (!closest_blocks) {
@@ -1067,11 +1066,13 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
   const int top = M.top_levels ? (M.n < kTopMaxScenes ? M.n : kTopMaxScenes) : 0;
   for (int pass = 0; pass < 2; pass++) {
     const AdjointDev A{H.dl, H.lrem, H.gcont, H.gslot, H.genv, H.dmat, H.denv, M.total_pixels, pass == 0 ? 1 : 0};
+    Paths P = M.paths;     // queue buffers swap with the sort buffer below
+    bool sorted = false;  // as in render_wave_multi: the rays of bounces 1 and 2 are sorted
     k_camera_multi<<<grid_for(M.total_paths, 256), 256, 0, s>>>(P, M.recs, M.path_base, M.n, M.sid, M.S);
     for (int b = 0; b <= M.max_bounces; b++) {
       const int cur = b & 1;
       k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
-      PathClosestMulti pc{P.ctr + kCtrQ0 + cur, P.nray, P.rng, P.hit, M.recs, M.any_alpha};
+      PathClosestMulti pc{P.ctr + kCtrQ0 + cur, sorted ? P.sray : P.nray, P.rng, P.hit, M.recs, M.any_alpha};
       TravArgs TA{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
                   nullptr, top};
       k_closest_fast_t<PathClosestMulti><<<closest_blocks, PathClosestMulti::kThreads, top_smem_bytes(top), s>>>(TA, pc);
@@ -1082,10 +1083,14 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
                   nullptr, top};
       k_anyhit_fast_t<PathShadowMulti><<<shade_blocks * 2, 256, top_smem_bytes(top), s>>>(TB, ps);
       k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, s>>>(TB, ps);
+      Paths Pr = P;  // resolve walks the pre-sort queue, in path order
+      if (sorted) Pr.q[cur] = P.sort_tmp;
       if (pass == 0)
-        k_resolve<<<shade_blocks, 128, 0, s>>>(P, cur);
+        k_resolve<<<shade_blocks, 128, 0, s>>>(Pr, cur);
       else
-        k_resolve_adjoint<<<shade_blocks, 128, 0, s>>>(P, A, rec, cur);
+        k_resolve_adjoint<<<shade_blocks, 128, 0, s>>>(Pr, A, rec, cur);
+      sorted = M.sort_rays && b < 2 && b < M.max_bounces;
+      if (sorted) sort_rays(M, P, cur ^ 1, shade_blocks, s);
     }
     if (pass == 0) k_seed_lrem<<<grid_for(M.total_paths, 256), 256, 0, s>>>(P, A, M.total_paths);
   }
