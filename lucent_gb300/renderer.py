@@ -344,14 +344,20 @@ class Batch:
         mb = max(r.settings.max_bounces for r in self.renderers)
         return "n%d_px%d_tri%d_b%d" % (len(self.renderers), px, tris, mb)
 
-    def autotune(self, samples=2, candidates=None, cache=None):
+    # Second tuning stage: one option at a time from the best wave configuration
+    # (ray sorting, the shared-memory top BVH levels, the grid of the shade /
+    # resolve / any-hit kernels); none of them changes an image.
+    REFINE = ({"sort_rays": False}, {"top_levels": False}, {"shade_blocks": 152 * 3}, {"shade_blocks": 152 * 8})
+
+    def autotune(self, samples=2, candidates=None, cache=None, refine=True):
         """Times at least `samples` samples (two full waves) under each
         candidate option set (wall clock around trace + synchronise, so launch
-        overhead counts) and keeps the fastest per sample. The samples are
-        real: reset the renderers afterwards for a fresh average. With `cache`
-        (a JSON file path) a result for the same signature() is reused, and
-        new results are stored there.
-        Returns (chosen options, {candidate index: seconds per sample})."""
+        overhead counts) and keeps the fastest per sample; then, if `refine`,
+        tries each REFINE change on top of the winner and keeps those that are
+        faster (coordinate descent). The samples are real: reset the renderers
+        afterwards for a fresh average. With `cache` (a JSON file path) a
+        result for the same signature() is reused, and new results are stored
+        there. Returns (chosen options, {candidate index: seconds per sample})."""
         import json
         import os
         key = self.signature()
@@ -368,17 +374,34 @@ class Batch:
                           for s in waves for g in (True, False)]
         base = dict(self.options)
         times = {}
-        for i, c in enumerate(candidates):
-            self.set_options(**{**base, **c})
-            n = max(samples, 2 * c.get("samples_per_wave", 1))  # at least two full waves
+
+        def measure(opts):
+            self.set_options(**opts)
+            n = max(samples, 2 * opts.get("samples_per_wave", 1))  # at least two full waves
             self.trace_samples(n)  # allocation and graph capture happen outside the timed call
             self.check()
             t0 = time.perf_counter()
             self.trace_samples(n)
             self.check()
-            times[i] = (time.perf_counter() - t0) / n  # seconds per sample
+            return (time.perf_counter() - t0) / n  # seconds per sample
+
+        for i, c in enumerate(candidates):
+            times[i] = measure({**base, **c})
         best = min(times, key=times.get)
-        self.set_options(**{**base, **candidates[best]})
+        chosen, best_t = {**base, **candidates[best]}, times[best]
+        tuned = dict(candidates[best])
+        if refine:
+            for j, change in enumerate(self.REFINE):
+                if all(chosen.get(k) == v for k, v in change.items()):
+                    continue
+                t = measure({**chosen, **change})
+                times["refine%d" % j] = t
+                if t < best_t:
+                    chosen, best_t = {**chosen, **change}, t
+                    tuned.update(change)
+        self.set_options(**chosen)
+        candidates = list(candidates) + [tuned]
+        best = len(candidates) - 1
         if cache:
             known = {}
             if os.path.exists(cache):

@@ -128,3 +128,22 @@ def test_batch_errors(specs):
         b.set_options(max_wave_paths=0)
     for x in (b, r, empty):
         x.dispose()
+
+
+def test_autotuned_batch_equals_renderers_alone(specs, solo):
+    # Whatever the autotuner picks (wave size, graph replay, ray sorting, top
+    # levels, grid sizes), the images are those of the renderers alone.
+    rs = _renderers(specs)
+    b = Batch(rs)
+    opts, times = b.autotune(samples=1)
+    assert len(times) >= 2 and set(opts) >= {"sort_rays", "top_levels", "shade_blocks"}
+    for i, r in enumerate(rs):
+        r.reset()
+        r.set_seed(100 * i)
+    b.trace_samples(5)
+    b.check()
+    for r, ref in zip(rs, solo):
+        assert _same(r.read(), ref)
+    b.dispose()
+    for r in rs:
+        r.dispose()
