@@ -490,50 +490,53 @@ ADJ_W, ADJ_SPP, ADJ_DEPTH, ADJ_VIEWS = 512, 32, 6, 8
 def run_ours_adjoint(args, rank, world, local):
     """Inverse rendering: workloads.adjoint_scene (the box scene's geometry,
     32 materials, 256x128 HDRI) seen from 8 views at 512x512, depth 6. One
-    step = one optimisation iteration: 32-spp forward renders of the 8 views
-    and the 32-spp path-replay backward of each (material and environment
-    gradients of an L2 image loss). value = backward / forward time ratio.
-    Also times the 8 forward views as one batch vs one by one, at 32 spp per
+    step = one optimisation iteration (inverse.InverseRendering): 32-spp
+    forward renders of the views and the 32-spp path-replay backward of each
+    against the L2 image loss, one all-reduce of the 98,503-value gradient
+    vector over the ranks (views are sharded v % world), one Adam step on
+    materials and environment. value = backward / forward time ratio. Also
+    times this rank's forward views as one batch vs one by one, at 32 spp per
     call and at 1 spp per call (progressive)."""
     import torch
     from lucent_gb300 import adjoint as AD
+    from lucent_gb300 import inverse as INV
     from lucent_gb300 import workloads as W
     from lucent_gb300.renderer import Batch, Renderer
     from lucent_gb300 import scene as S
     torch.cuda.set_device(local)
     sc = W.adjoint_scene(0, 6)
-    rs = []
-    for cam in W.adjoint_views(ADJ_VIEWS):
-        v = S.Scene(name=sc.name, camera=cam, env=sc.env, meshes=sc.meshes)
+    mine = INV.views_of_rank(ADJ_VIEWS, rank, world)
+    cams = W.adjoint_views(ADJ_VIEWS)
+    views = []
+    for v in mine:
         r = Renderer(ADJ_W, ADJ_W)
         r.settings.max_bounces = ADJ_DEPTH
-        r.load_scene(v)
-        rs.append(r)
-    targets = [AD.forward(r, ADJ_SPP, 0) for r in rs]
+        r.load_scene(S.Scene(name=sc.name, camera=cams[v], env=sc.env, meshes=sc.meshes))
+        views.append(INV.RendererView(r, AD.forward(r, ADJ_SPP, 0), ADJ_SPP, 1))
+    rs = [v.renderer for v in views]
     rng = np.random.default_rng(0)
-    theta = np.clip(AD.get_params(rs[0].packed.materials) + rng.normal(0, 0.1, (rs[0].packed.material_count, 6)),
-                    0, 1).astype(np.float32)
-
-    def step():
-        tf = tb = 0.0
-        loss = 0.0
-        for r, tgt in zip(rs, targets):
-            t0 = time.perf_counter()
-            img = AD.forward(r, ADJ_SPP, 1, theta=theta)
-            tf += time.perf_counter() - t0
-            loss += float(((img - tgt) ** 2).sum())
-            t0 = time.perf_counter()
-            AD.backward(r, ADJ_SPP, 1, 2.0 * (img - tgt))
-            tb += time.perf_counter() - t0
-        return tf, tb, loss
+    gt = AD.get_params(rs[0].packed.materials)
+    theta = np.clip(gt + rng.normal(0, 0.1, gt.shape), 0, 1)
+    env_gt = sc.env.map.data.reshape(sc.env.map.height, sc.env.map.width, 3).astype(np.float64)
+    env = np.maximum(env_gt + rng.normal(0, 0.1, env_gt.shape), 0)
+    reduce = INV.TorchAllReduce(device="cuda:%d" % local) if world > 1 else None
+    opt = INV.InverseRendering(views, theta, env, reduce=reduce)
 
     for _ in range(args.warmup):
-        step()
+        opt.step()
+    for v in views:
+        v.timing = dict.fromkeys(v.timing, 0.0)
+    opt.timing = dict.fromkeys(opt.timing, 0.0)
+    barrier(world)
     with Clocks(local) as clk:
-        res = [step() for _ in range(args.steps)]
-    tf = sum(x[0] for x in res)
-    tb = sum(x[1] for x in res)
-    paths = ADJ_VIEWS * ADJ_W * ADJ_W * ADJ_SPP * args.steps
+        for _ in range(args.steps):
+            opt.step()
+    barrier(world)
+    tf = max_over_ranks(sum(v.timing["forward"] for v in views), world)
+    tb = max_over_ranks(sum(v.timing["backward"] for v in views), world)
+    tu = max_over_ranks(sum(v.timing["upload"] for v in views) + opt.timing["update"], world)
+    tr = max_over_ranks(opt.timing["reduce"], world)
+    paths = len(views) * ADJ_W * ADJ_W * ADJ_SPP * args.steps
 
     # forward of the 8 views: one batch vs one renderer after another
     def timed(fn):
@@ -569,23 +572,27 @@ def run_ours_adjoint(args, rank, world, local):
         for r in rs:
             r.reset()
         tbt = timed(lambda: bat(spp, calls))
-        px = ADJ_VIEWS * ADJ_W * ADJ_W * spp * calls
+        px = len(rs) * ADJ_W * ADJ_W * spp * calls
         modes["%d_spp_per_call" % spp] = {"sequential_mpaths_per_s": round(px / ts / 1e6, 2),
                                           "batched_mpaths_per_s": round(px / tbt / 1e6, 2),
                                           "batched_over_sequential": round(ts / tbt, 3)}
     ratio = tb / tf
     return {
         "metric": "adjoint/forward time ratio: path-replay backward vs forward, 8 views 512x512, 32 spp, depth 6",
-        "value": round(ratio, 3), "unit": "x", "ms_per_step": round(1e3 * (tf + tb) / args.steps, 2),
+        "value": round(ratio, 3), "unit": "x", "ms_per_step": round(1e3 * (tf + tb + tu + tr) / args.steps, 2),
         "higher_is_better": False,
         "e2e": {"value": round(ratio, 3), "unit": "x", "h2d_bytes_per_step": ADJ_VIEWS * ADJ_W * ADJ_W * 16,
                 "d2h_bytes_per_step": ADJ_VIEWS * ADJ_W * ADJ_W * 52},
         "roofline": None, "clocks": clk.summary(), "gpu_launches": None, "dtype": "f32 (+f64 exact hit decisions)",
         "config": {"workload": "adjoint: adjoint_scene(0, 6) (81,956 triangles, 33 materials, 256x128 HDRI), "
                                "8 views 512x512, 32 spp forward / 32 replayed, depth 6"},
-        "extra": {"forward_ms_per_view": round(1e3 * tf / (ADJ_VIEWS * args.steps), 2),
-                  "backward_ms_per_view": round(1e3 * tb / (ADJ_VIEWS * args.steps), 2),
-                  "forward_mpaths_per_s": round(paths / tf / 1e6, 2), "loss_first_step": round(res[0][2], 3),
+        "extra": {"forward_ms_per_view": round(1e3 * tf / (len(views) * args.steps), 2),
+                  "backward_ms_per_view": round(1e3 * tb / (len(views) * args.steps), 2),
+                  "upload_and_adam_ms_per_step": round(1e3 * tu / args.steps, 2),
+                  "allreduce_ms_per_step": round(1e3 * tr / args.steps, 3),
+                  "views_per_rank": len(views), "gradient_values": opt.size,
+                  "forward_mpaths_per_s": round(paths / tf / 1e6, 2),
+                  "loss": [round(x, 3) for x in opt.history],
                   "batched_forward": modes},
     }
 
