@@ -82,12 +82,15 @@ void lucent_bvh_destroy(lucent_bvh* bvh);
 /* Node and triangle counts of an uploaded BVH. */
 lucent_status lucent_bvh_info(const lucent_bvh* bvh, uint32_t* node_count, uint32_t* tri_count);
 /* Traversal mode: 0 = f32 bounded-error path with binary64 fallback and the
- * top six BVH levels staged in shared memory (default), 1 = every decision in
- * binary64, 2 = mode 0 reading every node from global memory. All return
- * identical results. */
+ * top six BVH levels staged in shared memory, 1 = every decision in binary64,
+ * 2 = mode 0 reading every node from global memory, 3 = mode 0's decisions
+ * over a four-wide view of the tree (each inner step reads a node's four
+ * grandchildren; built on first use, 128 bytes per node; the default). All
+ * return identical results. lucent_bvh_intersect_noalloc always uses 0. */
 #define LUCENT_TRAVERSE_FAST 0
 #define LUCENT_TRAVERSE_EXACT 1
 #define LUCENT_TRAVERSE_FAST_GLOBAL 2
+#define LUCENT_TRAVERSE_WIDE 3
 lucent_status lucent_bvh_set_mode(lucent_bvh* bvh, int32_t mode);
 
 /* n rays, 6 floats each (origin xyz, direction xyz), host buffers. t_min and
@@ -232,7 +235,7 @@ typedef struct lucent_render_stats {
   /* device ms of the last trace per phase (camera, closest hit, shade, shadow
    * rays, resolve + queue upkeep, accumulate); zero unless profiling is on */
   double phase_ms[6];
-  /* closest-hit traversal counters accumulated while profiling is on: rays,
+  /* closest-hit traversal counters accumulated while profiling is 2: rays,
    * slab tests decided in binary64, triangle tests decided in binary64,
    * binary64 recomputations of the running closest distance, binary64 final
    * hit reports */
@@ -269,7 +272,11 @@ lucent_status lucent_renderer_read(lucent_renderer* r, float* color4, float* alb
 lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out);
 /* Records CUDA events between the kernels of each trace (the counterpart of
  * the reference's GPU timer queries, renderer.ts:668-700); results appear in
- * lucent_render_stats.phase_ms after lucent_renderer_check. */
+ * lucent_render_stats.phase_ms after lucent_renderer_check. enabled = 2 also
+ * counts the closest-hit traversal's binary64 decisions
+ * (lucent_render_stats.traversal); the counters are atomics on a few words
+ * and slow the closest-hit kernel down, so phase times taken with them are
+ * not the kernel's own. */
 lucent_status lucent_renderer_set_profiling(lucent_renderer* r, int32_t enabled);
 /* The texture arrays the scene's maps are sampled from (buildTextureArrays,
  * renderer.ts:314-333): *size = the layer size (0: no textures); color_out
@@ -285,6 +292,12 @@ lucent_status lucent_renderer_set_ray_sort(lucent_renderer* r, int32_t enabled);
  * memory (default on). Hits and images are the same either way; only where
  * the traversal reads those nodes changes. */
 lucent_status lucent_renderer_set_top_levels(lucent_renderer* r, int32_t enabled);
+/* Closest-hit rays over a four-wide view of the BVH (each inner step reads the
+ * four grandchildren of a node; built at scene load, 128 bytes per binary
+ * node; default on). Hits and images are the same either way: the
+ * grandchildren's boxes lie inside their parents', so the reference's cull
+ * decisions and visiting order are unchanged. */
+lucent_status lucent_renderer_set_wide_bvh(lucent_renderer* r, int32_t enabled);
 /* ---------------------------------------------------------------------------
  * Differentiable rendering (path replay backpropagation). No reference
  * counterpart: the reference renders forward only.
@@ -355,6 +368,7 @@ typedef struct lucent_batch_options {
   uint32_t shade_blocks;     /* grid of the shade / resolve kernels; 0 = all resident blocks */
   int32_t sort_rays;         /* sort the rays of bounces 1 and 2 (see lucent_renderer_set_ray_sort) */
   int32_t top_levels;        /* top BVH levels of the first 8 scenes in shared memory (lucent_renderer_set_top_levels) */
+  int32_t wide_bvh;          /* closest hit over the four-wide BVH views (lucent_renderer_set_wide_bvh) */
 } lucent_batch_options;
 typedef struct lucent_batch_stats {
   uint64_t closest_rays, shadow_rays; /* traced by this batch since creation */
@@ -366,7 +380,7 @@ typedef struct lucent_batch_stats {
 lucent_status lucent_batch_create(lucent_renderer* const* renderers, uint32_t n, lucent_batch** out);
 void lucent_batch_destroy(lucent_batch* batch);
 /* Defaults: samples_per_wave 0, max_wave_paths 2^25, use_graph 1, trace_blocks 0, shade_blocks 0,
- * sort_rays 1, top_levels 1. */
+ * sort_rays 1, top_levels 1, wide_bvh 1. */
 lucent_status lucent_batch_set_options(lucent_batch* batch, const lucent_batch_options* options);
 /* Asynchronous on `stream`. */
 lucent_status lucent_batch_trace(lucent_batch* batch, uint32_t samples, void* stream);

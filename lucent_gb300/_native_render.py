@@ -60,6 +60,7 @@ def declare(L, sig):
     sig(L, "lucent_renderer_trim", [VP])
     sig(L, "lucent_renderer_set_ray_sort", [VP, C.c_int32])
     sig(L, "lucent_renderer_set_top_levels", [VP, C.c_int32])
+    sig(L, "lucent_renderer_set_wide_bvh", [VP, C.c_int32])
     sig(L, "lucent_renderer_read_textures", [VP, U32P, U8P, U8P])
     sig(L, "lucent_renderer_set_materials", [VP, F32P, C.c_uint32])
     sig(L, "lucent_renderer_backward", [VP, C.c_uint32, C.c_uint32, F32P, F32P, F32P, VP])
@@ -74,7 +75,7 @@ def declare(L, sig):
 class BatchOptions(C.Structure):
     _fields_ = [("samples_per_wave", C.c_uint32), ("max_wave_paths", C.c_uint32), ("use_graph", C.c_int32),
                 ("trace_blocks", C.c_uint32), ("shade_blocks", C.c_uint32), ("sort_rays", C.c_int32),
-                ("top_levels", C.c_int32)]
+                ("top_levels", C.c_int32), ("wide_bvh", C.c_int32)]
 
 
 class BatchStats(C.Structure):

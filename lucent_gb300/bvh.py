@@ -69,11 +69,13 @@ class DeviceBVH:
 
     __del__ = close
 
-    def set_mode(self, exact, top_levels=True):
+    def set_mode(self, exact, top_levels=True, wide=True):
         """lucent_bvh_set_mode: all-binary64 traversal (exact), else the
-        binary32 path with (top_levels) or without the shared-memory copy of
+        binary32 path over the four-wide view of the tree (wide), or over the
+        binary nodes with (top_levels) or without the shared-memory copy of
         the top BVH levels. Results are identical in every mode."""
-        N.check(N.lib().lucent_bvh_set_mode(self._h, 1 if exact else 0 if top_levels else 2))
+        mode = 1 if exact else 3 if wide else 0 if top_levels else 2
+        N.check(N.lib().lucent_bvh_set_mode(self._h, mode))
 
     def intersect(self, rays, t_min=1e-5, t_max=math.inf, stream=None):
         """Closest hits of float32 rays [n, 6] -> (prim int32 (-1 miss), t, u, v) float32."""

@@ -62,8 +62,9 @@ struct lucent_bvh {
   // Tree depth (root = 0). Trees whose depth could overflow the reference's
   // 64-entry stack take the all-binary64 path, which reproduces the overflow.
   uint32_t depth = 0;
-  int mode = LUCENT_TRAVERSE_FAST;
+  int mode = LUCENT_TRAVERSE_WIDE;
   DeviceBuffer nodes, tris, scratch, stage;
+  DeviceBuffer wide;  // four-wide view of `nodes` (LUCENT_TRAVERSE_WIDE), built on first use
 };
 
 extern "C" {
@@ -257,7 +258,8 @@ lucent_status lucent_bvh_download(const lucent_bvh* b, float* nodes_out, uint32_
 lucent_status lucent_bvh_set_mode(lucent_bvh* b, int32_t mode) {
   clear_error();
   if (!b) return fail(LUCENT_ERR_INVALID, "null bvh");
-  if (mode != LUCENT_TRAVERSE_FAST && mode != LUCENT_TRAVERSE_EXACT && mode != LUCENT_TRAVERSE_FAST_GLOBAL)
+  if (mode != LUCENT_TRAVERSE_FAST && mode != LUCENT_TRAVERSE_EXACT && mode != LUCENT_TRAVERSE_FAST_GLOBAL &&
+      mode != LUCENT_TRAVERSE_WIDE)
     return fail(LUCENT_ERR_INVALID, "bad mode %d", mode);
   b->mode = mode;
   return LUCENT_OK;
@@ -299,9 +301,17 @@ lucent_status lucent_bvh_intersect_device(lucent_bvh* b, const float* rays_d, ui
     cudaError_t e = cudaMemsetAsync(prim_d, 0xff, (size_t)n * 4, s);
     return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "memset");
   }
+  const Node* wide = nullptr;
+  if (b->mode == LUCENT_TRAVERSE_WIDE) {
+    if (!b->wide.ptr) {
+      if ((st = b->wide.reserve((size_t)b->node_count * 4 * sizeof(Node)))) return st;
+      launch_wide_view((const Node*)b->nodes.ptr, b->node_count, (Node*)b->wide.ptr, s);
+    }
+    wide = (const Node*)b->wide.ptr;
+  }
   launch_closest((const Node*)b->nodes.ptr, b->node_count, (const float4*)b->tris.ptr, rays_d, n, t_min, t_max, prim_d, t_d, u_d,
                  v_d, queue, qlen, work, err, b->mode == LUCENT_TRAVERSE_EXACT || b->depth + 2 > kTsStack,
-                 b->mode != LUCENT_TRAVERSE_FAST_GLOBAL, s);
+                 b->mode == LUCENT_TRAVERSE_FAST, s, wide);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "closest-hit launch");
 }

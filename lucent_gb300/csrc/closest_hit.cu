@@ -2,7 +2,7 @@
 // rays as 6 floats (or doubles) each, results per ray, hit ids equal to the
 // reference's intersectBVH (src/math/bvh.ts:265-320).
 #include "internal.h"
-#include "traverse.cuh"
+#include "traverse_wide.cuh"
 
 namespace lucent {
 
@@ -138,7 +138,7 @@ void launch_unpack(const Node* nodes, uint32_t count, const float4* tris, uint32
 void launch_closest(const Node* nodes, uint32_t node_count, const float4* tris, const float* rays_d, uint32_t n,
                     double tMin, double tMax, int32_t* prim, float* t, float* u, float* v, uint32_t* queue,
                     uint32_t* queue_len, uint32_t* work, unsigned* err, bool exact_only, bool top_levels,
-                    cudaStream_t s) {
+                    cudaStream_t s, const Node* wide) {
   if (n == 0) return;
   const ApiPolicy P{rays_d, n, tris, prim, t, u, v};
   TravArgs A{nodes, node_count, tris, tMin, tMax, queue, queue_len, work, err, nullptr, top_levels ? 1 : 0};
@@ -148,12 +148,25 @@ void launch_closest(const Node* nodes, uint32_t node_count, const float4* tris, 
     k_closest_exact_t<ApiPolicy><<<grid_for(n, 128), 128, 0, s>>>(E, P);
     return;
   }
-  static int blocks = 0;
-  if (!blocks) blocks = persistent_blocks((const void*)k_closest_fast_t<ApiPolicy>, ApiPolicy::kThreads);
+  static int blocks = 0, wide_blocks = 0;
+  if (!blocks) {
+    blocks = persistent_blocks((const void*)k_closest_fast_t<ApiPolicy>, ApiPolicy::kThreads);
+    wide_blocks = persistent_blocks((const void*)k_closest_wide_t<ApiPolicy>, ApiPolicy::kThreads);
+  }
   const int want = (int)((n + ApiPolicy::kThreads - 1) / ApiPolicy::kThreads);
-  k_closest_fast_t<ApiPolicy><<<want < blocks ? want : blocks, ApiPolicy::kThreads, top_smem_bytes(A.top_scenes), s>>>(A, P);
+  if (wide) {
+    A.wide = wide;
+    A.top_scenes = 0;
+    k_closest_wide_t<ApiPolicy><<<want < wide_blocks ? want : wide_blocks, ApiPolicy::kThreads, 0, s>>>(A, P);
+  } else {
+    k_closest_fast_t<ApiPolicy><<<want < blocks ? want : blocks, ApiPolicy::kThreads, top_smem_bytes(A.top_scenes), s>>>(A, P);
+  }
   // Slow path over the rays the fast kernel queued (length read on the device).
   k_closest_exact_t<ApiPolicy><<<grid_for(n < 4096 ? n : 4096, 128), 128, 0, s>>>(A, P);
+}
+
+void launch_wide_view(const Node* nodes, uint32_t node_count, Node* wide, cudaStream_t s) {
+  launch_build_wide(nodes, node_count, wide, s);
 }
 
 void launch_closest_d(const Node* nodes, uint32_t node_count, const float4* tris, const double* rays_d, uint32_t n,

@@ -19,7 +19,10 @@ void launch_unpack(const Node* nodes, uint32_t count, const float4* tris, uint32
                    uint32_t* idx_d, cudaStream_t s);
 void launch_closest(const Node* nodes, uint32_t node_count, const float4* tris, const float* rays_d, uint32_t n, double tMin,
                     double tMax, int32_t* prim, float* t, float* u, float* v, uint32_t* queue, uint32_t* queue_len,
-                    uint32_t* work, unsigned* err, bool exact_only, bool top_levels, cudaStream_t s);
+                    uint32_t* work, unsigned* err, bool exact_only, bool top_levels, cudaStream_t s,
+                    const Node* wide = nullptr);
+// Four-wide view of a binary node array (traverse_wide.cuh): 4 records per node.
+void launch_wide_view(const Node* nodes, uint32_t node_count, Node* wide, cudaStream_t s);
 void launch_closest_d(const Node* nodes, uint32_t node_count, const float4* tris, const double* rays_d, uint32_t n, double tMin,
                       double tMax, int32_t* prim, double* t, double* u, double* v, unsigned* err, cudaStream_t s);
 

@@ -20,6 +20,7 @@
 #include "render_internal.h"
 #include "shade.cuh"
 #include "traverse.cuh"
+#include "traverse_wide.cuh"
 
 namespace lucent {
 
@@ -53,7 +54,7 @@ struct PathClosestMulti {
   __device__ BvhView bvh(uint32_t k) const { return scene_bvh(__float_as_int(rays[2 * (size_t)k + 1].w)); }
   __device__ BvhView scene_bvh(int sc) const {
     const SceneDev& S = recs[sc].scene;
-    return {S.nodes, S.geo, S.node_count, sc};
+    return {S.nodes, S.geo, S.node_count, sc, S.wide};
   }
   __device__ uint32_t key(uint32_t k) const { return rng[path(k)]; }
   __device__ bool alpha_any() const { return any_alpha != 0; }
@@ -93,7 +94,7 @@ struct PathShadowMulti {
   __device__ BvhView bvh(uint32_t k) const { return scene_bvh(__ldg(sid + queue[k] / 3)); }  // slot 3 * path + j
   __device__ BvhView scene_bvh(int sc) const {
     const SceneDev& S = recs[sc].scene;
-    return {S.nodes, S.geo, S.node_count, sc};
+    return {S.nodes, S.geo, S.node_count, sc, S.wide};
   }
   __device__ double tmax(uint32_t k) const { return (double)so[k].w; }
   __device__ uint32_t key(uint32_t k) const { return __float_as_uint(sd[k].w); }
@@ -1001,6 +1002,16 @@ static void sort_rays(const MultiLaunch& M, Paths& P, int nxt, int blocks, cudaS
 }
 
 // ------------------------------------------------------------ one wave
+// Closest hit of a bounce: over the scenes' four-wide BVH views, or the
+// binary nodes with the top levels staged in shared memory. Hits are the same.
+static void launch_closest_multi(int wide, int blocks, int top, const TravArgs& A, const PathClosestMulti& pc,
+                                 cudaStream_t s) {
+  if (wide)
+    k_closest_wide_t<PathClosestMulti><<<blocks, PathClosestMulti::kThreads, 0, s>>>(A, pc);
+  else
+    k_closest_fast_t<PathClosestMulti><<<blocks, PathClosestMulti::kThreads, top_smem_bytes(top), s>>>(A, pc);
+}
+
 void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
   Paths P = M.paths;  // queue buffers swap with the sort buffer below
   PhaseEvents none{nullptr, nullptr, 0, 0};
@@ -1008,12 +1019,13 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
   E.mark(-1, s);
   k_camera_multi<<<grid_for(M.total_paths, 256), 256, 0, s>>>(P, M.recs, M.path_base, M.n, M.sid, M.S);
   E.mark(kPhCamera, s);
-  static int max_closest = 0, max_shade = 0;
+  static int max_closest = 0, max_wide = 0, max_shade = 0;
   if (!max_closest) {
     max_closest = persistent_blocks((const void*)k_closest_fast_t<PathClosestMulti>, PathClosestMulti::kThreads);
+    max_wide = persistent_blocks((const void*)k_closest_wide_t<PathClosestMulti>, PathClosestMulti::kThreads);
     max_shade = persistent_blocks((const void*)k_shade_t<SceneTable>, 128);
   }
-  const int closest_blocks = M.trace_blocks > 0 ? M.trace_blocks : max_closest;
+  const int closest_blocks = M.trace_blocks > 0 ? M.trace_blocks : M.wide ? max_wide : max_closest;
   const int shade_blocks = M.shade_blocks > 0 ? M.shade_blocks : max_shade;
   const int top = M.top_levels ? (M.n < kTopMaxScenes ? M.n : kTopMaxScenes) : 0;
   bool sorted = false;  // the rays of this bounce are in the sorted stream
@@ -1024,7 +1036,7 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     PathClosestMulti pc{P.ctr + kCtrQ0 + cur, sorted ? P.sray : P.nray, P.rng, P.hit, M.recs, M.any_alpha};
     TravArgs A{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
                M.trav_stats, top};
-    k_closest_fast_t<PathClosestMulti><<<closest_blocks, PathClosestMulti::kThreads, top_smem_bytes(top), s>>>(A, pc);
+    launch_closest_multi(M.wide, closest_blocks, top, A, pc, s);
     k_closest_exact_t<PathClosestMulti><<<64, 128, 0, s>>>(A, pc);
     E.mark(kPhClosest, s);
     k_shade_t<SceneTable><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b);
@@ -1058,11 +1070,13 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
 // then propagating dl through every vertex.
 void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t s) {
   const SceneRec* rec = M.recs;
-  static int closest_blocks = 0, shade_blocks = 0;
-  if (!closest_blocks) {
-    closest_blocks = persistent_blocks((const void*)k_closest_fast_t<PathClosestMulti>, PathClosestMulti::kThreads);
+  static int binary_blocks = 0, wide_blocks = 0, shade_blocks = 0;
+  if (!binary_blocks) {
+    binary_blocks = persistent_blocks((const void*)k_closest_fast_t<PathClosestMulti>, PathClosestMulti::kThreads);
+    wide_blocks = persistent_blocks((const void*)k_closest_wide_t<PathClosestMulti>, PathClosestMulti::kThreads);
     shade_blocks = persistent_blocks((const void*)k_shade_t<SceneTable, true>, 128);
   }
+  const int closest_blocks = M.wide ? wide_blocks : binary_blocks;
   const int top = M.top_levels ? (M.n < kTopMaxScenes ? M.n : kTopMaxScenes) : 0;
   for (int pass = 0; pass < 2; pass++) {
     const AdjointDev A{H.dl, H.lrem, H.gcont, H.gslot, H.genv, H.dmat, H.denv, M.total_pixels, pass == 0 ? 1 : 0};
@@ -1075,7 +1089,7 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
       PathClosestMulti pc{P.ctr + kCtrQ0 + cur, sorted ? P.sray : P.nray, P.rng, P.hit, M.recs, M.any_alpha};
       TravArgs TA{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
                   nullptr, top};
-      k_closest_fast_t<PathClosestMulti><<<closest_blocks, PathClosestMulti::kThreads, top_smem_bytes(top), s>>>(TA, pc);
+      launch_closest_multi(M.wide, closest_blocks, top, TA, pc, s);
       k_closest_exact_t<PathClosestMulti><<<64, 128, 0, s>>>(TA, pc);
       k_shade_t<SceneTable, true><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b, A);
       PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};

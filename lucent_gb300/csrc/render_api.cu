@@ -221,7 +221,8 @@ static void wave_key(const MultiLaunch& M, uint64_t key[4]) {
   key[1] = (uint64_t)M.total_pixels | ((uint64_t)(uint32_t)M.trace_blocks << 32);
   key[2] = ((uint64_t)(uintptr_t)M.paths.rec) ^ ((uint64_t)M.max_bounces << 48) ^ ((uint64_t)M.shade_blocks << 56);
   key[3] = ((uint64_t)(uintptr_t)M.recs) ^ ((uint64_t)(uintptr_t)M.path_base << 20) ^ ((uint64_t)M.any_alpha << 59) ^
-           ((uint64_t)M.any_tex << 60) ^ ((uint64_t)M.sort_rays << 61) ^ ((uint64_t)M.top_levels << 62) ^
+           ((uint64_t)M.wide << 58) ^ ((uint64_t)M.any_tex << 60) ^ ((uint64_t)M.sort_rays << 61) ^
+           ((uint64_t)M.top_levels << 62) ^
            ((uint64_t)(M.trav_stats != nullptr) << 63);
 }
 
@@ -229,6 +230,7 @@ struct lucent_renderer {
   uint32_t W = 1, H = 1;
   // scene
   DeviceBuffer nodes, geo, attr, mats, spheres, sph_mat, sph_light, lights;
+  DeviceBuffer wide;  // four-wide view of `nodes` (traverse_wide.cuh)
   // texture arrays (sRGB colour layers, linear data layers), decode tables, layer size (0: none)
   DeviceBuffer color_maps, data_maps, texel_lut;
   int tex_size = 0;
@@ -254,6 +256,7 @@ struct lucent_renderer {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // optional per-phase timing (lucent_renderer_set_profiling)
   bool profiling = false;
+  bool trav_counters = false;  // closest-hit traversal counters (profiling mode 2)
   std::vector<cudaEvent_t> pev;
   std::vector<int> ptag;
   int pn = 0;
@@ -269,6 +272,7 @@ struct lucent_renderer {
   uint32_t waves = 0;
   int sort_rays = 1;   // sort the rays of bounces 1 and 2 (lucent_renderer_set_ray_sort)
   int top_levels = 1;  // top BVH levels in shared memory (lucent_renderer_set_top_levels)
+  int wide_bvh = 1;    // four-wide closest-hit traversal (lucent_renderer_set_wide_bvh)
   // temporal reprojection (renderer.ts:441-451, 717-731): the view the accumulation was traced with
   int temporal = 1;
   bool has_history = false, reproject_pending = false;
@@ -398,7 +402,7 @@ static SceneRec scene_rec(const lucent_renderer* r) {
              (const int*)r->sph_light.ptr, (int)r->sphere_count, (const float4*)r->lights.ptr, (int)r->light_count,
              r->ground_enabled ? r->ground_material : -1, r->ground_height, r->any_alpha,
              (const uchar4*)r->color_maps.ptr, (const uchar4*)r->data_maps.ptr, (const float*)r->texel_lut.ptr,
-             r->tex_size};
+             r->tex_size, (const Node*)r->wide.ptr};
   R.light = r->light;
   R.cam = r->cam;
   R.accum = {(float4*)r->color.ptr, (half4*)r->albedo.ptr, (half4*)r->normal.ptr, (float*)r->history.ptr};
@@ -483,6 +487,7 @@ static lucent_status single_launch(lucent_renderer* r, uint32_t S, uint32_t tail
   M.any_alpha = r->any_alpha;
   M.sort_rays = r->sort_rays;
   M.top_levels = r->top_levels;
+  M.wide = r->wide_bvh;
   M.any_tex = r->tex_size > 0;
   return LUCENT_OK;
 }
@@ -636,6 +641,8 @@ lucent_status lucent_renderer_load_scene(lucent_renderer* r, const lucent_scene_
   const uint32_t nc = (uint32_t)(ref.size() / 8);
   if (tree_depth(ref.data(), nc, n) + 2 > kTsStack)
     return cleanup(fail(LUCENT_ERR_UNSUPPORTED, "BVH deeper than the reference's 64-entry traversal stack"));
+  if ((st = r->wide.reserve((size_t)nc * 4 * sizeof(Node)))) return cleanup(st);
+  launch_wide_view((const Node*)r->nodes.ptr, nc, (Node*)r->wide.ptr, s);
   if ((st = upload(idx, tri.data(), (size_t)n * 4)) || (st = r->geo.reserve((size_t)(n ? n : 1) * 48)) ||
       (st = r->attr.reserve((size_t)(n ? n : 1) * 64)))
     return cleanup(st);
@@ -794,7 +801,7 @@ lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* 
   lucent_status st = prepare_reprojection(r, s);
   if (!st) st = single_launch(r, batch, tail, r->seed, s, M);
   if (st) return st;
-  M.trav_stats = r->profiling ? (unsigned long long*)((uint32_t*)r->ctr.ptr + kCtrTrav) : nullptr;
+  M.trav_stats = r->trav_counters ? (unsigned long long*)((uint32_t*)r->ctr.ptr + kCtrTrav) : nullptr;
   cudaEventRecord(r->ev0, s);
   PhaseEvents pe{r->pev.data(), r->ptag.data(), (int)r->pev.size(), 0};
   uint64_t key[4];
@@ -910,6 +917,13 @@ lucent_status lucent_renderer_set_top_levels(lucent_renderer* r, int32_t enabled
   return LUCENT_OK;
 }
 
+lucent_status lucent_renderer_set_wide_bvh(lucent_renderer* r, int32_t enabled) {
+  clear_error();
+  if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  r->wide_bvh = enabled ? 1 : 0;
+  return LUCENT_OK;
+}
+
 lucent_status lucent_renderer_trim(lucent_renderer* r) {
   clear_error();
   if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
@@ -926,6 +940,7 @@ lucent_status lucent_renderer_set_profiling(lucent_renderer* r, int32_t enabled)
   clear_error();
   if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
   r->profiling = enabled != 0;
+  r->trav_counters = enabled == 2;
   if (r->profiling && r->pev.empty()) {
     r->pev.resize(1024);
     r->ptag.resize(1024);
@@ -1066,7 +1081,7 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
 
 struct lucent_batch {
   std::vector<lucent_renderer*> rs;
-  lucent_batch_options opt{0, 1u << 25, 1, 0, 0, 1, 1};
+  lucent_batch_options opt{0, 1u << 25, 1, 0, 0, 1, 1, 1};
   DeviceBuffer recs, bases, tail_bases, sid, paths, ctr;
   uint32_t path_cap = 0, sid_cap = 0;
   Paths P{};
@@ -1177,6 +1192,7 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
   M.shade_blocks = (int)b->opt.shade_blocks;
   M.sort_rays = b->opt.sort_rays;
   M.top_levels = b->opt.top_levels;
+  M.wide = b->opt.wide_bvh;
   for (lucent_renderer* rr : b->rs) M.any_tex |= rr->tex_size > 0;
   auto setup = [&](uint32_t s_wave, const DeviceBuffer& base) {
     M.S = (int)s_wave;

@@ -113,6 +113,7 @@ struct MultiLaunch {
   int sort_rays;                   // after bounces 0 and 1, sort the rays by scene, direction octant and origin cell
   int top_levels;                  // stage the top BVH levels of (up to 8) scenes in shared memory
   int any_tex;                     // some scene has texture maps: launch the TEX shade instantiation
+  int wide;                        // closest hit over the scenes' four-wide BVH views
 };
 
 // Optional per-phase timing: events recorded between launches, each tagged

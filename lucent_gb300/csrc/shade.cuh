@@ -151,6 +151,7 @@ struct SceneDev {
   const uchar4* data_maps;
   const float* texel_lut;
   int tex_size;
+  const Node* wide;  // four-wide view of `nodes` (traverse_wide.cuh) or nullptr
 };
 
 // transformUV (scene.glsl:95-97): rows of a 2x3 affine map.

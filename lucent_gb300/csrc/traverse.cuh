@@ -76,6 +76,8 @@ struct TravArgs {
   // Scenes (0, 1, ... top_scenes - 1) whose top BVH levels each block stages
   // in shared memory (0 = off); the launch passes top_smem_bytes(top_scenes).
   int top_scenes = 0;
+  // Four-wide view of `nodes` (traverse_wide.cuh) for the wide kernels.
+  const Node* wide = nullptr;
 };
 
 
@@ -90,6 +92,7 @@ struct BvhView {
   const float4* tris;
   uint32_t node_limit;
   int scene;
+  const Node* wide = nullptr;  // four-wide view (traverse_wide.cuh), when built
 };
 template <class Pol>
 __device__ __forceinline__ BvhView bvh_of(const TravArgs& A, const Pol& P, uint32_t k) {
@@ -239,7 +242,7 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_fast
   const uint32_t n = P.count();
   const bool use_alpha = P.alpha_any();
 
-  bool active = false, exhausted = false, have_cur = false, c_exact = true, best_exact = false;
+  bool active = false, exhausted = false, have_cur = false, c_exact = true, best_exact = false, have_est = false;
   uint32_t ri = 0, iters = 0, key = 0;
   Ray32 r;
   float c_lo = 0.f, c_hi = 0.f;
@@ -281,6 +284,7 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_fast
             c64 = A.tMax;
             c_exact = true;
             best_exact = false;
+            have_est = false;
             best = -1;
             sp = 0;
             iters = 0;
@@ -328,16 +332,31 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_fast
       if (sp == 0) {  // finished
         if (best < 0) {
           P.miss(ri);
-        } else if (best_exact) {
-          P.hit(ri, best, c64, bu64, bv64);
         } else if (P.exact_output()) {  // the reference's binary64 t, u, v
-          count_stat(A, 4);
+          if (best_exact) {
+            P.hit(ri, best, c64, bu64, bv64);
+          } else {
+            count_stat(A, 4);
+            const float4 a = __ldg(bv.tris + 3 * (size_t)best), b = __ldg(bv.tris + 3 * (size_t)best + 1),
+                         c = __ldg(bv.tris + 3 * (size_t)best + 2);
+            const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, INF64);
+            P.hit(ri, best, h.t, h.u, h.v);
+          }
+        } else if (have_est) {  // binary32 t, u, v like the GLSL's own
+          P.hit32(ri, best, best_est);
+        } else {
+          // Accepted in binary64. The output is a function of the ray and the
+          // triangle alone, whatever decisions led there: the binary32
+          // estimate where binary32 accepts the triangle at c = tMax (as it
+          // does for every triangle accepted in binary32), else binary64's.
           const float4 a = __ldg(bv.tris + 3 * (size_t)best), b = __ldg(bv.tris + 3 * (size_t)best + 1),
                        c = __ldg(bv.tris + 3 * (size_t)best + 2);
-          const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, INF64);
-          P.hit(ri, best, h.t, h.u, h.v);
-        } else {  // same triangle; binary32 t, u, v like the GLSL's own
-          P.hit32(ri, best, best_est);
+          float tl, th;
+          float3 est;
+          if (mt_classify(r, a, b, c, tmin_lo, tmin_hi, cmax_lo, cmax_hi, tl, th, est) == kTriAccept)
+            P.hit32(ri, best, est);
+          else
+            P.hit(ri, best, c64, bu64, bv64);
         }
         active = false;
         continue;
@@ -378,6 +397,7 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_fast
         if (tc == kTriAccept) {
           best = slot;
           best_est = est;
+          have_est = true;
           best_exact = false;
           c_exact = false;
           c_lo = tl;
@@ -389,6 +409,7 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_fast
         const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, cc);
         if (h.hit) {
           best = slot;
+          have_est = false;
           c64 = h.t;
           bu64 = h.u;
           bv64 = h.v;

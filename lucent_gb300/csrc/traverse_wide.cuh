@@ -1,0 +1,306 @@
+// Four-wide traversal over the reference's binary BVH, with the reference's
+// decisions and order.
+//
+// The wide view holds, for every inner binary node n, four records: the
+// grandchildren of n in the reference's visiting order (left subtree first),
+// where a child of n that is a leaf stands in for its two (absent)
+// grandchildren. One expansion therefore descends two levels with one
+// 128-byte read instead of two dependent 64-byte reads, and skips the box
+// tests of n's inner children.
+//
+// Skipping those tests changes no decision. A child's box lies inside its
+// parent's (the builder's parent bounds are the union of its children's), so
+// per axis the child's entry distance is >= the parent's and its exit <= the
+// parent's, in binary32 and binary64 alike (rounding is monotone, and the
+// fast path only takes rays whose inverse direction is finite). The
+// reference's cull test, max(0, entries) > min(closest, exits), therefore
+// culls a grandchild whenever it culls the child above it, and testing the
+// grandchild alone gives the reference's answer for it. The other rules are
+// those of the binary kernel: the first record that passes continues at once
+// (nothing between the parent's test and the reference's pop of it can lower
+// the closest distance), the others are pushed with an upper bound on their
+// entry distance and re-tested on pop only if the closest distance has
+// dropped below it.
+//
+// A record is a binary node record: box, then (lo.w) its own binary index for
+// an inner node (count 0) or its first triangle slot for a leaf (count > 0);
+// count -1 marks an unused record.
+#pragma once
+#include "traverse.cuh"
+
+namespace lucent {
+
+constexpr int kWide = 4;
+// Pending records: at most 3 per expansion, one expansion per two levels of a
+// tree at most 62 deep (the reference's 64-entry stack less the root and one).
+constexpr int kWideStack = 96;
+
+__device__ __forceinline__ Node wide_record(const Node* nodes, int c, uint32_t n_nodes) {
+  Node r = load_node(nodes, c);
+  if (node_count(r) == 0) r.lo.w = __int_as_float(c);
+  return r;
+}
+
+// Fills wide[4 n .. 4 n + 3] for every binary node n (unused records for leaves).
+static __global__ void k_build_wide(const Node* nodes, uint32_t n_nodes, Node* wide) {
+  const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= n_nodes) return;
+  const float inf = __int_as_float(0x7f800000);
+  Node rec[kWide];
+  for (int k = 0; k < kWide; k++) rec[k] = {make_float4(inf, inf, inf, 0.f), make_float4(-inf, -inf, -inf, __int_as_float(-1))};
+  const Node nd = load_node(nodes, n);
+  const int f = node_first(nd);
+  if (node_count(nd) == 0 && f > 0 && (uint32_t)f + 1 < n_nodes) {
+    int m = 0;
+    for (int c = f; c <= f + 1; c++) {
+      const Node cn = load_node(nodes, c);
+      const int g = node_first(cn);
+      if (node_count(cn) > 0) {
+        rec[m++] = cn;
+      } else if (g > 0 && (uint32_t)g + 1 < n_nodes) {
+        rec[m++] = wide_record(nodes, g, n_nodes);
+        rec[m++] = wide_record(nodes, g + 1, n_nodes);
+      }
+    }
+  }
+  float4* out = reinterpret_cast<float4*>(wide + (size_t)kWide * n);
+  for (int k = 0; k < kWide; k++) {
+    out[2 * k] = rec[k].lo;
+    out[2 * k + 1] = rec[k].hi;
+  }
+}
+
+static inline void launch_build_wide(const Node* nodes, uint32_t n_nodes, Node* wide, cudaStream_t s) {
+  if (n_nodes) k_build_wide<<<(n_nodes + 255) / 256, 256, 0, s>>>(nodes, n_nodes, wide);
+}
+
+struct WidePending {
+  int rec;    // index of the record in the wide array (4 n + k)
+  float ehi;  // upper bound on its entry distance when it was pushed
+};
+
+// Closest hit over the wide view: k_closest_fast_t's persistent warps, per-lane
+// refill, bounded-error binary32 decisions and binary64 fallbacks, with each
+// inner step expanding four records (bv.wide must be set).
+template <class Pol>
+__global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide_t(TravArgs A, Pol P) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const float tmin_lo = __double2float_rd(A.tMin), tmin_hi = __double2float_ru(A.tMin);
+  const float cmax_lo = __double2float_rd(A.tMax), cmax_hi = __double2float_ru(A.tMax);
+  const double INF64 = __longlong_as_double(0x7ff0000000000000ll);
+  const uint32_t n = P.count();
+  const bool use_alpha = P.alpha_any();
+
+  bool active = false, exhausted = false, have_cur = false, c_exact = true, best_exact = false, have_est = false;
+  uint32_t ri = 0, iters = 0, key = 0;
+  Ray32 r;
+  float c_lo = 0.f, c_hi = 0.f;
+  double c64 = A.tMax, bu64 = 0, bv64 = 0;
+  float3 best_est = make_float3(0.f, 0.f, 0.f);
+  int best = -1, sp = 0;
+  BvhView bv{A.nodes, A.tris, A.node_limit, 0, A.wide};
+  Node cur;
+  WidePending stack[kWideStack];
+
+  while (true) {
+    const bool need = !active && !exhausted;
+    const unsigned m = __ballot_sync(FULL, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(A.work, (uint32_t)__popc(m));
+      base = __shfl_sync(FULL, base, leader);
+      if (need) {
+        ri = base + __popc(m & lt);
+        if (ri >= n) {
+          exhausted = true;
+        } else {
+          float3 o, d;
+          P.ray(ri, o, d);
+          if (!safe_ray(o, d)) {
+            A.queue[atomicAdd(A.queue_len, 1u)] = ri;
+          } else {
+            r = make_ray32(o, d);
+            key = P.key(ri);
+            if constexpr (Pol::kMultiScene) bv = P.bvh(ri);
+            c_lo = cmax_lo;
+            c_hi = cmax_hi;
+            c64 = A.tMax;
+            c_exact = true;
+            best_exact = false;
+            have_est = false;
+            best = -1;
+            sp = 0;
+            iters = 0;
+            count_stat(A, 0);
+            cur = wide_record(bv.nodes, 0, bv.node_limit);  // the reference pops the root first and tests its box
+            SlabClass cl = classify_slab(r, cur.lo, cur.hi, c_lo, c_hi);
+            if (cl == kAmbiguous) {
+              count_stat(A, 1);
+              cl = slab_f64_culled(cur.lo, cur.hi, o, d, c64) ? kCulled : kPass;
+            }
+            have_cur = cl != kCulled;
+            active = true;
+          }
+        }
+      }
+    }
+    if (__all_sync(FULL, exhausted)) break;
+    if (!active) continue;
+
+    auto exact_c = [&]() {  // the reference's binary64 `closest`, on demand
+      if (!c_exact) {
+        count_stat(A, 3);
+        const float4 a = __ldg(bv.tris + 3 * (size_t)best), b = __ldg(bv.tris + 3 * (size_t)best + 1),
+                     c = __ldg(bv.tris + 3 * (size_t)best + 2);
+        const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, INF64);
+        c64 = h.t;
+        bu64 = h.u;
+        bv64 = h.v;
+        c_exact = true;
+        best_exact = true;
+        c_lo = __double2float_rd(h.t);
+        c_hi = __double2float_ru(h.t);
+      }
+      return c64;
+    };
+    auto slab_decide = [&](const Node& nd, SlabClass cl) {
+      if (cl != kAmbiguous) return cl;
+      count_stat(A, 1);
+      return slab_f64_culled(nd.lo, nd.hi, r.o, r.d, exact_c()) ? kCulled : kPass;
+    };
+
+    if (!have_cur) {
+      if (sp == 0) {  // finished
+        if (best < 0) {
+          P.miss(ri);
+        } else if (P.exact_output()) {  // the reference's binary64 t, u, v
+          if (best_exact) {
+            P.hit(ri, best, c64, bu64, bv64);
+          } else {
+            count_stat(A, 4);
+            const float4 a = __ldg(bv.tris + 3 * (size_t)best), b = __ldg(bv.tris + 3 * (size_t)best + 1),
+                         c = __ldg(bv.tris + 3 * (size_t)best + 2);
+            const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, INF64);
+            P.hit(ri, best, h.t, h.u, h.v);
+          }
+        } else if (have_est) {  // binary32 t, u, v like the GLSL's own
+          P.hit32(ri, best, best_est);
+        } else {
+          // Accepted in binary64. The output is a function of the ray and the
+          // triangle alone, whatever decisions led there: the binary32
+          // estimate where binary32 accepts the triangle at c = tMax (as it
+          // does for every triangle accepted in binary32), else binary64's.
+          const float4 a = __ldg(bv.tris + 3 * (size_t)best), b = __ldg(bv.tris + 3 * (size_t)best + 1),
+                       c = __ldg(bv.tris + 3 * (size_t)best + 2);
+          float tl, th;
+          float3 est;
+          if (mt_classify(r, a, b, c, tmin_lo, tmin_hi, cmax_lo, cmax_hi, tl, th, est) == kTriAccept)
+            P.hit32(ri, best, est);
+          else
+            P.hit(ri, best, c64, bu64, bv64);
+        }
+        active = false;
+        continue;
+      }
+      const WidePending e = stack[--sp];
+      const Node nd = load_node(bv.wide, e.rec);
+      if (e.ehi > c_lo && slab_decide(nd, classify_slab(r, nd.lo, nd.hi, c_lo, c_hi)) == kCulled) continue;
+      cur = nd;
+      have_cur = true;
+    }
+    if (++iters > bv.node_limit) {  // a valid BVH visits each node at most once per ray
+      atomicOr(A.err, kErrIterations);
+      P.fail(ri);
+      active = false;
+      have_cur = false;
+      continue;
+    }
+    const int cnt = node_count(cur), first = node_first(cur);
+    if (cnt > 0) {
+      bool defer = false;
+      for (int k = 0; k < cnt; k++) {
+        const int slot = first + k;
+        const float4 a = __ldg(bv.tris + 3 * (size_t)slot), b = __ldg(bv.tris + 3 * (size_t)slot + 1),
+                     c = __ldg(bv.tris + 3 * (size_t)slot + 2);
+        float tl, th;
+        float3 est;
+        const TriClass tc = mt_classify(r, a, b, c, tmin_lo, tmin_hi, c_lo, c_hi, tl, th, est);
+        if (tc == kTriReject) continue;
+        if (use_alpha) {
+          const AlphaAnswer aa = P.alpha_fast(bv.scene, slot, key);
+          if (aa == kAlphaDefer) {
+            defer = true;
+            break;
+          }
+          if (aa == kAlphaPass) continue;
+        }
+        if (tc == kTriAccept) {
+          best = slot;
+          best_est = est;
+          have_est = true;
+          best_exact = false;
+          c_exact = false;
+          c_lo = tl;
+          c_hi = th;
+          continue;
+        }
+        count_stat(A, 2);
+        const double cc = exact_c();
+        const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, cc);
+        if (h.hit) {
+          best = slot;
+          have_est = false;
+          c64 = h.t;
+          bu64 = h.u;
+          bv64 = h.v;
+          c_exact = true;
+          best_exact = true;
+          c_lo = __double2float_rd(h.t);
+          c_hi = __double2float_ru(h.t);
+        }
+      }
+      have_cur = false;
+      if (defer) {  // a textured alpha test: the binary64 kernel traces this ray
+        A.queue[atomicAdd(A.queue_len, 1u)] = ri;
+        active = false;
+        continue;
+      }
+    } else {
+      // Expand: the four records of `cur`, last to first, so that the first
+      // that passes continues and the others are pushed in reverse order.
+      const int base = kWide * first;
+      int pend = -1;
+      float pend_ehi = 0.f;
+      Node next;
+      bool overflow = false;
+#pragma unroll
+      for (int k = kWide - 1; k >= 0; k--) {
+        const Node s = load_node(bv.wide, base + k);
+        if (node_count(s) < 0) continue;
+        float eh;
+        if (slab_decide(s, classify_slab_e(r, s.lo, s.hi, c_lo, c_hi, eh)) != kPass) continue;
+        if (pend >= 0) {
+          if (sp >= kWideStack) overflow = true;
+          else stack[sp++] = {base + pend, pend_ehi};
+        }
+        pend = k;
+        pend_ehi = eh;
+        next = s;
+      }
+      if (overflow) {  // unreachable for trees the reference's stack can traverse
+        atomicOr(A.err, kErrStack);
+        P.fail(ri);
+        active = false;
+        have_cur = false;
+        continue;
+      }
+      if (pend >= 0) cur = next;
+      else have_cur = false;
+    }
+  }
+}
+
+}  // namespace lucent

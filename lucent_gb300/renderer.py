@@ -209,6 +209,10 @@ class Renderer:
                                                       N.ptr(dat, C.c_uint8)))
         return col, dat
 
+    def set_wide_bvh(self, enabled=True):
+        """Closest hit over the four-wide BVH view (lucent_renderer_set_wide_bvh)."""
+        N.check(N.lib().lucent_renderer_set_wide_bvh(self._h, 1 if enabled else 0))
+
     def set_top_levels(self, enabled=True):
         """Stage the top BVH levels in shared memory (lucent_renderer_set_top_levels)."""
         N.check(N.lib().lucent_renderer_set_top_levels(self._h, 1 if enabled else 0))
@@ -217,8 +221,10 @@ class Renderer:
         """Frees the path-state buffers until the next trace (lucent_renderer_trim)."""
         N.check(N.lib().lucent_renderer_trim(self._h))
 
-    def set_profiling(self, enabled=True):
-        N.check(N.lib().lucent_renderer_set_profiling(self._h, 1 if enabled else 0))
+    def set_profiling(self, enabled=True, counters=False):
+        """Per-phase event timing (lucent_renderer_set_profiling); `counters`
+        adds the closest-hit traversal counters, which slow that kernel."""
+        N.check(N.lib().lucent_renderer_set_profiling(self._h, (2 if counters else 1) if enabled else 0))
 
     # --------------------------------------------------------- denoise/display
     def samples(self):
@@ -303,11 +309,11 @@ class Batch:
     each renderer alone would give. Options (lucent_batch_options):
     samples_per_wave (0 = as many as max_wave_paths allows), max_wave_paths,
     use_graph (replay a captured wave), trace_blocks / shade_blocks (grid
-    sizes, 0 = all resident blocks), sort_rays, top_levels (as the
-    renderer's set_ray_sort / set_top_levels)."""
+    sizes, 0 = all resident blocks), sort_rays, top_levels, wide_bvh (as
+    the renderer's set_ray_sort / set_top_levels / set_wide_bvh)."""
 
     DEFAULTS = {"samples_per_wave": 0, "max_wave_paths": 1 << 25, "use_graph": True, "trace_blocks": 0,
-                "shade_blocks": 0, "sort_rays": True, "top_levels": True}
+                "shade_blocks": 0, "sort_rays": True, "top_levels": True, "wide_bvh": True}
 
     def __init__(self, renderers, **options):
         self.renderers = list(renderers)
@@ -326,7 +332,7 @@ class Batch:
         o = self.options
         d = NR.BatchOptions(o["samples_per_wave"], o["max_wave_paths"], 1 if o["use_graph"] else 0,
                             o["trace_blocks"], o["shade_blocks"], 1 if o["sort_rays"] else 0,
-                            1 if o["top_levels"] else 0)
+                            1 if o["top_levels"] else 0, 1 if o["wide_bvh"] else 0)
         N.check(N.lib().lucent_batch_set_options(self._h, C.byref(d)))
 
     def trace_samples(self, count, stream=None):

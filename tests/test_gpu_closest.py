@@ -16,19 +16,20 @@ pytestmark = pytest.mark.gpu
 
 def _compare(dev, ob, pos, rays32, t_min=1e-5, t_max=math.inf):
     ids_o, t_o, u_o, v_o = oracle.intersect_bvh(ob, pos, rays32, t_min, t_max)
-    # binary32 path with and without the shared-memory top levels, then all binary64
-    for exact, top in ((False, True), (False, False), (True, True)):
-        dev.set_mode(exact, top_levels=top)
+    # binary32 path with and without the shared-memory top levels, over the
+    # four-wide view, then all binary64
+    for exact, top, wide in ((False, True, False), (False, False, False), (False, False, True), (True, True, False)):
+        dev.set_mode(exact, top_levels=top, wide=wide)
         prim, t, u, v = dev.intersect(rays32, t_min, t_max)
         bad = np.nonzero(prim != ids_o)[0]
-        assert bad.size == 0, "exact=%s top=%s: %d id mismatches, first ray %d: gpu %d oracle %d" % (
-            exact, top, bad.size, bad[:1], prim[bad[:1]], ids_o[bad[:1]])
+        assert bad.size == 0, "exact=%s top=%s wide=%s: %d id mismatches, first ray %d: gpu %d oracle %d" % (
+            exact, top, wide, bad.size, bad[:1], prim[bad[:1]], ids_o[bad[:1]])
         hit = ids_o >= 0
         assert np.array_equal(t[hit], t_o[hit].astype(np.float32))
         assert np.array_equal(u[hit], u_o[hit].astype(np.float32))
         assert np.array_equal(v[hit], v_o[hit].astype(np.float32))
         assert np.all(np.isinf(t[~hit]))
-    dev.set_mode(False)
+    dev.set_mode(False)  # the default: four-wide
     return ids_o
 
 

@@ -152,3 +152,19 @@ def test_texture_errors(textured):
     with pytest.raises(LucentError):  # an empty image
         r.load_scene(bad)
     r.dispose()
+
+
+def test_wide_traversal_changes_no_pixel_with_alpha_cutouts(textured):
+    # The textured model has an alpha-mask cutout: deferred texture-alpha rays
+    # go to the binary64 kernel from the wide traversal as from the binary one.
+    out = []
+    for wide in (True, False):
+        r = Renderer(64, 64)
+        r.settings.max_bounces = 6
+        r.load_scene(textured)
+        r.set_wide_bvh(wide)
+        r.set_seed(3)
+        r.trace_samples(4)
+        out.append(r.read())
+        r.dispose()
+    assert all(np.array_equal(a, b) for a, b in zip(*out))
