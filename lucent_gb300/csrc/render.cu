@@ -1012,6 +1012,14 @@ static void launch_closest_multi(int wide, int blocks, int top, const TravArgs& 
     k_closest_fast_t<PathClosestMulti><<<blocks, PathClosestMulti::kThreads, top_smem_bytes(top), s>>>(A, pc);
 }
 
+static void launch_shadow_multi(int wide, int blocks, int top, const TravArgs& A, const PathShadowMulti& ps,
+                                cudaStream_t s) {
+  if (wide)
+    k_anyhit_wide_t<PathShadowMulti><<<blocks, 256, 0, s>>>(A, ps);
+  else
+    k_anyhit_fast_t<PathShadowMulti><<<blocks, 256, top_smem_bytes(top), s>>>(A, ps);
+}
+
 void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
   Paths P = M.paths;  // queue buffers swap with the sort buffer below
   PhaseEvents none{nullptr, nullptr, 0, 0};
@@ -1045,7 +1053,7 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};
     TravArgs B{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr,
                nullptr, top};
-    k_anyhit_fast_t<PathShadowMulti><<<shade_blocks * 2, 256, top_smem_bytes(top), s>>>(B, ps);
+    launch_shadow_multi(M.wide, shade_blocks * 2, top, B, ps, s);
     k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, s>>>(B, ps);
     E.mark(kPhShadow, s);
     // Resolve is per path: it walks the queue as it was before the sort (still
@@ -1095,7 +1103,7 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
       PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};
       TravArgs TB{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr,
                   nullptr, top};
-      k_anyhit_fast_t<PathShadowMulti><<<shade_blocks * 2, 256, top_smem_bytes(top), s>>>(TB, ps);
+      launch_shadow_multi(M.wide, shade_blocks * 2, top, TB, ps, s);
       k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, s>>>(TB, ps);
       Paths Pr = P;  // resolve walks the pre-sort queue, in path order
       if (sorted) Pr.q[cur] = P.sort_tmp;

@@ -303,4 +303,96 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
   }
 }
 
+// Any hit over the wide view: one ray per thread (grid-stride), as
+// k_anyhit_fast_t. With the cull distance fixed at tMax the answer does not
+// depend on visiting order, and a leaf is reached exactly when its own box
+// passes (a culled ancestor implies a culled leaf), so testing every
+// expanded record once gives the reference's answer. Pushed records have
+// passed their test; a pop only expands or tests triangles.
+template <class Pol>
+__global__ void __launch_bounds__(256, 4) k_anyhit_wide_t(TravArgs A, Pol P) {
+  const float tmin_lo = __double2float_rd(A.tMin), tmin_hi = __double2float_ru(A.tMin);
+  const uint32_t n = P.count();
+  const bool use_alpha = P.alpha_any();
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    float3 o, d;
+    P.ray(k, o, d);
+    if (!safe_ray(o, d)) {
+      A.queue[atomicAdd(A.queue_len, 1u)] = k;
+      continue;
+    }
+    const Ray32 r = make_ray32(o, d);
+    const uint32_t key = P.key(k);
+    const double tmax = P.tmax(k);
+    BvhView bv = bvh_of(A, P, k);
+    if constexpr (!Pol::kMultiScene) bv.wide = A.wide;
+    const float c_lo = __double2float_rd(tmax), c_hi = __double2float_ru(tmax);
+    auto passes = [&](const Node& nd) {
+      SlabClass cl = classify_slab(r, nd.lo, nd.hi, c_lo, c_hi);
+      if (cl == kAmbiguous) cl = ts_slab_culled(nd.lo, nd.hi, {o.x, o.y, o.z}, inv_exact(d), tmax) ? kCulled : kPass;
+      return cl == kPass;
+    };
+    int stack[kWideStack];  // indices of records that passed their box test
+    int sp = 0;
+    bool occ = false, ok = true, defer = false;
+    uint32_t iters = 0;
+    Node cur = wide_record(bv.nodes, 0, bv.node_limit);
+    bool have = passes(cur);
+    while (have) {
+      if (++iters > bv.node_limit) {
+        atomicOr(A.err, kErrIterations);
+        ok = false;
+        break;
+      }
+      const int cnt = node_count(cur), first = node_first(cur);
+      if (cnt > 0) {
+        for (int q = 0; q < cnt && !occ && !defer; q++) {
+          const int slot = first + q;
+          const float4 a = __ldg(bv.tris + 3 * (size_t)slot), b = __ldg(bv.tris + 3 * (size_t)slot + 1),
+                       c = __ldg(bv.tris + 3 * (size_t)slot + 2);
+          float tl, th;
+          float3 est;
+          const TriClass tc = mt_classify(r, a, b, c, tmin_lo, tmin_hi, c_lo, c_hi, tl, th, est);
+          if (tc == kTriReject) continue;
+          if (use_alpha) {
+            const AlphaAnswer aa = P.alpha_fast(bv.scene, slot, key);
+            if (aa == kAlphaDefer) {
+              defer = true;
+              continue;
+            }
+            if (aa == kAlphaPass) continue;
+          }
+          if (tc == kTriAccept) {
+            occ = true;
+          } else {
+            double t, u, v;
+            occ = ts_triangle({o.x, o.y, o.z}, {d.x, d.y, d.z}, d3f(a), d3f(b), d3f(c), A.tMin, tmax, t, u, v);
+          }
+        }
+        if (occ || defer) break;
+      } else {
+        const int base = kWide * first;
+#pragma unroll
+        for (int q = 0; q < kWide; q++) {
+          const Node s = load_node(bv.wide, base + q);
+          if (node_count(s) < 0 || !passes(s)) continue;
+          if (sp >= kWideStack) ok = false;
+          else stack[sp++] = base + q;
+        }
+        if (!ok) {  // unreachable for trees the reference's stack can traverse
+          atomicOr(A.err, kErrStack);
+          break;
+        }
+      }
+      have = sp > 0;
+      if (have) cur = load_node(bv.wide, stack[--sp]);
+    }
+    if (defer && ok) {  // a textured alpha test: the binary64 kernel answers this ray
+      A.queue[atomicAdd(A.queue_len, 1u)] = k;
+      continue;
+    }
+    P.shadow(k, ok ? occ : true);
+  }
+}
+
 }  // namespace lucent
