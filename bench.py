@@ -182,7 +182,8 @@ def run_ours_closest(args, rank, world, local):
         achieved = per_launch / (sum(ms) / len(ms) / 1000.0) / 1e9
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": NCU_DRAM_BYTES_CLOSEST_LAUNCH,
-                "peak_source": which, "bytes_per_ray": alg["bytes_per_ray"]}
+                "peak_source": which, "kernel": "k_closest_wide_t<ApiPolicy> (+ slow path)",
+                "bytes_per_ray": alg["bytes_per_ray"]}
     return {
         "metric": "closest-hit Mrays/s (intersectBVH, 65,536-triangle soup, 1e6 rays)",
         "value": round(value, 2), "unit": "Mrays/s", "ms_per_step": round(sum(ms) / len(ms), 4),
@@ -210,9 +211,9 @@ def cpu_closest(threads, sample_rays=1_000_000, reps=3):
 PT_W, PT_H, PT_SPP, PT_DEPTH = 512, 512, 16, 8
 CPU_BASELINE_SECONDS = 10.0
 # dram__bytes_read.sum + dram__bytes_write.sum from ncu captures of the same
-# workloads (profiles/closest_pt_box512_16spp.md, closest_fast_soup65k_1Mrays.md).
-NCU_DRAM_BYTES_PT_FRAME = 1_478_600_000
-NCU_DRAM_BYTES_CLOSEST_LAUNCH = 164_400_000
+# workloads (profiles/closest_pt_box512_16spp.md, closest_wide_soup65k_1Mrays.md).
+NCU_DRAM_BYTES_PT_FRAME = 824_400_000
+NCU_DRAM_BYTES_CLOSEST_LAUNCH = 115_400_000
 PT_METRIC = ("closest-hit Mrays/s inside path tracing: box scene (81,956 triangles), 512x512, 16 spp, "
              "max depth 8 (also spp/s)")
 
@@ -304,7 +305,7 @@ def run_ours_pt(args, rank, world, local):
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": NCU_DRAM_BYTES_PT_FRAME,
                 "traffic_scope": "DRAM bytes of the frame's 9 closest-hit launches (ncu), like achieved",
-                "peak_source": which, "kernel": "k_closest_fast_t<PathClosestMulti> (+ slow path)",
+                "peak_source": which, "kernel": "k_closest_wide_t<PathClosestMulti> (+ slow path)",
                 "bytes_per_closest_ray": alg["bytes_per_closest_ray"],
                 "closest_ms_per_frame": round(ph["closest"], 3)}
     # camera, accumulate, seed advance; 8 per bounce (counters, closest fast + exact, shade, any-hit fast +
