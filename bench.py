@@ -351,15 +351,27 @@ def cpu_pt(threads, reps=1, crop=512):
 BATCH_SPP, BATCH_DEPTH = 64, 8
 
 
-def _batch_setup(n):
+def _batch_setup(n, timing=None):
+    """Renderers for batch scenes 0..n-1; `timing` collects seconds spent
+    generating the synthetic scenes ("generate") and loading them through
+    the C ABI ("load": packing, GPU BVH build, wide view, upload, lighting)."""
+    import torch
     from lucent_gb300 import workloads as W
     from lucent_gb300.renderer import Renderer
+    timing = {} if timing is None else timing
+    timing.setdefault("generate", 0.0)
+    timing.setdefault("load", 0.0)
     rs = []
     for seed in range(n):
+        t0 = time.perf_counter()
         sc, res = W.batch_scene(seed)
+        t1 = time.perf_counter()
         r = Renderer(res, res)
         r.settings.max_bounces = BATCH_DEPTH
         r.load_scene(sc)
+        torch.cuda.synchronize()
+        timing["generate"] += t1 - t0
+        timing["load"] += time.perf_counter() - t1
         rs.append(r)
     return rs
 
@@ -386,7 +398,8 @@ def run_ours_batch(args, rank, world, local):
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
     t_setup = time.perf_counter()
-    rs = _batch_setup(args.batch_scenes)
+    setup_t = {}
+    rs = _batch_setup(args.batch_scenes, setup_t)
     setup_s = time.perf_counter() - t_setup
     px = sum(r.width * r.height for r in rs)
     tris = sum(r.stats()["triangles"] for r in rs)
@@ -413,7 +426,7 @@ def run_ours_batch(args, rank, world, local):
         r.trace_samples(1, sp)
         r.check(sp)
         r.trim()
-    tuned, trials = b.autotune(samples=2)
+    tuned, trials = b.autotune(samples=8)
     barrier(world)
     torch.cuda.synchronize()
     for _ in range(args.warmup):
@@ -462,7 +475,9 @@ def run_ours_batch(args, rank, world, local):
         "extra": {"sequential_mpaths_per_s": round(seq_value, 2), "batched_over_sequential": round(dev_s / dev_b, 3),
                   "identical_images": bool(same), "tuned_options": tuned,
                   "autotune_trials_s": {str(k): round(v, 4) for k, v in trials.items()},
-                  "waves_per_step": st["waves"] // max(1, args.steps + args.warmup + 1), "setup_s": round(setup_s, 1)},
+                  "waves_per_step": st["waves"] // max(1, args.steps + args.warmup + 1), "setup_s": round(setup_s, 1),
+                  "generate_s": round(setup_t["generate"], 2), "load_s": round(setup_t["load"], 2),
+                  "load_ms_per_scene": round(1e3 * setup_t["load"] / len(rs), 1)},
     }
 
 

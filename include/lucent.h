@@ -369,6 +369,9 @@ typedef struct lucent_batch_options {
   int32_t sort_rays;         /* sort the rays of bounces 1 and 2 (see lucent_renderer_set_ray_sort) */
   int32_t top_levels;        /* top BVH levels of the first 8 scenes in shared memory (lucent_renderer_set_top_levels) */
   int32_t wide_bvh;          /* closest hit over the four-wide BVH views (lucent_renderer_set_wide_bvh) */
+  uint32_t scenes_per_wave;  /* waves hold consecutive groups of this many scenes, each group traced for all
+                                samples before the next (samples_per_wave / max_wave_paths then apply per
+                                group); 0 = every scene in every wave */
 } lucent_batch_options;
 typedef struct lucent_batch_stats {
   uint64_t closest_rays, shadow_rays; /* traced by this batch since creation */
@@ -380,7 +383,7 @@ typedef struct lucent_batch_stats {
 lucent_status lucent_batch_create(lucent_renderer* const* renderers, uint32_t n, lucent_batch** out);
 void lucent_batch_destroy(lucent_batch* batch);
 /* Defaults: samples_per_wave 0, max_wave_paths 2^25, use_graph 1, trace_blocks 0, shade_blocks 0,
- * sort_rays 1, top_levels 1, wide_bvh 1. */
+ * sort_rays 1, top_levels 1, wide_bvh 1, scenes_per_wave 0. */
 lucent_status lucent_batch_set_options(lucent_batch* batch, const lucent_batch_options* options);
 /* Asynchronous on `stream`. */
 lucent_status lucent_batch_trace(lucent_batch* batch, uint32_t samples, void* stream);

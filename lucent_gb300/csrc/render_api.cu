@@ -1081,13 +1081,19 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
 
 struct lucent_batch {
   std::vector<lucent_renderer*> rs;
-  lucent_batch_options opt{0, 1u << 25, 1, 0, 0, 1, 1, 1};
-  DeviceBuffer recs, bases, tail_bases, sid, paths, ctr;
+  lucent_batch_options opt{0, 1u << 25, 1, 0, 0, 1, 1, 1, 0};
+  DeviceBuffer recs, bases, sid, paths, ctr;
   uint32_t path_cap = 0, sid_cap = 0;
   Paths P{};
-  WaveGraph wave_graph;  // captured full wave
+  std::vector<WaveGraph> graphs;  // a captured full wave per group of scenes
   uint32_t waves = 0, graph_waves = 0;
-  void drop_graph() { wave_graph.drop(); }
+  void drop_graphs() {
+    for (WaveGraph& g : graphs) g.drop();
+  }
+  void destroy_graphs() {
+    for (WaveGraph& g : graphs) g.destroy();
+    graphs.clear();
+  }
 };
 
 
@@ -1111,8 +1117,8 @@ lucent_status lucent_batch_create(lucent_renderer* const* renderers, uint32_t n,
 
 void lucent_batch_destroy(lucent_batch* b) {
   if (!b) return;
-  b->wave_graph.destroy();
-  for (DeviceBuffer* d : {&b->recs, &b->bases, &b->tail_bases, &b->sid, &b->paths, &b->ctr}) d->release();
+  b->destroy_graphs();
+  for (DeviceBuffer* d : {&b->recs, &b->bases, &b->sid, &b->paths, &b->ctr}) d->release();
   delete b;
 }
 
@@ -1121,7 +1127,7 @@ lucent_status lucent_batch_set_options(lucent_batch* b, const lucent_batch_optio
   if (!b || !o) return fail(LUCENT_ERR_INVALID, "null argument");
   if (o->max_wave_paths == 0) return fail(LUCENT_ERR_INVALID, "max_wave_paths must be positive");
   b->opt = *o;
-  b->drop_graph();
+  b->drop_graphs();
   return LUCENT_OK;
 }
 
@@ -1145,79 +1151,112 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
     max_bounces = std::max(max_bounces, (int)r->max_bounces);
     any_alpha |= r->any_alpha;
   }
-  // Samples per wave: as many as fit in max_wave_paths (at least one).
-  uint64_t S = b->opt.samples_per_wave ? b->opt.samples_per_wave : std::max<uint64_t>(1, b->opt.max_wave_paths / pixels);
-  S = std::min<uint64_t>(S, samples);
-  if (pixels * S * 3 >= (1ull << 32)) return fail(LUCENT_ERR_UNSUPPORTED, "wave of %llu paths exceeds the 32-bit path index",
-                                                  (unsigned long long)(pixels * S));
-  const uint32_t cap = (uint32_t)(pixels * S);
+  // Waves hold consecutive groups of scenes_per_wave scenes (0: all of them),
+  // each group traced for all `samples` before the next; samples per wave, per
+  // group: samples_per_wave, or as many as fit in max_wave_paths (at least one).
+  const int k = b->opt.scenes_per_wave ? (int)std::min<uint32_t>(b->opt.scenes_per_wave, (uint32_t)n) : n;
+  struct Group {
+    int i0, i1, max_bounces, any_alpha, any_tex;
+    uint64_t pixels;
+    uint32_t S, full, tail;
+    size_t base;  // offset of the group's bases (full waves, then the tail wave) in b->bases, in words
+  };
+  std::vector<Group> gs;
+  std::vector<uint32_t> hb;
+  uint64_t cap64 = 0;
+  auto make_bases = [&](const Group& G, uint32_t s_wave) {
+    const int ng = G.i1 - G.i0;
+    const size_t o = hb.size();
+    hb.resize(o + 2 * (ng + 1), 0);
+    for (int i = 0; i < ng; i++) {
+      const uint32_t wh = (uint32_t)recs[G.i0 + i].W * recs[G.i0 + i].H;
+      hb[o + i + 1] = hb[o + i] + wh * s_wave;                   // path_base
+      hb[o + ng + 1 + i + 1] = hb[o + ng + 1 + i] + wh;          // pix_base
+    }
+  };
+  for (int i0 = 0; i0 < n; i0 += k) {
+    Group G{i0, std::min(n, i0 + k), 0, 0, 0, 0, 0, 0, 0, hb.size()};
+    for (int i = G.i0; i < G.i1; i++) {
+      G.pixels += (uint64_t)recs[i].W * recs[i].H;
+      G.max_bounces = std::max(G.max_bounces, (int)b->rs[i]->max_bounces);
+      G.any_alpha |= b->rs[i]->any_alpha;
+      G.any_tex |= b->rs[i]->tex_size > 0;
+    }
+    uint64_t S = b->opt.samples_per_wave ? b->opt.samples_per_wave
+                                         : std::max<uint64_t>(1, b->opt.max_wave_paths / G.pixels);
+    S = std::min<uint64_t>(S, samples);
+    if (G.pixels * S * 3 >= (1ull << 32))
+      return fail(LUCENT_ERR_UNSUPPORTED, "wave of %llu paths exceeds the 32-bit path index",
+                  (unsigned long long)(G.pixels * S));
+    G.S = (uint32_t)S;
+    G.full = samples / G.S;
+    G.tail = samples % G.S;
+    cap64 = std::max(cap64, G.pixels * S);
+    make_bases(G, G.S);
+    make_bases(G, G.tail ? G.tail : G.S);
+    gs.push_back(G);
+  }
+  (void)pixels;
+  (void)max_bounces;
+  (void)any_alpha;
+  const uint32_t cap = (uint32_t)cap64;
   lucent_status st = alloc_path_buffers(b->paths, b->ctr, b->path_cap, b->P, cap);
   if (st) return st;
   if (cap > b->sid_cap) {
     if ((st = b->sid.reserve((size_t)cap * 2))) return st;
     if (cudaMemset(b->sid.ptr, 0, (size_t)cap * 2) != cudaSuccess) return cuda_fail(cudaGetLastError(), "clear sid");
     b->sid_cap = cap;
-    b->drop_graph();
+    b->drop_graphs();
   }
-  if ((st = b->recs.reserve(sizeof(SceneRec) * n)) || (st = b->bases.reserve(8 * (n + 1))) ||
-      (st = b->tail_bases.reserve(8 * (n + 1))))
-    return st;
-  auto make_bases = [&](uint32_t s_wave, std::vector<uint32_t>& hb) {
-    hb.assign(2 * (n + 1), 0);
-    for (int i = 0; i < n; i++) {
-      const uint32_t wh = (uint32_t)recs[i].W * recs[i].H;
-      hb[i + 1] = hb[i] + wh * s_wave;                   // path_base
-      hb[n + 1 + i + 1] = hb[n + 1 + i] + wh;            // pix_base
-    }
-  };
-  std::vector<uint32_t> hb, tb;
-  make_bases((uint32_t)S, hb);
+  if ((st = b->recs.reserve(sizeof(SceneRec) * n)) || (st = b->bases.reserve(4 * hb.size()))) return st;
   cudaError_t e = cudaMemcpyAsync(b->recs.ptr, recs.data(), sizeof(SceneRec) * n, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(b->bases.ptr, hb.data(), 4 * hb.size(), cudaMemcpyHostToDevice, s);
-  const uint32_t tail = samples % (uint32_t)S;
-  if (e == cudaSuccess && tail) {
-    make_bases(tail, tb);
-    e = cudaMemcpyAsync(b->tail_bases.ptr, tb.data(), 4 * tb.size(), cudaMemcpyHostToDevice, s);
-  }
   if (e != cudaSuccess) return cuda_fail(e, "upload batch tables");
+  if (b->graphs.size() != gs.size()) {
+    b->destroy_graphs();
+    b->graphs.resize(gs.size());
+  }
   MultiLaunch M{};
   M.paths = b->P;
-  M.recs = (SceneRec*)b->recs.ptr;
   M.sid = (uint16_t*)b->sid.ptr;
-  M.n = n;
-  M.max_bounces = max_bounces;
-  M.any_alpha = any_alpha;
-  M.total_pixels = (uint32_t)pixels;
   M.trace_blocks = (int)b->opt.trace_blocks;
   M.shade_blocks = (int)b->opt.shade_blocks;
   M.sort_rays = b->opt.sort_rays;
   M.top_levels = b->opt.top_levels;
   M.wide = b->opt.wide_bvh;
-  for (lucent_renderer* rr : b->rs) M.any_tex |= rr->tex_size > 0;
-  auto setup = [&](uint32_t s_wave, const DeviceBuffer& base) {
-    M.S = (int)s_wave;
-    M.total_paths = (uint32_t)(pixels * s_wave);
-    M.path_base = (const uint32_t*)base.ptr;
-    M.pix_base = (const uint32_t*)base.ptr + (n + 1);
-  };
-  const uint32_t full = samples / (uint32_t)S;
-  for (uint32_t w = 0; w < full; w++) {
-    setup((uint32_t)S, b->bases);
-    uint64_t key[4];
-    wave_key(M, key);
-    if (b->opt.use_graph && b->waves > 0) {  // first wave ever runs uncaptured (one-time setup inside)
-      const lucent_status gst = b->wave_graph.run(M, key, s);
-      if (gst) return gst;
-      b->graph_waves++;
-    } else {
-      render_wave_multi(M, s);
+  for (size_t g = 0; g < gs.size(); g++) {
+    const Group& G = gs[g];
+    const int ng = G.i1 - G.i0;
+    M.recs = (SceneRec*)b->recs.ptr + G.i0;
+    M.n = ng;
+    M.max_bounces = G.max_bounces;
+    M.any_alpha = G.any_alpha;
+    M.any_tex = G.any_tex;
+    M.total_pixels = (uint32_t)G.pixels;
+    auto setup = [&](uint32_t s_wave, size_t base) {
+      M.S = (int)s_wave;
+      M.total_paths = (uint32_t)(G.pixels * s_wave);
+      M.path_base = (const uint32_t*)b->bases.ptr + base;
+      M.pix_base = M.path_base + (ng + 1);
+    };
+    for (uint32_t w = 0; w < G.full; w++) {
+      setup(G.S, G.base);
+      uint64_t key[4];
+      wave_key(M, key);
+      if (b->opt.use_graph && b->waves > 0) {  // first wave ever runs uncaptured (one-time setup inside)
+        const lucent_status gst = b->graphs[g].run(M, key, s);
+        if (gst) return gst;
+        b->graph_waves++;
+      } else {
+        render_wave_multi(M, s);
+      }
+      b->waves++;
     }
-    b->waves++;
-  }
-  if (tail) {
-    setup(tail, b->tail_bases);
-    render_wave_multi(M, s);
-    b->waves++;
+    if (G.tail) {
+      setup(G.tail, G.base + 2 * (ng + 1));
+      render_wave_multi(M, s);
+      b->waves++;
+    }
   }
   for (lucent_renderer* r : b->rs) {
     r->seed += samples;

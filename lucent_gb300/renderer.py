@@ -310,10 +310,12 @@ class Batch:
     samples_per_wave (0 = as many as max_wave_paths allows), max_wave_paths,
     use_graph (replay a captured wave), trace_blocks / shade_blocks (grid
     sizes, 0 = all resident blocks), sort_rays, top_levels, wide_bvh (as
-    the renderer's set_ray_sort / set_top_levels / set_wide_bvh)."""
+    the renderer's set_ray_sort / set_top_levels / set_wide_bvh),
+    scenes_per_wave (waves hold groups of this many consecutive scenes,
+    each traced for all samples before the next; 0 = all scenes)."""
 
     DEFAULTS = {"samples_per_wave": 0, "max_wave_paths": 1 << 25, "use_graph": True, "trace_blocks": 0,
-                "shade_blocks": 0, "sort_rays": True, "top_levels": True, "wide_bvh": True}
+                "shade_blocks": 0, "sort_rays": True, "top_levels": True, "wide_bvh": True, "scenes_per_wave": 0}
 
     def __init__(self, renderers, **options):
         self.renderers = list(renderers)
@@ -332,7 +334,7 @@ class Batch:
         o = self.options
         d = NR.BatchOptions(o["samples_per_wave"], o["max_wave_paths"], 1 if o["use_graph"] else 0,
                             o["trace_blocks"], o["shade_blocks"], 1 if o["sort_rays"] else 0,
-                            1 if o["top_levels"] else 0, 1 if o["wide_bvh"] else 0)
+                            1 if o["top_levels"] else 0, 1 if o["wide_bvh"] else 0, o["scenes_per_wave"])
         N.check(N.lib().lucent_batch_set_options(self._h, C.byref(d)))
 
     def trace_samples(self, count, stream=None):
@@ -376,8 +378,11 @@ class Batch:
         if candidates is None:  # wave budgets of 2^23 .. 2^25 paths, with and without graph replay
             px = sum(r.width * r.height for r in self.renderers)
             waves = sorted({max(1, (1 << k) // px) for k in (23, 24, 25)})
-            candidates = [{"samples_per_wave": s, "use_graph": g, "max_wave_paths": max(s * px, 1)}
-                          for s in waves for g in (True, False)]
+            candidates = [{"samples_per_wave": s, "use_graph": g, "max_wave_paths": max(s * px, 1),
+                           "scenes_per_wave": 0} for s in waves for g in (True, False)]
+            # waves of a few consecutive scenes at a time (each group traced for all its samples)
+            candidates += [{"samples_per_wave": 0, "use_graph": True, "max_wave_paths": 1 << 25, "scenes_per_wave": k}
+                           for k in (1, 2, 4, 8, 16) if k < len(self.renderers)]
         base = dict(self.options)
         times = {}
 

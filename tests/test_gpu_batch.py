@@ -59,7 +59,9 @@ def solo(specs):
 
 @pytest.mark.parametrize("opts", [{}, {"samples_per_wave": 2}, {"samples_per_wave": 1, "use_graph": False},
                                   {"max_wave_paths": 5000}, {"samples_per_wave": 3},
-                                  {"sort_rays": False, "top_levels": False}, {"wide_bvh": False}])
+                                  {"sort_rays": False, "top_levels": False}, {"wide_bvh": False},
+                                  {"scenes_per_wave": 1}, {"scenes_per_wave": 2, "samples_per_wave": 2},
+                                  {"scenes_per_wave": 2, "use_graph": False, "max_wave_paths": 5000}])
 def test_batch_equals_renderers_alone(specs, solo, opts):
     rs = _renderers(specs)
     b = Batch(rs, **opts)
