@@ -884,6 +884,24 @@ __global__ void k_zero_counters(uint32_t* ctr, int nxt) {
   }
 }
 
+// k_zero_counters in two halves, for a bounce whose predecessor's shadow rays
+// run on the side stream: the closest-hit counters before the closest hit,
+// the rest after the join.
+__global__ void k_zero_closest_counters(uint32_t* ctr) {
+  if (threadIdx.x == 0) {
+    ctr[kCtrWork] = 0;
+    ctr[kCtrSlow] = 0;
+  }
+}
+__global__ void k_zero_shade_counters(uint32_t* ctr, int nxt) {
+  if (threadIdx.x == 0) {
+    ctr[kCtrQ0 + nxt] = 0;
+    ctr[kCtrShadow] = 0;
+    ctr[kCtrWork2] = 0;
+    ctr[kCtrSlow2] = 0;
+    ctr[kCtrTex] = 0;
+  }
+}
 __global__ void k_count_rays(uint32_t* ctr, int cur) {  // statistics: rays traced this bounce
   if (threadIdx.x == 0) {
     atomicAdd((unsigned long long*)(ctr + kCtrStatClosest), (unsigned long long)ctr[kCtrQ0 + cur]);
@@ -1037,9 +1055,13 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
   const int shade_blocks = M.shade_blocks > 0 ? M.shade_blocks : max_shade;
   const int top = M.top_levels ? (M.n < kTopMaxScenes ? M.n : kTopMaxScenes) : 0;
   bool sorted = false;  // the rays of this bounce are in the sorted stream
+  bool forked = false;  // the previous bounce's shadow rays and resolve run on M.side
   for (int b = 0; b <= M.max_bounces; b++) {
     const int cur = b & 1;
-    k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
+    if (forked)  // the side stream still reads the other counters
+      k_zero_closest_counters<<<1, 32, 0, s>>>(P.ctr);
+    else
+      k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
     E.mark(kPhResolve, s);
     PathClosestMulti pc{P.ctr + kCtrQ0 + cur, sorted ? P.sray : P.nray, P.rng, P.hit, M.recs, M.any_alpha};
     TravArgs A{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
@@ -1047,21 +1069,38 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     launch_closest_multi(M.wide, closest_blocks, top, A, pc, s);
     k_closest_exact_t<PathClosestMulti><<<64, 128, 0, s>>>(A, pc);
     E.mark(kPhClosest, s);
+    if (forked) {  // join: the previous bounce's radiance is resolved before this bounce shades
+      cudaStreamWaitEvent(s, M.ev_join, 0);
+      k_zero_shade_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
+    }
     k_shade_t<SceneTable><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b);
     if (M.any_tex) k_shade_t<SceneTable, false, true><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b);
     E.mark(kPhShade, s);
+    // From bounce 2 on (no ray sort after it), this bounce's shadow rays and
+    // resolve do not depend on the next bounce's closest hit, nor it on them:
+    // they run side by side on two streams, so the short launches of the deep
+    // bounces overlap. Profiling keeps one stream (phase times).
+    const bool fork = M.side && !pe && b >= 2 && b < M.max_bounces;
+    cudaStream_t t = s;
+    if (fork) {
+      cudaEventRecord(M.ev_fork, s);
+      cudaStreamWaitEvent(M.side, M.ev_fork, 0);
+      t = M.side;
+    }
     PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};
     TravArgs B{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr,
                nullptr, top};
-    launch_shadow_multi(M.wide, shade_blocks * 2, top, B, ps, s);
-    k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, s>>>(B, ps);
+    launch_shadow_multi(M.wide, shade_blocks * 2, top, B, ps, t);
+    k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, t>>>(B, ps);
     E.mark(kPhShadow, s);
     // Resolve is per path: it walks the queue as it was before the sort (still
     // intact in sort_tmp), in path order, so its reads stay coalesced.
     Paths Pr = P;
     if (sorted) Pr.q[cur] = P.sort_tmp;
-    k_resolve<<<shade_blocks, 128, 0, s>>>(Pr, cur);
-    k_count_rays<<<1, 32, 0, s>>>(P.ctr, cur);
+    k_resolve<<<shade_blocks, 128, 0, t>>>(Pr, cur);
+    k_count_rays<<<1, 32, 0, t>>>(P.ctr, cur);
+    if (fork) cudaEventRecord(M.ev_join, t);
+    forked = fork;
     sorted = M.sort_rays && b < 2 && b < M.max_bounces;  // the two largest queues
     if (sorted) sort_rays(M, P, cur ^ 1, shade_blocks, s);
   }

@@ -215,13 +215,42 @@ struct WaveGraph {
   }
 };
 
+// The second stream of a wave (MultiLaunch::side) with its fork / join events.
+struct SideStream {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  lucent_status ensure() {
+    if (stream) return LUCENT_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      destroy();
+      return cuda_fail(e, "side stream");
+    }
+    return LUCENT_OK;
+  }
+  void set(MultiLaunch& M) const {
+    M.side = stream;
+    M.ev_fork = fork;
+    M.ev_join = join;
+  }
+  void destroy() {
+    if (join) cudaEventDestroy(join);
+    if (fork) cudaEventDestroy(fork);
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+    fork = join = nullptr;
+  }
+};
+
 // Everything a captured wave bakes in besides the buffer contents.
 static void wave_key(const MultiLaunch& M, uint64_t key[4]) {
   key[0] = (uint64_t)(uint32_t)M.S | ((uint64_t)(uint32_t)M.n << 32);
   key[1] = (uint64_t)M.total_pixels | ((uint64_t)(uint32_t)M.trace_blocks << 32);
   key[2] = ((uint64_t)(uintptr_t)M.paths.rec) ^ ((uint64_t)M.max_bounces << 48) ^ ((uint64_t)M.shade_blocks << 56);
   key[3] = ((uint64_t)(uintptr_t)M.recs) ^ ((uint64_t)(uintptr_t)M.path_base << 20) ^ ((uint64_t)M.any_alpha << 59) ^
-           ((uint64_t)M.wide << 58) ^ ((uint64_t)M.any_tex << 60) ^ ((uint64_t)M.sort_rays << 61) ^
+           ((uint64_t)(M.side != nullptr) << 57) ^ ((uint64_t)M.wide << 58) ^ ((uint64_t)M.any_tex << 60) ^ ((uint64_t)M.sort_rays << 61) ^
            ((uint64_t)M.top_levels << 62) ^
            ((uint64_t)(M.trav_stats != nullptr) << 63);
 }
@@ -269,6 +298,7 @@ struct lucent_renderer {
   DeviceBuffer rec1, base1, sid1;
   uint32_t sid_cap = 0;
   WaveGraph wave_graph;  // full waves of a trace replay a captured graph (not while profiling)
+  SideStream side;       // second stream of the waves
   uint32_t waves = 0;
   int sort_rays = 1;   // sort the rays of bounces 1 and 2 (lucent_renderer_set_ray_sort)
   int top_levels = 1;  // top BVH levels in shared memory (lucent_renderer_set_top_levels)
@@ -489,6 +519,8 @@ static lucent_status single_launch(lucent_renderer* r, uint32_t S, uint32_t tail
   M.top_levels = r->top_levels;
   M.wide = r->wide_bvh;
   M.any_tex = r->tex_size > 0;
+  if (lucent_status st = r->side.ensure()) return st;
+  r->side.set(M);
   return LUCENT_OK;
 }
 
@@ -536,6 +568,7 @@ void lucent_renderer_destroy(lucent_renderer* r) {
                           &r->color_maps, &r->data_maps, &r->texel_lut})
     b->release();
   r->wave_graph.destroy();
+  r->side.destroy();
   if (r->ev0) cudaEventDestroy(r->ev0);
   if (r->ev1) cudaEventDestroy(r->ev1);
   for (cudaEvent_t e : r->pev) cudaEventDestroy(e);
@@ -1086,6 +1119,7 @@ struct lucent_batch {
   uint32_t path_cap = 0, sid_cap = 0;
   Paths P{};
   std::vector<WaveGraph> graphs;  // a captured full wave per group of scenes
+  SideStream side;                // second stream of the waves
   uint32_t waves = 0, graph_waves = 0;
   void drop_graphs() {
     for (WaveGraph& g : graphs) g.drop();
@@ -1118,6 +1152,7 @@ lucent_status lucent_batch_create(lucent_renderer* const* renderers, uint32_t n,
 void lucent_batch_destroy(lucent_batch* b) {
   if (!b) return;
   b->destroy_graphs();
+  b->side.destroy();
   for (DeviceBuffer* d : {&b->recs, &b->bases, &b->sid, &b->paths, &b->ctr}) d->release();
   delete b;
 }
@@ -1216,7 +1251,9 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
     b->destroy_graphs();
     b->graphs.resize(gs.size());
   }
+  if ((st = b->side.ensure())) return st;
   MultiLaunch M{};
+  b->side.set(M);
   M.paths = b->P;
   M.sid = (uint16_t*)b->sid.ptr;
   M.trace_blocks = (int)b->opt.trace_blocks;

@@ -114,6 +114,10 @@ struct MultiLaunch {
   int top_levels;                  // stage the top BVH levels of (up to 8) scenes in shared memory
   int any_tex;                     // some scene has texture maps: launch the TEX shade instantiation
   int wide;                        // closest hit over the scenes' four-wide BVH views
+  // Second stream and fork / join events (nullptr: one stream): the deep
+  // bounces' shadow rays run beside the next bounce's closest hit.
+  cudaStream_t side;
+  cudaEvent_t ev_fork, ev_join;
 };
 
 // Optional per-phase timing: events recorded between launches, each tagged
