@@ -1005,18 +1005,25 @@ __global__ void k_sort_scatter(Paths P, int nxt) {
   }
 }
 
-// Sorts the rays of queue `nxt` into the ray stream and the queue into
-// sort_tmp, then swaps the two queue buffers in P (the caller's copy of the
-// path state; every wave starts from the launch's own pointers, so a
-// captured wave replays the same sequence of swaps).
-static void sort_rays(const MultiLaunch& M, Paths& P, int nxt, int blocks, cudaStream_t s) {
+// Sorts the rays of queue `nxt` into the ray stream and the queue into the
+// free queue buffer `dst`, which becomes queue `nxt`; returns the buffer of
+// the pre-sort queue. P is the caller's copy of the path state: every wave
+// starts from the launch's own pointers, so a captured wave replays the same
+// sequence of buffer rotations.
+static uint32_t* sort_rays_into(const MultiLaunch& M, Paths& P, int nxt, int blocks, cudaStream_t s, uint32_t* dst) {
+  Paths Ps = P;
+  Ps.sort_tmp = dst;
   cudaMemsetAsync(P.sort_hist, 0, (size_t)kSortBins * 4, s);
-  k_sort_keys<<<blocks, 256, 0, s>>>(P, M.recs, M.n, nxt);
+  k_sort_keys<<<blocks, 256, 0, s>>>(Ps, M.recs, M.n, nxt);
   k_sort_scan<<<1, 1024, 0, s>>>(P.sort_hist);
-  k_sort_scatter<<<blocks, 256, 0, s>>>(P, nxt);
-  uint32_t* t = P.q[nxt];
-  P.q[nxt] = P.sort_tmp;
-  P.sort_tmp = t;
+  k_sort_scatter<<<blocks, 256, 0, s>>>(Ps, nxt);
+  uint32_t* pre = P.q[nxt];
+  P.q[nxt] = dst;
+  return pre;
+}
+// The sorted queue into sort_tmp, the pre-sort queue kept there in its place.
+static void sort_rays(const MultiLaunch& M, Paths& P, int nxt, int blocks, cudaStream_t s) {
+  P.sort_tmp = sort_rays_into(M, P, nxt, blocks, s, P.sort_tmp);
 }
 
 // ------------------------------------------------------------ one wave
@@ -1076,11 +1083,11 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     k_shade_t<SceneTable><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b);
     if (M.any_tex) k_shade_t<SceneTable, false, true><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b);
     E.mark(kPhShade, s);
-    // From bounce 2 on (no ray sort after it), this bounce's shadow rays and
-    // resolve do not depend on the next bounce's closest hit, nor it on them:
-    // they run side by side on two streams, so the short launches of the deep
-    // bounces overlap. Profiling keeps one stream (phase times).
-    const bool fork = M.side && !pe && b >= 2 && b < M.max_bounces;
+    // This bounce's shadow rays and resolve do not depend on the next bounce's
+    // ray sort and closest hit, nor they on them: they run side by side on two
+    // streams, so the short launches of the deep bounces overlap. Profiling
+    // keeps one stream (phase times).
+    const bool fork = M.side && !pe && b < M.max_bounces;
     cudaStream_t t = s;
     if (fork) {
       cudaEventRecord(M.ev_fork, s);
@@ -1101,8 +1108,19 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     k_count_rays<<<1, 32, 0, t>>>(P.ctr, cur);
     if (fork) cudaEventRecord(M.ev_join, t);
     forked = fork;
+    const bool was_sorted = sorted;
     sorted = M.sort_rays && b < 2 && b < M.max_bounces;  // the two largest queues
-    if (sorted) sort_rays(M, P, cur ^ 1, shade_blocks, s);
+    if (sorted && was_sorted) {
+      // This bounce's resolve (perhaps still running on the side stream) reads
+      // its pre-sort queue in sort_tmp; its sorted queue buffer is free once
+      // shaded, so the next queue is sorted into that one instead, and
+      // sort_tmp becomes the next-but-one queue after the join.
+      uint32_t* busy = P.sort_tmp;
+      P.sort_tmp = sort_rays_into(M, P, cur ^ 1, shade_blocks, s, P.q[cur]);
+      P.q[cur] = busy;
+    } else if (sorted) {
+      sort_rays(M, P, cur ^ 1, shade_blocks, s);
+    }
   }
   E.mark(kPhResolve, s);
   k_accumulate_multi<<<grid_for(M.total_pixels, 256), 256, 0, s>>>(P, M.recs, M.pix_base, M.path_base, M.n, M.S);
