@@ -1147,29 +1147,53 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
     const AdjointDev A{H.dl, H.lrem, H.gcont, H.gslot, H.genv, H.dmat, H.denv, M.total_pixels, pass == 0 ? 1 : 0};
     Paths P = M.paths;     // queue buffers swap with the sort buffer below
     bool sorted = false;  // as in render_wave_multi: the rays of bounces 1 and 2 are sorted
+    bool forked = false;  // as in render_wave_multi: shadow rays and resolve on M.side
     k_camera_multi<<<grid_for(M.total_paths, 256), 256, 0, s>>>(P, M.recs, M.path_base, M.n, M.sid, M.S);
     for (int b = 0; b <= M.max_bounces; b++) {
       const int cur = b & 1;
-      k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
+      if (forked)
+        k_zero_closest_counters<<<1, 32, 0, s>>>(P.ctr);
+      else
+        k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
       PathClosestMulti pc{P.ctr + kCtrQ0 + cur, sorted ? P.sray : P.nray, P.rng, P.hit, M.recs, M.any_alpha};
       TravArgs TA{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
                   nullptr, top};
       launch_closest_multi(M.wide, closest_blocks, top, TA, pc, s);
       k_closest_exact_t<PathClosestMulti><<<64, 128, 0, s>>>(TA, pc);
+      if (forked) {  // the previous bounce's resolve (lrem, radiance) precedes this shade
+        cudaStreamWaitEvent(s, M.ev_join, 0);
+        k_zero_shade_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
+      }
       k_shade_t<SceneTable, true><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b, A);
+      const bool fork = M.side && b < M.max_bounces;
+      cudaStream_t t = s;
+      if (fork) {
+        cudaEventRecord(M.ev_fork, s);
+        cudaStreamWaitEvent(M.side, M.ev_fork, 0);
+        t = M.side;
+      }
       PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};
       TravArgs TB{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr,
                   nullptr, top};
-      launch_shadow_multi(M.wide, shade_blocks * 2, top, TB, ps, s);
-      k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, s>>>(TB, ps);
+      launch_shadow_multi(M.wide, shade_blocks * 2, top, TB, ps, t);
+      k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, t>>>(TB, ps);
       Paths Pr = P;  // resolve walks the pre-sort queue, in path order
       if (sorted) Pr.q[cur] = P.sort_tmp;
       if (pass == 0)
-        k_resolve<<<shade_blocks, 128, 0, s>>>(Pr, cur);
+        k_resolve<<<shade_blocks, 128, 0, t>>>(Pr, cur);
       else
-        k_resolve_adjoint<<<shade_blocks, 128, 0, s>>>(Pr, A, rec, cur);
+        k_resolve_adjoint<<<shade_blocks, 128, 0, t>>>(Pr, A, rec, cur);
+      if (fork) cudaEventRecord(M.ev_join, t);
+      forked = fork;
+      const bool was_sorted = sorted;
       sorted = M.sort_rays && b < 2 && b < M.max_bounces;
-      if (sorted) sort_rays(M, P, cur ^ 1, shade_blocks, s);
+      if (sorted && was_sorted) {  // as in render_wave_multi
+        uint32_t* busy = P.sort_tmp;
+        P.sort_tmp = sort_rays_into(M, P, cur ^ 1, shade_blocks, s, P.q[cur]);
+        P.q[cur] = busy;
+      } else if (sorted) {
+        sort_rays(M, P, cur ^ 1, shade_blocks, s);
+      }
     }
     if (pass == 0) k_seed_lrem<<<grid_for(M.total_paths, 256), 256, 0, s>>>(P, A, M.total_paths);
   }
