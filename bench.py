@@ -524,10 +524,14 @@ def run_ours_adjoint(args, rank, world, local):
     mine = INV.views_of_rank(ADJ_VIEWS, rank, world)
     cams = W.adjoint_views(ADJ_VIEWS)
     views = []
-    for v in mine:
-        r = Renderer(ADJ_W, ADJ_W)
+    for v in mine:  # the first renderer loads the scene, the others are views of it (shared device data)
+        if not views:
+            r = Renderer(ADJ_W, ADJ_W)
+            r.load_scene(S.Scene(name=sc.name, camera=cams[v], env=sc.env, meshes=sc.meshes))
+        else:
+            r = Renderer.view(views[0].renderer, ADJ_W, ADJ_W, camera=cams[v])
         r.settings.max_bounces = ADJ_DEPTH
-        r.load_scene(S.Scene(name=sc.name, camera=cams[v], env=sc.env, meshes=sc.meshes))
+        r.apply_settings()
         views.append(INV.RendererView(r, AD.forward(r, ADJ_SPP, 0), ADJ_SPP, 1))
     rs = [v.renderer for v in views]
     rng = np.random.default_rng(0)
@@ -601,7 +605,8 @@ def run_ours_adjoint(args, rank, world, local):
                 "d2h_bytes_per_step": ADJ_VIEWS * ADJ_W * ADJ_W * 52},
         "roofline": None, "clocks": clk.summary(), "gpu_launches": None, "dtype": "f32 (+f64 exact hit decisions)",
         "config": {"workload": "adjoint: adjoint_scene(0, 6) (81,956 triangles, 33 materials, 256x128 HDRI), "
-                               "8 views 512x512, 32 spp forward / 32 replayed, depth 6"},
+                               "8 views 512x512 (renderer views sharing one scene), 32 spp forward / 32 replayed, "
+                               "depth 6"},
         "extra": {"forward_ms_per_view": round(1e3 * tf / (len(views) * args.steps), 2),
                   "backward_ms_per_view": round(1e3 * tb / (len(views) * args.steps), 2),
                   "upload_and_adam_ms_per_step": round(1e3 * tu / args.steps, 2),

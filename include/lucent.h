@@ -298,6 +298,18 @@ lucent_status lucent_renderer_set_top_levels(lucent_renderer* r, int32_t enabled
  * grandchildren's boxes lie inside their parents', so the reference's cull
  * decisions and visiting order are unchanged. */
 lucent_status lucent_renderer_set_wide_bvh(lucent_renderer* r, int32_t enabled);
+/* A renderer of width x height that renders `src`'s scene: geometry, BVH
+ * and its wide view, triangle attributes, materials, spheres, lights and
+ * texture arrays are read from src's device memory, not copied. The view
+ * has its own targets, camera, settings, ground switch and lighting (call
+ * lucent_renderer_upload_lighting on it). Materials are shared:
+ * lucent_renderer_set_materials on src or any view changes them for all
+ * (each renderer resets only its own average). src must keep its scene and
+ * outlive its views; src cannot load another scene while views exist (a
+ * view that loads a scene stops being a view). No reference counterpart:
+ * the reference has one view per renderer; this serves many cameras of one
+ * scene (multi-view inverse rendering, batches of views). */
+lucent_status lucent_renderer_create_view(lucent_renderer* src, uint32_t width, uint32_t height, lucent_renderer** out);
 /* ---------------------------------------------------------------------------
  * Differentiable rendering (path replay backpropagation). No reference
  * counterpart: the reference renders forward only.

@@ -260,6 +260,10 @@ struct lucent_renderer {
   // scene
   DeviceBuffer nodes, geo, attr, mats, spheres, sph_mat, sph_light, lights;
   DeviceBuffer wide;  // four-wide view of `nodes` (traverse_wide.cuh)
+  // A view (lucent_renderer_create_view) renders `src`'s scene: the scene
+  // fields below are read from src; n_views counts the views of this one.
+  lucent_renderer* src = nullptr;
+  int n_views = 0;
   // texture arrays (sRGB colour layers, linear data layers), decode tables, layer size (0: none)
   DeviceBuffer color_maps, data_maps, texel_lut;
   int tex_size = 0;
@@ -425,14 +429,19 @@ static lucent_status load_textures(lucent_renderer* r, const lucent_scene_desc* 
   return LUCENT_OK;
 }
 
+// The renderer holding r's scene: r itself, or the source of a view.
+static lucent_renderer* scene_owner(lucent_renderer* r) { return r->src ? r->src : r; }
+static const lucent_renderer* scene_owner(const lucent_renderer* r) { return r->src ? r->src : r; }
+
 static SceneRec scene_rec(const lucent_renderer* r) {
   SceneRec R{};
-  R.scene = {(const Node*)r->nodes.ptr, r->node_count, (const float4*)r->geo.ptr, (const float4*)r->attr.ptr,
-             (const float4*)r->mats.ptr, (const float4*)r->spheres.ptr, (const int*)r->sph_mat.ptr,
-             (const int*)r->sph_light.ptr, (int)r->sphere_count, (const float4*)r->lights.ptr, (int)r->light_count,
-             r->ground_enabled ? r->ground_material : -1, r->ground_height, r->any_alpha,
-             (const uchar4*)r->color_maps.ptr, (const uchar4*)r->data_maps.ptr, (const float*)r->texel_lut.ptr,
-             r->tex_size, (const Node*)r->wide.ptr};
+  const lucent_renderer* o = scene_owner(r);
+  R.scene = {(const Node*)o->nodes.ptr, o->node_count, (const float4*)o->geo.ptr, (const float4*)o->attr.ptr,
+             (const float4*)o->mats.ptr, (const float4*)o->spheres.ptr, (const int*)o->sph_mat.ptr,
+             (const int*)o->sph_light.ptr, (int)o->sphere_count, (const float4*)o->lights.ptr, (int)o->light_count,
+             r->ground_enabled ? o->ground_material : -1, r->ground_height, o->any_alpha,
+             (const uchar4*)o->color_maps.ptr, (const uchar4*)o->data_maps.ptr, (const float*)o->texel_lut.ptr,
+             o->tex_size, (const Node*)o->wide.ptr};
   R.light = r->light;
   R.cam = r->cam;
   R.accum = {(float4*)r->color.ptr, (half4*)r->albedo.ptr, (half4*)r->normal.ptr, (float*)r->history.ptr};
@@ -514,11 +523,11 @@ static lucent_status single_launch(lucent_renderer* r, uint32_t S, uint32_t tail
   M.max_bounces = (int)r->max_bounces;
   M.total_paths = WH * S;
   M.total_pixels = WH;
-  M.any_alpha = r->any_alpha;
+  M.any_alpha = scene_owner(r)->any_alpha;
   M.sort_rays = r->sort_rays;
   M.top_levels = r->top_levels;
   M.wide = r->wide_bvh;
-  M.any_tex = r->tex_size > 0;
+  M.any_tex = scene_owner(r)->tex_size > 0;
   if (lucent_status st = r->side.ensure()) return st;
   r->side.set(M);
   return LUCENT_OK;
@@ -560,9 +569,25 @@ lucent_status lucent_renderer_create(uint32_t width, uint32_t height, lucent_ren
   return LUCENT_OK;
 }
 
+lucent_status lucent_renderer_create_view(lucent_renderer* src, uint32_t width, uint32_t height, lucent_renderer** out) {
+  clear_error();
+  if (!src || !out) return fail(LUCENT_ERR_INVALID, "null argument");
+  *out = nullptr;
+  src = scene_owner(src);  // a view of a view renders the same scene
+  if (!src->has_scene) return fail(LUCENT_ERR_INVALID, "create_view before the source's load_scene");
+  lucent_renderer* r = nullptr;
+  lucent_status st = lucent_renderer_create(width, height, &r);
+  if (st) return st;
+  r->src = src;
+  src->n_views++;
+  *out = r;
+  return LUCENT_OK;
+}
+
 void lucent_renderer_destroy(lucent_renderer* r) {
   if (!r) return;
-  for (DeviceBuffer* b : {&r->nodes, &r->geo, &r->attr, &r->mats, &r->spheres, &r->sph_mat, &r->sph_light,
+  if (r->src) r->src->n_views--;
+  for (DeviceBuffer* b : {&r->nodes, &r->wide, &r->geo, &r->attr, &r->mats, &r->spheres, &r->sph_mat, &r->sph_light,
                           &r->lights, &r->env_rgb, &r->env_alias, &r->sheen, &r->color, &r->albedo, &r->normal,
                           &r->history, &r->paths, &r->ctr, &r->den_a, &r->den_b, &r->guide0, &r->guide1, &r->disp, &r->adj_dl, &r->adj_path, &r->adj_grad, &r->rec1, &r->base1, &r->sid1, &r->prev,
                           &r->color_maps, &r->data_maps, &r->texel_lut})
@@ -586,6 +611,11 @@ static lucent_status upload(DeviceBuffer& b, const void* src, size_t bytes) {
 lucent_status lucent_renderer_load_scene(lucent_renderer* r, const lucent_scene_desc* d) {
   clear_error();
   if (!r || !d) return fail(LUCENT_ERR_INVALID, "null argument");
+  if (r->n_views > 0) return fail(LUCENT_ERR_INVALID, "renderer has %d views of its scene", r->n_views);
+  if (r->src) {  // a view loading a scene of its own stops being a view
+    r->src->n_views--;
+    r->src = nullptr;
+  }
   const uint32_t n = d->tri_count;
   if (n && (!d->positions || !d->normals || !d->tri_material))
     return fail(LUCENT_ERR_INVALID, "triangles need positions, normals and material ids");
@@ -823,7 +853,8 @@ lucent_status lucent_renderer_set_seed(lucent_renderer* r, uint32_t seed) {
 lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* stream) {
   clear_error();
   if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
-  if (!r->has_scene || !r->has_lighting) return fail(LUCENT_ERR_INVALID, "trace before load_scene / upload_lighting");
+  if (!scene_owner(r)->has_scene || !r->has_lighting)
+    return fail(LUCENT_ERR_INVALID, "trace before load_scene / upload_lighting");
   if (samples == 0) return LUCENT_OK;
   cudaStream_t s = (cudaStream_t)stream;
   const uint32_t WH = r->W * r->H;
@@ -860,12 +891,13 @@ lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* 
 lucent_status lucent_renderer_set_materials(lucent_renderer* r, const float* materials, uint32_t count) {
   clear_error();
   if (!r || !materials) return fail(LUCENT_ERR_INVALID, "null argument");
-  if (!r->has_scene) return fail(LUCENT_ERR_INVALID, "set_materials before load_scene");
-  if (count != r->material_count)
-    return fail(LUCENT_ERR_INVALID, "scene has %u materials, got %u", r->material_count, count);
+  lucent_renderer* o = scene_owner(r);  // a view's materials are its source's (shared)
+  if (!o->has_scene) return fail(LUCENT_ERR_INVALID, "set_materials before load_scene");
+  if (count != o->material_count)
+    return fail(LUCENT_ERR_INVALID, "scene has %u materials, got %u", o->material_count, count);
   for (size_t i = 0; i < (size_t)count * 40; i++)
     if (!std::isfinite(materials[i])) return fail(LUCENT_ERR_INVALID, "material value %zu is not finite", i);
-  cudaError_t e = cudaMemcpy(r->mats.ptr, materials, (size_t)count * 160, cudaMemcpyHostToDevice);
+  cudaError_t e = cudaMemcpy(o->mats.ptr, materials, (size_t)count * 160, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(e, "upload materials");
   return lucent_renderer_reset(r);
 }
@@ -874,9 +906,10 @@ lucent_status lucent_renderer_backward(lucent_renderer* r, uint32_t samples, uin
                                        float* d_materials, float* d_env, void* stream) {
   clear_error();
   if (!r || !dl_dimage || !d_materials) return fail(LUCENT_ERR_INVALID, "null argument");
-  if (!r->has_scene || !r->has_lighting) return fail(LUCENT_ERR_INVALID, "backward before load_scene / upload_lighting");
+  if (!scene_owner(r)->has_scene || !r->has_lighting)
+    return fail(LUCENT_ERR_INVALID, "backward before load_scene / upload_lighting");
   // The parameters are the material factors; with maps the BSDF sees factor x texel.
-  if (r->tex_size > 0) return fail(LUCENT_ERR_UNSUPPORTED, "backward through texture-mapped materials");
+  if (scene_owner(r)->tex_size > 0) return fail(LUCENT_ERR_UNSUPPORTED, "backward through texture-mapped materials");
   if (samples == 0) return LUCENT_OK;
   cudaStream_t s = (cudaStream_t)stream;
   const uint32_t WH = r->W * r->H;
@@ -885,7 +918,7 @@ lucent_status lucent_renderer_backward(lucent_renderer* r, uint32_t samples, uin
   lucent_status st = alloc_paths(r, batch * WH);
   if (st) return st;
   const size_t cap = r->path_cap;
-  const size_t nmat = (size_t)r->material_count * 6;
+  const size_t nmat = (size_t)scene_owner(r)->material_count * 6;
   const size_t nenv = d_env ? (size_t)r->light.env_w * r->light.env_h * 3 : 0;
   // per path: lrem 1 + gcont 5 + genv 2 float4; per shadow slot: gslot 2 float4 (3 slots per path)
   if ((st = r->adj_dl.reserve((size_t)WH * 16)) || (st = r->adj_path.reserve(cap * 16 * (1 + 5 + 2 + 6))) ||
@@ -934,6 +967,7 @@ lucent_status lucent_renderer_set_ray_sort(lucent_renderer* r, int32_t enabled) 
 lucent_status lucent_renderer_read_textures(lucent_renderer* r, uint32_t* size, uint8_t* color_out, uint8_t* data_out) {
   clear_error();
   if (!r || !size) return fail(LUCENT_ERR_INVALID, "null argument");
+  r = scene_owner(r);
   *size = (uint32_t)r->tex_size;
   const size_t layer = (size_t)r->tex_size * r->tex_size * 4;
   cudaError_t e = cudaSuccess;
@@ -1089,8 +1123,8 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
   out->seed = r->seed;
   out->width = r->W;
   out->height = r->H;
-  out->triangles = r->tri_count;
-  out->bvh_nodes = r->node_count;
+  out->triangles = scene_owner(r)->tri_count;
+  out->bvh_nodes = scene_owner(r)->node_count;
   if (r->ctr.ptr) {
     uint64_t c[2] = {0, 0};
     cudaError_t e = cudaMemcpy(c, (uint32_t*)r->ctr.ptr + kCtrStatClosest, 16, cudaMemcpyDeviceToHost);
@@ -1177,14 +1211,14 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
   cudaStream_t s = (cudaStream_t)stream;
   for (int i = 0; i < n; i++) {
     lucent_renderer* r = b->rs[i];
-    if (!r->has_scene || !r->has_lighting)
+    if (!scene_owner(r)->has_scene || !r->has_lighting)
       return fail(LUCENT_ERR_INVALID, "renderer %d: trace before load_scene / upload_lighting", i);
     lucent_status st = prepare_reprojection(r, s);
     if (st) return st;
     recs[i] = scene_rec(r);
     pixels += (uint64_t)r->W * r->H;
     max_bounces = std::max(max_bounces, (int)r->max_bounces);
-    any_alpha |= r->any_alpha;
+    any_alpha |= scene_owner(r)->any_alpha;
   }
   // Waves hold consecutive groups of scenes_per_wave scenes (0: all of them),
   // each group traced for all `samples` before the next; samples per wave, per
@@ -1214,8 +1248,8 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
     for (int i = G.i0; i < G.i1; i++) {
       G.pixels += (uint64_t)recs[i].W * recs[i].H;
       G.max_bounces = std::max(G.max_bounces, (int)b->rs[i]->max_bounces);
-      G.any_alpha |= b->rs[i]->any_alpha;
-      G.any_tex |= b->rs[i]->tex_size > 0;
+      G.any_alpha |= scene_owner(b->rs[i])->any_alpha;
+      G.any_tex |= scene_owner(b->rs[i])->tex_size > 0;
     }
     uint64_t S = b->opt.samples_per_wave ? b->opt.samples_per_wave
                                          : std::max<uint64_t>(1, b->opt.max_wave_paths / G.pixels);

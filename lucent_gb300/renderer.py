@@ -60,6 +60,32 @@ class Renderer:
         self._keep = []
         self.camera_state = None
 
+    @classmethod
+    def view(cls, src, width, height, camera=None):
+        """A renderer of `src`'s loaded scene seen from `camera` (default:
+        the scene's), sharing the scene's device data instead of copying it
+        (lucent_renderer_create_view): geometry, BVH, materials, textures.
+        Targets, camera, settings, ground and lighting are the view's own;
+        materials set through any of them change for all."""
+        from dataclasses import replace
+        r = cls.__new__(cls)
+        r.settings = RenderSettings()
+        h = C.c_void_p()
+        N.check(N.lib().lucent_renderer_create_view(src.handle, width, height, C.byref(h)))
+        r._h = h
+        r.width, r.height = width, height
+        r._keep = []
+        r.camera_state = None
+        r.source = src  # the source must outlive its views
+        r.packed = src.packed
+        r.scene = replace(src.scene, camera=camera) if camera is not None else src.scene
+        r.upload_ground(r.scene.ground)
+        r.upload_lighting(r.scene)
+        r.upload_camera(r.scene.camera, False)
+        r.apply_settings()
+        r.reset()
+        return r
+
     @property
     def handle(self):
         return self._h

@@ -13,7 +13,8 @@ import pytest
 
 from oracle import render as OR
 from lucent_gb300 import workloads as W
-from lucent_gb300.renderer import Renderer
+from lucent_gb300._native import LucentError
+from lucent_gb300.renderer import Batch, Renderer
 
 pytestmark = pytest.mark.gpu
 
@@ -135,3 +136,54 @@ def test_graph_replay_changes_no_pixel():
         out.append(r.read())
         r.dispose()
     assert all(np.array_equal(a, b) for a, b in zip(*out))
+
+
+def test_views_share_the_scene_and_render_the_same_images():
+    # A view renders its source's scene from its own camera with the scene's
+    # device data shared: the image equals a renderer that loaded its own copy.
+    from dataclasses import replace
+    from lucent_gb300 import scene as S
+    sc = W.adjoint_scene(1, 3)
+    cams = W.adjoint_views(3)
+    src = Renderer(48, 40)
+    src.settings.max_bounces = 5
+    src.load_scene(replace(sc, camera=cams[0]))
+    views = [Renderer.view(src, 48, 40, camera=c) for c in cams[1:]]
+    own = []
+    for c in cams[1:]:
+        r = Renderer(48, 40)
+        r.settings.max_bounces = 5
+        r.load_scene(replace(sc, camera=c))
+        own.append(r)
+    for r in views:
+        r.settings.max_bounces = 5
+        r.apply_settings()
+    for r in [src] + views + own:
+        r.set_seed(5)
+        r.trace_samples(3)
+    for v, o in zip(views, own):
+        assert all(np.array_equal(a, b) for a, b in zip(v.read(), o.read()))
+        assert v.stats()["triangles"] == o.stats()["triangles"]
+    # a batch of the source and its views equals them traced alone
+    alone = [r.read()[0].copy() for r in [src] + views]
+    for r in [src] + views:
+        r.reset()
+        r.set_seed(5)
+    b = Batch([src] + views)
+    b.trace_samples(3)
+    b.check()
+    for r, a in zip([src] + views, alone):
+        assert np.array_equal(r.read()[0], a)
+    # materials are shared; the source cannot load another scene while views exist
+    from lucent_gb300 import adjoint as AD
+    m = np.array(src.packed.materials, np.float32).reshape(-1, 40)
+    m[:, 0:3] *= 0.5
+    AD.set_materials(views[0], m.reshape(-1))
+    src.reset()
+    src.set_seed(5)
+    src.trace_samples(3)
+    assert not np.array_equal(src.read()[0], alone[0])
+    with pytest.raises(LucentError):
+        src.load_scene(sc)
+    for r in views + own + [src]:
+        r.dispose()
