@@ -922,10 +922,10 @@ __device__ __forceinline__ uint32_t spread3(uint32_t x) {  // 4 bits -> every th
   return x;
 }
 
-__global__ void k_sort_keys(Paths P, const SceneRec* __restrict__ recs, int n_scenes, int nxt) {
+__global__ void k_sort_keys(Paths P, const SceneRec* __restrict__ recs, int n_classes, int nxt) {
   const uint32_t n = P.ctr[kCtrQ0 + nxt];
   int sbits = 0;
-  while ((1 << sbits) < n_scenes) sbits++;
+  while ((1 << sbits) < n_classes) sbits++;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const float4 o = P.nray[2 * (size_t)k], d = P.nray[2 * (size_t)k + 1];  // the queue's rays, in order
     const int sc = __float_as_int(d.w);
@@ -939,7 +939,8 @@ __global__ void k_sort_keys(Paths P, const SceneRec* __restrict__ recs, int n_sc
                        (spread3(cell(o.z, lo.z, hi.z)) << 2);
     const uint32_t oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
     const uint32_t local = (oct << 12) | m;  // 15 bits
-    const uint32_t key = ((uint32_t)sc << (kSortBits - sbits)) | (local >> sbits);
+    const uint32_t cls = (uint32_t)min(max(recs[sc].sort_class, 0), n_classes - 1);  // keys stay below kSortBins
+    const uint32_t key = (cls << (kSortBits - sbits)) | (local >> sbits);
     P.sort_keys[k] = key;
     const unsigned peers = __match_any_sync(__activemask(), key);  // one atomic per distinct key per warp
     if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(P.sort_hist + key, (uint32_t)__popc(peers));
@@ -1014,7 +1015,7 @@ static uint32_t* sort_rays_into(const MultiLaunch& M, Paths& P, int nxt, int blo
   Paths Ps = P;
   Ps.sort_tmp = dst;
   cudaMemsetAsync(P.sort_hist, 0, (size_t)kSortBins * 4, s);
-  k_sort_keys<<<blocks, 256, 0, s>>>(Ps, M.recs, M.n, nxt);
+  k_sort_keys<<<blocks, 256, 0, s>>>(Ps, M.recs, M.sort_classes > 0 ? M.sort_classes : M.n, nxt);
   k_sort_scan<<<1, 1024, 0, s>>>(P.sort_hist);
   k_sort_scatter<<<blocks, 256, 0, s>>>(Ps, nxt);
   uint32_t* pre = P.q[nxt];

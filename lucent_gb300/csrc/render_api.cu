@@ -247,7 +247,7 @@ struct SideStream {
 // Everything a captured wave bakes in besides the buffer contents.
 static void wave_key(const MultiLaunch& M, uint64_t key[4]) {
   key[0] = (uint64_t)(uint32_t)M.S | ((uint64_t)(uint32_t)M.n << 32);
-  key[1] = (uint64_t)M.total_pixels | ((uint64_t)(uint32_t)M.trace_blocks << 32);
+  key[1] = (uint64_t)M.total_pixels | ((uint64_t)(uint32_t)M.trace_blocks << 32) ^ ((uint64_t)M.sort_classes << 48);
   key[2] = ((uint64_t)(uintptr_t)M.paths.rec) ^ ((uint64_t)M.max_bounces << 48) ^ ((uint64_t)M.shade_blocks << 56);
   key[3] = ((uint64_t)(uintptr_t)M.recs) ^ ((uint64_t)(uintptr_t)M.path_base << 20) ^ ((uint64_t)M.any_alpha << 59) ^
            ((uint64_t)(M.side != nullptr) << 57) ^ ((uint64_t)M.wide << 58) ^ ((uint64_t)M.any_tex << 60) ^ ((uint64_t)M.sort_rays << 61) ^
@@ -527,6 +527,7 @@ static lucent_status single_launch(lucent_renderer* r, uint32_t S, uint32_t tail
   M.sort_rays = r->sort_rays;
   M.top_levels = r->top_levels;
   M.wide = r->wide_bvh;
+  M.sort_classes = 1;
   M.any_tex = scene_owner(r)->tex_size > 0;
   if (lucent_status st = r->side.ensure()) return st;
   r->side.set(M);
@@ -1225,7 +1226,7 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
   // group: samples_per_wave, or as many as fit in max_wave_paths (at least one).
   const int k = b->opt.scenes_per_wave ? (int)std::min<uint32_t>(b->opt.scenes_per_wave, (uint32_t)n) : n;
   struct Group {
-    int i0, i1, max_bounces, any_alpha, any_tex;
+    int i0, i1, max_bounces, any_alpha, any_tex, classes;
     uint64_t pixels;
     uint32_t S, full, tail;
     size_t base;  // offset of the group's bases (full waves, then the tail wave) in b->bases, in words
@@ -1244,13 +1245,20 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
     }
   };
   for (int i0 = 0; i0 < n; i0 += k) {
-    Group G{i0, std::min(n, i0 + k), 0, 0, 0, 0, 0, 0, 0, hb.size()};
+    Group G{i0, std::min(n, i0 + k), 0, 0, 0, 0, 0, 0, 0, 0, hb.size()};
+    std::vector<const Node*> bvhs;  // ray-sort classes: scenes sharing a BVH (views) sort together
     for (int i = G.i0; i < G.i1; i++) {
+      const Node* nodes = recs[i].scene.nodes;
+      int c = 0;
+      while (c < (int)bvhs.size() && bvhs[c] != nodes) c++;
+      if (c == (int)bvhs.size()) bvhs.push_back(nodes);
+      recs[i].sort_class = c;
       G.pixels += (uint64_t)recs[i].W * recs[i].H;
       G.max_bounces = std::max(G.max_bounces, (int)b->rs[i]->max_bounces);
       G.any_alpha |= scene_owner(b->rs[i])->any_alpha;
       G.any_tex |= scene_owner(b->rs[i])->tex_size > 0;
     }
+    G.classes = (int)bvhs.size();
     uint64_t S = b->opt.samples_per_wave ? b->opt.samples_per_wave
                                          : std::max<uint64_t>(1, b->opt.max_wave_paths / G.pixels);
     S = std::min<uint64_t>(S, samples);
@@ -1304,6 +1312,7 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
     M.any_alpha = G.any_alpha;
     M.any_tex = G.any_tex;
     M.total_pixels = (uint32_t)G.pixels;
+    M.sort_classes = G.classes;
     auto setup = [&](uint32_t s_wave, size_t base) {
       M.S = (int)s_wave;
       M.total_paths = (uint32_t)(G.pixels * s_wave);

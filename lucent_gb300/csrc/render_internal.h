@@ -95,6 +95,10 @@ struct SceneRec {
   AccumDev prev;       // copy of the targets as the previous view left them
   sh::CameraDev prev_cam;
   int prev_w, prev_h;
+  // Ray-sort class: scenes of a wave that traverse the same BVH (views of
+  // one scene) share a class, 0 .. MultiLaunch::sort_classes - 1, so their
+  // rays sort together by direction and origin.
+  int sort_class;
 };
 
 constexpr float kHistoryCap = 8.f;  // HISTORY_CAP (renderer.ts:139)
@@ -114,6 +118,7 @@ struct MultiLaunch {
   int top_levels;                  // stage the top BVH levels of (up to 8) scenes in shared memory
   int any_tex;                     // some scene has texture maps: launch the TEX shade instantiation
   int wide;                        // closest hit over the scenes' four-wide BVH views
+  int sort_classes;                // distinct SceneRec::sort_class values (>= 1)
   // Second stream and fork / join events (nullptr: one stream): the deep
   // bounces' shadow rays run beside the next bounce's closest hit.
   cudaStream_t side;
