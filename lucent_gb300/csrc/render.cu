@@ -564,53 +564,61 @@ __global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_consta
         if (!done) tint = tint * s.albedo;
         const float3 so = offset_ray(pos, gn);
         const float3 n = s.n;
-        if (L.sun_enabled) {  // :216-225
-          const float u0 = rnd(st), u1 = rnd(st);
-          float3 t, b;
-          basis(L.sun_dir, t, b);
-          const float3 wi = to_world(uniform_cone(u0, u1, L.sun_cos), t, b, L.sun_dir);
-          const float NdotL = dot3(n, wi);
-          if (NdotL > 0.f && dot3(gn, wi) > 0.f && !analytic_occluded(S, so, wi, INF)) {
-            float pb;
-            const float3 f = eval_opaque(L, s, wo, wi, pb);
-            const float w = mis(L.sun_pdf, pb);
-            const float3 c = clamp_c(thr * f * NdotL * L.sun_radiance * (w / L.sun_pdf), bounce, uclamp);
-            emit_shadow(P, p, 0, so, wi, INF, st, c);
-            if (adj) nee_grad(A, L, s, wo, wi, dl, c, material, 3 * p + 0);
+        // Next-event estimation (:216-252): sun, environment, then one light,
+        // each with the reference's sampling and MIS. One loop body evaluates
+        // the BSDF for all three, so the kernel holds one copy of the layered
+        // BSDF evaluation instead of three (instruction-cache pressure).
+#pragma unroll 1
+        for (int j = 0; j < 3; j++) {
+          float3 wi, le;
+          float pdf, tmax;
+          bool ok;
+          float2 env_uv = make_float2(0.f, 0.f);
+          if (j == 0) {  // sun (:216-225)
+            if (!L.sun_enabled) continue;
+            const float u0 = rnd(st), u1 = rnd(st);
+            float3 t, b;
+            basis(L.sun_dir, t, b);
+            wi = to_world(uniform_cone(u0, u1, L.sun_cos), t, b, L.sun_dir);
+            le = L.sun_radiance;
+            pdf = L.sun_pdf;
+            tmax = INF;
+            ok = true;
+          } else if (j == 1) {  // environment (:228-237)
+            if (!L.env_sampling) continue;
+            const LightSample ls = sample_environment(L, st);
+            wi = ls.dir;
+            le = ls.radiance;
+            pdf = ls.pdf;
+            tmax = INF;
+            ok = ls.pdf > 0.f;
+            env_uv = ls.uv;
+          } else {  // one light, chosen uniformly (:240-252)
+            if (S.light_count <= 0) continue;
+            const int li = min((int)(rnd(st) * (float)S.light_count), S.light_count - 1);
+            const float u0 = rnd(st), u1 = rnd(st);
+            const LightSample ls = sample_light(S, li, pos, u0, u1);
+            wi = ls.dir;
+            le = ls.radiance;
+            pdf = ls.pdf / (float)S.light_count;
+            tmax = ls.dist * (1.f - 1e-4f);
+            ok = ls.pdf > 0.f;
           }
-        }
-        if (L.env_sampling) {  // :228-237
-          const LightSample ls = sample_environment(L, st);
-          const float NdotL = dot3(n, ls.dir);
-          if (ls.pdf > 0.f && NdotL > 0.f && dot3(gn, ls.dir) > 0.f && !analytic_occluded(S, so, ls.dir, INF)) {
-            float pb;
-            const float3 f = eval_opaque(L, s, wo, ls.dir, pb);
-            const float w = mis(ls.pdf, pb);
-            const float3 cu = thr * f * NdotL * ls.radiance * (w / ls.pdf);
-            const float3 c = clamp_c(cu, bounce, uclamp);
-            emit_shadow(P, p, 1, so, ls.dir, INF, st, c);
-            if (adj) {
-              nee_grad(A, L, s, wo, ls.dir, dl, c, material, 3 * p + 1);
-              const float3 sv = thr * f * (clamp_scale(cu, bounce, uclamp) * NdotL * (w / ls.pdf) * L.env_intensity);
-              A.genv[2 * (size_t)p] = make_float4(ls.uv.x, ls.uv.y, sv.x, sv.y);
+          const float NdotL = dot3(n, wi);
+          if (!(ok && NdotL > 0.f && dot3(gn, wi) > 0.f && !analytic_occluded(S, so, wi, tmax))) continue;
+          float pb;
+          const float3 f = eval_opaque(L, s, wo, wi, pb);
+          const float w = mis(pdf, pb);
+          const float3 cu = thr * f * NdotL * le * (w / pdf);
+          const float3 c = clamp_c(cu, bounce, uclamp);
+          emit_shadow(P, p, j, so, wi, tmax, st, c);
+          if (adj) {
+            nee_grad(A, L, s, wo, wi, dl, c, material, 3 * p + j);
+            if (j == 1) {
+              const float3 sv = thr * f * (clamp_scale(cu, bounce, uclamp) * NdotL * (w / pdf) * L.env_intensity);
+              A.genv[2 * (size_t)p] = make_float4(env_uv.x, env_uv.y, sv.x, sv.y);
               A.genv[2 * (size_t)p + 1] = make_float4(sv.z, 0.f, 0.f, 0.f);
             }
-          }
-        }
-        if (S.light_count > 0) {  // :240-252
-          const int li = min((int)(rnd(st) * (float)S.light_count), S.light_count - 1);
-          const float u0 = rnd(st), u1 = rnd(st);
-          const LightSample ls = sample_light(S, li, pos, u0, u1);
-          const float NdotL = dot3(n, ls.dir);
-          const float tmax = ls.dist * (1.f - 1e-4f);
-          if (ls.pdf > 0.f && NdotL > 0.f && dot3(gn, ls.dir) > 0.f && !analytic_occluded(S, so, ls.dir, tmax)) {
-            const float pl = ls.pdf / (float)S.light_count;
-            float pb;
-            const float3 f = eval_opaque(L, s, wo, ls.dir, pb);
-            const float w = mis(pl, pb);
-            const float3 c = clamp_c(thr * f * NdotL * ls.radiance * (w / pl), bounce, uclamp);
-            emit_shadow(P, p, 2, so, ls.dir, tmax, st, c);
-            if (adj) nee_grad(A, L, s, wo, ls.dir, dl, c, material, 3 * p + 2);
           }
         }
         const BsdfSample bs = sample_opaque(L, s, wo, U);  // :255-261

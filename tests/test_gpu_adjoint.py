@@ -146,7 +146,8 @@ def test_views_split_over_ranks_sum_to_the_whole_gradient():
     # one-rank vector: what one all-reduce per iteration gives every rank. The
     # backward accumulates with binary32 atomics, whose order varies from run
     # to run, so gradients agree to binary32 accumulation noise (1e-4); the
-    # forward is deterministic, so the losses agree exactly.
+    # forward is deterministic, so the per-view losses are equal and their
+    # binary64 sums differ only by the order of the additions.
     from lucent_gb300.inverse import InverseRendering, views_of_rank
     sc = W.adjoint_scene(1, 3)
     views = _views(sc, 6)
@@ -159,7 +160,7 @@ def test_views_split_over_ranks_sum_to_the_whole_gradient():
         parts = [InverseRendering([views[v] for v in views_of_rank(6, k, world)], theta, env).partial()
                  for k in range(world)]
         total = sum(parts)
-        assert total[-1] == whole[-1]
+        assert abs(total[-1] - whole[-1]) <= 1e-12 * abs(whole[-1])
         np.testing.assert_allclose(total[:-1], whole[:-1], rtol=1e-4, atol=1e-5 * np.abs(whole[:-1]).max())
     for v in views:
         v.renderer.dispose()
