@@ -352,9 +352,11 @@ static __device__ __forceinline__ MapSample sample_maps(const SceneDev& S, const
 // textured-hit queue untouched, so untextured shading carries none of the
 // texture code; the TEX launch then shades exactly those paths. Which
 // instantiation shades a hit depends on the hit alone, never on the launch,
-// so a scene renders the same alone and in a batch.
+// so a scene renders the same alone and in a batch. Four blocks of 128 per
+// SM: 128 registers a thread, no spills (measured faster than five blocks
+// at 96 registers with spills, and than six).
 template <class Src, bool ADJ = false, bool TEX = false>
-__global__ void __launch_bounds__(128, 5) k_shade_t(Paths P, const __grid_constant__ Src src, int cur, int bounce,
+__global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_constant__ Src src, int cur, int bounce,
                                                     const __grid_constant__ AdjointDev A = AdjointDev{}) {
   const uint32_t n = TEX ? P.ctr[kCtrTex] : P.ctr[kCtrQ0 + cur];
   const uint32_t* q = P.q[cur];
@@ -1036,6 +1038,20 @@ static void sort_rays(const MultiLaunch& M, Paths& P, int nxt, int blocks, cudaS
 }
 
 // ------------------------------------------------------------ one wave
+// Grid of the any-hit (twice this many blocks of 256), resolve and sort
+// kernels: five 128-thread blocks per SM (measured; smaller grids slowed the
+// any-hit and resolve kernels).
+static int aux_blocks() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    n = 5 * (sms > 0 ? sms : 152);
+  }
+  return n;
+}
+
 // Closest hit of a bounce: over the scenes' four-wide BVH views, or the
 // binary nodes with the top levels staged in shared memory. Hits are the same.
 static void launch_closest_multi(int wide, int blocks, int top, const TravArgs& A, const PathClosestMulti& pc,
@@ -1069,6 +1085,7 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
   }
   const int closest_blocks = M.trace_blocks > 0 ? M.trace_blocks : M.wide ? max_wide : max_closest;
   const int shade_blocks = M.shade_blocks > 0 ? M.shade_blocks : max_shade;
+  const int aux = M.shade_blocks > 0 ? M.shade_blocks : aux_blocks();
   const int top = M.top_levels ? (M.n < kTopMaxScenes ? M.n : kTopMaxScenes) : 0;
   bool sorted = false;  // the rays of this bounce are in the sorted stream
   bool forked = false;  // the previous bounce's shadow rays and resolve run on M.side
@@ -1106,14 +1123,14 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};
     TravArgs B{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr,
                nullptr, top};
-    launch_shadow_multi(M.wide, shade_blocks * 2, top, B, ps, t);
+    launch_shadow_multi(M.wide, aux * 2, top, B, ps, t);
     k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, t>>>(B, ps);
     E.mark(kPhShadow, s);
     // Resolve is per path: it walks the queue as it was before the sort (still
     // intact in sort_tmp), in path order, so its reads stay coalesced.
     Paths Pr = P;
     if (sorted) Pr.q[cur] = P.sort_tmp;
-    k_resolve<<<shade_blocks, 128, 0, t>>>(Pr, cur);
+    k_resolve<<<aux, 128, 0, t>>>(Pr, cur);
     k_count_rays<<<1, 32, 0, t>>>(P.ctr, cur);
     if (fork) cudaEventRecord(M.ev_join, t);
     forked = fork;
@@ -1125,10 +1142,10 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
       // shaded, so the next queue is sorted into that one instead, and
       // sort_tmp becomes the next-but-one queue after the join.
       uint32_t* busy = P.sort_tmp;
-      P.sort_tmp = sort_rays_into(M, P, cur ^ 1, shade_blocks, s, P.q[cur]);
+      P.sort_tmp = sort_rays_into(M, P, cur ^ 1, aux, s, P.q[cur]);
       P.q[cur] = busy;
     } else if (sorted) {
-      sort_rays(M, P, cur ^ 1, shade_blocks, s);
+      sort_rays(M, P, cur ^ 1, aux, s);
     }
   }
   E.mark(kPhResolve, s);
@@ -1151,6 +1168,7 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
     shade_blocks = persistent_blocks((const void*)k_shade_t<SceneTable, true>, 128);
   }
   const int closest_blocks = M.wide ? wide_blocks : binary_blocks;
+  const int aux = aux_blocks();
   const int top = M.top_levels ? (M.n < kTopMaxScenes ? M.n : kTopMaxScenes) : 0;
   for (int pass = 0; pass < 2; pass++) {
     const AdjointDev A{H.dl, H.lrem, H.gcont, H.gslot, H.genv, H.dmat, H.denv, M.total_pixels, pass == 0 ? 1 : 0};
@@ -1184,24 +1202,24 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
       PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};
       TravArgs TB{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr,
                   nullptr, top};
-      launch_shadow_multi(M.wide, shade_blocks * 2, top, TB, ps, t);
+      launch_shadow_multi(M.wide, aux * 2, top, TB, ps, t);
       k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, t>>>(TB, ps);
       Paths Pr = P;  // resolve walks the pre-sort queue, in path order
       if (sorted) Pr.q[cur] = P.sort_tmp;
       if (pass == 0)
-        k_resolve<<<shade_blocks, 128, 0, t>>>(Pr, cur);
+        k_resolve<<<aux, 128, 0, t>>>(Pr, cur);
       else
-        k_resolve_adjoint<<<shade_blocks, 128, 0, t>>>(Pr, A, rec, cur);
+        k_resolve_adjoint<<<aux, 128, 0, t>>>(Pr, A, rec, cur);
       if (fork) cudaEventRecord(M.ev_join, t);
       forked = fork;
       const bool was_sorted = sorted;
       sorted = M.sort_rays && b < 2 && b < M.max_bounces;
       if (sorted && was_sorted) {  // as in render_wave_multi
         uint32_t* busy = P.sort_tmp;
-        P.sort_tmp = sort_rays_into(M, P, cur ^ 1, shade_blocks, s, P.q[cur]);
+        P.sort_tmp = sort_rays_into(M, P, cur ^ 1, aux, s, P.q[cur]);
         P.q[cur] = busy;
       } else if (sorted) {
-        sort_rays(M, P, cur ^ 1, shade_blocks, s);
+        sort_rays(M, P, cur ^ 1, aux, s);
       }
     }
     if (pass == 0) k_seed_lrem<<<grid_for(M.total_paths, 256), 256, 0, s>>>(P, A, M.total_paths);
