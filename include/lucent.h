@@ -384,6 +384,9 @@ typedef struct lucent_batch_options {
   uint32_t scenes_per_wave;  /* waves hold consecutive groups of this many scenes, each group traced for all
                                 samples before the next (samples_per_wave / max_wave_paths then apply per
                                 group); 0 = every scene in every wave */
+  uint32_t streams;          /* 1..16: the renderers in this many consecutive parts, each traced as a batch
+                                of its own (these options, path buffers of its own) on a stream of its own,
+                                side by side; forked from and joined into the caller's stream */
 } lucent_batch_options;
 typedef struct lucent_batch_stats {
   uint64_t closest_rays, shadow_rays; /* traced by this batch since creation */
@@ -395,7 +398,7 @@ typedef struct lucent_batch_stats {
 lucent_status lucent_batch_create(lucent_renderer* const* renderers, uint32_t n, lucent_batch** out);
 void lucent_batch_destroy(lucent_batch* batch);
 /* Defaults: samples_per_wave 0, max_wave_paths 2^25, use_graph 1, trace_blocks 0, shade_blocks 0,
- * sort_rays 1, top_levels 1, wide_bvh 1, scenes_per_wave 0. */
+ * sort_rays 1, top_levels 1, wide_bvh 1, scenes_per_wave 0, streams 1. */
 lucent_status lucent_batch_set_options(lucent_batch* batch, const lucent_batch_options* options);
 /* Asynchronous on `stream`. */
 lucent_status lucent_batch_trace(lucent_batch* batch, uint32_t samples, void* stream);

@@ -76,7 +76,8 @@ def declare(L, sig):
 class BatchOptions(C.Structure):
     _fields_ = [("samples_per_wave", C.c_uint32), ("max_wave_paths", C.c_uint32), ("use_graph", C.c_int32),
                 ("trace_blocks", C.c_uint32), ("shade_blocks", C.c_uint32), ("sort_rays", C.c_int32),
-                ("top_levels", C.c_int32), ("wide_bvh", C.c_int32), ("scenes_per_wave", C.c_uint32)]
+                ("top_levels", C.c_int32), ("wide_bvh", C.c_int32), ("scenes_per_wave", C.c_uint32),
+                ("streams", C.c_uint32)]
 
 
 class BatchStats(C.Structure):

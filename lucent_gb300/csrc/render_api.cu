@@ -339,6 +339,14 @@ static lucent_status alloc_targets(lucent_renderer* r, uint32_t w, uint32_t h) {
 // Path buffers for `cap` paths (bytes per path: the 128-byte path record, the
 // radiance, the hit, 3 shadow slots of 3 float4, rng, occlusion flags, queues, slow-path
 // queues, the sort key, the ray streams, the sorted and textured-hit queues).
+// cudaMemset runs on the legacy default stream, which does not order itself
+// with non-blocking streams (a batch's parts, the side streams): wait for it
+// before any stream's kernels may touch the memory.
+static cudaError_t clear_now(void* p, size_t bytes) {
+  cudaError_t e = cudaMemset(p, 0, bytes);
+  return e == cudaSuccess ? cudaStreamSynchronize(0) : e;
+}
+
 static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, uint32_t& path_cap, Paths& P,
                                         uint32_t cap) {
   if (cap <= path_cap) return LUCENT_OK;
@@ -385,8 +393,8 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
   P.sort_hist = (uint32_t*)take((size_t)kSortBins * 4);
   if (off > paths.cap) return fail(LUCENT_ERR_DEVICE, "path buffer layout overflow");
   P.ctr = (uint32_t*)ctr.ptr;
-  cudaError_t e = cudaMemset(P.sh_c, 0, (size_t)cap * 48);
-  if (e == cudaSuccess) e = cudaMemset(P.ctr, 0, kCtrWords * 4);
+  cudaError_t e = clear_now(P.sh_c, (size_t)cap * 48);
+  if (e == cudaSuccess) e = clear_now(P.ctr, kCtrWords * 4);
   if (e != cudaSuccess) return cuda_fail(e, "clear path buffers");
   path_cap = cap;
   return LUCENT_OK;
@@ -501,7 +509,7 @@ static lucent_status single_launch(lucent_renderer* r, uint32_t S, uint32_t tail
   if (st) return st;
   if (r->path_cap > r->sid_cap) {
     if ((st = r->sid1.reserve((size_t)r->path_cap * 2))) return st;
-    if (cudaMemset(r->sid1.ptr, 0, (size_t)r->path_cap * 2) != cudaSuccess) return cuda_fail(cudaGetLastError(), "clear sid");
+    if (clear_now(r->sid1.ptr, (size_t)r->path_cap * 2) != cudaSuccess) return cuda_fail(cudaGetLastError(), "clear sid");
     r->sid_cap = r->path_cap;
   }
   if ((st = r->rec1.reserve(sizeof(SceneRec))) || (st = r->base1.reserve(32))) return st;
@@ -950,7 +958,7 @@ lucent_status lucent_renderer_backward(lucent_renderer* r, uint32_t samples, uin
   uint32_t word = 0;
   cudaMemcpy(&word, (uint32_t*)r->ctr.ptr + kCtrErr, 4, cudaMemcpyDeviceToHost);
   if (word) {
-    cudaMemset((uint32_t*)r->ctr.ptr + kCtrErr, 0, 4);
+    clear_now((uint32_t*)r->ctr.ptr + kCtrErr, 4);
     return fail(LUCENT_ERR_DEVICE, "backward raised device error word 0x%x", word);
   }
   for (size_t i = 0; i < nmat; i++) d_materials[i] += g[i];
@@ -1041,7 +1049,7 @@ lucent_status lucent_renderer_check(lucent_renderer* r, void* stream) {
     r->pn = 0;
   }
   if (word) {
-    cudaMemset((uint32_t*)r->ctr.ptr + kCtrErr, 0, 4);
+    clear_now((uint32_t*)r->ctr.ptr + kCtrErr, 4);
     return fail(LUCENT_ERR_DEVICE, "render raised device error word 0x%x", word);
   }
   return LUCENT_OK;
@@ -1149,12 +1157,16 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
 
 struct lucent_batch {
   std::vector<lucent_renderer*> rs;
-  lucent_batch_options opt{0, 1u << 25, 1, 0, 0, 1, 1, 1, 0};
+  lucent_batch_options opt{0, 1u << 25, 1, 0, 0, 1, 1, 1, 0, 1};
   DeviceBuffer recs, bases, sid, paths, ctr;
   uint32_t path_cap = 0, sid_cap = 0;
   Paths P{};
   std::vector<WaveGraph> graphs;  // a captured full wave per group of scenes
   SideStream side;                // second stream of the waves
+  // opt.streams > 1: consecutive parts of the renderers traced as batches of
+  // their own, side by side on their own streams
+  std::vector<lucent_batch*> parts;
+  std::vector<SideStream> part_streams;  // stream + done event per part (fork: part_streams[0].fork)
   uint32_t waves = 0, graph_waves = 0;
   void drop_graphs() {
     for (WaveGraph& g : graphs) g.drop();
@@ -1184,8 +1196,16 @@ lucent_status lucent_batch_create(lucent_renderer* const* renderers, uint32_t n,
   return LUCENT_OK;
 }
 
+static void drop_parts(lucent_batch* b) {
+  for (lucent_batch* q : b->parts) lucent_batch_destroy(q);
+  for (SideStream& s : b->part_streams) s.destroy();
+  b->parts.clear();
+  b->part_streams.clear();
+}
+
 void lucent_batch_destroy(lucent_batch* b) {
   if (!b) return;
+  drop_parts(b);
   b->destroy_graphs();
   b->side.destroy();
   for (DeviceBuffer* d : {&b->recs, &b->bases, &b->sid, &b->paths, &b->ctr}) d->release();
@@ -1196,8 +1216,41 @@ lucent_status lucent_batch_set_options(lucent_batch* b, const lucent_batch_optio
   clear_error();
   if (!b || !o) return fail(LUCENT_ERR_INVALID, "null argument");
   if (o->max_wave_paths == 0) return fail(LUCENT_ERR_INVALID, "max_wave_paths must be positive");
+  if (o->streams == 0 || o->streams > 16) return fail(LUCENT_ERR_INVALID, "streams must be 1 to 16, got %u", o->streams);
   b->opt = *o;
   b->drop_graphs();
+  drop_parts(b);
+  return LUCENT_OK;
+}
+
+// opt.streams > 1: the renderers in that many consecutive parts, each a
+// batch of its own (same options, one stream) on a stream of its own, forked
+// from and joined back into the caller's stream.
+static lucent_status trace_parts(lucent_batch* b, uint32_t samples, cudaStream_t s) {
+  const uint32_t n = (uint32_t)b->rs.size(), k = std::min<uint32_t>(b->opt.streams, n);
+  lucent_status st;
+  if (b->parts.size() != k) {
+    drop_parts(b);
+    lucent_batch_options o = b->opt;
+    o.streams = 1;
+    for (uint32_t i = 0; i < k; i++) {
+      const uint32_t i0 = n * i / k, i1 = n * (i + 1) / k;
+      lucent_batch* q = nullptr;
+      if ((st = lucent_batch_create(b->rs.data() + i0, i1 - i0, &q))) return st;
+      b->parts.push_back(q);
+      if ((st = lucent_batch_set_options(q, &o))) return st;
+      b->part_streams.emplace_back();
+      if ((st = b->part_streams.back().ensure())) return st;
+    }
+  }
+  cudaEventRecord(b->part_streams[0].fork, s);
+  for (uint32_t i = 0; i < k; i++) {
+    SideStream& ps = b->part_streams[i];
+    cudaStreamWaitEvent(ps.stream, b->part_streams[0].fork, 0);
+    if ((st = lucent_batch_trace(b->parts[i], samples, ps.stream))) return st;
+    cudaEventRecord(ps.join, ps.stream);
+    cudaStreamWaitEvent(s, ps.join, 0);
+  }
   return LUCENT_OK;
 }
 
@@ -1205,6 +1258,12 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
   clear_error();
   if (!b) return fail(LUCENT_ERR_INVALID, "null batch");
   if (samples == 0) return LUCENT_OK;
+  if (b->opt.streams > 1 && b->rs.size() > 1) {
+    for (size_t i = 0; i < b->rs.size(); i++)
+      if (!scene_owner(b->rs[i])->has_scene || !b->rs[i]->has_lighting)
+        return fail(LUCENT_ERR_INVALID, "renderer %zu: trace before load_scene / upload_lighting", i);
+    return trace_parts(b, samples, (cudaStream_t)stream);
+  }
   const int n = (int)b->rs.size();
   std::vector<SceneRec> recs(n);
   uint64_t pixels = 0;
@@ -1281,7 +1340,7 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
   if (st) return st;
   if (cap > b->sid_cap) {
     if ((st = b->sid.reserve((size_t)cap * 2))) return st;
-    if (cudaMemset(b->sid.ptr, 0, (size_t)cap * 2) != cudaSuccess) return cuda_fail(cudaGetLastError(), "clear sid");
+    if (clear_now(b->sid.ptr, (size_t)cap * 2) != cudaSuccess) return cuda_fail(cudaGetLastError(), "clear sid");
     b->sid_cap = cap;
     b->drop_graphs();
   }
@@ -1352,20 +1411,34 @@ lucent_status lucent_batch_check(lucent_batch* b, void* stream, lucent_batch_sta
   if (!b) return fail(LUCENT_ERR_INVALID, "null batch");
   cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "synchronize");
-  if (out) std::memset(out, 0, sizeof *out);
+  lucent_batch_stats acc;
+  std::memset(&acc, 0, sizeof acc);
+  for (lucent_batch* q : b->parts) {  // parts traced on their own streams (the caller's joined them)
+    lucent_batch_stats ps;
+    if (lucent_status st = lucent_batch_check(q, stream, &ps)) return st;
+    acc.closest_rays += ps.closest_rays;
+    acc.shadow_rays += ps.shadow_rays;
+    acc.waves += ps.waves;
+    acc.graph_waves += ps.graph_waves;
+    acc.wave_paths += ps.wave_paths;
+  }
+  if (out) *out = acc;
   if (!b->ctr.ptr) return LUCENT_OK;
   uint32_t words[kCtrWords];
   e = cudaMemcpy(words, b->ctr.ptr, sizeof words, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "read batch counters");
   if (out) {
-    std::memcpy(&out->closest_rays, words + kCtrStatClosest, 8);
-    std::memcpy(&out->shadow_rays, words + kCtrStatShadow, 8);
-    out->waves = b->waves;
-    out->graph_waves = b->graph_waves;
-    out->wave_paths = b->path_cap;
+    uint64_t c = 0, sh = 0;
+    std::memcpy(&c, words + kCtrStatClosest, 8);
+    std::memcpy(&sh, words + kCtrStatShadow, 8);
+    out->closest_rays += c;
+    out->shadow_rays += sh;
+    out->waves += b->waves;
+    out->graph_waves += b->graph_waves;
+    out->wave_paths += b->path_cap;
   }
   if (words[kCtrErr]) {
-    cudaMemset((uint32_t*)b->ctr.ptr + kCtrErr, 0, 4);
+    clear_now((uint32_t*)b->ctr.ptr + kCtrErr, 4);
     return fail(LUCENT_ERR_DEVICE, "batch raised device error word 0x%x", words[kCtrErr]);
   }
   return LUCENT_OK;

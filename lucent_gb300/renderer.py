@@ -338,10 +338,13 @@ class Batch:
     sizes, 0 = all resident blocks), sort_rays, top_levels, wide_bvh (as
     the renderer's set_ray_sort / set_top_levels / set_wide_bvh),
     scenes_per_wave (waves hold groups of this many consecutive scenes,
-    each traced for all samples before the next; 0 = all scenes)."""
+    each traced for all samples before the next; 0 = all scenes), streams
+    (the renderers in that many parts, traced side by side on their own
+    streams)."""
 
     DEFAULTS = {"samples_per_wave": 0, "max_wave_paths": 1 << 25, "use_graph": True, "trace_blocks": 0,
-                "shade_blocks": 0, "sort_rays": True, "top_levels": True, "wide_bvh": True, "scenes_per_wave": 0}
+                "shade_blocks": 0, "sort_rays": True, "top_levels": True, "wide_bvh": True, "scenes_per_wave": 0,
+                "streams": 1}
 
     def __init__(self, renderers, **options):
         self.renderers = list(renderers)
@@ -360,7 +363,8 @@ class Batch:
         o = self.options
         d = NR.BatchOptions(o["samples_per_wave"], o["max_wave_paths"], 1 if o["use_graph"] else 0,
                             o["trace_blocks"], o["shade_blocks"], 1 if o["sort_rays"] else 0,
-                            1 if o["top_levels"] else 0, 1 if o["wide_bvh"] else 0, o["scenes_per_wave"])
+                            1 if o["top_levels"] else 0, 1 if o["wide_bvh"] else 0, o["scenes_per_wave"],
+                            o["streams"])
         N.check(N.lib().lucent_batch_set_options(self._h, C.byref(d)))
 
     def trace_samples(self, count, stream=None):
@@ -381,7 +385,8 @@ class Batch:
     # Second tuning stage: one option at a time from the best wave configuration
     # (ray sorting, the shared-memory top BVH levels, the grid of the shade /
     # resolve / any-hit kernels); none of them changes an image.
-    REFINE = ({"sort_rays": False}, {"top_levels": False}, {"shade_blocks": 152 * 3}, {"shade_blocks": 152 * 8})
+    REFINE = ({"sort_rays": False}, {"top_levels": False}, {"shade_blocks": 152 * 3}, {"shade_blocks": 152 * 8},
+              {"streams": 2})
 
     def autotune(self, samples=2, candidates=None, cache=None, refine=True):
         """Times at least `samples` samples (two full waves) under each

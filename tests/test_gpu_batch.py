@@ -61,7 +61,8 @@ def solo(specs):
                                   {"max_wave_paths": 5000}, {"samples_per_wave": 3},
                                   {"sort_rays": False, "top_levels": False}, {"wide_bvh": False},
                                   {"scenes_per_wave": 1}, {"scenes_per_wave": 2, "samples_per_wave": 2},
-                                  {"scenes_per_wave": 2, "use_graph": False, "max_wave_paths": 5000}])
+                                  {"scenes_per_wave": 2, "use_graph": False, "max_wave_paths": 5000},
+                                  {"streams": 2}, {"streams": 3, "scenes_per_wave": 1, "samples_per_wave": 2}])
 def test_batch_equals_renderers_alone(specs, solo, opts):
     rs = _renderers(specs)
     b = Batch(rs, **opts)
@@ -128,6 +129,12 @@ def test_batch_errors(specs):
         b.trace_samples(1)
     with pytest.raises(LucentError):
         b.set_options(max_wave_paths=0)
+    for bad in (0, 17):
+        with pytest.raises(LucentError):
+            b.set_options(max_wave_paths=1 << 20, streams=bad)
+    b.set_options(streams=2)  # a part without a scene fails as the whole batch does
+    with pytest.raises(LucentError):
+        b.trace_samples(1)
     for x in (b, r, empty):
         x.dispose()
 
