@@ -920,11 +920,12 @@ __global__ void k_count_rays(uint32_t* ctr, int cur) {  // statistics: rays trac
 }
 
 // ------------------------------------------------------------ ray reordering
-// Between bounces the queue of surviving paths is counting-sorted by a key
-// of (scene, direction octant, Morton code of the origin in a 16^3 grid over
-// its scene's bounds), so that a warp's rays start in similar places and head
-// the same way: fewer divergent traversal steps and more cache reuse. Paths
-// are independent, so the order changes no result.
+// Between bounces the queue of surviving paths is counting-sorted by a
+// 15-bit key of (BVH class, direction: cube-map face and a 4 x 4 cell on it,
+// origin: Morton code of an 8^3 grid over its scene's bounds), so that a
+// warp's rays start in similar places and head the same way: fewer divergent
+// traversal steps and more cache reuse. Paths are independent, so the order
+// changes no result.
 __device__ __forceinline__ uint32_t spread3(uint32_t x) {  // 4 bits -> every third bit
   x &= 15u;
   x = (x | (x << 4)) & 0x0C3u;
@@ -945,10 +946,19 @@ __global__ void k_sort_keys(Paths P, const SceneRec* __restrict__ recs, int n_cl
       const float t = (v - a) / fmaxf(b - a, 1e-20f);
       return (uint32_t)fminf(fmaxf(t * 16.f, 0.f), 15.f);
     };
-    const uint32_t m = spread3(cell(o.x, lo.x, hi.x)) | (spread3(cell(o.y, lo.y, hi.y)) << 1) |
-                       (spread3(cell(o.z, lo.z, hi.z)) << 2);
-    const uint32_t oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
-    const uint32_t local = (oct << 12) | m;  // 15 bits
+    // origin: Morton code of an 8^3 grid over the scene box (9 bits)
+    const uint32_t m = spread3(cell(o.x, lo.x, hi.x) >> 1) | (spread3(cell(o.y, lo.y, hi.y) >> 1) << 1) |
+                       (spread3(cell(o.z, lo.z, hi.z) >> 1) << 2);
+    // direction: cube-map face (major axis and sign) and a 4 x 4 cell on it (7 bits)
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    uint32_t face;
+    float fu, fv, fm;
+    if (ax >= ay && ax >= az) { face = d.x < 0.f ? 1u : 0u; fu = d.y; fv = d.z; fm = ax; }
+    else if (ay >= az) { face = d.y < 0.f ? 3u : 2u; fu = d.x; fv = d.z; fm = ay; }
+    else { face = d.z < 0.f ? 5u : 4u; fu = d.x; fv = d.y; fm = az; }
+    const uint32_t cu = (uint32_t)fminf(fmaxf((fu / fm + 1.f) * 2.f, 0.f), 3.f);
+    const uint32_t cv = (uint32_t)fminf(fmaxf((fv / fm + 1.f) * 2.f, 0.f), 3.f);
+    const uint32_t local = (((face << 4) | (cu << 2) | cv) << 9 | m) >> 1;  // 15 bits (the finest origin bit dropped)
     const uint32_t cls = (uint32_t)min(max(recs[sc].sort_class, 0), n_classes - 1);  // keys stay below kSortBins
     const uint32_t key = (cls << (kSortBits - sbits)) | (local >> sbits);
     P.sort_keys[k] = key;

@@ -61,7 +61,7 @@ struct Paths {
   uint32_t* qs;
   uint32_t* slow;
   uint32_t* slow2;
-  uint32_t* sort_keys;  // per queued path: ray-sort key (scene, direction octant, origin cell)
+  uint32_t* sort_keys;  // per queued path: ray-sort key (BVH class, direction cell, origin cell)
   float4* nray;         // the bounce's rays in queue order: 2 float4 each (origin + path id, direction + scene)
   float4* sray;         // the same sorted (after a ray sort)
   uint32_t* sort_tmp;   // the sorted queue, swapped with the queue it sorts
@@ -114,7 +114,7 @@ struct MultiLaunch {
   int any_alpha;
   int trace_blocks, shade_blocks;  // 0 = all resident blocks
   unsigned long long* trav_stats;  // closest-hit traversal counters (profiling) or nullptr
-  int sort_rays;                   // after bounces 0 and 1, sort the rays by scene, direction octant and origin cell
+  int sort_rays;                   // after bounces 0 and 1, sort the rays by BVH class, direction and origin cell
   int top_levels;                  // stage the top BVH levels of (up to 8) scenes in shared memory
   int any_tex;                     // some scene has texture maps: launch the TEX shade instantiation
   int wide;                        // closest hit over the scenes' four-wide BVH views
