@@ -283,9 +283,9 @@ lucent_status lucent_renderer_set_profiling(lucent_renderer* r, int32_t enabled)
  * and data_out (either may be NULL) receive color/data layer count x size x
  * size x 4 bytes (sRGB codes / linear codes), layers in packScene's order. */
 lucent_status lucent_renderer_read_textures(lucent_renderer* r, uint32_t* size, uint8_t* color_out, uint8_t* data_out);
-/* After bounces 0 and 1, sort the surviving rays by direction cell (cube-map
- * face, 4 x 4 cells a face) and origin cell (counting sort into a ray stream
- * the closest-hit traversal
+/* After bounces 0 and 1 (and 2 in waves of 2^21 paths or more), sort the
+ * surviving rays by direction cell (cube-map face, 4 x 4 cells a face) and
+ * origin cell (counting sort into a ray stream the closest-hit traversal
  * reads in order; default on). Paths are independent: images are the same
  * either way; only the traversal's coherence changes. */
 lucent_status lucent_renderer_set_ray_sort(lucent_renderer* r, int32_t enabled);

@@ -1145,7 +1145,9 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     if (fork) cudaEventRecord(M.ev_join, t);
     forked = fork;
     const bool was_sorted = sorted;
-    sorted = M.sort_rays && b < 2 && b < M.max_bounces;  // the two largest queues
+    // The two largest queues; the third too in waves of 2^21 paths or more
+    // (measured: it pays for its sort there, not in smaller waves).
+    sorted = M.sort_rays && b < M.max_bounces && (b < 2 || (b == 2 && M.total_paths >= (1u << 21)));
     if (sorted && was_sorted) {
       // This bounce's resolve (perhaps still running on the side stream) reads
       // its pre-sort queue in sort_tmp; its sorted queue buffer is free once
