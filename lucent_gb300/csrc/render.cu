@@ -1225,7 +1225,7 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
       if (fork) cudaEventRecord(M.ev_join, t);
       forked = fork;
       const bool was_sorted = sorted;
-      sorted = M.sort_rays && b < 2 && b < M.max_bounces;
+      sorted = M.sort_rays && b < M.max_bounces && (b < 2 || (b == 2 && M.total_paths >= (1u << 21)));
       if (sorted && was_sorted) {  // as in render_wave_multi
         uint32_t* busy = P.sort_tmp;
         P.sort_tmp = sort_rays_into(M, P, cur ^ 1, aux, s, P.q[cur]);
