@@ -35,7 +35,7 @@ constexpr int kWide = 4;
 // tree at most 62 deep (the reference's 64-entry stack less the root and one).
 constexpr int kWideStack = 96;
 
-__device__ __forceinline__ Node wide_record(const Node* nodes, int c, uint32_t n_nodes) {
+__device__ __forceinline__ Node wide_record(const Node* nodes, int c) {
   Node r = load_node(nodes, c);
   if (node_count(r) == 0) r.lo.w = __int_as_float(c);
   return r;
@@ -58,8 +58,8 @@ static __global__ void k_build_wide(const Node* nodes, uint32_t n_nodes, Node* w
       if (node_count(cn) > 0) {
         rec[m++] = cn;
       } else if (g > 0 && (uint32_t)g + 1 < n_nodes) {
-        rec[m++] = wide_record(nodes, g, n_nodes);
-        rec[m++] = wide_record(nodes, g + 1, n_nodes);
+        rec[m++] = wide_record(nodes, g);
+        rec[m++] = wide_record(nodes, g + 1);
       }
     }
   }
@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
             sp = 0;
             iters = 0;
             count_stat(A, 0);
-            cur = wide_record(bv.nodes, 0, bv.node_limit);  // the reference pops the root first and tests its box
+            cur = wide_record(bv.nodes, 0);  // the reference pops the root first and tests its box
             SlabClass cl = classify_slab(r, cur.lo, cur.hi, c_lo, c_hi);
             if (cl == kAmbiguous) {
               count_stat(A, 1);
@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_wide_t(TravArgs A, Pol P) {
     int sp = 0;
     bool occ = false, ok = true, defer = false;
     uint32_t iters = 0;
-    Node cur = wide_record(bv.nodes, 0, bv.node_limit);
+    Node cur = wide_record(bv.nodes, 0);
     bool have = passes(cur);
     while (have) {
       if (++iters > bv.node_limit) {
