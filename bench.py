@@ -15,6 +15,15 @@ Workloads:
            256^2..1024^2 pixels), 64 spp, depth 8: one step renders every
            scene as one batch; reports the one-renderer-after-another figure
            beside it and whether both give identical images
+  knot     the large-mesh frame: 2,000,000-triangle displaced torus knot at
+           1920x1080, depth 12, thin lens, lognormal HDRI with a sun disk:
+           one step = --knot-spp samples of the frame (the 256-spp frame's
+           rate without rendering all of it); value = spp/s, with closest-hit
+           Mrays/s, its roofline and the 5-iteration a-trous time
+The default workload's line also carries, in extra.targets, the figures of
+the other configurations measured in the same run (large-mesh spp/s, the
+adjoint/forward ratio, batched vs per-scene spp/s with identical images);
+--no-targets skips them.
 Under torchrun (N > 1) every rank runs an independent replica of the same
 workload on its own GPU (weak scaling: the work is rays, which need no
 exchange); the timed region is bracketed by barriers and the max over ranks
@@ -182,15 +191,15 @@ def run_ours_closest(args, rank, world, local):
         achieved = per_launch / (sum(ms) / len(ms) / 1000.0) / 1e9
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": NCU_DRAM_BYTES_CLOSEST_LAUNCH,
+                "traffic_scope": "DRAM bytes of one launch over the 1e6 rays; ncu capture of this workload "
+                                 "summarised in profiles/closest_wide_soup65k_1Mrays.md",
                 "peak_source": which, "kernel": "k_closest_wide_t<ApiPolicy> (+ slow path)",
                 "bytes_per_ray": alg["bytes_per_ray"]}
     return {
         "metric": "closest-hit Mrays/s (intersectBVH, 65,536-triangle soup, 1e6 rays)",
         "value": round(value, 2), "unit": "Mrays/s", "ms_per_step": round(sum(ms) / len(ms), 4),
         "wall_s": round(wall, 3), "e2e": e2e, "roofline": roof, "clocks": clk.summary(),
-        "gpu_launches": 2 * args.steps, "dtype": "f32+f64",
-        "config": {"workload": "closest: random soup 65,536 tris (PCG64 seed 0), 1e6 sphere rays, tMin 1e-5",
-                   "l2": "flushed between timed steps (256 MB write)", "hit_ids": "bit-exact vs intersectBVH"},
+        "gpu_launches": 2 * args.steps, "dtype": "f32+f64", "config": CONFIGS["closest"],
     }
 
 
@@ -210,12 +219,30 @@ def cpu_closest(threads, sample_rays=1_000_000, reps=3):
 # ----------------------------------------------------------------------------- path-tracing workload
 PT_W, PT_H, PT_SPP, PT_DEPTH = 512, 512, 16, 8
 CPU_BASELINE_SECONDS = 10.0
-# dram__bytes_read.sum + dram__bytes_write.sum from ncu captures of the same
-# workloads (profiles/closest_pt_box512_16spp.md, closest_wide_soup65k_1Mrays.md).
+# dram__bytes_read.sum + dram__bytes_write.sum of the closest-hit launches,
+# from ncu captures of the same workloads (the source is named in each line's
+# traffic_scope).
 NCU_DRAM_BYTES_PT_FRAME = 828_700_000
 NCU_DRAM_BYTES_CLOSEST_LAUNCH = 115_400_000
 PT_METRIC = ("closest-hit Mrays/s inside path tracing: box scene (81,956 triangles), 512x512, 16 spp, "
              "max depth 8 (also spp/s)")
+CONFIGS = {
+    "pt": {"workload": "pt: box scene seed 0 (5 Lambert walls, quad light 15, 2 rotated boxes, "
+                       "81,920-triangle icosphere, layered BSDF), 512x512, 16 spp, depth 8, RR from bounce 2",
+           "l2": "flushed between timed frames (256 MB write)",
+           "hit_ids": "bit-exact vs intersectBVH (tMin 1e-6, tMax 1e30)"},
+    "closest": {"workload": "closest: random soup 65,536 tris (PCG64 seed 0), 1e6 sphere rays, tMin 1e-5",
+                "l2": "flushed between timed steps (256 MB write)", "hit_ids": "bit-exact vs intersectBVH"},
+    "knot": {"workload": "knot: torus knot (2,3) 2,000,000 triangles, 3-octave displacement 0.05, 16 materials "
+                         "(4 dielectrics, 10% alpha-blended), 1024x512 lognormal HDRI + 0.5 deg sun disk, thin lens "
+                         "0.02, 1920x1080, depth 12, a-trous 5 iterations",
+             "l2": "working set above L2 (224 MB of triangles and attributes, 1.5 GB of path state)"},
+    "build": {"workload": "build: soup_65k (config 1), box_82k (config 2), knot_2m (config 3); maxLeafSize 4, "
+                          "12 bins"},
+    "adjoint": {"workload": "adjoint: adjoint_scene(0, 6) (81,956 triangles, 33 materials, 256x128 HDRI), "
+                            "8 views 512x512 (renderer views sharing one scene), 32 spp forward / 32 replayed, "
+                            "depth 6"},
+}
 
 
 def run_ours_pt(args, rank, world, local):
@@ -304,25 +331,26 @@ def run_ours_pt(args, rank, world, local):
         achieved = per_frame / (ph["closest"] / 1000.0) / 1e9
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": NCU_DRAM_BYTES_PT_FRAME,
-                "traffic_scope": "DRAM bytes of the frame's 9 closest-hit launches (ncu), like achieved",
+                "traffic_scope": "DRAM bytes of the frame's 9 closest-hit launches, like achieved; ncu capture of "
+                                 "this workload summarised in profiles/closest_pt_box512_16spp.md",
                 "peak_source": which, "kernel": "k_closest_wide_t<PathClosestMulti> (+ slow path)",
                 "bytes_per_closest_ray": alg["bytes_per_closest_ray"],
                 "closest_ms_per_frame": round(ph["closest"], 3)}
     # camera, accumulate, seed advance; 8 per bounce (counters, closest fast + exact, shade, any-hit fast +
     # exact, resolve, ray count); 3 per ray sort (after bounces 0 and 1)
     launches_per_frame = 3 + 8 * (PT_DEPTH + 1) + 3 * 2
+    r.dispose()
+    extra = {"mpaths_per_s": round(paths / dev_s / 1e6, 2), "shadow_mrays_per_s": round(shadow / dev_s / 1e6, 2),
+             "closest_rays_per_frame": int(per_frame_closest),
+             "phase_ms_per_frame": {k: round(v, 3) for k, v in ph.items()}}
+    if args.targets and world == 1:
+        extra["targets"] = run_targets(args, local)
     return {
         "metric": PT_METRIC, "value": round(value, 2), "unit": "Mrays/s", "ms_per_step": round(sum(ms) / len(ms), 4),
         "wall_s": round(wall, 3), "e2e": e2e, "roofline": roof, "clocks": clk.summary(),
         "gpu_launches": launches_per_frame * args.steps, "dtype": "f32 (+f64 exact hit decisions)",
-        "spp_per_s": round(spp_per_s, 2),
-        "extra": {"mpaths_per_s": round(paths / dev_s / 1e6, 2), "shadow_mrays_per_s": round(shadow / dev_s / 1e6, 2),
-                  "closest_rays_per_frame": int(per_frame_closest),
-                  "phase_ms_per_frame": {k: round(v, 3) for k, v in ph.items()}},
-        "config": {"workload": "pt: box scene seed 0 (5 Lambert walls, quad light 15, 2 rotated boxes, "
-                               "81,920-triangle icosphere, layered BSDF), 512x512, 16 spp, depth 8, RR from bounce 2",
-                   "l2": "flushed between timed frames (256 MB write)",
-                   "hit_ids": "bit-exact vs intersectBVH (tMin 1e-6, tMax 1e30)"},
+        "spp_per_s": round(spp_per_s, 2), "extra": extra,
+        "config": CONFIGS["pt"],
     }
 
 
@@ -347,6 +375,282 @@ def cpu_pt(threads, reps=1, crop=512):
     return rays / dt / 1e6, "%dx%d centre crop of the 512x512 frame, 16 spp x %d reps" % (crop, crop, reps)
 
 
+# ----------------------------------------------------------------------------- BVH build workload
+def _build_meshes():
+    """Positions of the configurations' meshes: config 1's soup (65,536
+    triangles), config 2's box scene (81,956) and config 3's displaced knot
+    (2,000,000)."""
+    from lucent_gb300 import scene as S
+    from lucent_gb300 import workloads as W
+    soup, _ = W.soup_and_rays(seed=0, n_tri=65536, n_rays=1)
+    return {"soup_65k": soup, "box_82k": S.pack_scene(W.box_scene(0, 6)).positions,
+            "knot_2m": W.knot_mesh(0).positions}
+
+
+def run_ours_build(args, rank, world, local):
+    """buildBVH on the GPU (lucent_bvh_build_device from device-resident
+    positions; the build is synchronous and includes its host steps). One
+    step = one build of each mesh; value = triangles per second over the
+    three. Also the reference-facing call (lucent_bvh_build: host positions
+    in, the reference's node array and triIndices out) per mesh."""
+    import torch
+    from lucent_gb300 import bvh as B
+    torch.cuda.set_device(local)
+    meshes = _build_meshes()
+    dev = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in meshes.items()}
+    for k in meshes:  # warm-up
+        for _ in range(max(1, args.warmup)):
+            B.build_device(dev[k].data_ptr(), meshes[k].size // 9).close()
+    torch.cuda.synchronize()
+    per = {k: [] for k in meshes}
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            for k in meshes:
+                t0 = time.perf_counter()
+                B.build_device(dev[k].data_ptr(), meshes[k].size // 9).close()
+                per[k].append(time.perf_counter() - t0)
+    e2e = {}
+    for k, v in meshes.items():
+        t0 = time.perf_counter()
+        b = B.build_bvh(v)
+        e2e[k] = time.perf_counter() - t0
+        b._device.close()
+    tris = sum(v.size // 9 for v in meshes.values())
+    total = max_over_ranks(sum(min(x) for x in per.values()), world)
+    return {
+        "metric": "GPU BVH build Mtris/s (buildBVH, bit-exact nodes): configs 1-3 meshes (65,536 / 81,956 / "
+                  "2,000,000 triangles)",
+        "value": round(tris * world / total / 1e6, 3), "unit": "Mtris/s", "ms_per_step": round(1e3 * total, 3),
+        "higher_is_better": True,
+        "e2e": {"value": round(tris / sum(e2e.values()) / 1e6, 3), "unit": "Mtris/s",
+                "h2d_bytes_per_step": int(sum(v.nbytes for v in meshes.values())),
+                "d2h_bytes_per_step": int(sum((2 * (v.size // 9) - 1) * 32 + (v.size // 9) * 4
+                                              for v in meshes.values()))},
+        "roofline": None, "clocks": clk.summary(), "gpu_launches": None, "dtype": "f32 data, f64 decisions",
+        "config": CONFIGS["build"],
+        "extra": {"build_ms": {k: round(1e3 * min(v), 3) for k, v in per.items()},
+                  "reference_call_ms": {k: round(1e3 * v, 3) for k, v in e2e.items()}},
+    }
+
+
+def cpu_build(threads, reps=1):
+    """The oracle's buildBVH (single-threaded, like the reference) on the same meshes."""
+    import oracle
+    global _BUILD_MESHES
+    if _BUILD_MESHES is None:
+        _BUILD_MESHES = _build_meshes()
+    t0 = time.perf_counter()
+    tris = 0
+    for _ in range(reps):
+        for v in _BUILD_MESHES.values():
+            oracle.build_bvh(v)
+            tris += v.size // 9
+    dt = time.perf_counter() - t0
+    return tris / dt / 1e6, "the three meshes x %d reps, one thread (the reference builds on one worker)" % reps
+
+
+_BUILD_MESHES = None
+
+
+def cpu_build_ms():
+    """Per-mesh single-thread oracle build time (ms)."""
+    import oracle
+    global _BUILD_MESHES
+    if _BUILD_MESHES is None:
+        _BUILD_MESHES = _build_meshes()
+    out = {}
+    for k, v in _BUILD_MESHES.items():
+        t0 = time.perf_counter()
+        oracle.build_bvh(v)
+        out[k] = round(1e3 * (time.perf_counter() - t0), 2)
+    return out
+
+
+# ----------------------------------------------------------------------------- large-mesh workload
+KNOT_W, KNOT_H, KNOT_DEPTH, KNOT_ATROUS = 1920, 1080, 12, 5
+
+
+def run_ours_knot(args, rank, world, local):
+    """The large-mesh frame (workloads.knot_scene(0): 2,000,000 triangles at
+    1920x1080, depth 12). One step = --knot-spp samples of the frame traced
+    through the renderer (the full frame has 256); value = samples per second
+    of the whole frame. Also: closest-hit Mrays/s, the closest-hit roofline
+    (oracle bytes per ray of this scene over the phase's device time), and
+    the 5-iteration a-trous denoiser plus display pass at this size."""
+    import ctypes as C
+
+    import torch
+    from lucent_gb300 import _native as N
+    from lucent_gb300 import workloads as W
+    from lucent_gb300.renderer import Renderer
+    torch.cuda.set_device(local)
+    spp = args.knot_spp
+    t0 = time.perf_counter()
+    sc = W.knot_scene(0)
+    t1 = time.perf_counter()
+    r = Renderer(KNOT_W, KNOT_H)
+    r.settings.max_bounces = KNOT_DEPTH
+    r.load_scene(sc)
+    torch.cuda.synchronize()
+    load_s = time.perf_counter() - t1
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    def step():
+        r.reset()
+        r.trace_samples(spp, sp)
+
+    for _ in range(args.warmup):
+        step()
+    r.check(sp)
+    s0 = r.stats()
+    barrier(world)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            evs[k][0].record(stream)
+            step()
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+    r.check(sp)
+    s1 = r.stats()
+    ms = [a.elapsed_time(b) for a, b in evs]
+    dev_s = max_over_ranks(sum(ms) / 1000.0, world)
+    closest = (s1["closest_rays"] - s0["closest_rays"]) * world
+    value = spp * args.steps * world / dev_s
+    r.set_profiling(True)
+    step()
+    r.check(sp)
+    ph = r.stats()["phase_ms"]
+    per_frame_closest = (r.stats()["closest_rays"] - s1["closest_rays"])
+    r.set_profiling(False)
+    # denoiser (variance + 5 a-trous iterations, as the workload fixes) on the accumulated frame
+    dn = []
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r.denoise(levels=KNOT_ATROUS, stream=sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        dn.append(e0.elapsed_time(e1))
+    # end to end: camera and settings from host structs, trace, denoise, display to RGBA8 host memory
+    L = N.lib()
+    out8 = torch.empty(KNOT_W * KNOT_H * 4, dtype=torch.uint8).pin_memory()
+    cam = r.camera_state
+    from lucent_gb300 import _native_render as NR
+    settings = NR.SettingsDesc(KNOT_DEPTH, r.settings.firefly_clamp)
+
+    def e2e_step():
+        N.check(L.lucent_renderer_upload_camera(r.handle, C.byref(cam)))
+        N.check(L.lucent_renderer_apply_settings(r.handle, C.byref(settings)))
+        N.check(L.lucent_renderer_trace(r.handle, spp, sp))
+        N.check(L.lucent_renderer_denoise(r.handle, KNOT_ATROUS, 4.0, 64.0, 1.5, sp))
+        N.check(L.lucent_renderer_display(r.handle, 1.0, 0, 1.0, C.cast(out8.data_ptr(), N.U8P), None, sp))
+
+    e2e_step()
+    torch.cuda.synchronize()
+    t0e = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0e, world)
+    alg = json.load(open(ALG_BYTES)).get("pt_knot") if os.path.exists(ALG_BYTES) else None
+    peak, which = peaks()
+    roof = None
+    if alg and ph.get("closest"):
+        per_frame = alg["bytes_per_closest_ray"] * per_frame_closest
+        achieved = per_frame / (ph["closest"] / 1000.0) / 1e9
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None,
+                "traffic_scope": "not captured for this workload",
+                "peak_source": which, "kernel": "k_closest_wide_t<PathClosestMulti> (+ slow path)",
+                "bytes_per_closest_ray": alg["bytes_per_closest_ray"],
+                "closest_ms_per_step": round(ph["closest"], 3)}
+    r.dispose()
+    return {
+        "metric": "large-mesh spp/s: 2,000,000-triangle knot, 1920x1080, depth 12 (closest-hit Mrays/s beside it)",
+        "value": round(value, 3), "unit": "spp/s", "ms_per_step": round(sum(ms) / len(ms), 3),
+        "e2e": {"value": round(spp * args.steps * world / e2e_s, 3), "unit": "spp/s",
+                "h2d_bytes_per_step": C.sizeof(cam) + C.sizeof(settings),
+                "d2h_bytes_per_step": KNOT_W * KNOT_H * 4,
+                "includes": "trace, 5 a-trous iterations, display, RGBA8 read-back"},
+        "roofline": roof, "clocks": clk.summary(),
+        "gpu_launches": None, "dtype": "f32 (+f64 exact hit decisions)", "config": CONFIGS["knot"],
+        "extra": {"closest_mrays_per_s": round(closest / dev_s / 1e6, 2), "spp_per_step": spp,
+                  "frame_256spp_s_projected": round(256 / value, 3),
+                  "denoise_atrous5_ms": round(float(np.median(dn)), 3),
+                  "phase_ms_per_step": {k: round(v, 3) for k, v in ph.items()},
+                  "scene_generate_s": round(t1 - t0, 2), "scene_load_s": round(load_s, 2)},
+    }
+
+
+def cpu_knot(threads, reps=1, crop=32):
+    """Oracle on a crop x crop window at the frame centre, 1 spp: closest-hit rays per second."""
+    from oracle import render as R
+    from lucent_gb300 import workloads as W
+    global _KNOT_PREP
+    if _KNOT_PREP is None:
+        _KNOT_PREP = R.prepare(W.knot_scene(0))
+    x0, y0 = (KNOT_W - crop) // 2, (KNOT_H - crop) // 2
+    t0 = time.perf_counter()
+    px = 0
+    for _ in range(reps):
+        R.render(_KNOT_PREP, KNOT_W, KNOT_H, 0, 1, max_bounces=KNOT_DEPTH, crop=(x0, y0, crop, crop),
+                 threads=threads)
+        px += crop * crop
+    dt = time.perf_counter() - t0
+    # pixel-samples per second over the frame's pixels = frame samples per second
+    return px / dt / (KNOT_W * KNOT_H), "%dx%d centre crop of the 1920x1080 frame, 1 spp x %d reps" % (
+        crop, crop, reps)
+
+
+_KNOT_PREP = None
+
+
+def run_targets(args, local):
+    """The other configurations, measured after the default workload in the
+    same run: each a bounded run of its own workload (one timed step after
+    one warm-up, or a few samples of a frame)."""
+    import types
+    out = {}
+    t0 = time.perf_counter()
+    bb = run_ours_build(types.SimpleNamespace(steps=3, warmup=1), 0, 1, local)
+    out["bvh_build"] = {"gpu_ms": bb["extra"]["build_ms"], "reference_call_ms": bb["extra"]["reference_call_ms"],
+                        "cpu_oracle_single_thread_ms": cpu_build_ms(),
+                        "wall_s": round(time.perf_counter() - t0, 1)}
+    t0 = time.perf_counter()
+    k = run_ours_knot(types.SimpleNamespace(steps=2, warmup=1, knot_spp=args.knot_spp), 0, 1, local)
+    out["large_mesh"] = {"spp_per_s": k["value"], "closest_mrays_per_s": k["extra"]["closest_mrays_per_s"],
+                         "roofline_frac": k["roofline"]["frac"] if k["roofline"] else None,
+                         "roofline_achieved_gbs": k["roofline"]["achieved"] if k["roofline"] else None,
+                         "denoise_atrous5_ms": k["extra"]["denoise_atrous5_ms"],
+                         "e2e_spp_per_s": k["e2e"]["value"], "spp_per_step": args.knot_spp, "clocks": k["clocks"],
+                         "wall_s": round(time.perf_counter() - t0, 1)}
+    t0 = time.perf_counter()
+    a = run_ours_adjoint(types.SimpleNamespace(steps=1, warmup=1), 0, 1, local)
+    bf = a["extra"]["batched_forward"]
+    out["adjoint"] = {"backward_over_forward": a["value"], "target": "<= 3",
+                      "forward_ms_per_view": a["extra"]["forward_ms_per_view"],
+                      "backward_ms_per_view": a["extra"]["backward_ms_per_view"],
+                      "batched_over_sequential_32spp": bf["32_spp_per_call"]["batched_over_sequential"],
+                      "batched_over_sequential_1spp": bf["1_spp_per_call"]["batched_over_sequential"],
+                      "clocks": a["clocks"], "wall_s": round(time.perf_counter() - t0, 1)}
+    t0 = time.perf_counter()
+    # The autotuner's choice on this workload (waves of 8 consecutive scenes,
+    # two parts on two streams, measured with the full autotune of
+    # `--workload batch`), so this bounded run skips the tuning itself.
+    b = run_ours_batch(types.SimpleNamespace(steps=1, warmup=1, batch_scenes=64,
+                                             batch_options={"scenes_per_wave": 8, "streams": 2, "top_levels": False}),
+                       0, 1, local)
+    out["batch"] = {"batched_mpaths_per_s": b["value"], "sequential_mpaths_per_s": b["extra"]["sequential_mpaths_per_s"],
+                    "batched_over_sequential": b["extra"]["batched_over_sequential"], "target": ">= 2",
+                    "identical_images": b["extra"]["identical_images"], "tuned_options": b["extra"]["tuned_options"],
+                    "scenes": 64, "config": b["config"]["workload"], "clocks": b["clocks"],
+                    "setup_s": b["extra"]["setup_s"], "wall_s": round(time.perf_counter() - t0, 1)}
+    return out
+
+
 # ----------------------------------------------------------------------------- batch workload
 BATCH_SPP, BATCH_DEPTH = 64, 8
 
@@ -362,18 +666,33 @@ def _batch_setup(n, timing=None):
     timing.setdefault("generate", 0.0)
     timing.setdefault("load", 0.0)
     rs = []
+    t0 = time.perf_counter()
+    scenes = _generate_batch_scenes(n)
+    timing["generate"] += time.perf_counter() - t0
     for seed in range(n):
-        t0 = time.perf_counter()
-        sc, res = W.batch_scene(seed)
+        sc, res = scenes[seed]
+        scenes[seed] = None
         t1 = time.perf_counter()
         r = Renderer(res, res)
         r.settings.max_bounces = BATCH_DEPTH
         r.load_scene(sc)
         torch.cuda.synchronize()
-        timing["generate"] += t1 - t0
         timing["load"] += time.perf_counter() - t1
         rs.append(r)
     return rs
+
+
+def _generate_batch_scenes(n):
+    """workloads.batch_scene(0 .. n-1), generated by a pool of spawned
+    processes (host-only work; spawn, never fork, once CUDA is initialised)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    from lucent_gb300 import workloads as W
+    workers = min(n, max(1, (os.cpu_count() or 1)))
+    if workers <= 1:
+        return [W.batch_scene(seed) for seed in range(n)]
+    with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(W.batch_scene, range(n)))
 
 
 def _image_digest(r):
@@ -426,7 +745,12 @@ def run_ours_batch(args, rank, world, local):
         r.trace_samples(1, sp)
         r.check(sp)
         r.trim()
-    tuned, trials = b.autotune(samples=8)
+    if getattr(args, "batch_options", None):
+        # fixed options (the autotuner's choice on this workload), for bounded runs
+        b.set_options(**args.batch_options)
+        tuned, trials = dict(args.batch_options), {}
+    else:
+        tuned, trials = b.autotune(samples=8)
     barrier(world)
     torch.cuda.synchronize()
     for _ in range(args.warmup):
@@ -501,6 +825,7 @@ def cpu_batch(threads, reps=1, crop=16):
 
 # ----------------------------------------------------------------------------- adjoint workload
 ADJ_W, ADJ_SPP, ADJ_DEPTH, ADJ_VIEWS = 512, 32, 6, 8
+ADJ_METRIC = "adjoint/forward time ratio: path-replay backward vs forward, 8 views 512x512, 32 spp, depth 6"
 
 
 def run_ours_adjoint(args, rank, world, local):
@@ -603,15 +928,13 @@ def run_ours_adjoint(args, rank, world, local):
         modes["%d_spp_per_call" % spp] = m
     ratio = tb / tf
     return {
-        "metric": "adjoint/forward time ratio: path-replay backward vs forward, 8 views 512x512, 32 spp, depth 6",
+        "metric": ADJ_METRIC,
         "value": round(ratio, 3), "unit": "x", "ms_per_step": round(1e3 * (tf + tb + tu + tr) / args.steps, 2),
         "higher_is_better": False,
         "e2e": {"value": round(ratio, 3), "unit": "x", "h2d_bytes_per_step": ADJ_VIEWS * ADJ_W * ADJ_W * 16,
                 "d2h_bytes_per_step": ADJ_VIEWS * ADJ_W * ADJ_W * 52},
         "roofline": None, "clocks": clk.summary(), "gpu_launches": None, "dtype": "f32 (+f64 exact hit decisions)",
-        "config": {"workload": "adjoint: adjoint_scene(0, 6) (81,956 triangles, 33 materials, 256x128 HDRI), "
-                               "8 views 512x512 (renderer views sharing one scene), 32 spp forward / 32 replayed, "
-                               "depth 6"},
+        "config": CONFIGS["adjoint"],
         "extra": {"forward_ms_per_view": round(1e3 * tf / (len(views) * args.steps), 2),
                   "backward_ms_per_view": round(1e3 * tb / (len(views) * args.steps), 2),
                   "upload_and_adam_ms_per_step": round(1e3 * tu / args.steps, 2),
@@ -666,7 +989,12 @@ def max_over_ranks(x, world):
 
 
 WORKLOADS = {"closest": (run_ours_closest, cpu_closest, "Mrays/s"), "pt": (run_ours_pt, cpu_pt, "Mrays/s"),
-             "batch": (run_ours_batch, cpu_batch, "Mpaths/s"), "adjoint": (run_ours_adjoint, cpu_adjoint, "Mpaths/s")}
+             "batch": (run_ours_batch, cpu_batch, "Mpaths/s"), "adjoint": (run_ours_adjoint, cpu_adjoint, "Mpaths/s"),
+             "knot": (run_ours_knot, cpu_knot, "spp/s"), "build": (run_ours_build, cpu_build, "Mtris/s")}
+METRICS = {"closest": "closest-hit Mrays/s (intersectBVH, 65,536-triangle soup, 1e6 rays)", "pt": PT_METRIC,
+           "knot": "large-mesh spp/s: 2,000,000-triangle knot, 1920x1080, depth 12 (closest-hit Mrays/s beside it)",
+           "build": "GPU BVH build Mtris/s (buildBVH, bit-exact nodes): configs 1-3 meshes (65,536 / 81,956 / "
+                    "2,000,000 triangles)"}
 DEFAULT_WORKLOAD = "pt"
 
 
@@ -679,9 +1007,12 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes of the batch workload")
+    ap.add_argument("--knot-spp", type=int, default=8, help="samples per step of the large-mesh workload")
+    ap.add_argument("--no-targets", dest="targets", action="store_false",
+                    help="skip the other configurations' figures in the default line")
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = {"batch": 1, "adjoint": 3}.get(args.workload, 20)
+        args.steps = {"batch": 1, "adjoint": 3, "knot": 3}.get(args.workload, 20)
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     rank, world, local = dist_env()
     run, cpu, unit = WORKLOADS[args.workload]
@@ -689,6 +1020,18 @@ def main():
 
     if args.impl == "reference":
         if rank != 0:
+            return
+        if args.workload == "adjoint":
+            # Our line's value is a backward/forward time ratio; the reference
+            # renders forward only, so it has no such ratio to time.
+            print(json.dumps({"impl": "reference", "metric": ADJ_METRIC, "unavailable":
+                              "the reference has no backward pass (no differentiable renderer), so no "
+                              "backward/forward ratio exists to time"}), flush=True)
+            return
+        if args.workload == "batch":
+            print(json.dumps({"impl": "reference", "metric": None, "unavailable":
+                              "the reference renders one scene per WebGL context; its CPU code has no batch path"}),
+                  flush=True)
             return
         vals = []
         for _ in range(args.warmup):
@@ -705,10 +1048,8 @@ def main():
                                  "sample": sample + " (oracle: C++ restatement of the reference's TypeScript, "
                                                     "binary64, std::thread on all host cores; not V8)"},
                 "e2e": {"value": round(v, 3), "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        ours_metric = {"closest": "closest-hit Mrays/s (intersectBVH, 65,536-triangle soup, 1e6 rays)", "pt": PT_METRIC,
-                       "batch": "path-tracing Mpaths/s (batch scenes)"}
-        line["metric"] = ours_metric.get(args.workload, args.workload)
-        line["config"] = {"workload": args.workload}
+        line["metric"] = METRICS[args.workload]
+        line["config"] = CONFIGS[args.workload]
         print(json.dumps(line), flush=True)
         return
 

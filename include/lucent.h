@@ -127,10 +127,15 @@ lucent_status lucent_bvh_intersect_f64(lucent_bvh* bvh, const double* rays, uint
  * every GPU loading the library keeps until exit, so n is limited to
  * 1,048,576 rays per call (larger n fails with LUCENT_ERR_UNSUPPORTED). All
  * calls share that array: calls that overlap on the GPU (other threads, other
- * streams) race on it and must be serialised by the caller. The first call on
- * each device looks up the array's device address with that device current.
- * The call returns after the work completes (it synchronises `stream`) and
- * reports kernel errors like lucent_bvh_check. */
+ * streams) race on it and must be serialised by the caller. Every call looks
+ * up the array's device address with the calling thread's current device.
+ * The tree is checked on the device before any traversal reads it (children
+ * inside the node array and after their parent, leaf ranges inside the
+ * triangle array, finite bounds, source indices below tri_count); a tree that
+ * fails returns LUCENT_ERR_INVALID naming the first bad record, and nothing
+ * is written to the outputs. With tri_count == 0 every ray misses: prim = -1,
+ * t = +inf, u = v = 0. The call returns after the work completes (it
+ * synchronises `stream`) and reports kernel errors like lucent_bvh_check. */
 lucent_status lucent_bvh_intersect_noalloc(const float* nodes_d, uint32_t node_count, const float* tris_d,
                                            uint32_t tri_count, const float* rays_d, uint32_t n, double t_min,
                                            double t_max, int32_t* prim_d, float* t_d, float* u_d, float* v_d,
@@ -247,6 +252,14 @@ void lucent_renderer_destroy(lucent_renderer* r);
 /* loadScene(scene, bvh?) (renderer.ts:279-312). */
 lucent_status lucent_renderer_load_scene(lucent_renderer* r, const lucent_scene_desc* scene);
 lucent_status lucent_renderer_upload_lighting(lucent_renderer* r, const lucent_lighting* lighting);
+/* buildEnvSampler(img, maxWidth) (src/scene/environment.ts:52-85, with
+ * buildAliasTable, src/math/alias.ts:17-65): the table upload_lighting builds
+ * from an equirect RGB map (rows top to bottom). Host code, no device work.
+ * Writes *gw, *gh, and (each may be NULL) gw * gh * 4 floats to `table`
+ * (keep probability, alias cell, pdfUV, alias pdfUV) and the weight sum to
+ * *total (0: a black map, light sampling off). */
+lucent_status lucent_env_sampler(const float* rgb, uint32_t width, uint32_t height, uint32_t max_width, uint32_t* gw,
+                                 uint32_t* gh, float* table, double* total);
 /* uploadGround (renderer.ts:415-421). */
 lucent_status lucent_renderer_upload_ground(lucent_renderer* r, int32_t enabled, float height);
 /* With temporal on and samples accumulated, the history is kept and the
@@ -278,6 +291,25 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
  * and slow the closest-hit kernel down, so phase times taken with them are
  * not the kernel's own. */
 lucent_status lucent_renderer_set_profiling(lucent_renderer* r, int32_t enabled);
+/* Ray capture for parity checks of the traversal inside the renderer (no
+ * reference counterpart; the reference's shader traversal cannot be read
+ * back either). For every bounce b with bit b set in bounce_mask, the traces
+ * that follow copy the bounce's closest-hit rays with their hits and its
+ * shadow rays with their answers, at most max_rays of each per bounce, from
+ * the last wave traced (a trace of W * H * samples <= 2^23 paths is one
+ * wave). Waves launch directly while capture is on (no graph replay); images
+ * are unchanged. bounce_mask = 0 turns capture off and frees its memory
+ * (64 bytes per ray, two regions per bounce). */
+lucent_status lucent_renderer_capture_rays(lucent_renderer* r, uint32_t bounce_mask, uint32_t max_rays);
+/* Synchronises the legacy stream and copies the captured rays of `bounce`,
+ * 16 floats per ray, in queue order (out16 may be NULL; at most cap rays);
+ * *count = the bounce's queue length (may exceed what was captured).
+ * shadow = 0: closest-hit rays (origin xyz, path id bits, direction xyz,
+ * scene bits, hit t, u, v, BVH slot bits (-1 = no triangle hit), alpha key
+ * bits, 0, 0, 0). shadow = 1: shadow rays (origin xyz, t_max, direction xyz,
+ * alpha key bits, occluded (0/1), shadow slot bits, 0 x 6). */
+lucent_status lucent_renderer_read_rays(lucent_renderer* r, uint32_t bounce, int32_t shadow, float* out16,
+                                        uint32_t cap, uint32_t* count);
 /* The texture arrays the scene's maps are sampled from (buildTextureArrays,
  * renderer.ts:314-333): *size = the layer size (0: no textures); color_out
  * and data_out (either may be NULL) receive color/data layer count x size x

@@ -2,7 +2,7 @@
 import ctypes as C
 
 P = C.POINTER
-F32P, I32P, U32P, U8P, VP = P(C.c_float), P(C.c_int32), P(C.c_uint32), P(C.c_uint8), C.c_void_p
+F32P, F64P, I32P, U32P, U8P, VP = P(C.c_float), P(C.c_double), P(C.c_int32), P(C.c_uint32), P(C.c_uint8), C.c_void_p
 
 
 class SceneDesc(C.Structure):
@@ -46,6 +46,7 @@ def declare(L, sig):
     sig(L, "lucent_renderer_destroy", [VP], None)
     sig(L, "lucent_renderer_load_scene", [VP, P(SceneDesc)])
     sig(L, "lucent_renderer_upload_lighting", [VP, P(LightingDesc)])
+    sig(L, "lucent_env_sampler", [F32P, C.c_uint32, C.c_uint32, C.c_uint32, U32P, U32P, F32P, F64P])
     sig(L, "lucent_renderer_upload_ground", [VP, C.c_int32, C.c_float])
     sig(L, "lucent_renderer_upload_camera", [VP, P(CameraDesc)])
     sig(L, "lucent_renderer_apply_settings", [VP, P(SettingsDesc)])
@@ -58,6 +59,8 @@ def declare(L, sig):
     sig(L, "lucent_renderer_stats", [VP, P(RenderStats)])
     sig(L, "lucent_renderer_set_profiling", [VP, C.c_int32])
     sig(L, "lucent_renderer_trim", [VP])
+    sig(L, "lucent_renderer_capture_rays", [VP, C.c_uint32, C.c_uint32])
+    sig(L, "lucent_renderer_read_rays", [VP, C.c_uint32, C.c_int32, F32P, C.c_uint32, U32P])
     sig(L, "lucent_renderer_set_ray_sort", [VP, C.c_int32])
     sig(L, "lucent_renderer_set_top_levels", [VP, C.c_int32])
     sig(L, "lucent_renderer_set_wide_bvh", [VP, C.c_int32])

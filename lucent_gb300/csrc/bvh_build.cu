@@ -14,9 +14,9 @@
 //  * nodes are built in any order under temporary ids and renumbered at the
 //    end: the k-th inner node in left-first DFS preorder owns children
 //    (2k+1, 2k+2) (bvh.ts:238-242).
-// Big nodes (> kSmallMax triangles) are processed level by level with one
-// block per chunk of triangles; every smaller subtree is finished by a single
-// warp, depth first, smaller child first so its stack stays shallow.
+// Big nodes (> 2048 triangles) are processed level by level with one block
+// per chunk of triangles; smaller nodes level by level too, one warp per node,
+// every node of a level in parallel (k_small_level).
 #include <cfloat>
 
 #include "common.cuh"
@@ -27,7 +27,6 @@ namespace build {
 
 constexpr int kMaxBins = 32;
 constexpr int kChunk = 4096;  // triangles per block in the big-node pipeline
-constexpr int kWarpStack = 40;
 
 struct Task {
   uint32_t start, end;
@@ -292,7 +291,7 @@ __global__ void k_prim_bounds(const float* __restrict__ pos, uint32_t n, float4*
 }
 
 // ---------------------------------------------------------------------------
-// Warp-level node processing (used for every subtree of <= kSmallMax).
+// Warp-level node processing (used for every node of <= 2048 triangles).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float warp_min(float v) {
   for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -422,30 +421,28 @@ __device__ bool warp_node(const Ctx& cx, Task tk, int lane, unsigned* cnt, unsig
   return true;
 }
 
-// One warp finishes one small subtree, smaller child first.
-__global__ void __launch_bounds__(128) k_small_subtrees(Ctx cx, const Task* __restrict__ tasks,
-                                                        const uint32_t* __restrict__ ntasks) {
+// One level of the small nodes: warp w processes task w of `in` (grid-stride
+// over *n_in), and a node that splits appends its two children to `out`. The
+// host launches levels until no task is left, so every small node of a level
+// runs in parallel instead of one warp walking a whole subtree.
+__global__ void __launch_bounds__(128) k_small_level(Ctx cx, const Task* __restrict__ in,
+                                                     const uint32_t* __restrict__ n_in, Task* __restrict__ out,
+                                                     uint32_t* __restrict__ n_out) {
   __shared__ unsigned cnt_s[4][3 * kMaxBins];
   __shared__ unsigned box_s[4][3 * kMaxBins * 6];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t nt = min(*ntasks, cx.cap);
+  const uint32_t nt = min(*n_in, cx.cap);
   for (uint32_t w = blockIdx.x * 4 + warp; w < nt; w += gridDim.x * 4) {
-    Task stack[kWarpStack];
-    int sp = 0;
-    stack[sp++] = tasks[w];
-    while (sp > 0) {
-      const Task tk = stack[--sp];
-      Task a, b;
-      if (!warp_node(cx, tk, lane, cnt_s[warp], box_s[warp], &a, &b)) continue;
-      // Continue with the smaller child; the larger waits on the stack, so the
-      // stack never holds more than log2(kSmallMax) + 1 entries.
-      const bool a_small = (a.end - a.start) <= (b.end - b.start);
-      if (sp + 2 > kWarpStack) {
-        if (lane == 0) atomicOr(cx.err, kErrStack);
-        break;
+    Task a, b;
+    if (!warp_node(cx, in[w], lane, cnt_s[warp], box_s[warp], &a, &b)) continue;
+    if (lane == 0) {
+      const uint32_t k = atomicAdd(n_out, 2u);
+      if (k + 2 <= cx.cap) {
+        out[k] = a;
+        out[k + 1] = b;
+      } else {
+        atomicOr(cx.err, kErrQueue);
       }
-      stack[sp++] = a_small ? b : a;
-      stack[sp++] = a_small ? a : b;
     }
   }
 }

@@ -159,14 +159,34 @@ lucent_status gpu_build_bvh(const float* pos_d, uint32_t n, int max_leaf, int bi
     }
     std::swap(big_cur, big_nxt);
   }
-  uint32_t nsmall = 0;
-  BB_CUDA(cudaMemcpyAsync(&nsmall, cx.small_count, 4, cudaMemcpyDeviceToHost, s), "read small count");
-  BB_CUDA(cudaStreamSynchronize(s), "sync small count");
-  if (nsmall) {
-    int g = (int)((nsmall + 3) / 4);
-    if (g > 152 * 32) g = 152 * 32;
-    k_small_subtrees<<<g, 128, 0, s>>>(cx, cx.small, cx.small_count);
-    BB_CUDA(cudaGetLastError(), "small-subtree kernel");
+  // Small nodes level by level: the tasks of a level are processed by one
+  // warp each, their children form the next level. Two task lists alternate
+  // (the small list and a big-node list, free by now) with their counts in
+  // ctr[1] and ctr[2]; the host checks for an empty level every 8 levels.
+  {
+    Task* lv[2] = {cx.small, big_nxt};
+    uint32_t* lc[2] = {cx.small_count, cx.big_next_count};
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int g = 8 * (sms > 0 ? sms : 152);
+    int cur = 0;
+    for (int level = 0;; level++) {
+      if (level >= 4096) {
+        release_all();
+        return fail(LUCENT_ERR_DEVICE, "BVH build did not converge");
+      }
+      if (level % 8 == 0) {  // any task left in the current level?
+        uint32_t left = 0;
+        BB_CUDA(cudaMemcpyAsync(&left, lc[cur], 4, cudaMemcpyDeviceToHost, s), "read small count");
+        BB_CUDA(cudaStreamSynchronize(s), "sync small count");
+        if (left == 0) break;
+      }
+      BB_CUDA(cudaMemsetAsync(lc[cur ^ 1], 0, 4, s), "reset small count");
+      k_small_level<<<g, 128, 0, s>>>(cx, lv[cur], lc[cur], lv[cur ^ 1], lc[cur ^ 1]);
+      BB_CUDA(cudaGetLastError(), "small-level kernel");
+      cur ^= 1;
+    }
   }
   uint32_t ctr_h[4];
   BB_CUDA(cudaMemcpyAsync(ctr_h, ctr, sizeof ctr_h, cudaMemcpyDeviceToHost, s), "read counters");

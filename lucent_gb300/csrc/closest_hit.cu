@@ -21,6 +21,7 @@ struct ApiPolicy {
   const float4* tris;
   int32_t* prim;
   float *tout, *uout, *vout;
+  double tmin;
   __device__ uint32_t count() const { return n; }
   __device__ void ray(uint32_t k, float3& o, float3& d) const { load_ray6(rays, k, o, d); }
   __device__ uint32_t key(uint32_t) const { return 0; }
@@ -29,9 +30,13 @@ struct ApiPolicy {
   __device__ bool alpha(int, int, uint32_t, float, float) const { return true; }
   __device__ AlphaAnswer alpha_fast(int, int, uint32_t) const { return kAlphaBlock; }
   __device__ bool alpha_any() const { return false; }
-  // intersectBVH's t, u, v are binary64 values: always confirmed in binary64.
-  __device__ bool exact_output() const { return true; }
-  __device__ void hit32(uint32_t k, int slot, float3 e) const { hit(k, slot, e.x, e.y, e.z); }
+  // The hit triangle, encoded -3 - slot until k_refine_api computes its
+  // values with the warp converged (lanes finish their rays at different
+  // steps, so per-ray arithmetic here would run one lane at a time).
+  __device__ void finish(uint32_t k, int slot, const Ray32&, float4, float4, float4, float, float, float, float,
+                         double) const {
+    prim[k] = -3 - slot;
+  }
   __device__ void hit(uint32_t k, int slot, double t, double u, double v) const {
     prim[k] = __float_as_int(__ldg(tris + 3 * (size_t)slot).w);
     if (tout) tout[k] = __double2float_rn(t);
@@ -66,6 +71,29 @@ __global__ void k_closest_exact_d(TravArgs A, const double* __restrict__ rays, u
       tout[i] = t;
       uout[i] = u;
       vout[i] = v;
+    }
+  }
+}
+
+// The values of the hits the traversal found (prim = -3 - slot): the
+// reference's binary64 t, u, v rounded to binary32, from double-float
+// arithmetic where its bound proves the roundings of all three, else from
+// binary64; prim becomes the triangle's source index. One thread per ray.
+__global__ void k_refine_api(ApiPolicy P) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
+    const int32_t code = P.prim[k];
+    if (code > -3) continue;
+    const int slot = -3 - code;
+    float3 o, d;
+    P.ray(k, o, d);
+    const float4 a = __ldg(P.tris + 3 * (size_t)slot), b = __ldg(P.tris + 3 * (size_t)slot + 1),
+                 c = __ldg(P.tris + 3 * (size_t)slot + 2);
+    float3 tuv;
+    if (tri_df32(o, d, a, b, c, true, tuv)) {
+      P.hit(k, slot, tuv.x, tuv.y, tuv.z);
+    } else {
+      const Tri64 h = tri_f64(o, d, a, b, c, P.tmin, __longlong_as_double(0x7ff0000000000000ll));
+      P.hit(k, slot, h.t, h.u, h.v);
     }
   }
 }
@@ -140,7 +168,7 @@ void launch_closest(const Node* nodes, uint32_t node_count, const float4* tris, 
                     uint32_t* queue_len, uint32_t* work, unsigned* err, bool exact_only, bool top_levels,
                     cudaStream_t s, const Node* wide) {
   if (n == 0) return;
-  const ApiPolicy P{rays_d, n, tris, prim, t, u, v};
+  const ApiPolicy P{rays_d, n, tris, prim, t, u, v, tMin};
   TravArgs A{nodes, node_count, tris, tMin, tMax, queue, queue_len, work, err, nullptr, top_levels ? 1 : 0};
   if (exact_only) {
     TravArgs E = A;
@@ -163,6 +191,7 @@ void launch_closest(const Node* nodes, uint32_t node_count, const float4* tris, 
   }
   // Slow path over the rays the fast kernel queued (length read on the device).
   k_closest_exact_t<ApiPolicy><<<grid_for(n < 4096 ? n : 4096, 128), 128, 0, s>>>(A, P);
+  k_refine_api<<<grid_for(n, 256), 256, 0, s>>>(P);
 }
 
 void launch_wide_view(const Node* nodes, uint32_t node_count, Node* wide, cudaStream_t s) {

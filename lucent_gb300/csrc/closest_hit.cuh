@@ -201,4 +201,118 @@ LUCENT_DEV TriClass mt_classify(const Ray32& r, float4 a, float4 b, float4 c3, f
   return kTriAccept;
 }
 
+// ---------------------------------------------------------------------------
+// The hit's t, u, v as the reference reports them (binary64, ray.ts:30-44),
+// rounded to binary32, without binary64 arithmetic in the common case.
+//
+// Double-float values are pairs (hi, lo) of binary32 numbers with
+// hi = RN(hi + lo), about 48 significant bits, built from error-free
+// transformations (Knuth's TwoSum, Dekker's product through an FMA; Dekker
+// 1971, "A floating-point technique for extending the available precision").
+// Each double-float operation here errs by at most about 3 u^2 (u = 2^-24)
+// of its operands' magnitudes, so with exact differences e1, e2, s the
+// numerators U, V, T and det err by at most about 2^-44.5 x their
+// absolute-value evaluations (uA, vA, tA, dA below), and a quotient x = X/det
+// by 2^-44.5 (xA + |x| dA)/|det| plus 2^-46 |x|. Binary64's own rounding is
+// 2^-7 of that. The bound used is 2^-42 (xA + |x| dA)/|det|, 4x the estimate,
+// doubled for the binary32 rounding of the bound's own evaluation. When that
+// interval around a value cannot contain a binary32 rounding boundary, the
+// value's binary32 rounding equals the binary64 result's rounding; otherwise
+// the caller falls back to binary64.
+// ---------------------------------------------------------------------------
+struct DF {
+  float hi, lo;
+};
+LUCENT_DEV DF df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+LUCENT_DEV DF df_fast(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+LUCENT_DEV DF df_add(DF x, DF y) {
+  DF s = df_two_sum(x.hi, y.hi);
+  const DF t = df_two_sum(x.lo, y.lo);
+  s = df_fast(s.hi, __fadd_rn(s.lo, t.hi));
+  return df_fast(s.hi, __fadd_rn(s.lo, t.lo));
+}
+LUCENT_DEV DF df_sub(DF x, DF y) { return df_add(x, {-y.hi, -y.lo}); }
+LUCENT_DEV DF df_mul(DF x, DF y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  float e = __fmaf_rn(x.hi, y.hi, -p);
+  e = __fmaf_rn(x.hi, y.lo, e);
+  e = __fmaf_rn(x.lo, y.hi, e);
+  return df_fast(p, e);
+}
+LUCENT_DEV DF df_mul_f(DF x, float b) {
+  const float p = __fmul_rn(x.hi, b);
+  return df_fast(p, __fmaf_rn(x.lo, b, __fmaf_rn(x.hi, b, -p)));
+}
+LUCENT_DEV DF df_div(DF x, DF y) {
+  const float q1 = __fdiv_rn(x.hi, y.hi);
+  DF r = df_sub(x, df_mul_f(y, q1));
+  const float q2 = __fdiv_rn(r.hi, y.hi);
+  r = df_sub(r, df_mul_f(y, q2));
+  const float q3 = __fdiv_rn(r.hi, y.hi);
+  return df_add(df_fast(q1, q2), {q3, 0.f});
+}
+LUCENT_DEV DF df_dot(DF ax, DF ay, DF az, DF bx, DF by, DF bz) {
+  return df_add(df_add(df_mul(ax, bx), df_mul(ay, by)), df_mul(az, bz));
+}
+
+// True when every real number within `bound` of x.hi + x.lo rounds to x.hi in
+// binary32 (round to nearest even). Zero, subnormal-range and tie cases say no.
+LUCENT_DEV bool df_rounds_to_hi(DF x, float bound) {
+  const float a = fabsf(x.hi);
+  if (!(a >= 1e-30f) || !(a <= 1e30f)) return false;
+  const float up = __fsub_rn(__int_as_float(__float_as_int(a) + 1), a);
+  const float dn = __fsub_rn(a, __int_as_float(__float_as_int(a) - 1));
+  return __fadd_ru(fabsf(x.lo), bound) < 0.5f * fminf(up, dn);
+}
+
+// The hit's (t, u, v) rounded to binary32. t always equals the rounding of
+// the reference's binary64 t when this returns true; u and v are proven equal
+// to theirs too when `exact_uv`, and are otherwise the roundings of the
+// double-float values (at most one binary32 ulp from binary64's, and equal to
+// them in all but about one case in 10^2 to 10^3, the rest being within the
+// bound of a rounding boundary). False when the bound cannot prove what was
+// asked.
+static __device__ __noinline__ bool tri_df32(float3 o, float3 d, float4 a, float4 b, float4 c, bool exact_uv,
+                                             float3& out) {
+  const DF e1x = df_two_sum(b.x, -a.x), e1y = df_two_sum(b.y, -a.y), e1z = df_two_sum(b.z, -a.z);
+  const DF e2x = df_two_sum(c.x, -a.x), e2y = df_two_sum(c.y, -a.y), e2z = df_two_sum(c.z, -a.z);
+  const DF sx = df_two_sum(o.x, -a.x), sy = df_two_sum(o.y, -a.y), sz = df_two_sum(o.z, -a.z);
+  const DF px = df_sub(df_mul_f(e2z, d.y), df_mul_f(e2y, d.z));  // p = d x e2
+  const DF py = df_sub(df_mul_f(e2x, d.z), df_mul_f(e2z, d.x));
+  const DF pz = df_sub(df_mul_f(e2y, d.x), df_mul_f(e2x, d.y));
+  const DF det = df_dot(e1x, e1y, e1z, px, py, pz);
+  const DF qx = df_sub(df_mul(sy, e1z), df_mul(sz, e1y));  // q = s x e1
+  const DF qy = df_sub(df_mul(sz, e1x), df_mul(sx, e1z));
+  const DF qz = df_sub(df_mul(sx, e1y), df_mul(sy, e1x));
+  const DF U = df_dot(sx, sy, sz, px, py, pz);
+  const DF V = df_dot({d.x, 0.f}, {d.y, 0.f}, {d.z, 0.f}, qx, qy, qz);
+  const DF T = df_dot(e2x, e2y, e2z, qx, qy, qz);
+  const DF t = df_div(T, det), u = df_div(U, det), v = df_div(V, det);
+  // Absolute-value evaluations (binary32 is ample for a bound).
+  const float3 ad = make_float3(fabsf(d.x), fabsf(d.y), fabsf(d.z));
+  const float3 ae1 = make_float3(fabsf(e1x.hi), fabsf(e1y.hi), fabsf(e1z.hi));
+  const float3 ae2 = make_float3(fabsf(e2x.hi), fabsf(e2y.hi), fabsf(e2z.hi));
+  const float3 as = make_float3(fabsf(sx.hi), fabsf(sy.hi), fabsf(sz.hi));
+  const float3 ap = make_float3(ad.y * ae2.z + ad.z * ae2.y, ad.z * ae2.x + ad.x * ae2.z, ad.x * ae2.y + ad.y * ae2.x);
+  const float3 aq = make_float3(as.y * ae1.z + as.z * ae1.y, as.z * ae1.x + as.x * ae1.z, as.x * ae1.y + as.y * ae1.x);
+  const float dA = ae1.x * ap.x + ae1.y * ap.y + ae1.z * ap.z;
+  const float uA = as.x * ap.x + as.y * ap.y + as.z * ap.z;
+  const float vA = ad.x * aq.x + ad.y * aq.y + ad.z * aq.z;
+  const float tA = ae2.x * aq.x + ae2.y * aq.y + ae2.z * aq.z;
+  const float g = 4.54747351e-13f / fabsf(det.hi);  // 2^-41: 2^-42 x 2 for the binary32 rounding of this bound
+  if (!(g < 1e30f)) return false;
+  const bool ok = df_rounds_to_hi(t, g * (tA + fabsf(t.hi) * dA)) &&
+                  (!exact_uv || (df_rounds_to_hi(u, g * (uA + fabsf(u.hi) * dA)) &&
+                                 df_rounds_to_hi(v, g * (vA + fabsf(v.hi) * dA))));
+  out = make_float3(t.hi, u.hi, v.hi);
+  return ok;
+}
+
 }  // namespace lucent

@@ -102,6 +102,7 @@ enum : unsigned {
   kErrStack = 1u,       // a traversal needed more than the reference's 64 stack entries
   kErrIterations = 2u,  // a bounded loop hit its iteration cap
   kErrQueue = 4u,       // a work queue overflowed
+  kErrTree = 8u,        // a caller-supplied device tree failed its check (no-allocation entry point)
 };
 
 }  // namespace lucent

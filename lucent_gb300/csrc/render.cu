@@ -64,9 +64,20 @@ struct PathClosestMulti {
   __device__ AlphaAnswer alpha_fast(int sc, int slot, uint32_t key) const {
     return sh::alpha_fast(recs[sc].scene, slot, key);
   }
-  __device__ bool exact_output() const { return false; }
-  __device__ void hit32(uint32_t k, int slot, float3 e) const {
-    hits[k] = make_float4(e.x, e.y, e.z, __int_as_float(slot));
+  // Binary32 (t, u, v) of the hit triangle, like the GLSL's own hitTriangle,
+  // where binary32 accepts it at c = tMax (every triangle accepted in
+  // binary32 qualifies), else the binary64 values rounded: a function of the
+  // ray and the triangle alone, whatever decisions led to it.
+  __device__ void finish(uint32_t k, int slot, const Ray32& r, float4 a, float4 b, float4 c, float tmin_lo,
+                         float tmin_hi, float cmax_lo, float cmax_hi, double tMin) const {
+    float tl, th;
+    float3 est;
+    if (mt_classify(r, a, b, c, tmin_lo, tmin_hi, cmax_lo, cmax_hi, tl, th, est) == kTriAccept) {
+      hits[k] = make_float4(est.x, est.y, est.z, __int_as_float(slot));
+    } else {
+      const Tri64 h = tri_f64(r.o, r.d, a, b, c, tMin, __longlong_as_double(0x7ff0000000000000ll));
+      hit(k, slot, h.t, h.u, h.v);
+    }
   }
   __device__ void hit(uint32_t k, int slot, double t, double u, double v) const {
     hits[k] = make_float4(__double2float_rn(t), __double2float_rn(u), __double2float_rn(v), __int_as_float(slot));
@@ -112,8 +123,9 @@ struct PathShadowMulti {
 constexpr unsigned kSpecular = 1u, kGuideDone = 2u;
 
 // cameraRay (trace.frag:53-62) and the path's initial state; sample s of
-// pixel `pixel` draws from the stream seeded with (pixel, seed0 + s).
-__device__ __forceinline__ void camera_path(const Paths& P, uint32_t p, uint32_t pixel, uint32_t s,
+// pixel `pixel` draws from the stream seeded with (pixel, seed0 + s). Path p
+// takes position k of the first queue.
+__device__ __forceinline__ void camera_path(const Paths& P, uint32_t p, uint32_t k, uint32_t pixel, uint32_t s,
                                             const CameraDev& cam, int W, int H, uint32_t seed0, int scene) {
   const uint32_t x = pixel % W, y = pixel / W;
   uint32_t st = pixel * 1973u + (seed0 + s) * 9277u + 26699u;  // trace.frag:327-328
@@ -137,9 +149,9 @@ __device__ __forceinline__ void camera_path(const Paths& P, uint32_t p, uint32_t
   P.gnrm[p] = make_float4(-rd.x, -rd.y, -rd.z, 1e4f);
   P.gpos[p] = make_float4(0.f, 0.f, 0.f, 1.f);
   P.rng[p] = st;
-  P.q[0][p] = p;
-  P.nray[2 * (size_t)p] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(p));
-  P.nray[2 * (size_t)p + 1] = make_float4(rd.x, rd.y, rd.z, __int_as_float(scene));
+  P.q[0][k] = p;
+  P.nray[2 * (size_t)k] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(p));
+  P.nray[2 * (size_t)k + 1] = make_float4(rd.x, rd.y, rd.z, __int_as_float(scene));
 }
 
 // Index of the scene whose range [base[i], base[i + 1]) holds v (n scenes).
@@ -153,14 +165,20 @@ __device__ __forceinline__ int find_scene(const uint32_t* __restrict__ base, int
 }
 
 // Several scenes in one wave: scene i owns paths [path_base[i], path_base[i + 1]).
+// Path base + s * W * H + pixel is sample s of the pixel; the first queue
+// holds a scene's paths pixel-major (position base + pixel * S + s), so a
+// warp's primary rays are the samples of one or two pixels: nearly the same
+// ray, the same nodes, the same triangles. Paths are independent, so the
+// queue order changes no result.
 __global__ void k_camera_multi(Paths P, const SceneRec* __restrict__ recs, const uint32_t* __restrict__ path_base,
                                int n, uint16_t* __restrict__ sid, int S) {
   const uint32_t total = __ldg(path_base + n);
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
-    const int sc = find_scene(path_base, n, p);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+    const int sc = find_scene(path_base, n, k);
     const SceneRec& R = recs[sc];
-    const uint32_t WH = (uint32_t)R.W * R.H, local = p - __ldg(path_base + sc);
-    camera_path(P, p, local % WH, local / WH, R.cam, R.W, R.H, R.seed0, sc);
+    const uint32_t base = __ldg(path_base + sc), WH = (uint32_t)R.W * R.H, local = k - base;
+    const uint32_t pixel = local / (uint32_t)S, s = local % (uint32_t)S, p = base + s * WH + pixel;
+    camera_path(P, p, k, pixel, s, R.cam, R.W, R.H, R.seed0, sc);
     sid[p] = (uint16_t)sc;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) P.ctr[kCtrQ0] = total;
@@ -919,6 +937,40 @@ __global__ void k_count_rays(uint32_t* ctr, int cur) {  // statistics: rays trac
   }
 }
 
+// ------------------------------------------------------------ ray capture
+// Closest-hit rays of a bounce in queue order with their hits and alpha keys:
+// (origin, path id), (direction, scene), (t, u, v, slot), (key, 0, 0, 0).
+__global__ void k_capture_closest(const uint32_t* __restrict__ cnt, const float4* __restrict__ rays,
+                                  const float4* __restrict__ hits, const uint32_t* __restrict__ rng,
+                                  float4* __restrict__ out, uint32_t* __restrict__ count, uint32_t cap) {
+  const uint32_t n = *cnt, m = n < cap ? n : cap;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *count = n;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    const float4 a = rays[2 * (size_t)k], b = rays[2 * (size_t)k + 1];
+    out[4 * (size_t)k] = a;
+    out[4 * (size_t)k + 1] = b;
+    out[4 * (size_t)k + 2] = hits[k];
+    out[4 * (size_t)k + 3] = make_float4(__uint_as_float(rng[__float_as_uint(a.w)]), 0.f, 0.f, 0.f);
+  }
+}
+
+// Shadow rays of a bounce in shadow-queue order with their answers:
+// (origin, t_max), (direction, alpha key), (occluded, shadow slot, 0, 0), 0.
+__global__ void k_capture_shadow(const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ queue,
+                                 const float4* __restrict__ so, const float4* __restrict__ sd,
+                                 const uint8_t* __restrict__ occ, float4* __restrict__ out,
+                                 uint32_t* __restrict__ count, uint32_t cap) {
+  const uint32_t n = *cnt, m = n < cap ? n : cap;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *count = n;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    const uint32_t slot = queue[k];
+    out[4 * (size_t)k] = so[k];
+    out[4 * (size_t)k + 1] = sd[k];
+    out[4 * (size_t)k + 2] = make_float4((float)occ[slot], __uint_as_float(slot), 0.f, 0.f);
+    out[4 * (size_t)k + 3] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
 // ------------------------------------------------------------ ray reordering
 // Between bounces the queue of surviving paths is counting-sorted by a
 // 15-bit key of (BVH class, direction: cube-map face and a 4 x 4 cell on it,
@@ -1111,6 +1163,12 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
                M.trav_stats, top};
     launch_closest_multi(M.wide, closest_blocks, top, A, pc, s);
     k_closest_exact_t<PathClosestMulti><<<64, 128, 0, s>>>(A, pc);
+    const bool capture = M.cap && (M.cap_mask >> b & 1u);
+    const uint32_t region = capture ? 2u * (uint32_t)__builtin_popcount(M.cap_mask & ((1u << b) - 1u)) : 0u;
+    if (capture)
+      k_capture_closest<<<aux, 256, 0, s>>>(P.ctr + kCtrQ0 + cur, pc.rays, P.hit, P.rng,
+                                            M.cap + (size_t)region * M.cap_stride * 4, M.cap_count + region,
+                                            M.cap_stride);
     E.mark(kPhClosest, s);
     if (forked) {  // join: the previous bounce's radiance is resolved before this bounce shades
       cudaStreamWaitEvent(s, M.ev_join, 0);
@@ -1135,6 +1193,10 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
                nullptr, top};
     launch_shadow_multi(M.wide, aux * 2, top, B, ps, t);
     k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, t>>>(B, ps);
+    if (capture)
+      k_capture_shadow<<<aux, 256, 0, t>>>(P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ,
+                                           M.cap + (size_t)(region + 1) * M.cap_stride * 4, M.cap_count + region + 1,
+                                           M.cap_stride);
     E.mark(kPhShadow, s);
     // Resolve is per path: it walks the queue as it was before the sort (still
     // intact in sort_tmp), in path order, so its reads stay coalesced.

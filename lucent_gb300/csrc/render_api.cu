@@ -314,6 +314,9 @@ struct lucent_renderer {
   uint32_t hist_w = 0, hist_h = 0;
   DeviceBuffer prev;  // the targets as the previous view left them (36 B per pixel)
   const float4* denoised = nullptr;  // result of the last lucent_renderer_denoise, or null
+  // ray capture (lucent_renderer_capture_rays): bounces, rays per region, records and queue lengths
+  uint32_t cap_mask = 0, cap_rays = 0;
+  DeviceBuffer cap, cap_count;
 };
 
 static AccumDev accum_of(lucent_renderer* r) {
@@ -537,6 +540,12 @@ static lucent_status single_launch(lucent_renderer* r, uint32_t S, uint32_t tail
   M.wide = r->wide_bvh;
   M.sort_classes = 1;
   M.any_tex = scene_owner(r)->tex_size > 0;
+  if (r->cap_mask) {
+    M.cap_mask = r->cap_mask;
+    M.cap = (float4*)r->cap.ptr;
+    M.cap_count = (uint32_t*)r->cap_count.ptr;
+    M.cap_stride = r->cap_rays;
+  }
   if (lucent_status st = r->side.ensure()) return st;
   r->side.set(M);
   return LUCENT_OK;
@@ -881,7 +890,9 @@ lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* 
   wave_key(M, key);
   for (uint32_t w = 0; w < full + (tail ? 1 : 0); w++) {
     if (w == full) single_tail(r, tail, M);
-    if (w < full && !r->profiling && r->waves > 0) {  // the first wave ever runs uncaptured (one-time setup)
+    // The first wave ever runs uncaptured (one-time setup); profiling and ray
+    // capture launch directly.
+    if (w < full && !r->profiling && !r->cap_mask && r->waves > 0) {
       if ((st = r->wave_graph.run(M, key, s))) return st;
     } else {
       render_wave_multi(M, s, r->profiling ? &pe : nullptr);  // seeds advance on the device
@@ -1009,6 +1020,62 @@ lucent_status lucent_renderer_trim(lucent_renderer* r) {
   r->path_cap = 0;
   r->P = Paths{};
   r->P.ctr = (uint32_t*)r->ctr.ptr;
+  return LUCENT_OK;
+}
+
+lucent_status lucent_env_sampler(const float* rgb, uint32_t width, uint32_t height, uint32_t max_width, uint32_t* gw,
+                                 uint32_t* gh, float* table, double* total) {
+  clear_error();
+  if (!rgb || !gw || !gh || width == 0 || height == 0 || max_width == 0)
+    return fail(LUCENT_ERR_INVALID, "null argument or empty image");
+  uint32_t a = 0, b = 0;
+  double t = 0;
+  std::vector<float> tab;
+  if (!env_sampler(rgb, width, height, max_width, a, b, tab, t))
+    return fail(LUCENT_ERR_INVALID, "environment weights must be finite and >= 0");
+  *gw = a;
+  *gh = b;
+  if (total) *total = t;
+  if (table) std::memcpy(table, tab.data(), tab.size() * sizeof(float));
+  return LUCENT_OK;
+}
+
+lucent_status lucent_renderer_capture_rays(lucent_renderer* r, uint32_t bounce_mask, uint32_t max_rays) {
+  clear_error();
+  if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  if (bounce_mask == 0 || max_rays == 0) {
+    r->cap.release();
+    r->cap_count.release();
+    r->cap_mask = r->cap_rays = 0;
+    return LUCENT_OK;
+  }
+  const uint32_t regions = 2u * (uint32_t)__builtin_popcount(bounce_mask);
+  lucent_status st = r->cap.reserve((size_t)regions * max_rays * 64);
+  if (!st) st = r->cap_count.reserve(64 * 4);
+  if (st) return st;
+  if (clear_now(r->cap_count.ptr, 64 * 4) != cudaSuccess) return cuda_fail(cudaGetLastError(), "clear capture");
+  r->cap_mask = bounce_mask;
+  r->cap_rays = max_rays;
+  return LUCENT_OK;
+}
+
+lucent_status lucent_renderer_read_rays(lucent_renderer* r, uint32_t bounce, int32_t shadow, float* out16,
+                                        uint32_t cap, uint32_t* count) {
+  lucent_status st = lucent_renderer_check(r, nullptr);
+  if (st) return st;
+  if (!count) return fail(LUCENT_ERR_INVALID, "null argument");
+  if (bounce >= 32 || !(r->cap_mask >> bounce & 1u)) return fail(LUCENT_ERR_INVALID, "bounce %u is not captured", bounce);
+  const uint32_t region = 2u * (uint32_t)__builtin_popcount(r->cap_mask & ((1u << bounce) - 1u)) + (shadow ? 1u : 0u);
+  uint32_t n = 0;
+  cudaError_t e = cudaMemcpy(&n, (uint32_t*)r->cap_count.ptr + region, 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "read capture count");
+  *count = n;
+  const uint32_t m = std::min(std::min(n, cap), r->cap_rays);
+  if (out16 && m) {
+    e = cudaMemcpy(out16, (const char*)r->cap.ptr + (size_t)region * r->cap_rays * 64, (size_t)m * 64,
+                   cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "read captured rays");
+  }
   return LUCENT_OK;
 }
 

@@ -119,6 +119,15 @@ struct MultiLaunch {
   int any_tex;                     // some scene has texture maps: launch the TEX shade instantiation
   int wide;                        // closest hit over the scenes' four-wide BVH views
   int sort_classes;                // distinct SceneRec::sort_class values (>= 1)
+  // Ray capture (lucent_renderer_capture_rays; parity tests): for every
+  // bounce b in cap_mask, the bounce's closest-hit rays with their hits and
+  // its shadow rays with their answers are copied, 4 float4 per ray, into
+  // regions 2r and 2r + 1 of cap (r = rank of b in cap_mask, cap_stride rays
+  // each); cap_count[2r], cap_count[2r + 1] receive the queue lengths.
+  unsigned cap_mask;
+  float4* cap;
+  uint32_t* cap_count;
+  uint32_t cap_stride;
   // Second stream and fork / join events (nullptr: one stream): the deep
   // bounces' shadow rays run beside the next bounce's closest hit.
   cudaStream_t side;

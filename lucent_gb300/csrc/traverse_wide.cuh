@@ -93,12 +93,11 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
   const uint32_t n = P.count();
   const bool use_alpha = P.alpha_any();
 
-  bool active = false, exhausted = false, have_cur = false, c_exact = true, best_exact = false, have_est = false;
+  bool active = false, exhausted = false, have_cur = false, c_exact = true;
   uint32_t ri = 0, iters = 0, key = 0;
   Ray32 r;
   float c_lo = 0.f, c_hi = 0.f;
-  double c64 = A.tMax, bu64 = 0, bv64 = 0;
-  float3 best_est = make_float3(0.f, 0.f, 0.f);
+  double c64 = A.tMax;  // binary64 t of `best` when c_exact
   int best = -1, sp = 0;
   BvhView bv{A.nodes, A.tris, A.node_limit, 0, A.wide};
   Node cur;
@@ -129,8 +128,6 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
             c_hi = cmax_hi;
             c64 = A.tMax;
             c_exact = true;
-            best_exact = false;
-            have_est = false;
             best = -1;
             sp = 0;
             iters = 0;
@@ -157,10 +154,7 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
                      c = __ldg(bv.tris + 3 * (size_t)best + 2);
         const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, INF64);
         c64 = h.t;
-        bu64 = h.u;
-        bv64 = h.v;
         c_exact = true;
-        best_exact = true;
         c_lo = __double2float_rd(h.t);
         c_hi = __double2float_ru(h.t);
       }
@@ -176,31 +170,13 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
       if (sp == 0) {  // finished
         if (best < 0) {
           P.miss(ri);
-        } else if (P.exact_output()) {  // the reference's binary64 t, u, v
-          if (best_exact) {
-            P.hit(ri, best, c64, bu64, bv64);
-          } else {
-            count_stat(A, 4);
-            const float4 a = __ldg(bv.tris + 3 * (size_t)best), b = __ldg(bv.tris + 3 * (size_t)best + 1),
-                         c = __ldg(bv.tris + 3 * (size_t)best + 2);
-            const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, INF64);
-            P.hit(ri, best, h.t, h.u, h.v);
-          }
-        } else if (have_est) {  // binary32 t, u, v like the GLSL's own
-          P.hit32(ri, best, best_est);
         } else {
-          // Accepted in binary64. The output is a function of the ray and the
-          // triangle alone, whatever decisions led there: the binary32
-          // estimate where binary32 accepts the triangle at c = tMax (as it
-          // does for every triangle accepted in binary32), else binary64's.
+          // The hit's values are the policy's (P.finish): the BVH API
+          // computes them afterwards with its warps converged, the renderer
+          // takes the binary32 estimate of this one triangle.
           const float4 a = __ldg(bv.tris + 3 * (size_t)best), b = __ldg(bv.tris + 3 * (size_t)best + 1),
                        c = __ldg(bv.tris + 3 * (size_t)best + 2);
-          float tl, th;
-          float3 est;
-          if (mt_classify(r, a, b, c, tmin_lo, tmin_hi, cmax_lo, cmax_hi, tl, th, est) == kTriAccept)
-            P.hit32(ri, best, est);
-          else
-            P.hit(ri, best, c64, bu64, bv64);
+          P.finish(ri, best, r, a, b, c, tmin_lo, tmin_hi, cmax_lo, cmax_hi, A.tMin);
         }
         active = false;
         continue;
@@ -239,9 +215,6 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
         }
         if (tc == kTriAccept) {
           best = slot;
-          best_est = est;
-          have_est = true;
-          best_exact = false;
           c_exact = false;
           c_lo = tl;
           c_hi = th;
@@ -252,13 +225,9 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
         const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, cc);
         if (h.hit) {
           best = slot;
-          have_est = false;
           c64 = h.t;
-          bu64 = h.u;
-          bv64 = h.v;
           c_exact = true;
-          best_exact = true;
-          c_lo = __double2float_rd(h.t);
+            c_lo = __double2float_rd(h.t);
           c_hi = __double2float_ru(h.t);
         }
       }

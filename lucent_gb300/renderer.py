@@ -252,6 +252,28 @@ class Renderer:
         adds the closest-hit traversal counters, which slow that kernel."""
         N.check(N.lib().lucent_renderer_set_profiling(self._h, (2 if counters else 1) if enabled else 0))
 
+    def capture_rays(self, bounces=(), max_rays=1 << 22):
+        """Keep the closest-hit and shadow rays of these bounces of the next
+        traces' last wave (lucent_renderer_capture_rays); () turns it off."""
+        mask = 0
+        for b in bounces:
+            mask |= 1 << int(b)
+        N.check(N.lib().lucent_renderer_capture_rays(self._h, mask, max_rays if mask else 0))
+        self._cap_rays = max_rays if mask else 0
+
+    def read_rays(self, bounce, shadow=False):
+        """Captured rays of `bounce` as a [n, 16] float32 array (lucent_renderer_read_rays).
+        Closest: origin, path id bits, direction, scene bits, t, u, v, slot bits, key bits.
+        Shadow: origin, t_max, direction, key bits, occluded, shadow slot bits."""
+        count = C.c_uint32(0)
+        N.check(N.lib().lucent_renderer_read_rays(self._h, bounce, 1 if shadow else 0, None, 0, C.byref(count)))
+        m = min(count.value, getattr(self, "_cap_rays", 0))
+        out = np.zeros((m, 16), np.float32)
+        if m:
+            N.check(N.lib().lucent_renderer_read_rays(self._h, bounce, 1 if shadow else 0, _f(out), m,
+                                                      C.byref(count)))
+        return out
+
     # --------------------------------------------------------- denoise/display
     def samples(self):
         """Samples behind the current average (the reference's `frame`)."""

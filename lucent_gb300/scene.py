@@ -325,9 +325,8 @@ def direction_from_uv(u, v):
 def bake_sky(sky: Sky, sun: Sun, width=1024) -> HDRImage:
     """bakeSky (environment.ts:106-132): gradient sky plus the sun's glow."""
     height = width // 2
-    data = np.zeros((height, width, 3), np.float64)
     if not sky.enabled or sky.intensity <= 0:
-        return HDRImage(width, height, data.astype(np.float32).reshape(-1))
+        return HDRImage(width, height, np.zeros(width * height * 3, np.float32))
     sd = from_spherical(sun.elevation * math.pi / 180, sun.azimuth * math.pi / 180)
     sun_on = sun.intensity > 0 and sun.elevation > -sun.angular_radius
     x = (np.arange(width) + 0.5) / width
@@ -335,17 +334,19 @@ def bake_sky(sky: Sky, sun: Sun, width=1024) -> HDRImage:
     X, Y = np.meshgrid(x, y)
     dx, dy, dz = direction_from_uv(X, Y)
     t = dy
+    out = np.zeros((height, width, 3), np.float32)  # the reference's Float32Array: every store rounds
     for c in range(3):
         up = sky.horizon[c] + (sky.zenith[c] - sky.horizon[c]) * np.power(np.maximum(t, 0), 0.55)
         dn = sky.horizon[c] + (sky.ground[c] - sky.horizon[c]) * np.minimum(1, -t * 4)
-        data[..., c] = np.where(t >= 0, up, dn)
+        out[..., c] = np.where(t >= 0, up, dn)
     if sun_on:
         s = np.maximum(0, dx * sd[0] + dy * sd[1] + dz * sd[2])
         glow = 0.12 * s ** 24 + 0.5 * s ** 400
         for c in range(3):
-            data[..., c] += sun.color[c] * glow
-    data *= sky.intensity
-    return HDRImage(width, height, data.astype(np.float32).reshape(-1))
+            out[..., c] = out[..., c].astype(np.float64) + sun.color[c] * glow
+    for c in range(3):
+        out[..., c] = out[..., c].astype(np.float64) * sky.intensity
+    return HDRImage(width, height, out.reshape(-1))
 
 
 @dataclass

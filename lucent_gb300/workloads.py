@@ -121,16 +121,54 @@ def box_scene(seed=0, subdivisions=6, width=512, height=512):
     return sc
 
 
-def furnace_scene(albedo=1.0, roughness=1.0, ior=1.0, radiance=1.0):
-    """A sphere inside a uniform environment of the given radiance (white furnace)."""
+def furnace_scene(albedo=1.0, roughness=1.0, ior=1.0, radiance=1.0, **layers):
+    """A sphere inside a uniform environment of the given radiance (white
+    furnace). Extra keyword arguments set further material fields (clearcoat,
+    sheen_color, transmission, ...)."""
     from . import mesh as M
     from . import scene as S
     w, h = 16, 8
     env = S.Environment(map=S.HDRImage(w, h, np.full(w * h * 3, radiance, np.float32)), background=True)
     ball = M.icosphere(4, radius=1.0)
-    mat = S.material(albedo=(albedo, albedo, albedo), roughness=roughness, ior=ior)
+    mat = S.material(albedo=(albedo, albedo, albedo), roughness=roughness, ior=ior, **layers)
     cam = S.Camera(position=(0.0, 0.0, 4.0), target=(0.0, 0.0, 0.0), fov=30.0, focus_distance=4.0)
     return S.Scene(name="furnace", camera=cam, env=env, meshes=[S.MeshInstance(ball, mat)])
+
+
+def sky_scene(seed=0, subdivisions=3):
+    """Outdoor scene for the analytic parts of traceScene and the lights: the
+    procedural sky baked by bakeSky (no environment map, so the analytic sun
+    is on: renderer.ts:359-367), the ground plane, analytic spheres
+    (scene.glsl:132-144) of layered, metallic and dielectric materials, one
+    emissive sphere (a sphere light, lights.glsl:99-158), and an icosphere
+    mesh beside them (BVH triangles in the same frame).
+
+    Draw order from numpy.random.Generator(PCG64(seed)): sun elevation
+    U[20, 60], azimuth U[0, 360), 3 sphere albedos (3 x 3), the mesh albedo (3).
+    """
+    from . import mesh as M
+    from . import scene as S
+    rng = np.random.Generator(np.random.PCG64(seed))
+    elev, azim = rng.uniform(20.0, 60.0), rng.uniform(0.0, 360.0)
+    alb = rng.uniform(0.2, 0.8, (3, 3))
+    mesh_alb = rng.uniform(0.2, 0.8, 3)
+    spheres = [
+        S.Sphere((-1.1, 0.5, 0.0), 0.5, S.material(albedo=tuple(alb[0]), roughness=0.4, clearcoat=0.8,
+                                                   clearcoat_roughness=0.1, sheen_color=(0.5, 0.5, 0.5),
+                                                   sheen_roughness=0.4)),
+        S.Sphere((0.0, 0.45, -0.6), 0.45, S.metal(tuple(alb[1]), roughness=0.25)),
+        S.Sphere((1.05, 0.4, 0.2), 0.4, S.glass(ior=1.5, roughness=0.05)),
+        S.Sphere((0.3, 1.6, 0.9), 0.15, S.light((1.0, 0.8, 0.6), 30.0)),
+    ]
+    ball = M.icosphere(subdivisions, radius=0.35, center=(0.2, 0.35, 0.8))
+    meshes = [S.MeshInstance(ball, S.material(albedo=tuple(mesh_alb), roughness=0.6))]
+    sun = S.Sun(elevation=float(elev), azimuth=float(azim), color=(1.0, 0.95, 0.9), intensity=3.0,
+                angular_radius=2.0)
+    sky = S.Sky(enabled=True, intensity=1.0)
+    env = S.Environment(map=None, background=True)
+    ground = S.Ground(enabled=True, height=0.0, material=S.matte((0.45, 0.45, 0.42)))
+    cam = S.Camera(position=(0.0, 1.2, 4.0), target=(0.0, 0.45, 0.0), fov=45.0, focus_distance=4.0)
+    return S.Scene(name="sky", camera=cam, sun=sun, sky=sky, env=env, ground=ground, spheres=spheres, meshes=meshes)
 
 
 def knot_scene(seed=0, tubular=5000, radial=200, env_width=1024):
@@ -173,8 +211,7 @@ def knot_scene(seed=0, tubular=5000, radial=200, env_width=1024):
         mats.append(S.material(albedo=tuple(float(x) for x in alb), roughness=float(rough), metallic=metallic,
                                clearcoat=float(coat), clearcoat_roughness=float(coat_rough),
                                sheen_color=(float(sheen),) * 3, sheen_roughness=float(sheen_rough), **extra))
-    knot = M.displace(M.torus_knot(2, 3, radius=1.0, tube=0.32, tubular_segments=tubular, radial_segments=radial),
-                      0.05, octaves=3, seed=seed)
+    knot = knot_mesh(seed, tubular, radial)
     tube_index = np.arange(knot.triangle_count) // (2 * radial)
     r = ((160 * tube_index) // tubular) % 20
     pick = np.array([0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 4, 5, 6, 7, 14, 15])[r]
@@ -223,6 +260,33 @@ def env_lognormal(rng, width, height):
 BATCH_RESOLUTIONS = (256, 512, 768, 1024)
 
 
+def _batch_shape(rng, tri_lo, tri_hi):
+    """The first draws of batch_scene: (knot?, resolution, tubular, radial, icosphere subdivisions)."""
+    target = float(np.exp(rng.uniform(np.log(tri_lo), np.log(tri_hi))))
+    knot = rng.random() < 0.5
+    res = BATCH_RESOLUTIONS[int(rng.integers(0, len(BATCH_RESOLUTIONS)))]
+    radial = int(rng.integers(16, 64))
+    tubular = max(8, int(round(target / (2 * radial))))
+    sub = int(np.clip(np.round(np.log(target / 20.0) / np.log(4.0)), 0, 9))
+    return knot, res, tubular, radial, sub
+
+
+def batch_sizes(count=64, tri_lo=10_000, tri_hi=2_000_000):
+    """Triangle counts of batch_scene(0 .. count - 1), without building them."""
+    out = []
+    for seed in range(count):
+        knot, _, tubular, radial, sub = _batch_shape(np.random.Generator(np.random.PCG64(seed)), tri_lo, tri_hi)
+        out.append(2 * tubular * radial if knot else 20 * 4 ** sub)
+    return np.array(out, np.int64)
+
+
+def knot_mesh(seed=0, tubular=5000, radial=200):
+    """The displaced torus knot of knot_scene alone (2 * tubular * radial triangles)."""
+    from . import mesh as M
+    return M.displace(M.torus_knot(2, 3, radius=1.0, tube=0.32, tubular_segments=tubular, radial_segments=radial),
+                      0.05, octaves=3, seed=seed)
+
+
 def batch_scene(seed, tri_lo=10_000, tri_hi=2_000_000):
     """One scene of the batched workload: a displaced torus knot or
     icosphere with a triangle count log-uniform in [tri_lo, tri_hi], four
@@ -237,15 +301,10 @@ def batch_scene(seed, tri_lo=10_000, tri_hi=2_000_000):
     from . import mesh as M
     from . import scene as S
     rng = np.random.Generator(np.random.PCG64(seed))
-    target = float(np.exp(rng.uniform(np.log(tri_lo), np.log(tri_hi))))
-    knot = rng.random() < 0.5
-    res = BATCH_RESOLUTIONS[int(rng.integers(0, len(BATCH_RESOLUTIONS)))]
-    radial = int(rng.integers(16, 64))
+    knot, res, tubular, radial, sub = _batch_shape(rng, tri_lo, tri_hi)
     if knot:
-        tubular = max(8, int(round(target / (2 * radial))))
         mesh = M.torus_knot(2, 3, 1.0, 0.32, tubular, radial)
     else:
-        sub = int(np.clip(np.round(np.log(target / 20.0) / np.log(4.0)), 0, 9))
         mesh = M.icosphere(sub, radius=1.2)
     mesh = M.displace(mesh, 0.05, octaves=3, seed=seed)
     mats = []

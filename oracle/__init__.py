@@ -56,6 +56,8 @@ def _declare(L):
     L.orc_sheen_albedo.argtypes = [_D, _D, C.c_int]
     L.orc_sheen_albedo.restype = _D
     L.orc_sheen_lut.argtypes = [C.c_int, C.c_int, P(_F)]
+    L.orc_bake_sky.argtypes = [_U32, P(_D), P(_D), P(_D), _D, C.c_int, _D, _D, P(_D), _D, _D, P(_F)]
+    L.orc_bake_sky.restype = None
     try:
         from . import render as _render
         _render.declare(L)
@@ -222,6 +224,16 @@ def build_env_sampler(rgb, width, height, max_width=1024):
                                    C.byref(total)):
         raise OracleError("env sampler failed")
     return a.value, b.value, table[: a.value * b.value * 4].copy(), total.value
+
+
+def bake_sky(sky, sun, width=1024):
+    """bakeSky (src/scene/environment.ts:106-132) -> float32 [width/2, width, 3]."""
+    out = np.zeros(width * (width // 2) * 3, np.float32)
+    z, h, g, c = (np.ascontiguousarray(v, np.float64) for v in (sky.zenith, sky.horizon, sky.ground, sun.color))
+    lib().orc_bake_sky(width, _p(z, _D), _p(h, _D), _p(g, _D), float(sky.intensity), 1 if sky.enabled else 0,
+                       float(sun.elevation), float(sun.azimuth), _p(c, _D), float(sun.intensity),
+                       float(sun.angular_radius), _p(out, _F))
+    return out.reshape(width // 2, width, 3)
 
 
 def sheen_albedo(cos_v, roughness, steps=128):

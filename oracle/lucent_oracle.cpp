@@ -670,6 +670,44 @@ static double charlieD(double alpha, double cosH) {
 }
 static double neubeltV(double cosL, double cosV) { return 1 / (4 * (cosL + cosV - cosL * cosV)); }
 
+// bakeSky (src/scene/environment.ts:106-132): gradient sky plus the sun's
+// glow into a width x width/2 equirect map; every store rounds to binary32
+// (Float32Array), then the glow is added and the intensity applied as the
+// reference does, each a separate rounded store. directionFromUV :88-93,
+// fromSpherical src/math/vec3.ts:57-60.
+void orc_bake_sky(uint32_t width, const double* zenith, const double* horizon, const double* ground,
+                  double intensity, int enabled, double sun_elevation_deg, double sun_azimuth_deg,
+                  const double* sun_color, double sun_intensity, double sun_angular_radius_deg, float* out) {
+  const uint32_t height = width / 2;
+  const size_t n = (size_t)width * height * 3;
+  for (size_t i = 0; i < n; i++) out[i] = 0.0f;
+  if (!enabled || !(intensity > 0)) return;
+  const double pi = 3.141592653589793;
+  const double el = sun_elevation_deg * pi / 180, az = sun_azimuth_deg * pi / 180;
+  const double ce = std::cos(el);
+  const double sd[3] = {ce * std::sin(az), std::sin(el), ce * std::cos(az)};
+  const bool sun_on = sun_intensity > 0 && sun_elevation_deg > -sun_angular_radius_deg;
+  for (uint32_t y = 0; y < height; y++) {
+    for (uint32_t x = 0; x < width; x++) {
+      const double u = (x + 0.5) / width, v = (y + 0.5) / height;
+      const double phi = (u - 0.5) * 2 * pi, theta = v * pi;
+      const double st = std::sin(theta);
+      const double d[3] = {st * std::cos(phi), std::cos(theta), st * std::sin(phi)};
+      const double t = d[1];
+      float* o = out + ((size_t)y * width + x) * 3;
+      for (int c = 0; c < 3; c++)
+        o[c] = (float)(t >= 0 ? horizon[c] + (zenith[c] - horizon[c]) * std::pow(t, 0.55)
+                              : horizon[c] + (ground[c] - horizon[c]) * std::min(1.0, -t * 4));
+      if (sun_on) {
+        const double s = std::max(0.0, d[0] * sd[0] + d[1] * sd[1] + d[2] * sd[2]);
+        const double glow = 0.12 * std::pow(s, 24) + 0.5 * std::pow(s, 400);
+        for (int c = 0; c < 3; c++) o[c] = (float)((double)o[c] + sun_color[c] * glow);
+      }
+      for (int c = 0; c < 3; c++) o[c] = (float)((double)o[c] * intensity);
+    }
+  }
+}
+
 double orc_sheen_albedo(double cosV, double roughness, int steps) {
   const double r = std::max(0.07, roughness);
   const double alpha = r * r;

@@ -83,6 +83,11 @@ int orc_build_alias(const double* weights, uint32_t n, float* prob, uint32_t* al
 int orc_build_env_sampler(const float* rgb, uint32_t width, uint32_t height, uint32_t max_width,
                           uint32_t* gw, uint32_t* gh, float* table, double* total);
 
+/* bakeSky (src/scene/environment.ts:106-132): width x width/2 x 3 floats. */
+void orc_bake_sky(uint32_t width, const double* zenith, const double* horizon, const double* ground,
+                  double intensity, int enabled, double sun_elevation_deg, double sun_azimuth_deg,
+                  const double* sun_color, double sun_intensity, double sun_angular_radius_deg, float* out);
+
 /* sheenAlbedo / sheenAlbedoLUT (src/scene/sheen.ts:24-60). */
 double orc_sheen_albedo(double cos_v, double roughness, int steps);
 void orc_sheen_lut(int size, int steps, float* out);

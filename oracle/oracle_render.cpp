@@ -1506,6 +1506,40 @@ static int render_impl(const orc_scene* s, const orc_camera* cam, uint32_t max_b
   return 0;
 }
 
+// The triangle part of traceScene and occluded as the oracle decides it,
+// ray by ray: closest_tri (intersectBVH's binary64 order over slots with the
+// alpha test, bvh.ts:265-320, scene.glsl:176-189) for closest rays, any_tri for
+// shadow rays (t_max per ray in rays6's 7th float when stride is 7). Rays are
+// binary32 (origin xyz, direction xyz); keys are the alpha-blend hash keys.
+// Outputs: slot (-1 miss, -2 stack overflow) and binary64 t for closest rays;
+// 1/0 occluded for shadow rays.
+int orc_closest_slots(const orc_scene* s, const float* rays6, const uint32_t* keys, uint64_t n, double t_min,
+                      double t_max, int32_t* slot_out, double* t_out, int threads) {
+  par_for(n, threads, [&](uint64_t b, uint64_t e) {
+    for (uint64_t i = b; i < e; i++) {
+      const float* r = rays6 + i * 6;
+      TriHit h{-1, 0, 0, 0};
+      const bool ok = closest_tri(s, {(double)r[0], (double)r[1], (double)r[2]}, {(double)r[3], (double)r[4], (double)r[5]},
+                                  t_min, t_max, keys ? keys[i] : 0u, h);
+      slot_out[i] = ok ? h.slot : -2;
+      if (t_out) t_out[i] = h.slot >= 0 ? h.t : INFINITY;
+    }
+  });
+  return 0;
+}
+
+int orc_any_slots(const orc_scene* s, const float* rays7, const uint32_t* keys, uint64_t n, double t_min,
+                  uint8_t* occluded_out, int threads) {
+  par_for(n, threads, [&](uint64_t b, uint64_t e) {
+    for (uint64_t i = b; i < e; i++) {
+      const float* r = rays7 + i * 7;
+      occluded_out[i] = any_tri(s, {(double)r[0], (double)r[1], (double)r[2]}, {(double)r[3], (double)r[4], (double)r[5]},
+                                t_min, (double)r[6], keys ? keys[i] : 0u) ? 1 : 0;
+    }
+  });
+  return 0;
+}
+
 int orc_render(const orc_scene* s, const orc_camera* cam, uint32_t max_bounces, float clamp_lum, uint32_t width,
                uint32_t height, uint32_t x0, uint32_t y0, uint32_t cw, uint32_t ch, uint32_t seed0,
                uint32_t samples, int precision, float* color4, float* albedo4, float* normal4, float* history,

@@ -78,6 +78,17 @@ int orc_render_work(const orc_scene* s, const orc_camera* cam, uint32_t max_boun
                     uint32_t seed0, uint32_t samples, float* color4, float* albedo4, float* normal4,
                     float* history, int threads, int detailed, uint64_t* work_out);
 
+/* The triangle part of traceScene / occluded as orc_render decides it, ray by
+ * ray (binary32 rays, binary64 decisions of intersectBVH over BVH slots with
+ * the alpha test). orc_closest_slots: rays6 = 6 floats per ray, slot_out =
+ * slot or -1 (miss) / -2 (stack overflow), t_out (may be NULL) = binary64 t.
+ * orc_any_slots: rays7 = origin, direction, t_max; occluded_out = 1 / 0. keys:
+ * per-ray alpha-blend hash keys (NULL: 0). */
+int orc_closest_slots(const orc_scene* s, const float* rays6, const uint32_t* keys, uint64_t n, double t_min,
+                      double t_max, int32_t* slot_out, double* t_out, int threads);
+int orc_any_slots(const orc_scene* s, const float* rays7, const uint32_t* keys, uint64_t n, double t_min,
+                  uint8_t* occluded_out, int threads);
+
 /* One texture-array layer from a decoded RGBA8 image (rows top to bottom):
  * the resampling of buildTextureArrays (renderer.ts:314-333, resample.frag)
  * as the product defines it (box mip chain, level of detail log2(max(w, h) /

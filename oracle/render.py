@@ -48,6 +48,8 @@ def declare(L):
     L.orc_resample_layer.argtypes = [P(C.c_uint8), U32, U32, U32, C.c_int, P(C.c_uint8)]
     L.orc_texture_size.argtypes = [P(U32), P(U32), U32]
     L.orc_texture_size.restype = U32
+    L.orc_closest_slots.argtypes = [P(OrcScene), P(F), P(U32), C.c_uint64, D, D, P(I32), P(D), C.c_int]
+    L.orc_any_slots.argtypes = [P(OrcScene), P(F), P(U32), C.c_uint64, D, P(C.c_uint8), C.c_int]
 
 
 def half_lut():
@@ -193,6 +195,30 @@ def render_work(prep, width, height, seed0, samples, max_bounces=6, clamp=8.0, c
                           work.ctypes.data_as(P(C.c_uint64)))
     keys = ["closest_rays", "closest_inner", "closest_tris", "shadow_rays", "shadow_nodes", "shadow_tris"]
     return dict(zip(keys, (int(x) for x in work)))
+
+
+def closest_slots(prep, rays, keys=None, t_min=1e-6, t_max=1e30, threads=0):
+    """orc_closest_slots: (slot per ray, -1 on a miss; binary64 t) of the
+    renderer's triangle closest hit on binary32 rays [n, 6]."""
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+    n = r.shape[0]
+    k = None if keys is None else np.ascontiguousarray(keys, np.uint32)
+    slot = np.zeros(n, np.int32)
+    t = np.zeros(n, np.float64)
+    lib().orc_closest_slots(C.byref(prep.scene), _p(r, F), None if k is None else _p(k, U32), n, t_min, t_max,
+                            _p(slot, I32), _p(t, D), threads)
+    return slot, t
+
+
+def any_slots(prep, rays7, keys=None, t_min=1e-6, threads=0):
+    """orc_any_slots: occlusion (bool) of shadow rays [n, 7] = origin, direction, t_max."""
+    r = np.ascontiguousarray(rays7, np.float32).reshape(-1, 7)
+    n = r.shape[0]
+    k = None if keys is None else np.ascontiguousarray(keys, np.uint32)
+    occ = np.zeros(n, np.uint8)
+    lib().orc_any_slots(C.byref(prep.scene), _p(r, F), None if k is None else _p(k, U32), n, t_min,
+                        occ.ctypes.data_as(P(C.c_uint8)), threads)
+    return occ.astype(bool)
 
 
 def bsdf_tuples(tuples, precision=64, threads=0):

@@ -5,7 +5,8 @@ counted by the oracle under the reference's GLSL traversal order
 (src/shaders/scene.glsl:218-267: near-first, both child boxes read per inner
 node): 64 B per inner node visited + 48 B per triangle tested + 24 B ray in +
 16 B hit out. bench.py divides these by the measured kernel time for its
-roofline; tests/test_fixtures.py re-derives them so they cannot go stale.
+roofline; tests/test_fixtures.py re-derives the cheap ones so they cannot go
+stale.
 
 Run: python tests/golden/make_fixtures.py
 """
@@ -56,11 +57,30 @@ def box_scene_bytes(samples=1):
             "triangles_per_closest_ray": round(w["closest_tris"] / c, 3), "samples": samples}
 
 
+def knot_bytes(samples=1, crop=(720, 405, 480, 270)):
+    """Large-mesh workload (2,000,000-triangle displaced torus knot, 1920 x
+    1080, depth 12): the oracle renders `samples` spp of a centred 480 x 270
+    crop (a sixteenth of the frame) and tallies the reference GLSL traversal
+    work as box_scene_bytes does."""
+    from oracle import render as R
+    prep = R.prepare(workloads.knot_scene(0))
+    w = R.render_work(prep, 1920, 1080, 0, samples, max_bounces=12, crop=crop)
+    c, s = w["closest_rays"], w["shadow_rays"]
+    px = crop[2] * crop[3] * samples
+    return {"bytes_per_closest_ray": round((64.0 * w["closest_inner"] + 48.0 * w["closest_tris"]) / c + 40, 2),
+            "bytes_per_shadow_ray": round((32.0 * w["shadow_nodes"] + 48.0 * w["shadow_tris"]) / s + 40, 2),
+            "closest_rays_per_path": round(c / px, 4), "shadow_rays_per_path": round(s / px, 4),
+            "inner_nodes_per_closest_ray": round(w["closest_inner"] / c, 3),
+            "triangles_per_closest_ray": round(w["closest_tris"] / c, 3), "samples": samples,
+            "crop": list(crop)}
+
+
 def main():
     path = os.path.join(HERE, "algorithmic_bytes.json")
     out = json.load(open(path)) if os.path.exists(path) else {}
     out["closest"] = closest_bytes()
     out["pt_box"] = box_scene_bytes()
+    out["pt_knot"] = knot_bytes()
     json.dump(out, open(path, "w"), indent=1, sort_keys=True)
     print(json.dumps(out, indent=1))
 

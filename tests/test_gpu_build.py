@@ -64,6 +64,29 @@ def test_large_displaced_knot():
     _check(m.positions)
 
 
+def test_config3_knot_two_million():
+    """Config 3's mesh: the torus knot tessellated to 2,000,000 triangles with
+    3-octave value-noise displacement (amplitude 0.05), node array and
+    triIndices equal to the oracle's buildBVH."""
+    from lucent_gb300 import workloads as W
+    pos = W.knot_mesh(0).positions
+    assert pos.size == 9 * 2_000_000
+    _check(pos)
+
+
+def test_largest_batch_scene():
+    """The largest scene of the batched workload (config 5), built on the GPU
+    exactly as the batch loads it, against the oracle's buildBVH."""
+    from lucent_gb300 import workloads as W
+    sizes = W.batch_sizes()
+    big = int(np.argmax(sizes))
+    sc, _ = W.batch_scene(big)
+    from lucent_gb300 import scene as S
+    p = S.pack_scene(sc)
+    assert p.tri_count == sizes[big] > 1_000_000
+    _check(p.positions)
+
+
 def test_built_handle_intersects_like_oracle():
     pos, rays = workloads.soup_and_rays(seed=2, n_tri=20000, n_rays=50000)
     gb = B.build_bvh(pos)

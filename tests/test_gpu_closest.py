@@ -67,6 +67,15 @@ def test_random_soup_subset():
     assert (ids >= 0).mean() > 0.3
 
 
+def test_config1_all_rays():
+    """Config 1 whole: 65,536-triangle soup, all 10^6 rays of seed 0, tMin
+    1e-5, tMax inf, against the oracle's intersectBVH (ids, t, u, v)."""
+    pos, rays = workloads.soup_and_rays(seed=0, n_tri=65536, n_rays=1_000_000)
+    ob, dev = _dev(pos)
+    ids = _compare(dev, ob, pos, rays)
+    assert ids.size == 1_000_000 and (ids >= 0).mean() > 0.3
+
+
 def test_adversarial_rays_mesh():
     m = mesh.merge_meshes([mesh.torus_knot(tubular_segments=120, radial_segments=16),
                            mesh.box([-2, -2, -2], [2, 2, 2], inward=True),
