@@ -33,10 +33,7 @@ struct ApiPolicy {
   // The hit triangle, encoded -3 - slot until k_refine_api computes its
   // values with the warp converged (lanes finish their rays at different
   // steps, so per-ray arithmetic here would run one lane at a time).
-  __device__ void finish(uint32_t k, int slot, const Ray32&, float4, float4, float4, float, float, float, float,
-                         double) const {
-    prim[k] = -3 - slot;
-  }
+  __device__ void finish(uint32_t k, int slot) const { prim[k] = -3 - slot; }
   __device__ void hit(uint32_t k, int slot, double t, double u, double v) const {
     prim[k] = __float_as_int(__ldg(tris + 3 * (size_t)slot).w);
     if (tout) tout[k] = __double2float_rn(t);

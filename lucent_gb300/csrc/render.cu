@@ -64,21 +64,8 @@ struct PathClosestMulti {
   __device__ AlphaAnswer alpha_fast(int sc, int slot, uint32_t key) const {
     return sh::alpha_fast(recs[sc].scene, slot, key);
   }
-  // Binary32 (t, u, v) of the hit triangle, like the GLSL's own hitTriangle,
-  // where binary32 accepts it at c = tMax (every triangle accepted in
-  // binary32 qualifies), else the binary64 values rounded: a function of the
-  // ray and the triangle alone, whatever decisions led to it.
-  __device__ void finish(uint32_t k, int slot, const Ray32& r, float4 a, float4 b, float4 c, float tmin_lo,
-                         float tmin_hi, float cmax_lo, float cmax_hi, double tMin) const {
-    float tl, th;
-    float3 est;
-    if (mt_classify(r, a, b, c, tmin_lo, tmin_hi, cmax_lo, cmax_hi, tl, th, est) == kTriAccept) {
-      hits[k] = make_float4(est.x, est.y, est.z, __int_as_float(slot));
-    } else {
-      const Tri64 h = tri_f64(r.o, r.d, a, b, c, tMin, __longlong_as_double(0x7ff0000000000000ll));
-      hit(k, slot, h.t, h.u, h.v);
-    }
-  }
+  // The triangle only: the shade kernel computes t, u, v (hit_values).
+  __device__ void finish(uint32_t k, int slot) const { hits[k] = make_float4(0.f, 0.f, 0.f, __int_as_float(slot)); }
   __device__ void hit(uint32_t k, int slot, double t, double u, double v) const {
     hits[k] = make_float4(__double2float_rn(t), __double2float_rn(u), __double2float_rn(v), __int_as_float(slot));
   }
@@ -365,6 +352,24 @@ static __device__ __forceinline__ MapSample sample_maps(const SceneDev& S, const
   return out;
 }
 
+// The t, u, v the renderer shades with: the binary32 estimates of the
+// triangle's binary32 test at c = tMax (mt_classify; every triangle accepted
+// in binary32 has them), like the GLSL's own hitTriangle, else the binary64
+// values rounded. A function of the ray and the triangle alone, whatever
+// decisions the traversal took; computed one path per thread.
+static __device__ __forceinline__ float4 hit_values(const float4* __restrict__ geo, float3 ro, float3 rd, int slot) {
+  const float4 a = __ldg(geo + 3 * (size_t)slot), b = __ldg(geo + 3 * (size_t)slot + 1),
+               c = __ldg(geo + 3 * (size_t)slot + 2);
+  const Ray32 r = make_ray32(ro, rd);
+  float tl, th;
+  float3 est;
+  if (mt_classify(r, a, b, c, __double2float_rd(1e-6), __double2float_ru(1e-6), __double2float_rd(1e30),
+                  __double2float_ru(1e30), tl, th, est) == kTriAccept)
+    return make_float4(est.x, est.y, est.z, __int_as_float(slot));
+  const Tri64 h = tri_f64(ro, rd, a, b, c, 1e-6, __longlong_as_double(0x7ff0000000000000ll));
+  return make_float4(__double2float_rn(h.t), __double2float_rn(h.u), __double2float_rn(h.v), __int_as_float(slot));
+}
+
 // One bounce of every path in queue `cur`. Hits on texture-mapped materials
 // are shaded by a second instantiation, TEX: the first appends them to the
 // textured-hit queue untouched, so untextured shading carries none of the
@@ -394,7 +399,8 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
     bool spec = flags & kSpecular, done = flags & kGuideDone;
     float4 galb = P.galb[p], gnrm = P.gnrm[p];
     uint32_t st = P.rng[p];
-    const float4 hv = P.hit[kq];
+    float4 hv = P.hit[kq];
+    if (__float_as_int(hv.w) >= 0) hv = hit_values(S.geo, ro, rd, __float_as_int(hv.w));
     bool alive = false, deferred = false;
     float3 dl = f3(0.f, 0.f, 0.f), lrem = f3(0.f, 0.f, 0.f);
     int cont_mat = -1;
@@ -940,16 +946,23 @@ __global__ void k_count_rays(uint32_t* ctr, int cur) {  // statistics: rays trac
 // ------------------------------------------------------------ ray capture
 // Closest-hit rays of a bounce in queue order with their hits and alpha keys:
 // (origin, path id), (direction, scene), (t, u, v, slot), (key, 0, 0, 0).
+// The hit is the triangle the traversal found with the values the shade
+// kernel computes for it (hit_values).
 __global__ void k_capture_closest(const uint32_t* __restrict__ cnt, const float4* __restrict__ rays,
                                   const float4* __restrict__ hits, const uint32_t* __restrict__ rng,
-                                  float4* __restrict__ out, uint32_t* __restrict__ count, uint32_t cap) {
+                                  const SceneRec* __restrict__ recs, float4* __restrict__ out,
+                                  uint32_t* __restrict__ count, uint32_t cap) {
   const uint32_t n = *cnt, m = n < cap ? n : cap;
   if (blockIdx.x == 0 && threadIdx.x == 0) *count = n;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
     const float4 a = rays[2 * (size_t)k], b = rays[2 * (size_t)k + 1];
+    float4 h = hits[k];
+    if (__float_as_int(h.w) >= 0)
+      h = hit_values(recs[__float_as_int(b.w)].scene.geo, make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z),
+                     __float_as_int(h.w));
     out[4 * (size_t)k] = a;
     out[4 * (size_t)k + 1] = b;
-    out[4 * (size_t)k + 2] = hits[k];
+    out[4 * (size_t)k + 2] = h;
     out[4 * (size_t)k + 3] = make_float4(__uint_as_float(rng[__float_as_uint(a.w)]), 0.f, 0.f, 0.f);
   }
 }
@@ -1166,7 +1179,7 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     const bool capture = M.cap && (M.cap_mask >> b & 1u);
     const uint32_t region = capture ? 2u * (uint32_t)__builtin_popcount(M.cap_mask & ((1u << b) - 1u)) : 0u;
     if (capture)
-      k_capture_closest<<<aux, 256, 0, s>>>(P.ctr + kCtrQ0 + cur, pc.rays, P.hit, P.rng,
+      k_capture_closest<<<aux, 256, 0, s>>>(P.ctr + kCtrQ0 + cur, pc.rays, P.hit, P.rng, M.recs,
                                             M.cap + (size_t)region * M.cap_stride * 4, M.cap_count + region,
                                             M.cap_stride);
     E.mark(kPhClosest, s);

@@ -6,10 +6,10 @@
 // first, a node's box tested against the running closest distance `c` when it
 // is popped) and its binary64 decisions. Each decision is first tried with
 // binary32 arithmetic whose error is bounded (closest_hit.cuh); binary64 runs
-// only when the bound cannot decide. What the final hit reports is the
-// policy's: the BVH API's t, u, v are the reference's binary64 values
-// rounded to binary32 (tri_df32, after the traversal), the renderer's are
-// binary32 estimates like the GLSL's own hitTriangle.
+// only when the bound cannot decide. The traversal reports the hit triangle
+// only; its t, u, v are computed afterwards, one ray per thread: the BVH
+// API's are the reference's binary64 values rounded to binary32 (tri_df32),
+// the renderer's binary32 estimates like the GLSL's own hitTriangle.
 //
 // Any hit (shadow rays) answers: does some triangle pass the reference's
 // binary64 Moller-Trumbore in (tMin, tMax) inside boxes its slab test at tMax
@@ -27,8 +27,8 @@
 //   BvhView bvh(uint32_t k) const                 then the k-th ray's BVH (else TravArgs'),
 //   BvhView scene_bvh(int s) const                and scene s's BVH
 //   bool alpha_any() const                        false: no alpha-tested triangles
-//   void finish(uint32_t k, int slot, Ray32, float4 v0, v1, v2, tmin_lo, tmin_hi, cmax_lo, cmax_hi,
-//               double tMin)                      (closest) the hit triangle found; the policy stores it
+//   void finish(uint32_t k, int slot)             (closest) the hit triangle; its t, u, v are the policy's
+//                                                 to compute later, with the warp converged
 //   void hit(uint32_t k, int slot, double t, double u, double v)   a hit with its binary64 values
 //   void miss(uint32_t k); void fail(uint32_t k)
 //   void shadow(uint32_t k, bool occluded)        (any hit)
@@ -332,12 +332,10 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_fast
         if (best < 0) {
           P.miss(ri);
         } else {
-          // The hit's values are the policy's (P.finish): the BVH API
-          // computes them afterwards with its warps converged, the renderer
-          // takes the binary32 estimate of this one triangle.
-          const float4 a = __ldg(bv.tris + 3 * (size_t)best), b = __ldg(bv.tris + 3 * (size_t)best + 1),
-                       c = __ldg(bv.tris + 3 * (size_t)best + 2);
-          P.finish(ri, best, r, a, b, c, tmin_lo, tmin_hi, cmax_lo, cmax_hi, A.tMin);
+          // Only the triangle: its t, u, v are computed afterwards with the
+          // warp converged (lanes finish their rays at different steps, and
+          // work at this point stalls the warp for each lane in turn).
+          P.finish(ri, best);
         }
         active = false;
         continue;

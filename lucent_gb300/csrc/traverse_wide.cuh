@@ -171,12 +171,10 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
         if (best < 0) {
           P.miss(ri);
         } else {
-          // The hit's values are the policy's (P.finish): the BVH API
-          // computes them afterwards with its warps converged, the renderer
-          // takes the binary32 estimate of this one triangle.
-          const float4 a = __ldg(bv.tris + 3 * (size_t)best), b = __ldg(bv.tris + 3 * (size_t)best + 1),
-                       c = __ldg(bv.tris + 3 * (size_t)best + 2);
-          P.finish(ri, best, r, a, b, c, tmin_lo, tmin_hi, cmax_lo, cmax_hi, A.tMin);
+          // Only the triangle: its t, u, v are computed afterwards with the
+          // warp converged (lanes finish their rays at different steps, and
+          // work at this point stalls the warp for each lane in turn).
+          P.finish(ri, best);
         }
         active = false;
         continue;
