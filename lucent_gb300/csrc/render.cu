@@ -160,11 +160,14 @@ __device__ __forceinline__ int find_scene(const uint32_t* __restrict__ base, int
 __global__ void k_camera_multi(Paths P, const SceneRec* __restrict__ recs, const uint32_t* __restrict__ path_base,
                                int n, uint16_t* __restrict__ sid, int S) {
   const uint32_t total = __ldg(path_base + n);
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
-    const int sc = find_scene(path_base, n, k);
+  // One thread per path, in path order: the 128-byte path records are written
+  // coalesced; the queue entry and the 32-byte ray go to the path's queue
+  // position.
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+    const int sc = find_scene(path_base, n, p);
     const SceneRec& R = recs[sc];
-    const uint32_t base = __ldg(path_base + sc), WH = (uint32_t)R.W * R.H, local = k - base;
-    const uint32_t pixel = local / (uint32_t)S, s = local % (uint32_t)S, p = base + s * WH + pixel;
+    const uint32_t base = __ldg(path_base + sc), WH = (uint32_t)R.W * R.H, local = p - base;
+    const uint32_t pixel = local % WH, s = local / WH, k = base + pixel * (uint32_t)S + s;
     camera_path(P, p, k, pixel, s, R.cam, R.W, R.H, R.seed0, sc);
     sid[p] = (uint16_t)sc;
   }
@@ -711,11 +714,13 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
 
 // Adds the unoccluded next-event contributions of this bounce, per path, in
 // the reference's order (sun, environment, light).
-__global__ void k_resolve(Paths P, int cur) {
+// `all`: the queue holds every path of the wave (bounce 0, whose queue is
+// pixel-major): walk the paths in path order instead, so the reads coalesce.
+__global__ void k_resolve(Paths P, int cur, int all) {
   const uint32_t n = P.ctr[kCtrQ0 + cur];
   const uint32_t* q = P.q[cur];
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const uint32_t p = q[k];
+    const uint32_t p = all ? k : q[k];
     float4 r = P.rad[p];
     bool any = false;
     for (int j = 0; j < 3; j++) {
@@ -1215,7 +1220,7 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     // intact in sort_tmp), in path order, so its reads stay coalesced.
     Paths Pr = P;
     if (sorted) Pr.q[cur] = P.sort_tmp;
-    k_resolve<<<aux, 128, 0, t>>>(Pr, cur);
+    k_resolve<<<aux, 128, 0, t>>>(Pr, cur, b == 0);
     k_count_rays<<<1, 32, 0, t>>>(P.ctr, cur);
     if (fork) cudaEventRecord(M.ev_join, t);
     forked = fork;
@@ -1294,7 +1299,7 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
       Paths Pr = P;  // resolve walks the pre-sort queue, in path order
       if (sorted) Pr.q[cur] = P.sort_tmp;
       if (pass == 0)
-        k_resolve<<<aux, 128, 0, t>>>(Pr, cur);
+        k_resolve<<<aux, 128, 0, t>>>(Pr, cur, b == 0);
       else
         k_resolve_adjoint<<<aux, 128, 0, t>>>(Pr, A, rec, cur);
       if (fork) cudaEventRecord(M.ev_join, t);
