@@ -466,6 +466,45 @@ def cpu_build_ms():
     return out
 
 
+def env_sampler_times(local, reps=5):
+    """buildEnvSampler on the large-mesh workload's 1024 x 512 HDRI: the host
+    build (lucent_env_sampler, which upload_lighting runs) against the GPU
+    build (lucent_env_sampler_device from a device copy of the map)."""
+    import ctypes as C
+
+    import torch
+    from lucent_gb300 import _native as N
+    from lucent_gb300 import workloads as W
+    torch.cuda.set_device(local)
+    img = W.knot_scene(0, tubular=8, radial=4, env_width=1024).env.map
+    rgb = np.ascontiguousarray(img.data, np.float32)
+    L = N.lib()
+    gw, gh, tot = C.c_uint32(), C.c_uint32(), C.c_double()
+    table = np.zeros(1024 * 512 * 4, np.float32)
+    d_rgb = torch.from_numpy(rgb).cuda()
+    d_tab = torch.zeros(1024 * 512 * 4, dtype=torch.float32, device="cuda")
+
+    def host():
+        N.check(L.lucent_env_sampler(N.ptr(rgb, C.c_float), img.width, img.height, 1024, C.byref(gw), C.byref(gh),
+                                     N.ptr(table, C.c_float), C.byref(tot)))
+
+    def device():
+        N.check(L.lucent_env_sampler_device(d_rgb.data_ptr(), img.width, img.height, 1024, C.byref(gw),
+                                            C.byref(gh), d_tab.data_ptr(), C.byref(tot), None))
+
+    out = {}
+    for name, fn in (("host_ms", host), ("gpu_ms", device)):
+        fn()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        out[name] = round(1e3 * min(ts), 3)
+    out["cells"] = int(gw.value * gh.value)
+    return out
+
+
 # ----------------------------------------------------------------------------- large-mesh workload
 KNOT_W, KNOT_H, KNOT_DEPTH, KNOT_ATROUS = 1920, 1080, 12, 5
 
@@ -614,6 +653,7 @@ def run_targets(args, local):
     one warm-up, or a few samples of a frame)."""
     import types
     out = {}
+    out["env_sampler"] = env_sampler_times(local)
     t0 = time.perf_counter()
     bb = run_ours_build(types.SimpleNamespace(steps=3, warmup=1), 0, 1, local)
     out["bvh_build"] = {"gpu_ms": bb["extra"]["build_ms"], "reference_call_ms": bb["extra"]["reference_call_ms"],

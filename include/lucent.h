@@ -260,6 +260,31 @@ lucent_status lucent_renderer_upload_lighting(lucent_renderer* r, const lucent_l
  * *total (0: a black map, light sampling off). */
 lucent_status lucent_env_sampler(const float* rgb, uint32_t width, uint32_t height, uint32_t max_width, uint32_t* gw,
                                  uint32_t* gh, float* table, double* total);
+/* buildEnvSampler on the GPU from a device RGB map (width * height * 3
+ * floats, rows top to bottom): the same grid and table layout as
+ * lucent_env_sampler, written to table_d (gw * gh * 4 floats, device). The
+ * cell weights equal the reference's bit for bit; the total and the alias
+ * pairing (Vose's stack order in closed form over prefix sums of the light
+ * deficits and heavy excesses) use exact double-double scans where the
+ * reference sums left to right in binary64, so keep probabilities may differ
+ * from the host table by the reference's own rounding (about 1e-8); aliases
+ * and pdf columns match, the table reproduces the pmf (alias.test's
+ * criterion) and never draws a zero-weight cell. At most 1024 * 1024 cells. No reference counterpart (the
+ * reference builds the table on the CPU, environment.ts:52-85); for hosts
+ * whose map already lives on the device. Synchronises `stream`. */
+lucent_status lucent_env_sampler_device(const float* rgb_d, uint32_t width, uint32_t height, uint32_t max_width,
+                                        uint32_t* gw, uint32_t* gh, float* table_d, double* total, void* stream);
+/* Replaces the renderer's environment map with a device RGB map and builds
+ * its sampler on the GPU (lucent_env_sampler_device); the other lighting
+ * uniforms stay as lucent_renderer_upload_lighting set them. Resets the
+ * accumulation. For loops that change the map every step (inverse
+ * rendering): no host round trip, no host alias build. Synchronous. */
+lucent_status lucent_renderer_set_env_device(lucent_renderer* r, const float* rgb_d, uint32_t width, uint32_t height,
+                                             void* stream);
+/* Same from a host map (uploaded, sampler built on the GPU): what an
+ * optimiser keeping the map in host memory calls every step. */
+lucent_status lucent_renderer_set_env(lucent_renderer* r, const float* rgb, uint32_t width, uint32_t height,
+                                      void* stream);
 /* uploadGround (renderer.ts:415-421). */
 lucent_status lucent_renderer_upload_ground(lucent_renderer* r, int32_t enabled, float height);
 /* With temporal on and samples accumulated, the history is kept and the

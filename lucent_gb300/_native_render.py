@@ -47,6 +47,9 @@ def declare(L, sig):
     sig(L, "lucent_renderer_load_scene", [VP, P(SceneDesc)])
     sig(L, "lucent_renderer_upload_lighting", [VP, P(LightingDesc)])
     sig(L, "lucent_env_sampler", [F32P, C.c_uint32, C.c_uint32, C.c_uint32, U32P, U32P, F32P, F64P])
+    sig(L, "lucent_env_sampler_device", [VP, C.c_uint32, C.c_uint32, C.c_uint32, U32P, U32P, VP, F64P, VP])
+    sig(L, "lucent_renderer_set_env_device", [VP, VP, C.c_uint32, C.c_uint32, VP])
+    sig(L, "lucent_renderer_set_env", [VP, F32P, C.c_uint32, C.c_uint32, VP])
     sig(L, "lucent_renderer_upload_ground", [VP, C.c_int32, C.c_float])
     sig(L, "lucent_renderer_upload_camera", [VP, P(CameraDesc)])
     sig(L, "lucent_renderer_apply_settings", [VP, P(SettingsDesc)])

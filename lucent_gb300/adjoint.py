@@ -49,10 +49,11 @@ def set_materials(r: Renderer, packed):
 
 
 def set_env(r: Renderer, rgb):
-    """Replaces the environment map's texels (same size) and rebuilds its sampler."""
+    """Replaces the environment map's texels (same size); its sampler is
+    rebuilt on the GPU (lucent_renderer_set_env), not on the host."""
     env = r.scene.env.map
     env.data = np.ascontiguousarray(rgb, np.float32).reshape(-1)
-    r.upload_lighting(r.scene)
+    N.check(N.lib().lucent_renderer_set_env(r.handle, _f(env.data), env.width, env.height, None))
 
 
 def forward(r: Renderer, spp, seed, theta=None, env=None):

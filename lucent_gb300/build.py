@@ -16,8 +16,11 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liblucent_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "-I" + os.path.join(ROOT, "include")]
+# Host code restates reference arithmetic too (the environment sampler's
+# binary64 weights and alias table): no contraction into FMA on the host
+# side either, whatever the host compiler's default on the machine.
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 # Per-file extra flags. The BVH builder's binary64 arithmetic must match
 # JavaScript operation by operation, so no contraction into FMA there; the
 # denoiser and display pass keep the shaders' separate multiply and add so

@@ -36,6 +36,11 @@ int texture_array_size(const uint32_t* w, const uint32_t* h, const int32_t* laye
 lucent_status build_texture_layers(const uint8_t* const* images, const uint32_t* w, const uint32_t* h,
                                    const int32_t* layers, uint32_t n_layers, int size, bool srgb, const float* lut_d,
                                    const float* mid_d, uint8_t* out_d, cudaStream_t s);
+// buildEnvSampler on the GPU (env_sampler.cu): the sampler grid of a w x h
+// map, and the table (gw * gh float4) built from a device RGB map.
+void env_grid(uint32_t w, uint32_t h, uint32_t max_w, uint32_t& gw, uint32_t& gh);
+lucent_status gpu_env_sampler(const float* rgb_d, uint32_t w, uint32_t h, uint32_t max_w, uint32_t& gw, uint32_t& gh,
+                              float4* table_d, double& total, cudaStream_t s);
 lucent_status gpu_build_bvh(const float* pos_d, uint32_t n, int max_leaf, int bins, cudaStream_t s,
                             std::vector<float>& nodes_ref, std::vector<uint32_t>& tri_out, double bounds[6],
                             DeviceBuffer* nodes_dev, DeviceBuffer* tris_dev);

@@ -805,6 +805,47 @@ lucent_status lucent_renderer_upload_lighting(lucent_renderer* r, const lucent_l
   return lucent_renderer_reset(r);
 }
 
+// The environment map from host or device memory, its sampler built on the GPU.
+static lucent_status set_env_gpu(lucent_renderer* r, const float* rgb, bool on_device, uint32_t width,
+                                 uint32_t height, cudaStream_t s) {
+  if (!r || !rgb || width == 0 || height == 0) return fail(LUCENT_ERR_INVALID, "null argument or empty map");
+  if (!r->has_lighting) return fail(LUCENT_ERR_INVALID, "set_env before upload_lighting");
+  const size_t texels = (size_t)width * height;
+  uint32_t gw, gh;
+  env_grid(width, height, 1024, gw, gh);
+  lucent_status st = r->env_rgb.reserve(texels * 12);
+  if (!st) st = r->env_alias.reserve((size_t)gw * gh * 16);
+  if (st) return st;
+  cudaError_t e = cudaMemcpyAsync(r->env_rgb.ptr, rgb, texels * 12,
+                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "copy environment map");
+  double total = 0;
+  if ((st = gpu_env_sampler((const float*)r->env_rgb.ptr, width, height, 1024, gw, gh, (float4*)r->env_alias.ptr,
+                            total, s)))
+    return st;
+  sh::LightingDev& L = r->light;
+  L.env_rgb = (const float*)r->env_rgb.ptr;
+  L.env_w = (int)width;
+  L.env_h = (int)height;
+  L.env_alias = (const float4*)r->env_alias.ptr;
+  L.grid_w = (int)gw;
+  L.grid_h = (int)gh;
+  L.env_sampling = total > 0 ? 1 : 0;  // renderer.ts:412
+  return lucent_renderer_reset(r);
+}
+
+lucent_status lucent_renderer_set_env_device(lucent_renderer* r, const float* rgb_d, uint32_t width, uint32_t height,
+                                            void* stream) {
+  clear_error();
+  return set_env_gpu(r, rgb_d, true, width, height, (cudaStream_t)stream);
+}
+
+lucent_status lucent_renderer_set_env(lucent_renderer* r, const float* rgb, uint32_t width, uint32_t height,
+                                     void* stream) {
+  clear_error();
+  return set_env_gpu(r, rgb, false, width, height, (cudaStream_t)stream);
+}
+
 lucent_status lucent_renderer_upload_ground(lucent_renderer* r, int32_t enabled, float height) {
   clear_error();
   if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");

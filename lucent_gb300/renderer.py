@@ -252,6 +252,12 @@ class Renderer:
         adds the closest-hit traversal counters, which slow that kernel."""
         N.check(N.lib().lucent_renderer_set_profiling(self._h, (2 if counters else 1) if enabled else 0))
 
+    def set_env_device(self, rgb_ptr, width, height, stream=None):
+        """Replaces the environment map with a device RGB map (an int device
+        pointer, width * height * 3 floats) and builds its sampler on the GPU
+        (lucent_renderer_set_env_device); other lighting stays as uploaded."""
+        N.check(N.lib().lucent_renderer_set_env_device(self._h, rgb_ptr, width, height, stream))
+
     def capture_rays(self, bounces=(), max_rays=1 << 22):
         """Keep the closest-hit and shadow rays of these bounces of the next
         traces' last wave (lucent_renderer_capture_rays); () turns it off."""
