@@ -397,6 +397,20 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
     float3 ro = f3(P.ro[p]), rd = f3(P.rd[p]);
     const float4 thr4 = P.thr[p], tint4 = P.tint[p];
     float3 thr = f3(thr4), rad = f3(P.rad[p]), tint = f3(tint4);
+    // The forward render resolves the previous bounce's next-event
+    // contributions here (the backward replays keep their resolve kernels):
+    // the unoccluded ones join the radiance first, in the reference's order
+    // (sun, environment, light), as a separate resolve pass would add them.
+    unsigned pending = 0u, emitted = 0u;
+    if constexpr (!ADJ) {
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const float4 c = P.sh_c[3 * (size_t)p + j];
+        if (c.w == 0.f) continue;
+        pending |= 1u << j;
+        if (!P.sh_occ[3 * (size_t)p + j]) rad = rad + f3(c);
+      }
+    }
     float bsdf_pdf = thr4.w;
     unsigned flags = __float_as_uint(tint4.w);
     bool spec = flags & kSpecular, done = flags & kGuideDone;
@@ -641,6 +655,7 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
           const float3 cu = thr * f * NdotL * le * (w / pdf);
           const float3 c = clamp_c(cu, bounce, uclamp);
           emit_shadow(P, p, j, so, wi, tmax, st, c);
+          emitted |= 1u << j;
           if (adj) {
             nee_grad(A, L, s, wo, wi, dl, c, material, 3 * p + j);
             if (j == 1) {
@@ -696,6 +711,12 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
     }
 
     P.rad[p] = make_float4(rad.x, rad.y, rad.z, 0.f);
+    if constexpr (!ADJ) {  // resolved slots not refilled this bounce are no longer pending
+      const unsigned stale = pending & ~emitted;
+      if (stale)
+        for (int j = 0; j < 3; j++)
+          if (stale >> j & 1u) P.sh_c[3 * (size_t)p + j].w = 0.f;
+    }
     P.galb[p] = galb;
     P.gnrm[p] = gnrm;
     P.rng[p] = st;
@@ -873,6 +894,14 @@ __device__ __forceinline__ void accumulate_pixel(const Paths& P, const SceneRec&
   for (int s = 0; s < S; s++) {
     const uint32_t p = path_base + (uint32_t)s * WH + px;
     float4 c = P.rad[p];
+    // The contributions of the path's last shaded bounce, resolved here (the
+    // forward render folds resolve into the next shade and this pass).
+    for (int j = 0; j < 3; j++) {
+      const float4 e = P.sh_c[3 * (size_t)p + j];
+      if (e.w == 0.f) continue;
+      if (!P.sh_occ[3 * (size_t)p + j]) c = make_float4(c.x + e.x, c.y + e.y, c.z + e.z, c.w);
+      P.sh_c[3 * (size_t)p + j].w = 0.f;
+    }
     if (isnan(c.x) || isnan(c.y) || isnan(c.z) || isinf(c.x) || isinf(c.y) || isinf(c.z)) c = make_float4(0.f, 0.f, 0.f, 0.f);
     const float l = lum(f3(c));
     const float k = 1.f / (n + 1.f);
@@ -1216,11 +1245,8 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
                                            M.cap + (size_t)(region + 1) * M.cap_stride * 4, M.cap_count + region + 1,
                                            M.cap_stride);
     E.mark(kPhShadow, s);
-    // Resolve is per path: it walks the queue as it was before the sort (still
-    // intact in sort_tmp), in path order, so its reads stay coalesced.
-    Paths Pr = P;
-    if (sorted) Pr.q[cur] = P.sort_tmp;
-    k_resolve<<<aux, 128, 0, t>>>(Pr, cur, b == 0);
+    // No resolve launch: the next shade (or the accumulation, for paths
+    // that end here) adds this bounce's unoccluded contributions.
     k_count_rays<<<1, 32, 0, t>>>(P.ctr, cur);
     if (fork) cudaEventRecord(M.ev_join, t);
     forked = fork;
