@@ -336,9 +336,9 @@ def run_ours_pt(args, rank, world, local):
                 "peak_source": which, "kernel": "k_closest_wide_t<PathClosestMulti> (+ slow path)",
                 "bytes_per_closest_ray": alg["bytes_per_closest_ray"],
                 "closest_ms_per_frame": round(ph["closest"], 3)}
-    # camera, accumulate, seed advance; 8 per bounce (counters, closest fast + exact, shade, any-hit fast +
-    # exact, resolve, ray count); 3 per ray sort (after bounces 0 and 1)
-    launches_per_frame = 3 + 8 * (PT_DEPTH + 1) + 3 * 2
+    # Kernels launched in the timed frames, as the renderer counts them (reset + trace: camera, 7 per bounce,
+    # a counter reset per forked bounce, 3 per ray sort, accumulate, seed advance).
+    launches = s1["kernel_launches"] - s0["kernel_launches"]
     r.dispose()
     extra = {"mpaths_per_s": round(paths / dev_s / 1e6, 2), "shadow_mrays_per_s": round(shadow / dev_s / 1e6, 2),
              "closest_rays_per_frame": int(per_frame_closest),
@@ -348,7 +348,7 @@ def run_ours_pt(args, rank, world, local):
     return {
         "metric": PT_METRIC, "value": round(value, 2), "unit": "Mrays/s", "ms_per_step": round(sum(ms) / len(ms), 4),
         "wall_s": round(wall, 3), "e2e": e2e, "roofline": roof, "clocks": clk.summary(),
-        "gpu_launches": launches_per_frame * args.steps, "dtype": "f32 (+f64 exact hit decisions)",
+        "gpu_launches": int(launches), "dtype": "f32 (+f64 exact hit decisions)",
         "spp_per_s": round(spp_per_s, 2), "extra": extra,
         "config": CONFIGS["pt"],
     }
@@ -615,7 +615,8 @@ def run_ours_knot(args, rank, world, local):
                 "d2h_bytes_per_step": KNOT_W * KNOT_H * 4,
                 "includes": "trace, 5 a-trous iterations, display, RGBA8 read-back"},
         "roofline": roof, "clocks": clk.summary(),
-        "gpu_launches": None, "dtype": "f32 (+f64 exact hit decisions)", "config": CONFIGS["knot"],
+        "gpu_launches": int(s1["kernel_launches"] - s0["kernel_launches"]), "dtype": "f32 (+f64 exact hit decisions)",
+        "config": CONFIGS["knot"],
         "extra": {"closest_mrays_per_s": round(closest / dev_s / 1e6, 2), "spp_per_step": spp,
                   "frame_256spp_s_projected": round(256 / value, 3),
                   "denoise_atrous5_ms": round(float(np.median(dn)), 3),
@@ -810,10 +811,12 @@ def run_ours_batch(args, rank, world, local):
         st = b.check(sp)
         return e0.elapsed_time(e1), st
 
+    st0 = b.check(sp)
     for _ in range(args.warmup):
-        batch_step()
+        _, st0 = batch_step()
     with Clocks(local) as clk:
         bat = [batch_step() for _ in range(args.steps)]
+    launches = bat[-1][1]["kernel_launches"] - st0["kernel_launches"] if bat else 0
     bat_ms = [m for m, _ in bat]
     same = all(_image_digest(r) == d for r, d in zip(rs, digests))
     # end to end: the batched call plus every image read back to host memory
@@ -832,7 +835,7 @@ def run_ours_batch(args, rank, world, local):
         "value": round(value, 2), "unit": "Mpaths/s", "ms_per_step": round(sum(bat_ms) / len(bat_ms), 3),
         "e2e": {"value": round(paths_per_step * world / e2e_s / 1e6, 2), "unit": "Mpaths/s",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": px * 52},
-        "roofline": None, "clocks": clk.summary(), "gpu_launches": st["waves"] * (4 + 8 * (BATCH_DEPTH + 1)),
+        "roofline": None, "clocks": clk.summary(), "gpu_launches": int(launches),
         "dtype": "f32 (+f64 exact hit decisions)",
         "config": {"workload": "batch: %d scenes, %d triangles, %d pixels, %d spp, depth %d" % (
             len(rs), tris, px, BATCH_SPP, BATCH_DEPTH), "l2": "working set far above L2 (>10 GB of path state)"},

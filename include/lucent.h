@@ -245,6 +245,9 @@ typedef struct lucent_render_stats {
    * binary64 recomputations of the running closest distance, binary64 final
    * hit reports */
   uint64_t traversal[5];
+  /* kernels launched by lucent_renderer_reset and lucent_renderer_trace since
+   * creation (a replayed wave graph counts the kernels it holds) */
+  uint64_t kernel_launches;
 } lucent_render_stats;
 
 lucent_status lucent_renderer_create(uint32_t width, uint32_t height, lucent_renderer** out);
@@ -450,6 +453,7 @@ typedef struct lucent_batch_stats {
   uint64_t closest_rays, shadow_rays; /* traced by this batch since creation */
   uint32_t waves, graph_waves;        /* waves launched, of which replayed graphs */
   uint32_t wave_paths;                /* path capacity of a wave */
+  uint64_t kernel_launches;           /* kernels its traces launched (replayed graphs count theirs) */
 } lucent_batch_stats;
 /* The renderers must stay alive (and keep their scenes loaded) while the
  * batch is used; they may be traced on their own in between. */

@@ -38,7 +38,7 @@ class RenderStats(C.Structure):
     _fields_ = [("samples", C.c_uint32), ("seed", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
                 ("triangles", C.c_uint32), ("bvh_nodes", C.c_uint32), ("closest_rays", C.c_uint64),
                 ("shadow_rays", C.c_uint64), ("last_trace_ms", C.c_double), ("phase_ms", C.c_double * 6),
-                ("traversal", C.c_uint64 * 5)]
+                ("traversal", C.c_uint64 * 5), ("kernel_launches", C.c_uint64)]
 
 
 def declare(L, sig):
@@ -88,7 +88,7 @@ class BatchOptions(C.Structure):
 
 class BatchStats(C.Structure):
     _fields_ = [("closest_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("waves", C.c_uint32),
-                ("graph_waves", C.c_uint32), ("wave_paths", C.c_uint32)]
+                ("graph_waves", C.c_uint32), ("wave_paths", C.c_uint32), ("kernel_launches", C.c_uint64)]
 
 
 def declare_batch(L, sig):

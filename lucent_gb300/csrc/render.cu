@@ -1179,12 +1179,14 @@ static void launch_shadow_multi(int wide, int blocks, int top, const TravArgs& A
     k_anyhit_fast_t<PathShadowMulti><<<blocks, 256, top_smem_bytes(top), s>>>(A, ps);
 }
 
-void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
+int render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
+  int nl = 0;  // kernels launched
   Paths P = M.paths;  // queue buffers swap with the sort buffer below
   PhaseEvents none{nullptr, nullptr, 0, 0};
   PhaseEvents& E = pe ? *pe : none;
   E.mark(-1, s);
   k_camera_multi<<<grid_for(M.total_paths, 256), 256, 0, s>>>(P, M.recs, M.path_base, M.n, M.sid, M.S);
+  nl++;
   E.mark(kPhCamera, s);
   static int max_closest = 0, max_wide = 0, max_shade = 0;
   if (!max_closest) {
@@ -1204,25 +1206,30 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
       k_zero_closest_counters<<<1, 32, 0, s>>>(P.ctr);
     else
       k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
+    nl++;
     E.mark(kPhResolve, s);
     PathClosestMulti pc{P.ctr + kCtrQ0 + cur, sorted ? P.sray : P.nray, P.rng, P.hit, M.recs, M.any_alpha};
     TravArgs A{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
                M.trav_stats, top};
     launch_closest_multi(M.wide, closest_blocks, top, A, pc, s);
     k_closest_exact_t<PathClosestMulti><<<64, 128, 0, s>>>(A, pc);
+    nl += 2;
     const bool capture = M.cap && (M.cap_mask >> b & 1u);
     const uint32_t region = capture ? 2u * (uint32_t)__builtin_popcount(M.cap_mask & ((1u << b) - 1u)) : 0u;
     if (capture)
       k_capture_closest<<<aux, 256, 0, s>>>(P.ctr + kCtrQ0 + cur, pc.rays, P.hit, P.rng, M.recs,
                                             M.cap + (size_t)region * M.cap_stride * 4, M.cap_count + region,
                                             M.cap_stride);
+    nl += capture;
     E.mark(kPhClosest, s);
     if (forked) {  // join: the previous bounce's radiance is resolved before this bounce shades
       cudaStreamWaitEvent(s, M.ev_join, 0);
       k_zero_shade_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
+      nl++;
     }
     k_shade_t<SceneTable><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b);
     if (M.any_tex) k_shade_t<SceneTable, false, true><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b);
+    nl += 1 + (M.any_tex != 0);
     E.mark(kPhShade, s);
     // This bounce's shadow rays and resolve do not depend on the next bounce's
     // ray sort and closest hit, nor they on them: they run side by side on two
@@ -1240,20 +1247,24 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
                nullptr, top};
     launch_shadow_multi(M.wide, aux * 2, top, B, ps, t);
     k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, t>>>(B, ps);
+    nl += 2;
     if (capture)
       k_capture_shadow<<<aux, 256, 0, t>>>(P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ,
                                            M.cap + (size_t)(region + 1) * M.cap_stride * 4, M.cap_count + region + 1,
                                            M.cap_stride);
+    nl += capture;
     E.mark(kPhShadow, s);
     // No resolve launch: the next shade (or the accumulation, for paths
     // that end here) adds this bounce's unoccluded contributions.
     k_count_rays<<<1, 32, 0, t>>>(P.ctr, cur);
+    nl++;
     if (fork) cudaEventRecord(M.ev_join, t);
     forked = fork;
     const bool was_sorted = sorted;
     // The two largest queues; the third too in waves of 2^21 paths or more
     // (measured: it pays for its sort there, not in smaller waves).
     sorted = M.sort_rays && b < M.max_bounces && (b < 2 || (b == 2 && M.total_paths >= (1u << 21)));
+    nl += sorted ? 3 : 0;  // keys, scan, scatter
     if (sorted && was_sorted) {
       // This bounce's resolve (perhaps still running on the side stream) reads
       // its pre-sort queue in sort_tmp; its sorted queue buffer is free once
@@ -1270,6 +1281,7 @@ void render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
   k_accumulate_multi<<<grid_for(M.total_pixels, 256), 256, 0, s>>>(P, M.recs, M.pix_base, M.path_base, M.n, M.S);
   k_advance_seeds<<<1, 64, 0, s>>>(M.recs, M.n, M.S);
   E.mark(kPhAccumulate, s);
+  return nl + 2;
 }
 
 // ------------------------------------------------------------ path replay backpropagation

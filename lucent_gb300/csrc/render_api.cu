@@ -182,6 +182,7 @@ struct WaveGraph {
   cudaGraphExec_t exec = nullptr;
   uint64_t key[4] = {0, 0, 0, 0};
   cudaStream_t cap = nullptr;
+  int launches = 0;  // kernels in the captured wave
   void drop() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -201,7 +202,7 @@ struct WaveGraph {
         return cuda_fail(e, "capture stream");
       if ((e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
         return cuda_fail(e, "begin capture");
-      render_wave_multi(M, cap);
+      launches = render_wave_multi(M, cap);
       e = cudaStreamEndCapture(cap, &graph);
       if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
       if (e != cudaSuccess) {
@@ -304,6 +305,7 @@ struct lucent_renderer {
   WaveGraph wave_graph;  // full waves of a trace replay a captured graph (not while profiling)
   SideStream side;       // second stream of the waves
   uint32_t waves = 0;
+  uint64_t kernel_launches = 0;  // by reset and trace (lucent_render_stats)
   int sort_rays = 1;   // sort the rays of bounces 1 and 2 (lucent_renderer_set_ray_sort)
   int top_levels = 1;  // top BVH levels in shared memory (lucent_renderer_set_top_levels)
   int wide_bvh = 1;    // four-wide closest-hit traversal (lucent_renderer_set_wide_bvh)
@@ -895,6 +897,7 @@ lucent_status lucent_renderer_reset(lucent_renderer* r) {
   if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
   const uint32_t n = r->W * r->H;
   k_clear_accum<<<grid_for(n, 256), 256>>>(accum_of(r), n);
+  r->kernel_launches++;
   r->frame = 0;
   r->denoised = nullptr;
   r->has_history = r->reproject_pending = false;
@@ -935,8 +938,9 @@ lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* 
     // capture launch directly.
     if (w < full && !r->profiling && !r->cap_mask && r->waves > 0) {
       if ((st = r->wave_graph.run(M, key, s))) return st;
+      r->kernel_launches += r->wave_graph.launches;
     } else {
-      render_wave_multi(M, s, r->profiling ? &pe : nullptr);  // seeds advance on the device
+      r->kernel_launches += render_wave_multi(M, s, r->profiling ? &pe : nullptr);  // seeds advance on the device
     }
     r->waves++;
   }
@@ -1250,6 +1254,7 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
     out->shadow_rays = c[1];
   }
   out->last_trace_ms = r->last_ms;
+  out->kernel_launches = r->kernel_launches;
   for (int k = 0; k < kPhases; k++) out->phase_ms[k] = r->phase_ms[k];
   if (r->ctr.ptr) {
     cudaError_t e = cudaMemcpy(out->traversal, (uint32_t*)r->ctr.ptr + kCtrTrav, 40, cudaMemcpyDeviceToHost);
@@ -1276,6 +1281,7 @@ struct lucent_batch {
   std::vector<lucent_batch*> parts;
   std::vector<SideStream> part_streams;  // stream + done event per part (fork: part_streams[0].fork)
   uint32_t waves = 0, graph_waves = 0;
+  uint64_t kernel_launches = 0;  // by its traces (lucent_batch_stats)
   void drop_graphs() {
     for (WaveGraph& g : graphs) g.drop();
   }
@@ -1494,14 +1500,15 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
         const lucent_status gst = b->graphs[g].run(M, key, s);
         if (gst) return gst;
         b->graph_waves++;
+        b->kernel_launches += b->graphs[g].launches;
       } else {
-        render_wave_multi(M, s);
+        b->kernel_launches += render_wave_multi(M, s);
       }
       b->waves++;
     }
     if (G.tail) {
       setup(G.tail, G.base + 2 * (ng + 1));
-      render_wave_multi(M, s);
+      b->kernel_launches += render_wave_multi(M, s);
       b->waves++;
     }
   }
@@ -1529,6 +1536,7 @@ lucent_status lucent_batch_check(lucent_batch* b, void* stream, lucent_batch_sta
     acc.waves += ps.waves;
     acc.graph_waves += ps.graph_waves;
     acc.wave_paths += ps.wave_paths;
+    acc.kernel_launches += ps.kernel_launches;
   }
   if (out) *out = acc;
   if (!b->ctr.ptr) return LUCENT_OK;
@@ -1544,6 +1552,7 @@ lucent_status lucent_batch_check(lucent_batch* b, void* stream, lucent_batch_sta
     out->waves += b->waves;
     out->graph_waves += b->graph_waves;
     out->wave_paths += b->path_cap;
+    out->kernel_launches += b->kernel_launches;
   }
   if (words[kCtrErr]) {
     clear_now((uint32_t*)b->ctr.ptr + kCtrErr, 4);

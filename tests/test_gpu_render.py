@@ -181,6 +181,29 @@ def test_graph_replay_changes_no_pixel():
     assert all(np.array_equal(a, b) for a, b in zip(*out))
 
 
+def test_kernel_launch_count():
+    # lucent_render_stats.kernel_launches: a wave launches the camera kernel,
+    # 7 kernels a bounce, a shade-counter reset for each bounce after the
+    # first (the previous bounce's shadow rays run on the second stream), 3
+    # per ray sort (after bounces 0 and 1 in waves under 2^21 paths), the
+    # accumulation and the seed advance; a replayed graph counts as many;
+    # reset launches one.
+    r = Renderer(32, 32)
+    r.settings.max_bounces = 3
+    r.load_scene(W.box_scene(1, 3))
+    wave = 1 + 7 * 4 + 3 + 3 * 2 + 2
+    base = r.stats()["kernel_launches"]
+    counts = []
+    for _ in range(3):  # the first wave runs directly, the others replay its graph
+        r.trace_samples(1)
+        counts.append(r.stats()["kernel_launches"] - base)
+    r.reset()
+    after = r.stats()["kernel_launches"] - base
+    r.dispose()
+    assert counts == [wave, 2 * wave, 3 * wave]
+    assert after == 3 * wave + 1
+
+
 def test_views_share_the_scene_and_render_the_same_images():
     # A view renders its source's scene from its own camera with the scene's
     # device data shared: the image equals a renderer that loaded its own copy.
