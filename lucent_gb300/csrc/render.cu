@@ -94,7 +94,7 @@ struct PathShadowMulti {
     const SceneDev& S = recs[sc].scene;
     return {S.nodes, S.geo, S.node_count, sc, S.wide};
   }
-  __device__ double tmax(uint32_t k) const { return (double)so[k].w; }
+  __device__ float tmax32(uint32_t k) const { return so[k].w; }
   __device__ uint32_t key(uint32_t k) const { return __float_as_uint(sd[k].w); }
   __device__ bool alpha_any() const { return any_alpha != 0; }
   __device__ bool alpha(int sc, int slot, uint32_t key, float bu, float bv) const {
@@ -366,8 +366,10 @@ static __device__ __forceinline__ float4 hit_values(const float4* __restrict__ g
   const Ray32 r = make_ray32(ro, rd);
   float tl, th;
   float3 est;
-  if (mt_classify(r, a, b, c, __double2float_rd(1e-6), __double2float_ru(1e-6), __double2float_rd(1e30),
-                  __double2float_ru(1e30), tl, th, est) == kTriAccept)
+  // tMin = 1e-6 and tMax = 1e30 (binary64) rounded down and up to binary32.
+  const float tmin_lo = __int_as_float(0x358637bd), tmin_hi = __int_as_float(0x358637be);
+  const float cmax_lo = __int_as_float(0x7149f2c9), cmax_hi = __int_as_float(0x7149f2ca);
+  if (mt_classify(r, a, b, c, tmin_lo, tmin_hi, cmax_lo, cmax_hi, tl, th, est) == kTriAccept)
     return make_float4(est.x, est.y, est.z, __int_as_float(slot));
   const Tri64 h = tri_f64(ro, rd, a, b, c, 1e-6, __longlong_as_double(0x7ff0000000000000ll));
   return make_float4(__double2float_rn(h.t), __double2float_rn(h.u), __double2float_rn(h.v), __int_as_float(slot));

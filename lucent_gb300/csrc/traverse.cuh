@@ -31,6 +31,7 @@
 //                                                 to compute later, with the warp converged
 //   void hit(uint32_t k, int slot, double t, double u, double v)   a hit with its binary64 values
 //   void miss(uint32_t k); void fail(uint32_t k)
+//   float tmax32(uint32_t k) const                (any hit) the ray's tMax, a binary32 value
 //   void shadow(uint32_t k, bool occluded)        (any hit)
 #pragma once
 #include "closest_hit.cuh"
@@ -471,7 +472,7 @@ __device__ bool any_exact(const TravArgs& A, const Pol& P, const BvhView& bv, D3
   return false;
 }
 
-// Any-hit rays carry their own tMax: P.tmax(k).
+// Any-hit rays carry their own tMax: P.tmax32(k).
 template <class Pol>
 __global__ void k_anyhit_exact_t(TravArgs A, Pol P) {
   const uint32_t limit = *A.queue_len;
@@ -480,7 +481,7 @@ __global__ void k_anyhit_exact_t(TravArgs A, Pol P) {
     float3 o, d;
     P.ray(k, o, d);
     bool ok;
-    const bool occ = any_exact(A, P, bvh_of(A, P, k), {o.x, o.y, o.z}, {d.x, d.y, d.z}, P.key(k), P.tmax(k), ok);
+    const bool occ = any_exact(A, P, bvh_of(A, P, k), {o.x, o.y, o.z}, {d.x, d.y, d.z}, P.key(k), (double)P.tmax32(k), ok);
     P.shadow(k, ok ? occ : true);
   }
 }
@@ -505,9 +506,9 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
     }
     const Ray32 r = make_ray32(o, d);
     const uint32_t key = P.key(k);
-    const double tmax = P.tmax(k);
+    const float tmax32 = P.tmax32(k);  // binary32, so its bounds are itself
     const BvhView bv = bvh_of(A, P, k);
-    const float c_lo = __double2float_rd(tmax), c_hi = __double2float_ru(tmax);
+    const float c_lo = tmax32, c_hi = tmax32;
     const Node* sb = bv.scene < A.top_scenes ? s_top + bv.scene * kTopNodes : nullptr;
     int stack[kTsStack];  // node index, or -b for treelet node b
     int sp = 0;
@@ -523,7 +524,7 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
       const int e = stack[--sp];
       const Node nd = e < 0 ? sb[-e - 1] : load_node(bv.nodes, e);
       SlabClass cl = classify_slab(r, nd.lo, nd.hi, c_lo, c_hi);
-      if (cl == kAmbiguous) cl = ts_slab_culled(nd.lo, nd.hi, {o.x, o.y, o.z}, inv_exact(d), tmax) ? kCulled : kPass;
+      if (cl == kAmbiguous) cl = ts_slab_culled(nd.lo, nd.hi, {o.x, o.y, o.z}, inv_exact(d), (double)tmax32) ? kCulled : kPass;
       if (cl == kCulled) continue;
       const int cnt = node_count(nd), first = node_first(nd);
       if (cnt > 0) {
@@ -547,7 +548,7 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_fast_t(TravArgs A, Pol P) {
             occ = true;
           } else {
             double t, u, v;
-            occ = ts_triangle({o.x, o.y, o.z}, {d.x, d.y, d.z}, d3f(a), d3f(b), d3f(c), A.tMin, tmax, t, u, v);
+            occ = ts_triangle({o.x, o.y, o.z}, {d.x, d.y, d.z}, d3f(a), d3f(b), d3f(c), A.tMin, (double)tmax32, t, u, v);
           }
         }
       } else {

@@ -290,13 +290,13 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_wide_t(TravArgs A, Pol P) {
     }
     const Ray32 r = make_ray32(o, d);
     const uint32_t key = P.key(k);
-    const double tmax = P.tmax(k);
+    const float tmax32 = P.tmax32(k);  // binary32, so its bounds are itself
     BvhView bv = bvh_of(A, P, k);
     if constexpr (!Pol::kMultiScene) bv.wide = A.wide;
-    const float c_lo = __double2float_rd(tmax), c_hi = __double2float_ru(tmax);
+    const float c_lo = tmax32, c_hi = tmax32;
     auto passes = [&](const Node& nd) {
       SlabClass cl = classify_slab(r, nd.lo, nd.hi, c_lo, c_hi);
-      if (cl == kAmbiguous) cl = ts_slab_culled(nd.lo, nd.hi, {o.x, o.y, o.z}, inv_exact(d), tmax) ? kCulled : kPass;
+      if (cl == kAmbiguous) cl = ts_slab_culled(nd.lo, nd.hi, {o.x, o.y, o.z}, inv_exact(d), (double)tmax32) ? kCulled : kPass;
       return cl == kPass;
     };
     int stack[kWideStack];  // indices of records that passed their box test
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(256, 4) k_anyhit_wide_t(TravArgs A, Pol P) {
             occ = true;
           } else {
             double t, u, v;
-            occ = ts_triangle({o.x, o.y, o.z}, {d.x, d.y, d.z}, d3f(a), d3f(b), d3f(c), A.tMin, tmax, t, u, v);
+            occ = ts_triangle({o.x, o.y, o.z}, {d.x, d.y, d.z}, d3f(a), d3f(b), d3f(c), A.tMin, (double)tmax32, t, u, v);
           }
         }
         if (occ || defer) break;
