@@ -151,9 +151,11 @@ LUCENT_DEV bool mt_candidate(const Ray32& r, float4 a, float4 b, float4 c3, floa
 // (src/math/ray.ts:22-45) with tMin and the running closest c in [c_lo, c_hi]:
 //   kTriReject  the reference certainly rejects,
 //   kTriAccept  the reference certainly accepts; [t_lo, t_hi] bounds its t,
-//   kTriExact   undecided: recompute in binary64.
+//   kTriExact   undecided: recompute in binary64,
+//   kTriNearC   every condition certain but t < c: the reference accepts the
+//               triangle iff its binary64 t is below c; [t_lo, t_hi] bounds t.
 // Numerator bounds as in mt_candidate (2^-19 x absolute-value evaluation).
-enum TriClass { kTriReject = 0, kTriAccept = 1, kTriExact = 2 };
+enum TriClass { kTriReject = 0, kTriAccept = 1, kTriExact = 2, kTriNearC = 3 };
 
 LUCENT_DEV TriClass mt_classify(const Ray32& r, float4 a, float4 b, float4 c3, float tmin_lo, float tmin_hi,
                                 float c_lo, float c_hi, float& t_lo, float& t_hi, float3& est) {
@@ -189,12 +191,12 @@ LUCENT_DEV TriClass mt_classify(const Ray32& r, float4 a, float4 b, float4 c3, f
   if (Ta - eT >= c_hi * Ahi * 1.00000095f) return kTriReject;                       // t >= closest
   // Certain acceptance: every reference condition holds with margin.
   const bool inside = Ua - eU >= 0.f && Va - eV >= 0.f && Ua + Va + (eU + eV) <= Alo && Alo >= 1.0000001e-12f;
-  const bool t_ok = Ta - eT > tmin_hi * Ahi * 1.00000095f && Ta + eT < c_lo * Alo * 0.99999905f;
-  if (!(inside && t_ok)) return kTriExact;
+  if (!(inside && Ta - eT > tmin_hi * Ahi * 1.00000095f)) return kTriExact;
   // t = T/det lies in [(Ta-eT)/Ahi, (Ta+eT)/Alo]; round outward and widen by
   // one more ulp for the reference's own binary64 rounding.
   t_lo = __fmul_rd(__fdiv_rd(__fsub_rd(Ta, eT), Ahi), 0.99999994f);
   t_hi = __fmul_ru(__fdiv_ru(__fadd_ru(Ta, eT), Alo), 1.00000012f);
+  if (!(Ta + eT < c_lo * Alo * 0.99999905f)) return kTriNearC;
   // Binary32 estimates of (t, u, v), as the GLSL's own hitTriangle computes them.
   const float inv = 1.f / det;
   est = make_float3(T * inv, U * inv, V * inv);

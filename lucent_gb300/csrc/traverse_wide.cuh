@@ -98,7 +98,10 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
   Ray32 r;
   float c_lo = 0.f, c_hi = 0.f;
   double c64 = A.tMax;  // binary64 t of `best` when c_exact
-  int best = -1, sp = 0;
+  // pend: a triangle met at a distance tied with c within the binary32
+  // bounds (kTriNearC), not yet compared in binary64; [c_lo, c_hi] then
+  // spans both candidates' distances.
+  int best = -1, pend = -1, sp = 0;
   BvhView bv{A.nodes, A.tris, A.node_limit, 0, A.wide};
   Node cur;
   WidePending stack[kWideStack];
@@ -129,6 +132,7 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
             c64 = A.tMax;
             c_exact = true;
             best = -1;
+            pend = -1;
             sp = 0;
             iters = 0;
             count_stat(A, 0);
@@ -158,6 +162,19 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
         c_lo = __double2float_rd(h.t);
         c_hi = __double2float_ru(h.t);
       }
+      if (pend >= 0) {  // the deferred tie: the reference took it iff its binary64 t is below c
+        count_stat(A, 2);
+        const float4 a = __ldg(bv.tris + 3 * (size_t)pend), b = __ldg(bv.tris + 3 * (size_t)pend + 1),
+                     c = __ldg(bv.tris + 3 * (size_t)pend + 2);
+        const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, c64);
+        if (h.hit) {
+          best = pend;
+          c64 = h.t;
+        }
+        pend = -1;
+        c_lo = __double2float_rd(c64);
+        c_hi = __double2float_ru(c64);
+      }
       return c64;
     };
     auto slab_decide = [&](const Node& nd, SlabClass cl) {
@@ -168,6 +185,7 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
 
     if (!have_cur) {
       if (sp == 0) {  // finished
+        if (pend >= 0) exact_c();
         if (best < 0) {
           P.miss(ri);
         } else {
@@ -213,9 +231,16 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
         }
         if (tc == kTriAccept) {
           best = slot;
+          pend = -1;
           c_exact = false;
           c_lo = tl;
           c_hi = th;
+          continue;
+        }
+        if (tc == kTriNearC && pend < 0) {  // defer: a later certain hit below both makes it moot
+          pend = slot;
+          c_lo = fminf(c_lo, tl);
+          c_hi = fmaxf(c_hi, th);
           continue;
         }
         count_stat(A, 2);
