@@ -79,9 +79,55 @@ struct WidePending {
   float ehi;  // upper bound on its entry distance when it was pushed
 };
 
+// The running closest of a closest-hit ray: the reference's binary64
+// `closest` lies in [lo, hi]; `exact`: c64 is the binary64 t of `best`;
+// `pend`: a triangle met at a distance tied with it within the binary32
+// bounds (kTriNearC), not yet compared in binary64, [lo, hi] then spanning
+// both candidates' distances.
+struct Closest {
+  double c64;
+  float lo, hi;
+  int best, pend;
+  int exact;
+};
+
+// The reference's binary64 `closest`, for the decisions the binary32 bounds
+// leave open: the binary64 t of `best` if not yet known, then the deferred
+// tie resolved as the reference's test resolves it (taken iff its binary64
+// t is below). Out of line, one copy for every such decision of the kernel.
+static __device__ __noinline__ Closest closest_exact(Closest s, float3 o, float3 d, const float4* __restrict__ tris,
+                                                     double tmin, unsigned long long* stats) {
+  const D3 O{o.x, o.y, o.z}, Dd{d.x, d.y, d.z};
+  double t, u, v;
+  if (!s.exact) {
+    if (stats) atomicAdd(stats + 3, 1ull);
+    const float4* g = tris + 3 * (size_t)s.best;
+    ts_triangle(O, Dd, d3f(__ldg(g)), d3f(__ldg(g + 1)), d3f(__ldg(g + 2)), tmin,
+                __longlong_as_double(0x7ff0000000000000ll), t, u, v);
+    s.c64 = t;
+    s.exact = 1;
+  }
+  if (s.pend >= 0) {
+    if (stats) atomicAdd(stats + 2, 1ull);
+    const float4* g = tris + 3 * (size_t)s.pend;
+    if (ts_triangle(O, Dd, d3f(__ldg(g)), d3f(__ldg(g + 1)), d3f(__ldg(g + 2)), tmin, s.c64, t, u, v)) {
+      s.best = s.pend;
+      s.c64 = t;
+    }
+    s.pend = -1;
+  }
+  s.lo = __double2float_rd(s.c64);
+  s.hi = __double2float_ru(s.c64);
+  return s;
+}
+
 // Closest hit over the wide view: k_closest_fast_t's persistent warps, per-lane
 // refill, bounded-error binary32 decisions and binary64 fallbacks, with each
-// inner step expanding four records (bv.wide must be set).
+// inner step expanding four records (bv.wide must be set). Two deferrals keep
+// binary64 off the common path: a distance tie (Closest::pend), and a leaf
+// whose own slab test the binary32 bounds leave open (`cond`), which is
+// visited and decided in binary64 only if one of its triangles is not
+// certainly rejected (otherwise the leaf changes nothing either way).
 template <class Pol>
 __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide_t(TravArgs A, Pol P) {
   const unsigned FULL = 0xffffffffu;
@@ -89,19 +135,15 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
   const unsigned lt = (1u << lane) - 1u;
   const float tmin_lo = __double2float_rd(A.tMin), tmin_hi = __double2float_ru(A.tMin);
   const float cmax_lo = __double2float_rd(A.tMax), cmax_hi = __double2float_ru(A.tMax);
-  const double INF64 = __longlong_as_double(0x7ff0000000000000ll);
+  const float INF32 = __int_as_float(0x7f800000);
   const uint32_t n = P.count();
   const bool use_alpha = P.alpha_any();
 
-  bool active = false, exhausted = false, have_cur = false, c_exact = true;
+  bool active = false, exhausted = false, have_cur = false, cond = false;
   uint32_t ri = 0, iters = 0, key = 0;
   Ray32 r;
-  float c_lo = 0.f, c_hi = 0.f;
-  double c64 = A.tMax;  // binary64 t of `best` when c_exact
-  // pend: a triangle met at a distance tied with c within the binary32
-  // bounds (kTriNearC), not yet compared in binary64; [c_lo, c_hi] then
-  // spans both candidates' distances.
-  int best = -1, pend = -1, sp = 0;
+  Closest S{A.tMax, 0.f, 0.f, -1, -1, 1};
+  int sp = 0;
   BvhView bv{A.nodes, A.tris, A.node_limit, 0, A.wide};
   Node cur;
   WidePending stack[kWideStack];
@@ -127,20 +169,16 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
             r = make_ray32(o, d);
             key = P.key(ri);
             if constexpr (Pol::kMultiScene) bv = P.bvh(ri);
-            c_lo = cmax_lo;
-            c_hi = cmax_hi;
-            c64 = A.tMax;
-            c_exact = true;
-            best = -1;
-            pend = -1;
+            S = Closest{A.tMax, cmax_lo, cmax_hi, -1, -1, 1};
+            cond = false;
             sp = 0;
             iters = 0;
             count_stat(A, 0);
             cur = wide_record(bv.nodes, 0);  // the reference pops the root first and tests its box
-            SlabClass cl = classify_slab(r, cur.lo, cur.hi, c_lo, c_hi);
+            SlabClass cl = classify_slab(r, cur.lo, cur.hi, S.lo, S.hi);
             if (cl == kAmbiguous) {
               count_stat(A, 1);
-              cl = slab_f64_culled(cur.lo, cur.hi, o, d, c64) ? kCulled : kPass;
+              cl = slab_f64_culled(cur.lo, cur.hi, o, d, A.tMax) ? kCulled : kPass;
             }
             have_cur = cl != kCulled;
             active = true;
@@ -152,54 +190,39 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
     if (!active) continue;
 
     auto exact_c = [&]() {  // the reference's binary64 `closest`, on demand
-      if (!c_exact) {
-        count_stat(A, 3);
-        const float4 a = __ldg(bv.tris + 3 * (size_t)best), b = __ldg(bv.tris + 3 * (size_t)best + 1),
-                     c = __ldg(bv.tris + 3 * (size_t)best + 2);
-        const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, INF64);
-        c64 = h.t;
-        c_exact = true;
-        c_lo = __double2float_rd(h.t);
-        c_hi = __double2float_ru(h.t);
-      }
-      if (pend >= 0) {  // the deferred tie: the reference took it iff its binary64 t is below c
-        count_stat(A, 2);
-        const float4 a = __ldg(bv.tris + 3 * (size_t)pend), b = __ldg(bv.tris + 3 * (size_t)pend + 1),
-                     c = __ldg(bv.tris + 3 * (size_t)pend + 2);
-        const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, c64);
-        if (h.hit) {
-          best = pend;
-          c64 = h.t;
-        }
-        pend = -1;
-        c_lo = __double2float_rd(c64);
-        c_hi = __double2float_ru(c64);
-      }
-      return c64;
-    };
-    auto slab_decide = [&](const Node& nd, SlabClass cl) {
-      if (cl != kAmbiguous) return cl;
-      count_stat(A, 1);
-      return slab_f64_culled(nd.lo, nd.hi, r.o, r.d, exact_c()) ? kCulled : kPass;
+      if (!S.exact || S.pend >= 0) S = closest_exact(S, r.o, r.d, bv.tris, A.tMin, A.stats);
+      return S.c64;
     };
 
     if (!have_cur) {
       if (sp == 0) {  // finished
-        if (pend >= 0) exact_c();
-        if (best < 0) {
+        if (S.pend >= 0) exact_c();
+        if (S.best < 0) {
           P.miss(ri);
         } else {
           // Only the triangle: its t, u, v are computed afterwards with the
           // warp converged (lanes finish their rays at different steps, and
           // work at this point stalls the warp for each lane in turn).
-          P.finish(ri, best);
+          P.finish(ri, S.best);
         }
         active = false;
         continue;
       }
       const WidePending e = stack[--sp];
       const Node nd = load_node(bv.wide, e.rec);
-      if (e.ehi > c_lo && slab_decide(nd, classify_slab(r, nd.lo, nd.hi, c_lo, c_hi)) == kCulled) continue;
+      cond = false;
+      if (e.ehi > S.lo) {  // open leaves were pushed with ehi = inf: always re-tested
+        const SlabClass cl = classify_slab(r, nd.lo, nd.hi, S.lo, S.hi);
+        if (cl == kCulled) continue;
+        if (cl == kAmbiguous) {
+          if (node_count(nd) > 0) {
+            cond = true;
+          } else {
+            count_stat(A, 1);
+            if (slab_f64_culled(nd.lo, nd.hi, r.o, r.d, exact_c())) continue;
+          }
+        }
+      }
       cur = nd;
       have_cur = true;
     }
@@ -219,8 +242,13 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
                      c = __ldg(bv.tris + 3 * (size_t)slot + 2);
         float tl, th;
         float3 est;
-        const TriClass tc = mt_classify(r, a, b, c, tmin_lo, tmin_hi, c_lo, c_hi, tl, th, est);
+        const TriClass tc = mt_classify(r, a, b, c, tmin_lo, tmin_hi, S.lo, S.hi, tl, th, est);
         if (tc == kTriReject) continue;
+        if (cond) {  // this triangle may count: first the leaf's own test, as the reference made it
+          cond = false;
+          count_stat(A, 1);
+          if (slab_f64_culled(cur.lo, cur.hi, r.o, r.d, exact_c())) break;
+        }
         if (use_alpha) {
           const AlphaAnswer aa = P.alpha_fast(bv.scene, slot, key);
           if (aa == kAlphaDefer) {
@@ -230,28 +258,27 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
           if (aa == kAlphaPass) continue;
         }
         if (tc == kTriAccept) {
-          best = slot;
-          pend = -1;
-          c_exact = false;
-          c_lo = tl;
-          c_hi = th;
+          S.best = slot;
+          S.pend = -1;
+          S.exact = 0;
+          S.lo = tl;
+          S.hi = th;
           continue;
         }
-        if (tc == kTriNearC && pend < 0) {  // defer: a later certain hit below both makes it moot
-          pend = slot;
-          c_lo = fminf(c_lo, tl);
-          c_hi = fmaxf(c_hi, th);
+        if (tc == kTriNearC && S.pend < 0) {  // defer: a later certain hit below both makes it moot
+          S.pend = slot;
+          S.lo = fminf(S.lo, tl);
+          S.hi = fmaxf(S.hi, th);
           continue;
         }
         count_stat(A, 2);
         const double cc = exact_c();
         const Tri64 h = tri_f64(r.o, r.d, a, b, c, A.tMin, cc);
         if (h.hit) {
-          best = slot;
-          c64 = h.t;
-          c_exact = true;
-            c_lo = __double2float_rd(h.t);
-          c_hi = __double2float_ru(h.t);
+          S.best = slot;
+          S.c64 = h.t;
+          S.lo = __double2float_rd(h.t);
+          S.hi = __double2float_ru(h.t);
         }
       }
       have_cur = false;
@@ -261,26 +288,44 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
         continue;
       }
     } else {
-      // Expand: the four records of `cur`, last to first, so that the first
-      // that passes continues and the others are pushed in reverse order.
+      // Expand the four records of `cur`: binary32 tests of all four, then
+      // binary64 for inner records they leave open (one place in the code),
+      // then, as the reference's order has it, the first passing record
+      // continues and the others are pushed in reverse order. A leaf left
+      // open passes conditionally (`cond`).
       const int base = kWide * first;
-      int pend = -1;
-      float pend_ehi = 0.f;
-      Node next;
+      unsigned pass = 0, open_leaf = 0, open_inner = 0;
+      float eh[kWide];
+#pragma unroll
+      for (int k = 0; k < kWide; k++) {
+        const Node s = load_node(bv.wide, base + k);
+        eh[k] = 0.f;
+        if (node_count(s) < 0) continue;
+        const SlabClass cl = classify_slab_e(r, s.lo, s.hi, S.lo, S.hi, eh[k]);
+        if (cl == kPass) pass |= 1u << k;
+        else if (cl == kAmbiguous) (node_count(s) > 0 ? open_leaf : open_inner) |= 1u << k;
+      }
+      if (open_inner) {
+        const double cc = exact_c();
+        for (int k = 0; k < kWide; k++) {
+          if (!(open_inner >> k & 1u)) continue;
+          count_stat(A, 1);
+          const Node s = load_node(bv.wide, base + k);
+          if (!slab_f64_culled(s.lo, s.hi, r.o, r.d, cc)) pass |= 1u << k;
+        }
+      }
+      pass |= open_leaf;
+      if (!pass) {
+        have_cur = false;
+        continue;
+      }
+      const int go = __ffs(pass) - 1;
       bool overflow = false;
 #pragma unroll
-      for (int k = kWide - 1; k >= 0; k--) {
-        const Node s = load_node(bv.wide, base + k);
-        if (node_count(s) < 0) continue;
-        float eh;
-        if (slab_decide(s, classify_slab_e(r, s.lo, s.hi, c_lo, c_hi, eh)) != kPass) continue;
-        if (pend >= 0) {
-          if (sp >= kWideStack) overflow = true;
-          else stack[sp++] = {base + pend, pend_ehi};
-        }
-        pend = k;
-        pend_ehi = eh;
-        next = s;
+      for (int k = kWide - 1; k > 0; k--) {
+        if (k <= go || !(pass >> k & 1u)) continue;
+        if (sp >= kWideStack) overflow = true;
+        else stack[sp++] = {base + k, (open_leaf >> k & 1u) ? INF32 : eh[k]};
       }
       if (overflow) {  // unreachable for trees the reference's stack can traverse
         atomicOr(A.err, kErrStack);
@@ -289,11 +334,12 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
         have_cur = false;
         continue;
       }
-      if (pend >= 0) cur = next;
-      else have_cur = false;
+      cur = load_node(bv.wide, base + go);
+      cond = open_leaf >> go & 1u;
     }
   }
 }
+
 
 // Any hit over the wide view: one ray per thread (grid-stride), as
 // k_anyhit_fast_t. With the cull distance fixed at tMax the answer does not
