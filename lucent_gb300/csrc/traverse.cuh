@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_fast
             A.queue[atomicAdd(A.queue_len, 1u)] = ri;
           } else {
             r = make_ray32(o, d);
-            key = P.key(ri);
+            key = use_alpha ? P.key(ri) : 0u;  // read only where alpha tests use it
             if constexpr (Pol::kMultiScene) bv = P.bvh(ri);
             c_lo = cmax_lo;
             c_hi = cmax_hi;

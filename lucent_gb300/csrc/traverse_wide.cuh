@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
             A.queue[atomicAdd(A.queue_len, 1u)] = ri;
           } else {
             r = make_ray32(o, d);
-            key = P.key(ri);
+            key = use_alpha ? P.key(ri) : 0u;  // read only where alpha tests use it
             if constexpr (Pol::kMultiScene) bv = P.bvh(ri);
             S = Closest{A.tMax, cmax_lo, cmax_hi, -1, -1, 1};
             cond = false;
