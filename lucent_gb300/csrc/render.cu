@@ -38,7 +38,7 @@ using namespace sh;
 struct PathClosestMulti {
   const uint32_t* cnt;
   const float4* rays;  // 2 float4 per ray: origin + path id, direction + scene
-  const uint32_t* rng;
+  PathField ro;  // path records: the RNG state is origin.w
   float4* hits;
   const SceneRec* recs;
   int any_alpha;
@@ -56,7 +56,7 @@ struct PathClosestMulti {
     const SceneDev& S = recs[sc].scene;
     return {S.nodes, S.geo, S.node_count, sc, S.wide};
   }
-  __device__ uint32_t key(uint32_t k) const { return rng[path(k)]; }
+  __device__ uint32_t key(uint32_t k) const { return __float_as_uint(ro[path(k)].w); }
   __device__ bool alpha_any() const { return any_alpha != 0; }
   __device__ bool alpha(int sc, int slot, uint32_t key, float bu, float bv) const {
     return alpha_opaque(recs[sc].scene, slot, key, bu, bv);
@@ -127,7 +127,7 @@ __device__ __forceinline__ void camera_path(const Paths& P, uint32_t p, uint32_t
   const float2 lens = concentric_disk(l0, l1);
   const float3 ro = cam.pos + cam.right * (lens.x * cam.aperture) + cam.up * (lens.y * cam.aperture);
   const float3 rd = norm3(focus - ro);
-  P.ro[p] = make_float4(ro.x, ro.y, ro.z, 0.f);
+  P.ro[p] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(st));
   P.rd[p] = make_float4(rd.x, rd.y, rd.z, 0.f);
   P.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
   P.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -135,7 +135,6 @@ __device__ __forceinline__ void camera_path(const Paths& P, uint32_t p, uint32_t
   P.galb[p] = make_float4(1.f, 1.f, 1.f, 0.f);
   P.gnrm[p] = make_float4(-rd.x, -rd.y, -rd.z, 1e4f);
   P.gpos[p] = make_float4(0.f, 0.f, 0.f, 1.f);
-  P.rng[p] = st;
   P.q[0][k] = p;
   P.nray[2 * (size_t)k] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(p));
   P.nray[2 * (size_t)k + 1] = make_float4(rd.x, rd.y, rd.z, __int_as_float(scene));
@@ -396,7 +395,8 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
     const LightingDev& L = src.light(p);
     const int max_bounces = src.bounces(p);
     const float uclamp = src.uclamp(p);
-    float3 ro = f3(P.ro[p]), rd = f3(P.rd[p]);
+    const float4 ro4 = P.ro[p];
+    float3 ro = f3(ro4), rd = f3(P.rd[p]);
     const float4 thr4 = P.thr[p], tint4 = P.tint[p];
     float3 thr = f3(thr4), rad = f3(P.rad[p]), tint = f3(tint4);
     // The forward render resolves the previous bounce's next-event
@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
     unsigned flags = __float_as_uint(tint4.w);
     bool spec = flags & kSpecular, done = flags & kGuideDone;
     float4 galb = P.galb[p], gnrm = P.gnrm[p];
-    uint32_t st = P.rng[p];
+    uint32_t st = __float_as_uint(ro4.w);  // the path's RNG state
     float4 hv = P.hit[kq];
     if (__float_as_int(hv.w) >= 0) hv = hit_values(S.geo, ro, rd, __float_as_int(hv.w));
     bool alive = false, deferred = false;
@@ -721,9 +721,8 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
     }
     P.galb[p] = galb;
     P.gnrm[p] = gnrm;
-    P.rng[p] = st;
     if (alive) {
-      P.ro[p] = make_float4(ro.x, ro.y, ro.z, 0.f);
+      P.ro[p] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(st));
       P.rd[p] = make_float4(rd.x, rd.y, rd.z, 0.f);
       P.thr[p] = make_float4(thr.x, thr.y, thr.z, bsdf_pdf);
       P.tint[p] = make_float4(tint.x, tint.y, tint.z, __uint_as_float((spec ? kSpecular : 0u) | (done ? kGuideDone : 0u)));
@@ -985,7 +984,7 @@ __global__ void k_count_rays(uint32_t* ctr, int cur) {  // statistics: rays trac
 // The hit is the triangle the traversal found with the values the shade
 // kernel computes for it (hit_values).
 __global__ void k_capture_closest(const uint32_t* __restrict__ cnt, const float4* __restrict__ rays,
-                                  const float4* __restrict__ hits, const uint32_t* __restrict__ rng,
+                                  const float4* __restrict__ hits, PathField ro,
                                   const SceneRec* __restrict__ recs, float4* __restrict__ out,
                                   uint32_t* __restrict__ count, uint32_t cap) {
   const uint32_t n = *cnt, m = n < cap ? n : cap;
@@ -999,7 +998,7 @@ __global__ void k_capture_closest(const uint32_t* __restrict__ cnt, const float4
     out[4 * (size_t)k] = a;
     out[4 * (size_t)k + 1] = b;
     out[4 * (size_t)k + 2] = h;
-    out[4 * (size_t)k + 3] = make_float4(__uint_as_float(rng[__float_as_uint(a.w)]), 0.f, 0.f, 0.f);
+    out[4 * (size_t)k + 3] = make_float4(ro[__float_as_uint(a.w)].w, 0.f, 0.f, 0.f);
   }
 }
 
@@ -1210,7 +1209,7 @@ int render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
       k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
     nl++;
     E.mark(kPhResolve, s);
-    PathClosestMulti pc{P.ctr + kCtrQ0 + cur, sorted ? P.sray : P.nray, P.rng, P.hit, M.recs, M.any_alpha};
+    PathClosestMulti pc{P.ctr + kCtrQ0 + cur, sorted ? P.sray : P.nray, P.ro, P.hit, M.recs, M.any_alpha};
     TravArgs A{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
                M.trav_stats, top};
     launch_closest_multi(M.wide, closest_blocks, top, A, pc, s);
@@ -1219,7 +1218,7 @@ int render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     const bool capture = M.cap && (M.cap_mask >> b & 1u);
     const uint32_t region = capture ? 2u * (uint32_t)__builtin_popcount(M.cap_mask & ((1u << b) - 1u)) : 0u;
     if (capture)
-      k_capture_closest<<<aux, 256, 0, s>>>(P.ctr + kCtrQ0 + cur, pc.rays, P.hit, P.rng, M.recs,
+      k_capture_closest<<<aux, 256, 0, s>>>(P.ctr + kCtrQ0 + cur, pc.rays, P.hit, P.ro, M.recs,
                                             M.cap + (size_t)region * M.cap_stride * 4, M.cap_count + region,
                                             M.cap_stride);
     nl += capture;
@@ -1314,7 +1313,7 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
         k_zero_closest_counters<<<1, 32, 0, s>>>(P.ctr);
       else
         k_zero_counters<<<1, 32, 0, s>>>(P.ctr, cur ^ 1);
-      PathClosestMulti pc{P.ctr + kCtrQ0 + cur, sorted ? P.sray : P.nray, P.rng, P.hit, M.recs, M.any_alpha};
+      PathClosestMulti pc{P.ctr + kCtrQ0 + cur, sorted ? P.sray : P.nray, P.ro, P.hit, M.recs, M.any_alpha};
       TravArgs TA{nullptr, 0, nullptr, 1e-6, 1e30, P.slow, P.ctr + kCtrSlow, P.ctr + kCtrWork, P.ctr + kCtrErr,
                   nullptr, top};
       launch_closest_multi(M.wide, closest_blocks, top, TA, pc, s);

@@ -378,12 +378,11 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
   P.galb = {P.rec + 4};
   P.gnrm = {P.rec + 5};
   P.gpos = {P.rec + 6};
-  P.rad = (float4*)take((size_t)cap * 16);
+  P.rad = {P.rec + 7};
   P.hit = (float4*)take((size_t)cap * 16);
   P.sh_o = (float4*)take((size_t)cap * 48);
   P.sh_d = (float4*)take((size_t)cap * 48);
   P.sh_c = (float4*)take((size_t)cap * 48);
-  P.rng = (uint32_t*)take((size_t)cap * 4);
   P.sh_occ = (uint8_t*)take((size_t)cap * 3);
   P.q[0] = (uint32_t*)take((size_t)cap * 4);
   P.q[1] = (uint32_t*)take((size_t)cap * 4);

@@ -35,13 +35,12 @@ __device__ __forceinline__ half4 make_half4(float4 v) {
 }
 
 // Structure-of-arrays path state; shadow slots are 3 per path (sun, env, light).
-// Path state lives in one 128-byte record per path (8 float4: origin,
-// direction, throughput + bsdf pdf, guide tint + flags, guide albedo, guide
-// normal + depth, guide position + reuse, unused); field f of path p is
-// float4 number f of record p. A kernel that walks paths in sorted (not path)
-// order then touches one DRAM line per path instead of one per field. The
-// radiance has its own array: the resolve kernel, which touches nothing
-// else, reads and writes it in path order.
+// Path state lives in one 128-byte record per path (8 float4: origin + RNG
+// state bits, direction, throughput + bsdf pdf, guide tint + flags, guide
+// albedo, guide normal + depth, guide position + reuse, radiance); field f of
+// path p is float4 number f of record p. A kernel that walks paths in sorted
+// (not path) order then touches one DRAM line per path instead of one per
+// field.
 constexpr int kPathRecord = 8;
 struct PathField {
   float4* base;  // the field in record 0
@@ -52,10 +51,9 @@ struct Paths {
   float4* rec;  // path records
   PathField ro, rd, thr, tint, galb, gnrm;
   PathField gpos;  // guide: primary hit position (xyz) and how much history it may reuse (w)
-  float4* rad;     // radiance per path
+  PathField rad;   // radiance per path
   float4* hit;     // closest hit per position of the bounce's queue
   float4 *sh_o, *sh_d, *sh_c;
-  uint32_t* rng;
   uint8_t* sh_occ;
   uint32_t* q[2];
   uint32_t* qs;
