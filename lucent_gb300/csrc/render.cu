@@ -107,7 +107,12 @@ struct PathShadowMulti {
 };
 
 // ------------------------------------------------------------ kernels
+// Path flags (guide tint .w). Bits kPendShift.. mark the path's next-event
+// slots (sun, environment, light) whose shadow rays the last shade emitted:
+// the contributions that resolve (the next shade, or the accumulation)
+// still has to add.
 constexpr unsigned kSpecular = 1u, kGuideDone = 2u;
+constexpr int kPendShift = 2;
 
 // cameraRay (trace.frag:53-62) and the path's initial state; sample s of
 // pixel `pixel` draws from the stream seeded with (pixel, seed0 + s). Path p
@@ -403,18 +408,17 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
     // contributions here (the backward replays keep their resolve kernels):
     // the unoccluded ones join the radiance first, in the reference's order
     // (sun, environment, light), as a separate resolve pass would add them.
-    unsigned pending = 0u, emitted = 0u;
+    unsigned emitted = 0u;
+    const unsigned flags = __float_as_uint(tint4.w);
     if constexpr (!ADJ) {
+      const unsigned pending = flags >> kPendShift & 7u;
 #pragma unroll
       for (int j = 0; j < 3; j++) {
-        const float4 c = P.sh_c[3 * (size_t)p + j];
-        if (c.w == 0.f) continue;
-        pending |= 1u << j;
-        if (!P.sh_occ[3 * (size_t)p + j]) rad = rad + f3(c);
+        if (!(pending >> j & 1u)) continue;
+        if (!P.sh_occ[3 * (size_t)p + j]) rad = rad + f3(P.sh_c[3 * (size_t)p + j]);
       }
     }
     float bsdf_pdf = thr4.w;
-    unsigned flags = __float_as_uint(tint4.w);
     bool spec = flags & kSpecular, done = flags & kGuideDone;
     float4 galb = P.galb[p], gnrm = P.gnrm[p];
     uint32_t st = __float_as_uint(ro4.w);  // the path's RNG state
@@ -713,19 +717,15 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
     }
 
     P.rad[p] = make_float4(rad.x, rad.y, rad.z, 0.f);
-    if constexpr (!ADJ) {  // resolved slots not refilled this bounce are no longer pending
-      const unsigned stale = pending & ~emitted;
-      if (stale)
-        for (int j = 0; j < 3; j++)
-          if (stale >> j & 1u) P.sh_c[3 * (size_t)p + j].w = 0.f;
-    }
+    // Flags always (the slots this bounce left pending, for resolve), the rest if the path goes on.
+    P.tint[p] = make_float4(tint.x, tint.y, tint.z,
+                            __uint_as_float((spec ? kSpecular : 0u) | (done ? kGuideDone : 0u) | emitted << kPendShift));
     P.galb[p] = galb;
     P.gnrm[p] = gnrm;
     if (alive) {
       P.ro[p] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(st));
       P.rd[p] = make_float4(rd.x, rd.y, rd.z, 0.f);
       P.thr[p] = make_float4(thr.x, thr.y, thr.z, bsdf_pdf);
-      P.tint[p] = make_float4(tint.x, tint.y, tint.z, __uint_as_float((spec ? kSpecular : 0u) | (done ? kGuideDone : 0u)));
       const uint32_t pos = atomicAdd(&P.ctr[kCtrQ0 + (cur ^ 1)], 1u);
       qn[pos] = p;
       P.nray[2 * (size_t)pos] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(p));
@@ -743,21 +743,18 @@ __global__ void k_resolve(Paths P, int cur, int all) {
   const uint32_t* q = P.q[cur];
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const uint32_t p = all ? k : q[k];
+    const unsigned pending = __float_as_uint(P.tint[p].w) >> kPendShift & 7u;
+    if (!pending) continue;
     float4 r = P.rad[p];
-    bool any = false;
     for (int j = 0; j < 3; j++) {
       const uint32_t s = 3 * p + j;
+      if (!(pending >> j & 1u) || P.sh_occ[s]) continue;
       const float4 c = P.sh_c[s];
-      if (c.w == 0.f) continue;
-      any = true;
-      if (!P.sh_occ[s]) {
-        r.x += c.x;
-        r.y += c.y;
-        r.z += c.z;
-      }
-      P.sh_c[s].w = 0.f;
+      r.x += c.x;
+      r.y += c.y;
+      r.z += c.z;
     }
-    if (any) P.rad[p] = r;
+    P.rad[p] = r;
   }
 }
 
@@ -778,10 +775,11 @@ __global__ void k_resolve_adjoint(Paths P, const __grid_constant__ AdjointDev A,
     const float3 dl = l4.w == 0.f ? f3(A.dl[p % A.WH]) : f3(0.f, 0.f, 0.f);
     float g[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     int mat = -1;
+    const unsigned pending = __float_as_uint(P.tint[p].w) >> kPendShift & 7u;
     for (int j = 0; j < 3; j++) {
       const uint32_t s = 3 * p + j;
+      if (!(pending >> j & 1u)) continue;
       const float4 c = P.sh_c[s];
-      if (c.w == 0.f) continue;
       if (!P.sh_occ[s]) {
         r.x += c.x;
         r.y += c.y;
@@ -795,7 +793,6 @@ __global__ void k_resolve_adjoint(Paths P, const __grid_constant__ AdjointDev A,
           add_env_grad(A, L, make_float2(e0.x, e0.y), dl, f3(e0.z, e0.w, e1.x));
         }
       }
-      P.sh_c[s].w = 0.f;
     }
     const float4* gc = A.gcont + 5 * (size_t)p;
     const int cm = __float_as_int(gc[4].z);
@@ -897,11 +894,11 @@ __device__ __forceinline__ void accumulate_pixel(const Paths& P, const SceneRec&
     float4 c = P.rad[p];
     // The contributions of the path's last shaded bounce, resolved here (the
     // forward render folds resolve into the next shade and this pass).
+    const unsigned pending = __float_as_uint(P.tint[p].w) >> kPendShift & 7u;
     for (int j = 0; j < 3; j++) {
+      if (!(pending >> j & 1u) || P.sh_occ[3 * (size_t)p + j]) continue;
       const float4 e = P.sh_c[3 * (size_t)p + j];
-      if (e.w == 0.f) continue;
-      if (!P.sh_occ[3 * (size_t)p + j]) c = make_float4(c.x + e.x, c.y + e.y, c.z + e.z, c.w);
-      P.sh_c[3 * (size_t)p + j].w = 0.f;
+      c = make_float4(c.x + e.x, c.y + e.y, c.z + e.z, c.w);
     }
     if (isnan(c.x) || isnan(c.y) || isnan(c.z) || isinf(c.x) || isinf(c.y) || isinf(c.z)) c = make_float4(0.f, 0.f, 0.f, 0.f);
     const float l = lum(f3(c));
