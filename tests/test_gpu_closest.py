@@ -104,6 +104,36 @@ def test_coincident_and_duplicate_triangles():  # bvh.test.ts:78-86 plus exact t
     assert ids[0] >= 0
 
 
+def test_coplanar_ties_and_flat_leaves():
+    # Boxes standing on a floor (bottom faces in the floor's plane), a second
+    # triangulation of the floor (the other diagonal) and a few coplanar
+    # overlapping quads: rays from above and below meet two or more triangles
+    # at one distance, and flat leaf boxes whose entry equals the running
+    # closest. The kernels defer such ties and visit such leaves
+    # conditionally; the hits must still be the reference's.
+    floor_a = mesh.quad((-2, 0, 2), (2, 0, 2), (2, 0, -2), (-2, 0, -2))
+    floor_b = mesh.quad((2, 0, 2), (2, 0, -2), (-2, 0, -2), (-2, 0, 2))
+    parts = [floor_a, floor_b,
+             mesh.transform(mesh.box((-0.3, 0.0, -0.3), (0.3, 1.2, 0.3)), translate=(-0.4, 0.0, -0.35), rotate_y=0.4),
+             mesh.transform(mesh.box((-0.3, 0.0, -0.3), (0.3, 0.6, 0.3)), translate=(0.45, 0.0, 0.3), rotate_y=1.1),
+             mesh.quad((-1, 0.6, 1), (1, 0.6, 1), (1, 0.6, -1), (-1, 0.6, -1)),
+             mesh.quad((-0.5, 0.6, 0.5), (0.5, 0.6, 0.5), (0.5, 0.6, -0.5), (-0.5, 0.6, -0.5))]
+    m = mesh.merge_meshes(parts)
+    ob, dev = _dev(m.positions)
+    rng = np.random.Generator(np.random.PCG64(11))
+    n = 4000
+    o = np.concatenate([rng.uniform(-2, 2, (n, 1)), rng.uniform(0.7, 3.0, (n, 1)), rng.uniform(-2, 2, (n, 1))], 1)
+    d = np.concatenate([rng.normal(size=(n, 1)) * 0.5, -np.ones((n, 1)), rng.normal(size=(n, 1)) * 0.5], 1)
+    below = o * np.array([1, -1, 1]) + np.array([0, 0.3, 0])
+    up = d * np.array([1, -1, 1])
+    rays = np.concatenate([np.concatenate([o, d], 1), np.concatenate([below, up], 1)]).astype(np.float64)
+    rays[:, 3:] /= np.linalg.norm(rays[:, 3:], axis=1, keepdims=True)
+    rays = np.concatenate([rays, workloads.adversarial_rays(m.positions, rng, 800)]).astype(np.float32)
+    hits = [(_compare(dev, ob, m.positions, rays, t_min, t_max) >= 0).mean()
+            for t_min, t_max in ((1e-6, 1e30), (1e-5, math.inf), (0.0, 2.0))]
+    assert hits[0] > 0.5 and hits[2] > 0.2, hits
+
+
 def test_empty_and_single():
     ob = oracle.build_bvh(np.zeros(0, np.float32))
     dev = DeviceBVH(ob.nodes, ob.tri_indices, np.zeros(0, np.float32), ob.node_count)
