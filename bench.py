@@ -222,7 +222,7 @@ CPU_BASELINE_SECONDS = 10.0
 # dram__bytes_read.sum + dram__bytes_write.sum of the closest-hit launches,
 # from ncu captures of the same workloads (the source is named in each line's
 # traffic_scope).
-NCU_DRAM_BYTES_PT_FRAME = 828_700_000
+NCU_DRAM_BYTES_PT_FRAME = 553_000_000
 NCU_DRAM_BYTES_CLOSEST_LAUNCH = 115_400_000
 PT_METRIC = ("closest-hit Mrays/s inside path tracing: box scene (81,956 triangles), 512x512, 16 spp, "
              "max depth 8 (also spp/s)")
