@@ -656,6 +656,13 @@ def run_targets(args, local):
     out = {}
     out["env_sampler"] = env_sampler_times(local)
     t0 = time.perf_counter()
+    c = run_ours_closest(types.SimpleNamespace(steps=5, warmup=3), 0, 1, local)
+    out["bvh_closest"] = {"mrays_per_s": c["value"], "ms_per_1m_rays": c["ms_per_step"],
+                          "e2e_mrays_per_s": c["e2e"]["value"],
+                          "roofline_frac": c["roofline"]["frac"] if c["roofline"] else None,
+                          "config": c["config"]["workload"], "clocks": c["clocks"],
+                          "wall_s": round(time.perf_counter() - t0, 1)}
+    t0 = time.perf_counter()
     bb = run_ours_build(types.SimpleNamespace(steps=3, warmup=1), 0, 1, local)
     out["bvh_build"] = {"gpu_ms": bb["extra"]["build_ms"], "reference_call_ms": bb["extra"]["reference_call_ms"],
                         "cpu_oracle_single_thread_ms": cpu_build_ms(),

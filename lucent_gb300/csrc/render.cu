@@ -132,17 +132,26 @@ __device__ __forceinline__ void camera_path(const Paths& P, uint32_t p, uint32_t
   const float2 lens = concentric_disk(l0, l1);
   const float3 ro = cam.pos + cam.right * (lens.x * cam.aperture) + cam.up * (lens.y * cam.aperture);
   const float3 rd = norm3(focus - ro);
+  // The rest of the record starts as constants that the bounce-0 shade
+  // takes without reading them (first_record_field).
   P.ro[p] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(st));
   P.rd[p] = make_float4(rd.x, rd.y, rd.z, 0.f);
-  P.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
-  P.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-  P.tint[p] = make_float4(1.f, 1.f, 1.f, __uint_as_float(kSpecular));
-  P.galb[p] = make_float4(1.f, 1.f, 1.f, 0.f);
-  P.gnrm[p] = make_float4(-rd.x, -rd.y, -rd.z, 1e4f);
-  P.gpos[p] = make_float4(0.f, 0.f, 0.f, 1.f);
   P.q[0][k] = p;
   P.nray[2 * (size_t)k] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(p));
   P.nray[2 * (size_t)k + 1] = make_float4(rd.x, rd.y, rd.z, __int_as_float(scene));
+}
+
+// A path record field as the bounce-0 shade starts from it: throughput 1
+// (no BSDF pdf yet), no radiance, guide tint 1 with the specular flag, guide
+// albedo 1, guide normal -rd at depth 1e4; later bounces read the record.
+__device__ __forceinline__ float4 first_record_field(int f, float3 rd) {
+  switch (f) {
+    case 2: return make_float4(1.f, 1.f, 1.f, 0.f);                                  // throughput + pdf
+    case 3: return make_float4(1.f, 1.f, 1.f, __uint_as_float(kSpecular));           // tint + flags
+    case 4: return make_float4(1.f, 1.f, 1.f, 0.f);                                  // guide albedo
+    case 5: return make_float4(-rd.x, -rd.y, -rd.z, 1e4f);                           // guide normal + depth
+    default: return make_float4(0.f, 0.f, 0.f, 0.f);                                 // radiance
+  }
 }
 
 // Index of the scene whose range [base[i], base[i + 1]) holds v (n scenes).
@@ -402,8 +411,10 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
     const float uclamp = src.uclamp(p);
     const float4 ro4 = P.ro[p];
     float3 ro = f3(ro4), rd = f3(P.rd[p]);
-    const float4 thr4 = P.thr[p], tint4 = P.tint[p];
-    float3 thr = f3(thr4), rad = f3(P.rad[p]), tint = f3(tint4);
+    const bool first = bounce == 0;  // the camera wrote only origin and direction
+    const float4 thr4 = first ? first_record_field(2, rd) : P.thr[p];
+    const float4 tint4 = first ? first_record_field(3, rd) : P.tint[p];
+    float3 thr = f3(thr4), rad = f3(first ? first_record_field(7, rd) : P.rad[p]), tint = f3(tint4);
     // The forward render resolves the previous bounce's next-event
     // contributions here (the backward replays keep their resolve kernels):
     // the unoccluded ones join the radiance first, in the reference's order
@@ -420,7 +431,8 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
     }
     float bsdf_pdf = thr4.w;
     bool spec = flags & kSpecular, done = flags & kGuideDone;
-    float4 galb = P.galb[p], gnrm = P.gnrm[p];
+    float4 galb = first ? first_record_field(4, rd) : P.galb[p];
+    float4 gnrm = first ? first_record_field(5, rd) : P.gnrm[p];
     uint32_t st = __float_as_uint(ro4.w);  // the path's RNG state
     float4 hv = P.hit[kq];
     if (__float_as_int(hv.w) >= 0) hv = hit_values(S.geo, ro, rd, __float_as_int(hv.w));
@@ -461,6 +473,7 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
     }
     do {
       if (!tri && best_sphere < 0 && !ground) {  // miss (trace.frag:146-155)
+        if (bounce == 0) P.gpos[p] = make_float4(0.f, 0.f, 0.f, 1.f);  // no guide position: full reuse
         const float3 env = bounce == 0 && !L.env_background ? L.backdrop : environment(L, rd, spec, bsdf_pdf);
         rad = rad + clamp_c(thr * env, bounce, uclamp);
         if (adj) {
