@@ -11,7 +11,9 @@
 //               opaque: next-event estimation (sun, environment, one light)
 //               into per-path shadow slots, BSDF sample, Russian roulette
 //   any-hit  -> shadow rays
-//   resolve  -> unoccluded NEE added in the reference's order (sun, env, light)
+//   resolve  -> unoccluded NEE added in the reference's order (sun, env, light):
+//               at the start of the next shade, or in the accumulation for a
+//               path that ends (the backward replays keep a resolve kernel)
 // Accumulation replays the running mean (trace.frag:350-354) sample by
 // sample per pixel, so a batch equals S sequential draws.
 #include <cuda_fp16.h>
