@@ -356,7 +356,7 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
                                         uint32_t cap) {
   if (cap <= path_cap) return LUCENT_OK;
   // Per-path arrays in allocation order (bytes per path); each starts on a 256-byte boundary.
-  static const size_t kPer[] = {16 * kPathRecord, 16, 16, 48, 48, 48, 4, 3, 4, 4, 12, 4, 12, 4, 32, 32, 4, 4};
+  static const size_t kPer[] = {16 * kPathRecord, 16, 48, 48, 48, 3, 4, 4, 12, 4, 12, 4, 32, 32, 4, 4};
   size_t total = 0;
   for (size_t b : kPer) total += ((size_t)cap * b + 255) & ~(size_t)255;
   total += (size_t)kSortBins * 4;
