@@ -421,6 +421,15 @@ lucent_status lucent_renderer_read_denoised(lucent_renderer* r, float* out4);
  * quantization to host memory (either may be NULL); synchronous. */
 lucent_status lucent_renderer_display(lucent_renderer* r, float denoise_weight, int32_t tonemap, float exposure,
                                       uint8_t* rgba8_out, float* rgb_out, void* stream);
+/* The same display pass with the renderer's targets as the traced region
+ * (uRenderSize) shown in a view_w x view_h canvas (uViewSize): when the sizes
+ * differ, display.frag's Catmull-Rom upsampling (display.frag:44-60), the
+ * reference's reduced-resolution preview while the camera moves
+ * (renderer.ts:524-541). Outputs view_w * view_h pixels; otherwise as
+ * lucent_renderer_display, which is this call at the renderer's size. */
+lucent_status lucent_renderer_display_view(lucent_renderer* r, uint32_t view_w, uint32_t view_h, float denoise_weight,
+                                           int32_t tonemap, float exposure, uint8_t* rgba8_out, float* rgb_out,
+                                           void* stream);
 
 /* ---------------------------------------------------------------------------
  * Multi-scene batches. No reference counterpart: the reference renders one

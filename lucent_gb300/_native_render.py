@@ -73,6 +73,7 @@ def declare(L, sig):
     sig(L, "lucent_renderer_backward", [VP, C.c_uint32, C.c_uint32, F32P, F32P, F32P, VP])
     sig(L, "lucent_renderer_denoise", [VP, C.c_uint32, C.c_float, C.c_float, C.c_float, VP])
     sig(L, "lucent_renderer_display", [VP, C.c_float, C.c_int32, C.c_float, U8P, F32P, VP])
+    sig(L, "lucent_renderer_display_view", [VP, C.c_uint32, C.c_uint32, C.c_float, C.c_int32, C.c_float, U8P, F32P, VP])
     sig(L, "lucent_renderer_read_denoised", [VP, F32P])
     sig(L, "lucent_bsdf_eval_tuples", [F32P, C.c_uint32, F32P])
     sig(L, "lucent_bsdf_grad_tuples", [F32P, C.c_uint32, F32P])

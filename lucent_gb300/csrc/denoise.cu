@@ -231,26 +231,63 @@ __global__ void __launch_bounds__(256) k_atrous_tiled(const float4* __restrict__
   out[p] = make_float4(sum.x / wsum, sum.y / wsum, sum.z / wsum, sumVar / (wsum * wsum));
 }
 
-// display.frag:42-67 (render size == view size): remodulate and blend the
-// denoised image, exposure, tone map, sRGB, IGN dither, RGBA8.
-__global__ void k_display(AccumDev A, const float4* __restrict__ den, int W, int H, float weight, float exposure,
-                          int tonemap, uchar4* __restrict__ rgba8, float* __restrict__ rgb) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= W || y >= H) return;
-  const size_t p = (size_t)y * W + x;
+// display.frag:33-40: a texel of the traced region (clamped to it) with the
+// remodulated denoised image blended in.
+__device__ __forceinline__ float3 display_radiance(const AccumDev& A, const float4* __restrict__ den, int RW, int RH,
+                                                   int x, int y, float weight) {
+  x = min(max(x, 0), RW - 1);
+  y = min(max(y, 0), RH - 1);
+  const size_t p = (size_t)y * RW + x;
   const float4 raw = A.color[p];
-  float c[3] = {raw.x, raw.y, raw.z};
+  float3 c = make_float3(raw.x, raw.y, raw.z);
   if (weight > 0.f && den) {
     const float4 a = h4(A.albedo[p]);
     if (a.w >= 0.5f) {
       const float4 d = den[p];
-      const float dv[3] = {d.x * fmaxf(a.x, 1e-3f), d.y * fmaxf(a.y, 1e-3f), d.z * fmaxf(a.z, 1e-3f)};
-      for (int k = 0; k < 3; k++) c[k] = c[k] * (1.f - weight) + dv[k] * weight;
+      c = make_float3(c.x * (1.f - weight) + d.x * fmaxf(a.x, 1e-3f) * weight,
+                      c.y * (1.f - weight) + d.y * fmaxf(a.y, 1e-3f) * weight,
+                      c.z * (1.f - weight) + d.z * fmaxf(a.z, 1e-3f) * weight);
     }
   }
-  const float t = 0.06711056f * ((float)x + 0.5f) + 0.00583715f * ((float)y + 0.5f);
+  return c;
+}
+
+// display.frag:42-67: the traced region (RW x RH, the targets) shown in a
+// VW x VH view; Catmull-Rom upsampling (:47-60) when the sizes differ (the
+// reference's reduced-resolution preview while the camera moves). Then
+// exposure, tone map, sRGB, IGN dither, RGBA8.
+__global__ void k_display(AccumDev A, const float4* __restrict__ den, int RW, int RH, int VW, int VH, float weight,
+                          float exposure, int tonemap, uchar4* __restrict__ rgba8, float* __restrict__ rgb) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= VW || y >= VH) return;
+  const float fx = (float)x + 0.5f, fy = (float)y + 0.5f;  // gl_FragCoord.xy
+  float3 c3;
+  if (RW == VW && RH == VH) {
+    c3 = display_radiance(A, den, RW, RH, x, y, weight);
+  } else {
+    const float srx = fx * ((float)RW / (float)VW) - 0.5f, sry = fy * ((float)RH / (float)VH) - 0.5f;
+    const int ix = (int)floorf(srx), iy = (int)floorf(sry);
+    const float tx = srx - floorf(srx), ty = sry - floorf(sry);
+    const float wx[4] = {tx * (-0.5f + tx * (1.f - 0.5f * tx)), 1.f + tx * tx * (-2.5f + 1.5f * tx),
+                         tx * (0.5f + tx * (2.f - 1.5f * tx)), tx * tx * (-0.5f + 0.5f * tx)};
+    const float wy[4] = {ty * (-0.5f + ty * (1.f - 0.5f * ty)), 1.f + ty * ty * (-2.5f + 1.5f * ty),
+                         ty * (0.5f + ty * (2.f - 1.5f * ty)), ty * ty * (-0.5f + 0.5f * ty)};
+    c3 = make_float3(0.f, 0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const float3 r = display_radiance(A, den, RW, RH, ix + i - 1, iy + j - 1, weight);
+        const float w = wx[i] * wy[j];
+        c3 = make_float3(c3.x + r.x * w, c3.y + r.y * w, c3.z + r.z * w);
+      }
+    c3 = make_float3(fmaxf(c3.x, 0.f), fmaxf(c3.y, 0.f), fmaxf(c3.z, 0.f));
+  }
+  const float c[3] = {c3.x, c3.y, c3.z};
+  const float t = 0.06711056f * fx + 0.00583715f * fy;
   const float u = 52.9829189f * (t - floorf(t));
   const float ign = u - floorf(u);
+  const size_t p = (size_t)y * VW + x;
   unsigned char q[3];
   for (int k = 0; k < 3; k++) {
     float v = c[k] * exposure;
@@ -293,10 +330,10 @@ float4* denoise_run(AccumDev A, const CameraDev& cam, int W, int H, int levels, 
   return rd;
 }
 
-void display_run(AccumDev A, const float4* den, int W, int H, float weight, float exposure, int tonemap,
-                 uchar4* rgba8, float* rgb, cudaStream_t s) {
-  const dim3 blk(16, 16), grd((W + 15) / 16, (H + 15) / 16);
-  k_display<<<grd, blk, 0, s>>>(A, den, W, H, weight, exposure, tonemap, rgba8, rgb);
+void display_run(AccumDev A, const float4* den, int W, int H, int VW, int VH, float weight, float exposure,
+                 int tonemap, uchar4* rgba8, float* rgb, cudaStream_t s) {
+  const dim3 blk(16, 16), grd((VW + 15) / 16, (VH + 15) / 16);
+  k_display<<<grd, blk, 0, s>>>(A, den, W, H, VW, VH, weight, exposure, tonemap, rgba8, rgb);
 }
 
 }  // namespace lucent

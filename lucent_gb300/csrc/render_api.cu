@@ -1216,18 +1216,27 @@ lucent_status lucent_renderer_display(lucent_renderer* r, float denoise_weight, 
                                       uint8_t* rgba8_out, float* rgb_out, void* stream) {
   clear_error();
   if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  return lucent_renderer_display_view(r, r->W, r->H, denoise_weight, tonemap, exposure, rgba8_out, rgb_out, stream);
+}
+
+lucent_status lucent_renderer_display_view(lucent_renderer* r, uint32_t view_w, uint32_t view_h, float denoise_weight,
+                                           int32_t tonemap, float exposure, uint8_t* rgba8_out, float* rgb_out,
+                                           void* stream) {
+  clear_error();
+  if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  if (view_w == 0 || view_h == 0 || (uint64_t)view_w * view_h > (1u << 26)) return fail(LUCENT_ERR_INVALID, "bad view size");
   if (tonemap < 0 || tonemap > 2) return fail(LUCENT_ERR_INVALID, "tonemap must be 0 (ACES), 1 (Reinhard) or 2 (none)");
   if (!(denoise_weight >= 0.f && denoise_weight <= 1.f)) return fail(LUCENT_ERR_INVALID, "denoise weight outside [0, 1]");
   if (denoise_weight > 0.f && !r->denoised)
     return fail(LUCENT_ERR_INVALID, "denoise weight > 0 with no denoised image since the last reset");
-  const size_t n = (size_t)r->W * r->H;
+  const size_t n = (size_t)view_w * view_h;
   lucent_status st = r->disp.reserve(n * 16);
   if (st) return st;
   uchar4* d8 = (uchar4*)r->disp.ptr;
   float* drgb = (float*)((char*)r->disp.ptr + n * 4);
   cudaStream_t s = (cudaStream_t)stream;
-  display_run(accum_of(r), denoise_weight > 0.f ? r->denoised : nullptr, (int)r->W, (int)r->H, denoise_weight,
-              exposure, tonemap, rgba8_out ? d8 : nullptr, rgb_out ? drgb : nullptr, s);
+  display_run(accum_of(r), denoise_weight > 0.f ? r->denoised : nullptr, (int)r->W, (int)r->H, (int)view_w,
+              (int)view_h, denoise_weight, exposure, tonemap, rgba8_out ? d8 : nullptr, rgb_out ? drgb : nullptr, s);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && rgba8_out) e = cudaMemcpyAsync(rgba8_out, d8, n * 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess && rgb_out) e = cudaMemcpyAsync(rgb_out, drgb, n * 12, cudaMemcpyDeviceToHost, s);

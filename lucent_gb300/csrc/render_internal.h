@@ -175,8 +175,9 @@ void sheen_lut_half(float* out);
 // Returns fa or fb, whichever holds the result.
 float4* denoise_run(AccumDev A, const sh::CameraDev& cam, int W, int H, int levels, float sigma_l, float sigma_n,
                     float sigma_p, float4* fa, float4* fb, float4* g0, float4* g1, cudaStream_t s);
-// Display pass: RGBA8 and/or the pre-quantization RGB floats (either may be null).
-void display_run(AccumDev A, const float4* den, int W, int H, float weight, float exposure, int tonemap,
-                 uchar4* rgba8, float* rgb, cudaStream_t s);
+// Display pass of the W x H targets into a VW x VH view: RGBA8 and/or the
+// pre-quantization RGB floats (either may be null).
+void display_run(AccumDev A, const float4* den, int W, int H, int VW, int VH, float weight, float exposure,
+                 int tonemap, uchar4* rgba8, float* rgb, cudaStream_t s);
 
 }  // namespace lucent

@@ -297,18 +297,21 @@ class Renderer:
         N.check(N.lib().lucent_renderer_read_denoised(self._h, _f(out)))
         return out.reshape(self.height, self.width, 4)
 
-    def display(self, denoise_weight=0.0, exposure=None, tonemap=None, want_float=False, stream=None):
+    def display(self, denoise_weight=0.0, exposure=None, tonemap=None, want_float=False, stream=None, view=None):
         """The display pass (renderer.ts:573-591): RGBA8 canvas [H, W, 4], row 0 = bottom;
-        with want_float also the RGB values before quantization."""
+        with want_float also the RGB values before quantization. `view` = (width, height)
+        shows the renderer's image in a canvas of that size (Catmull-Rom upsampling of the
+        reduced-resolution preview, display.frag:44-60; lucent_renderer_display_view)."""
         exposure = self.settings.exposure if exposure is None else exposure
         tm = TONEMAPS[self.settings.tonemap if tonemap is None else tonemap]
-        n = self.width * self.height
+        vw, vh = (self.width, self.height) if view is None else (int(view[0]), int(view[1]))
+        n = vw * vh
         rgba = np.empty(n * 4, np.uint8)
         rgb = np.empty(n * 3, np.float32) if want_float else None
-        N.check(N.lib().lucent_renderer_display(self._h, denoise_weight, tm, exposure, N.ptr(rgba, C.c_uint8),
-                                                _f(rgb), stream))
-        img = rgba.reshape(self.height, self.width, 4)
-        return (img, rgb.reshape(self.height, self.width, 3)) if want_float else img
+        N.check(N.lib().lucent_renderer_display_view(self._h, vw, vh, denoise_weight, tm, exposure,
+                                                     N.ptr(rgba, C.c_uint8), _f(rgb), stream))
+        img = rgba.reshape(vh, vw, 4)
+        return (img, rgb.reshape(vh, vw, 3)) if want_float else img
 
     def render(self):
         """render() (renderer.ts:553-611) with a fixed samples_per_frame budget:

@@ -1757,27 +1757,60 @@ int orc_denoise(const float* color4, const float* albedo4, const float* normal4,
 
 // display.frag :42-67 with uRenderSize == uViewSize. out_rgb: the value
 // written to the RGBA8 target before quantization (dither included).
-int orc_display(const float* color4, const float* albedo4, const float* denoised4, uint32_t w, uint32_t h,
-                float denoise_weight, float exposure, int tonemap, float* out_rgb) {
-  for (uint32_t y = 0; y < h; y++)
-    for (uint32_t x = 0; x < w; x++) {
-      const size_t p = (size_t)y * w + x;
-      float c[3] = {color4[4 * p], color4[4 * p + 1], color4[4 * p + 2]};
-      if (denoise_weight > 0.0f) {
-        const float* a = albedo4 + 4 * p;
-        if (a[3] >= 0.5f)
-          for (int k = 0; k < 3; k++) {
-            const float dn = denoised4[4 * p + k] * std::max(a[k], 1e-3f);
-            c[k] = c[k] * (1.0f - denoise_weight) + dn * denoise_weight;
+// display.frag:42-67: the traced region (rw x rh, at the start of the
+// targets) shown in a vw x vh view; Catmull-Rom upsampling (:47-60) when the
+// sizes differ. `radiance` is display.frag:33-40 (coordinates clamped to the
+// region, denoised blend).
+int orc_display_view(const float* color4, const float* albedo4, const float* denoised4, uint32_t rw, uint32_t rh,
+                     uint32_t vw, uint32_t vh, float denoise_weight, float exposure, int tonemap, float* out_rgb) {
+  auto radiance = [&](int px, int py, float* c) {
+    px = std::min(std::max(px, 0), (int)rw - 1);
+    py = std::min(std::max(py, 0), (int)rh - 1);
+    const size_t p = (size_t)py * rw + px;
+    for (int k = 0; k < 3; k++) c[k] = color4[4 * p + k];
+    if (denoise_weight > 0.0f) {
+      const float* a = albedo4 + 4 * p;
+      if (a[3] >= 0.5f)
+        for (int k = 0; k < 3; k++) {
+          const float dn = denoised4[4 * p + k] * std::max(a[k], 1e-3f);
+          c[k] = c[k] * (1.0f - denoise_weight) + dn * denoise_weight;
+        }
+    }
+  };
+  const bool same = rw == vw && rh == vh;
+  const float sx = (float)rw / (float)vw, sy = (float)rh / (float)vh;  // uRenderSize / uViewSize
+  for (uint32_t y = 0; y < vh; y++)
+    for (uint32_t x = 0; x < vw; x++) {
+      const float fx = (float)x + 0.5f, fy = (float)y + 0.5f;  // gl_FragCoord.xy
+      float c[3];
+      if (same) {
+        radiance((int)x, (int)y, c);
+      } else {
+        const float srx = fx * sx - 0.5f, sry = fy * sy - 0.5f;
+        const int ix = (int)std::floor(srx), iy = (int)std::floor(sry);
+        const float f[2] = {srx - std::floor(srx), sry - std::floor(sry)};
+        float w[4][2];
+        for (int a = 0; a < 2; a++) {
+          const float t = f[a];
+          w[0][a] = t * (-0.5f + t * (1.0f - 0.5f * t));
+          w[1][a] = 1.0f + t * t * (-2.5f + 1.5f * t);
+          w[2][a] = t * (0.5f + t * (2.0f - 1.5f * t));
+          w[3][a] = t * t * (-0.5f + 0.5f * t);
+        }
+        c[0] = c[1] = c[2] = 0.0f;
+        for (int yy = 0; yy < 4; yy++)
+          for (int xx = 0; xx < 4; xx++) {
+            float r[3];
+            radiance(ix + xx - 1, iy + yy - 1, r);
+            const float wt = w[xx][0] * w[yy][1];
+            for (int k = 0; k < 3; k++) c[k] += r[k] * wt;
           }
+        for (int k = 0; k < 3; k++) c[k] = std::max(c[k], 0.0f);
       }
-      const float ign = [&]() {
-        const float fx = (float)x + 0.5f, fy = (float)y + 0.5f;
-        const float t = 0.06711056f * fx + 0.00583715f * fy;
-        const float f1 = t - std::floor(t);
-        const float u = 52.9829189f * f1;
-        return u - std::floor(u);
-      }();
+      const float t = 0.06711056f * fx + 0.00583715f * fy;
+      const float u = 52.9829189f * (t - std::floor(t));
+      const float ign = u - std::floor(u);
+      const size_t p = (size_t)y * vw + x;
       for (int k = 0; k < 3; k++) {
         float v = c[k] * exposure;
         if (tonemap == 0)
@@ -1791,6 +1824,11 @@ int orc_display(const float* color4, const float* albedo4, const float* denoised
       }
     }
   return 0;
+}
+
+int orc_display(const float* color4, const float* albedo4, const float* denoised4, uint32_t w, uint32_t h,
+                float denoise_weight, float exposure, int tonemap, float* out_rgb) {
+  return orc_display_view(color4, albedo4, denoised4, w, h, w, h, denoise_weight, exposure, tonemap, out_rgb);
 }
 
 // BSDF tuples. in: 32 floats per tuple

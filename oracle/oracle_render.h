@@ -111,6 +111,9 @@ int orc_denoise(const float* color4, const float* albedo4, const float* normal4,
                 float sigma_p, float* out4);
 int orc_display(const float* color4, const float* albedo4, const float* denoised4, uint32_t w, uint32_t h,
                 float denoise_weight, float exposure, int tonemap, float* out_rgb);
+/* display.frag with the traced region rw x rh shown in a vw x vh view (Catmull-Rom when they differ). */
+int orc_display_view(const float* color4, const float* albedo4, const float* denoised4, uint32_t rw, uint32_t rh,
+                     uint32_t vw, uint32_t vh, float denoise_weight, float exposure, int tonemap, float* out_rgb);
 
 /* The previous view of a temporal reprojection: its camera, size and
  * targets (w x h, albedo/normal as the RGBA16F values). */

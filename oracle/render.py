@@ -45,6 +45,7 @@ def declare(L):
     L.orc_detached_dot.argtypes = [P(OrcScene), P(OrcCamera), U32, F, U32, U32, U32, U32, P(F), P(F), P(F), C.c_int]
     L.orc_detached_dot.restype = C.c_double
     L.orc_display.argtypes = [P(F), P(F), P(F), U32, U32, F, F, C.c_int, P(F)]
+    L.orc_display_view.argtypes = [P(F), P(F), P(F), U32, U32, U32, U32, F, F, C.c_int, P(F)]
     L.orc_resample_layer.argtypes = [P(C.c_uint8), U32, U32, U32, C.c_int, P(C.c_uint8)]
     L.orc_texture_size.argtypes = [P(U32), P(U32), U32]
     L.orc_texture_size.restype = U32
@@ -254,6 +255,18 @@ def display(color4, albedo4, denoised4, denoise_weight, exposure=1.0, tonemap=0)
     d = _c32(denoised4 if denoised4 is not None else np.zeros((h, w, 4)), (h, w, 4))
     out = np.zeros((h, w, 3), np.float32)
     lib().orc_display(_p(c, F), _p(a, F), _p(d, F), w, h, denoise_weight, exposure, tonemap, _p(out, F))
+    return out
+
+
+def display_view(color4, albedo4, denoised4, view_w, view_h, denoise_weight, exposure=1.0, tonemap=0):
+    """orc_display_view: the [H, W] targets shown in a view_h x view_w view (Catmull-Rom when the sizes
+    differ), [view_h, view_w, 3] float32 values before quantization."""
+    h, w = color4.shape[:2]
+    c, a = _c32(color4, (h, w, 4)), _c32(albedo4, (h, w, 4))
+    d = _c32(denoised4 if denoised4 is not None else np.zeros((h, w, 4)), (h, w, 4))
+    out = np.zeros((view_h, view_w, 3), np.float32)
+    lib().orc_display_view(_p(c, F), _p(a, F), _p(d, F), w, h, view_w, view_h, denoise_weight, exposure, tonemap,
+                           _p(out, F))
     return out
 
 

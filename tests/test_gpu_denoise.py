@@ -106,6 +106,29 @@ def test_display_matches_oracle(tonemap, tm, weight, exposure):
     r.dispose()
 
 
+@pytest.mark.parametrize("view", [(100, 75), (128, 96), (50, 31), (64, 48)])
+def test_display_view_matches_oracle(view):
+    # display.frag's Catmull-Rom branch: the renderer's 64 x 48 targets as the
+    # traced region shown in a view of another size (the reference's preview
+    # while the camera moves); at equal sizes the plain display pass.
+    r = _renderer(W.box_scene(0, 3), 64, 48, 8, seed=3)
+    r.denoise(3)
+    den = r.read_denoised()
+    col, alb, *_ = r.read()
+    for weight, tonemap, tm in ((0.0, "aces", 0), (0.6, "reinhard", 1), (0.3, "none", 2)):
+        img, rgb = r.display(weight, exposure=1.5, tonemap=tonemap, want_float=True, view=view)
+        assert img.shape == (view[1], view[0], 4) and rgb.shape == (view[1], view[0], 3)
+        o = OR.display_view(col, alb, den, view[0], view[1], weight, 1.5, tm)
+        assert np.abs(rgb - o).max() < 1e-4, np.abs(rgb - o).max()
+        q = np.rint(np.clip(o, 0, 1) * 255).astype(np.int32)
+        d = np.abs(img[..., :3].astype(np.int32) - q)
+        assert d.max() <= 1 and (d == 0).mean() > 0.995
+    if view == (64, 48):
+        assert np.array_equal(r.display(0.3, exposure=1.5, tonemap="none"),
+                              r.display(0.3, exposure=1.5, tonemap="none", view=view))
+    r.dispose()
+
+
 def test_render_loop_denoises_then_presents():
     # render() traces samples_per_frame, denoises with atrousLevels(frame)
     # and blends with denoiseWeight(frame), like the reference's render().
