@@ -131,7 +131,9 @@ export interface LucentAddon {
   resize(r: NativeHandle, width: number, height: number): void;
   trace(r: NativeHandle, samples: number): void;
   denoise(r: NativeHandle, levels: number, sigmaL?: number, sigmaN?: number, sigmaP?: number): void;
-  display(r: NativeHandle, denoiseWeight: number, tonemap: 0 | 1 | 2, exposure: number): Uint8Array;
+  /** viewWidth/viewHeight: show the image in a canvas of that size (Catmull-Rom preview upsampling). */
+  display(r: NativeHandle, denoiseWeight: number, tonemap: 0 | 1 | 2, exposure: number, viewWidth?: number,
+          viewHeight?: number): Uint8Array;
   stats(r: NativeHandle): NativeStats;
   read(r: NativeHandle): NativeTargets;
   setMaterials(r: NativeHandle, materials: Float32Array): void;

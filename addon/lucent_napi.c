@@ -612,12 +612,14 @@ static napi_value Denoise(napi_env env, napi_callback_info info) {
   return undefined(env);
 }
 
-/* display(r, denoiseWeight, tonemap (0 ACES, 1 Reinhard, 2 none), exposure)
- * -> Uint8Array RGBA8 canvas (rows bottom to top), renderer.ts:573-591. */
+/* display(r, denoiseWeight, tonemap (0 ACES, 1 Reinhard, 2 none), exposure
+ * [, viewWidth, viewHeight]) -> Uint8Array RGBA8 canvas (rows bottom to top),
+ * renderer.ts:573-591; a view size other than the renderer's shows its image
+ * through display.frag's Catmull-Rom upsampling (the preview). */
 static napi_value Display(napi_env env, napi_callback_info info) {
-  napi_value argv[4];
+  napi_value argv[6];
   size_t argc;
-  args(env, info, 4, argv, &argc);
+  args(env, info, 6, argv, &argc);
   lucent_renderer* r = argc >= 1 ? renderer_arg(env, argv[0]) : NULL;
   if (!r) return NULL;
   double weight = 0, exposure = 1;
@@ -627,10 +629,15 @@ static napi_value Display(napi_env env, napi_callback_info info) {
   if (argc > 3) napi_get_value_double(env, argv[3], &exposure);
   lucent_render_stats st;
   if (lucent_renderer_stats(r, &st)) return throw_last(env);
+  uint32_t vw = st.width, vh = st.height;
+  if (argc > 5) {
+    napi_get_value_uint32(env, argv[4], &vw);
+    napi_get_value_uint32(env, argv[5], &vh);
+  }
   void* px;
-  napi_value out = new_typed(env, napi_uint8_array, 1, (size_t)st.width * st.height * 4, &px);
+  napi_value out = new_typed(env, napi_uint8_array, 1, (size_t)vw * vh * 4, &px);
   if (!out) return NULL;
-  if (lucent_renderer_display(r, (float)weight, tonemap, (float)exposure, (uint8_t*)px, NULL, NULL))
+  if (lucent_renderer_display_view(r, vw, vh, (float)weight, tonemap, (float)exposure, (uint8_t*)px, NULL, NULL))
     return throw_last(env);
   return out;
 }
