@@ -80,7 +80,7 @@ struct PathShadowMulti {
   const uint32_t* queue;
   const float4* so;
   const float4* sd;
-  uint8_t* occ;
+  float4* sh_c;  // per shadow slot: contribution, w = 1 until the ray is found occluded
   const SceneRec* recs;
   const uint16_t* sid;
   int any_alpha;
@@ -105,7 +105,9 @@ struct PathShadowMulti {
   __device__ AlphaAnswer alpha_fast(int sc, int slot, uint32_t key) const {
     return sh::alpha_fast(recs[sc].scene, slot, key);
   }
-  __device__ void shadow(uint32_t k, bool occluded) const { occ[queue[k]] = occluded ? 1 : 0; }
+  __device__ void shadow(uint32_t k, bool occluded) const {
+    if (occluded) sh_c[queue[k]].w = 0.f;
+  }
 };
 
 // ------------------------------------------------------------ kernels
@@ -428,7 +430,8 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
 #pragma unroll
       for (int j = 0; j < 3; j++) {
         if (!(pending >> j & 1u)) continue;
-        if (!P.sh_occ[3 * (size_t)p + j]) rad = rad + f3(P.sh_c[3 * (size_t)p + j]);
+        const float4 c = P.sh_c[3 * (size_t)p + j];
+        if (c.w != 0.f) rad = rad + f3(c);  // unoccluded
       }
     }
     float bsdf_pdf = thr4.w;
@@ -763,8 +766,9 @@ __global__ void k_resolve(Paths P, int cur, int all) {
     float4 r = P.rad[p];
     for (int j = 0; j < 3; j++) {
       const uint32_t s = 3 * p + j;
-      if (!(pending >> j & 1u) || P.sh_occ[s]) continue;
+      if (!(pending >> j & 1u)) continue;
       const float4 c = P.sh_c[s];
+      if (c.w == 0.f) continue;  // occluded
       r.x += c.x;
       r.y += c.y;
       r.z += c.z;
@@ -795,7 +799,7 @@ __global__ void k_resolve_adjoint(Paths P, const __grid_constant__ AdjointDev A,
       const uint32_t s = 3 * p + j;
       if (!(pending >> j & 1u)) continue;
       const float4 c = P.sh_c[s];
-      if (!P.sh_occ[s]) {
+      if (c.w != 0.f) {  // unoccluded
         r.x += c.x;
         r.y += c.y;
         r.z += c.z;
@@ -911,8 +915,9 @@ __device__ __forceinline__ void accumulate_pixel(const Paths& P, const SceneRec&
     // forward render folds resolve into the next shade and this pass).
     const unsigned pending = __float_as_uint(P.tint[p].w) >> kPendShift & 7u;
     for (int j = 0; j < 3; j++) {
-      if (!(pending >> j & 1u) || P.sh_occ[3 * (size_t)p + j]) continue;
+      if (!(pending >> j & 1u)) continue;
       const float4 e = P.sh_c[3 * (size_t)p + j];
+      if (e.w == 0.f) continue;  // occluded
       c = make_float4(c.x + e.x, c.y + e.y, c.z + e.z, c.w);
     }
     if (isnan(c.x) || isnan(c.y) || isnan(c.z) || isinf(c.x) || isinf(c.y) || isinf(c.z)) c = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1018,7 +1023,7 @@ __global__ void k_capture_closest(const uint32_t* __restrict__ cnt, const float4
 // (origin, t_max), (direction, alpha key), (occluded, shadow slot, 0, 0), 0.
 __global__ void k_capture_shadow(const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ queue,
                                  const float4* __restrict__ so, const float4* __restrict__ sd,
-                                 const uint8_t* __restrict__ occ, float4* __restrict__ out,
+                                 const float4* __restrict__ sh_c, float4* __restrict__ out,
                                  uint32_t* __restrict__ count, uint32_t cap) {
   const uint32_t n = *cnt, m = n < cap ? n : cap;
   if (blockIdx.x == 0 && threadIdx.x == 0) *count = n;
@@ -1026,7 +1031,7 @@ __global__ void k_capture_shadow(const uint32_t* __restrict__ cnt, const uint32_
     const uint32_t slot = queue[k];
     out[4 * (size_t)k] = so[k];
     out[4 * (size_t)k + 1] = sd[k];
-    out[4 * (size_t)k + 2] = make_float4((float)occ[slot], __uint_as_float(slot), 0.f, 0.f);
+    out[4 * (size_t)k + 2] = make_float4(sh_c[slot].w == 0.f ? 1.f : 0.f, __uint_as_float(slot), 0.f, 0.f);
     out[4 * (size_t)k + 3] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
@@ -1255,14 +1260,14 @@ int render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
       cudaStreamWaitEvent(M.side, M.ev_fork, 0);
       t = M.side;
     }
-    PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};
+    PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_c, M.recs, M.sid, M.any_alpha};
     TravArgs B{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr,
                nullptr, top};
     launch_shadow_multi(M.wide, aux * 2, top, B, ps, t);
     k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, t>>>(B, ps);
     nl += 2;
     if (capture)
-      k_capture_shadow<<<aux, 256, 0, t>>>(P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ,
+      k_capture_shadow<<<aux, 256, 0, t>>>(P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_c,
                                            M.cap + (size_t)(region + 1) * M.cap_stride * 4, M.cap_count + region + 1,
                                            M.cap_stride);
     nl += capture;
@@ -1342,7 +1347,7 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
         cudaStreamWaitEvent(M.side, M.ev_fork, 0);
         t = M.side;
       }
-      PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_occ, M.recs, M.sid, M.any_alpha};
+      PathShadowMulti ps{P.ctr + kCtrShadow, P.qs, P.sh_o, P.sh_d, P.sh_c, M.recs, M.sid, M.any_alpha};
       TravArgs TB{nullptr, 0, nullptr, 1e-6, 1e30, P.slow2, P.ctr + kCtrSlow2, P.ctr + kCtrWork2, P.ctr + kCtrErr,
                   nullptr, top};
       launch_shadow_multi(M.wide, aux * 2, top, TB, ps, t);

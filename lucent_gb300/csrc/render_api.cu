@@ -342,8 +342,9 @@ static lucent_status alloc_targets(lucent_renderer* r, uint32_t w, uint32_t h) {
 }
 
 // Path buffers for `cap` paths (bytes per path: the 128-byte path record, the
-// radiance, the hit, 3 shadow slots of 3 float4, rng, occlusion flags, queues, slow-path
-// queues, the sort key, the ray streams, the sorted and textured-hit queues).
+// hit, 3 shadow slots of 3 float4 (ray origin + tMax, direction + key,
+// contribution + unoccluded flag), queues, slow-path queues, the sort key,
+// the ray streams, the sorted and textured-hit queues).
 // cudaMemset runs on the legacy default stream, which does not order itself
 // with non-blocking streams (a batch's parts, the side streams): wait for it
 // before any stream's kernels may touch the memory.
@@ -356,7 +357,7 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
                                         uint32_t cap) {
   if (cap <= path_cap) return LUCENT_OK;
   // Per-path arrays in allocation order (bytes per path); each starts on a 256-byte boundary.
-  static const size_t kPer[] = {16 * kPathRecord, 16, 48, 48, 48, 3, 4, 4, 12, 4, 12, 4, 32, 32, 4, 4};
+  static const size_t kPer[] = {16 * kPathRecord, 16, 48, 48, 48, 4, 4, 12, 4, 12, 4, 32, 32, 4, 4};
   size_t total = 0;
   for (size_t b : kPer) total += ((size_t)cap * b + 255) & ~(size_t)255;
   total += (size_t)kSortBins * 4;
@@ -383,7 +384,6 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
   P.sh_o = (float4*)take((size_t)cap * 48);
   P.sh_d = (float4*)take((size_t)cap * 48);
   P.sh_c = (float4*)take((size_t)cap * 48);
-  P.sh_occ = (uint8_t*)take((size_t)cap * 3);
   P.q[0] = (uint32_t*)take((size_t)cap * 4);
   P.q[1] = (uint32_t*)take((size_t)cap * 4);
   P.qs = (uint32_t*)take((size_t)cap * 12);

@@ -54,7 +54,6 @@ struct Paths {
   PathField rad;   // radiance per path
   float4* hit;     // closest hit per position of the bounce's queue
   float4 *sh_o, *sh_d, *sh_c;
-  uint8_t* sh_occ;
   uint32_t* q[2];
   uint32_t* qs;
   uint32_t* slow;
