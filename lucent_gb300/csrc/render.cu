@@ -197,11 +197,11 @@ __device__ __forceinline__ float3 clamp_c(float3 c, int bounce, float uclamp) { 
   return l > uclamp ? c * (uclamp / l) : c;
 }
 
-// Shadow ray j of path p: its slot s = 3p + j holds the contribution +
-// pending flag (and, after the any-hit launch, the occlusion flag), read by
-// resolve per path; the ray itself (origin + tmax, direction + alpha key) is
-// stored at its position in the shadow queue, so the any-hit kernel reads
-// the rays in order.
+// Shadow ray j of path p: its slot s = 3p + j holds the contribution and a
+// flag (w) that the any-hit kernels clear when the ray is occluded, read by
+// resolve per path (the path's flags say which slots are pending); the ray
+// itself (origin + tmax, direction + alpha key) is stored at its position in
+// the shadow queue, so the any-hit kernel reads the rays in order.
 __device__ __forceinline__ void emit_shadow(const Paths& P, uint32_t p, int j, float3 o, float3 d, float tmax,
                                             uint32_t key, float3 c) {
   const uint32_t s = 3 * p + j;
@@ -1249,10 +1249,10 @@ int render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     if (M.any_tex) k_shade_t<SceneTable, false, true><<<shade_blocks, 128, 0, s>>>(P, SceneTable{M.recs, M.sid}, cur, b);
     nl += 1 + (M.any_tex != 0);
     E.mark(kPhShade, s);
-    // This bounce's shadow rays and resolve do not depend on the next bounce's
-    // ray sort and closest hit, nor they on them: they run side by side on two
-    // streams, so the short launches of the deep bounces overlap. Profiling
-    // keeps one stream (phase times).
+    // This bounce's shadow rays do not depend on the next bounce's ray sort
+    // and closest hit, nor they on them: they run side by side on two streams,
+    // so the short launches of the deep bounces overlap; the next shade, which
+    // resolves them, waits for both. Profiling keeps one stream (phase times).
     const bool fork = M.side && !pe && b < M.max_bounces;
     cudaStream_t t = s;
     if (fork) {
@@ -1284,10 +1284,11 @@ int render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     sorted = M.sort_rays && b < M.max_bounces && (b < 2 || (b == 2 && M.total_paths >= (1u << 21)));
     nl += sorted ? 3 : 0;  // keys, scan, scatter
     if (sorted && was_sorted) {
-      // This bounce's resolve (perhaps still running on the side stream) reads
-      // its pre-sort queue in sort_tmp; its sorted queue buffer is free once
-      // shaded, so the next queue is sorted into that one instead, and
-      // sort_tmp becomes the next-but-one queue after the join.
+      // This bounce's pre-sort queue in sort_tmp stays as it is (the backward
+      // replays' resolve, perhaps still running on the side stream, walks it);
+      // its sorted queue buffer is free once shaded, so the next queue is
+      // sorted into that one instead, and sort_tmp becomes the next-but-one
+      // queue after the join.
       uint32_t* busy = P.sort_tmp;
       P.sort_tmp = sort_rays_into(M, P, cur ^ 1, aux, s, P.q[cur]);
       P.q[cur] = busy;
