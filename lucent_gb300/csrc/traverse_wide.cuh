@@ -340,7 +340,6 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
   }
 }
 
-
 // Any hit over the wide view: one ray per thread (grid-stride), as
 // k_anyhit_fast_t. With the cull distance fixed at tMax the answer does not
 // depend on visiting order, and a leaf is reached exactly when its own box
