@@ -419,13 +419,14 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
     const float4 thr4 = first ? first_record_field(2, rd) : P.thr[p];
     const float4 tint4 = first ? first_record_field(3, rd) : P.tint[p];
     float3 thr = f3(thr4), rad = f3(first ? first_record_field(7, rd) : P.rad[p]), tint = f3(tint4);
-    // The forward render resolves the previous bounce's next-event
-    // contributions here (the backward replays keep their resolve kernels):
-    // the unoccluded ones join the radiance first, in the reference's order
-    // (sun, environment, light), as a separate resolve pass would add them.
+    // The forward render and the backward's primal replay resolve the
+    // previous bounce's next-event contributions here (the adjoint replay
+    // keeps its resolve kernel, which also gathers gradients): the unoccluded
+    // ones join the radiance first, in the reference's order (sun,
+    // environment, light), as a separate resolve pass would add them.
     unsigned emitted = 0u;
     const unsigned flags = __float_as_uint(tint4.w);
-    if constexpr (!ADJ) {
+    if (!ADJ || A.primal) {
       const unsigned pending = flags >> kPendShift & 7u;
 #pragma unroll
       for (int j = 0; j < 3; j++) {
@@ -752,32 +753,7 @@ __global__ void __launch_bounds__(128, 4) k_shade_t(Paths P, const __grid_consta
   }
 }
 
-// Adds the unoccluded next-event contributions of this bounce, per path, in
-// the reference's order (sun, environment, light).
-// `all`: the queue holds every path of the wave (bounce 0, whose queue is
-// pixel-major): walk the paths in path order instead, so the reads coalesce.
-__global__ void k_resolve(Paths P, int cur, int all) {
-  const uint32_t n = P.ctr[kCtrQ0 + cur];
-  const uint32_t* q = P.q[cur];
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const uint32_t p = all ? k : q[k];
-    const unsigned pending = __float_as_uint(P.tint[p].w) >> kPendShift & 7u;
-    if (!pending) continue;
-    float4 r = P.rad[p];
-    for (int j = 0; j < 3; j++) {
-      const uint32_t s = 3 * p + j;
-      if (!(pending >> j & 1u)) continue;
-      const float4 c = P.sh_c[s];
-      if (c.w == 0.f) continue;  // occluded
-      r.x += c.x;
-      r.y += c.y;
-      r.z += c.z;
-    }
-    P.rad[p] = r;
-  }
-}
-
-// k_resolve for the adjoint replay: the unoccluded next-event contributions
+// Resolve for the adjoint replay: the unoccluded next-event contributions
 // leave the path's remaining radiance and add their material (and
 // environment) gradients; what remains is the radiance that followed the
 // BSDF-sampled direction, whose gradient is lrem (.) dl (.) df/f.
@@ -830,9 +806,18 @@ __global__ void k_resolve_adjoint(Paths P, const __grid_constant__ AdjointDev A,
 
 // Primal radiance of each replayed sample -> the adjoint replay's remaining
 // radiance (a dropped NaN/inf sample is flagged in w and contributes nothing).
+// The primal replay's last shaded bounce is resolved here, as the forward
+// render's accumulation resolves it.
 __global__ void k_seed_lrem(Paths P, AdjointDev A, uint32_t total) {
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
-    const float4 c = P.rad[p];
+    float4 c = P.rad[p];
+    const unsigned pending = __float_as_uint(P.tint[p].w) >> kPendShift & 7u;
+    for (int j = 0; j < 3; j++) {
+      if (!(pending >> j & 1u)) continue;
+      const float4 e = P.sh_c[3 * (size_t)p + j];
+      if (e.w == 0.f) continue;  // occluded
+      c = make_float4(c.x + e.x, c.y + e.y, c.z + e.z, c.w);
+    }
     const bool bad = isnan(c.x) || isnan(c.y) || isnan(c.z) || isinf(c.x) || isinf(c.y) || isinf(c.z);
     A.lrem[p] = bad ? make_float4(0.f, 0.f, 0.f, 1.f) : make_float4(c.x, c.y, c.z, 0.f);
   }
@@ -1355,9 +1340,7 @@ void render_backward(const MultiLaunch& M, const AdjointDevHost& H, cudaStream_t
       k_anyhit_exact_t<PathShadowMulti><<<64, 128, 0, t>>>(TB, ps);
       Paths Pr = P;  // resolve walks the pre-sort queue, in path order
       if (sorted) Pr.q[cur] = P.sort_tmp;
-      if (pass == 0)
-        k_resolve<<<aux, 128, 0, t>>>(Pr, cur, b == 0);
-      else
+      if (pass == 1)  // the primal replay resolves in its next shade and in k_seed_lrem
         k_resolve_adjoint<<<aux, 128, 0, t>>>(Pr, A, rec, cur);
       if (fork) cudaEventRecord(M.ev_join, t);
       forked = fork;
