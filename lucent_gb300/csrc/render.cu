@@ -222,7 +222,8 @@ __device__ __forceinline__ bool analytic_occluded(const SceneDev& S, float3 ro, 
 // Gradients are of sum_pixels dl[pixel] . (mean radiance of the replayed
 // samples) with respect to each material's base colour (3), roughness,
 // metallic and clearcoat (dmat, 6 floats per material) and to the
-// environment texels (denv, 3 floats per texel). Sampling (directions,
+// environment texels (denv, RGB + one pad float per texel, 16-byte aligned, so
+// that a tap is one vector atomic). Sampling (directions,
 // pdfs, MIS weights, lobe and Russian-roulette choices, the firefly clamp's
 // scale) is held fixed, as in path replay backpropagation.
 struct AdjointDev {
@@ -255,17 +256,19 @@ __device__ __forceinline__ void add_material_grad(float* dmat, int mat, const fl
       if (sum[k] != 0.f) atomicAdd(dmat + (size_t)mat * 6 + k, sum[k]);
 }
 
-// Environment texel gradient: sv_c * bilinear weight into each of 4 texels.
+// Environment texel gradient: sv_c * bilinear weight into each of 4 texels,
+// one float4 atomic per tap (the texels' RGB gradients are float4s).
 __device__ __forceinline__ void add_env_grad(const AdjointDev& A, const LightingDev& L, float2 uv, float3 dl, float3 sv) {
   int idx[4];
   float wt[4];
   bilinear_taps(L.env_w, L.env_h, uv.x, uv.y, true, idx, wt);
   const float g[3] = {dl.x * sv.x, dl.y * sv.y, dl.z * sv.z};
+  float4* const d4 = reinterpret_cast<float4*>(A.denv);
 #pragma unroll
-  for (int k = 0; k < 4; k++)
-#pragma unroll
-    for (int c = 0; c < 3; c++)
-      if (g[c] * wt[k] != 0.f) atomicAdd(A.denv + (size_t)idx[k] * 3 + c, g[c] * wt[k]);
+  for (int k = 0; k < 4; k++) {
+    const float4 v = make_float4(g[0] * wt[k], g[1] * wt[k], g[2] * wt[k], 0.f);
+    if (v.x != 0.f || v.y != 0.f || v.z != 0.f) atomicAdd(d4 + idx[k], v);
+  }
 }
 
 // The clamp_c scale factor (1 when unclamped).

@@ -983,10 +983,12 @@ lucent_status lucent_renderer_backward(lucent_renderer* r, uint32_t samples, uin
   if (st) return st;
   const size_t cap = r->path_cap;
   const size_t nmat = (size_t)scene_owner(r)->material_count * 6;
-  const size_t nenv = d_env ? (size_t)r->light.env_w * r->light.env_h * 3 : 0;
+  const size_t texels = d_env ? (size_t)r->light.env_w * r->light.env_h : 0;
+  const size_t env_off = (nmat + 3) & ~(size_t)3;  // the env gradients: float4 per texel, 16-byte aligned
+  const size_t nenv = texels * 4;
   // per path: lrem 1 + gcont 5 + genv 2 float4; per shadow slot: gslot 2 float4 (3 slots per path)
   if ((st = r->adj_dl.reserve((size_t)WH * 16)) || (st = r->adj_path.reserve(cap * 16 * (1 + 5 + 2 + 6))) ||
-      (st = r->adj_grad.reserve((nmat + nenv) * 4 + 16)))
+      (st = r->adj_grad.reserve((env_off + nenv) * 4 + 16)))
     return st;
   std::vector<float> dl((size_t)WH * 4);
   const float inv = 1.f / (float)samples;
@@ -995,18 +997,18 @@ lucent_status lucent_renderer_backward(lucent_renderer* r, uint32_t samples, uin
     dl[i] = dl_dimage[i] * inv;
   }
   cudaError_t e = cudaMemcpyAsync(r->adj_dl.ptr, dl.data(), dl.size() * 4, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(r->adj_grad.ptr, 0, (nmat + nenv) * 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(r->adj_grad.ptr, 0, (env_off + nenv) * 4, s);
   if (e != cudaSuccess) return cuda_fail(e, "backward setup");
   float4* base = (float4*)r->adj_path.ptr;
   AdjointDevHost H{(const float4*)r->adj_dl.ptr, base, base + cap, base + 6 * cap, base + 12 * cap,
-                   (float*)r->adj_grad.ptr, nenv ? (float*)r->adj_grad.ptr + nmat : nullptr};
+                   (float*)r->adj_grad.ptr, nenv ? (float*)r->adj_grad.ptr + env_off : nullptr};
   for (uint32_t done = 0; done < samples; done += batch) {
     const uint32_t S = std::min(batch, samples - done);
     MultiLaunch M{};
     if ((st = single_launch(r, S, 0, seed + done, s, M))) return st;
     render_backward(M, H, s);
   }
-  std::vector<float> g(nmat + nenv);
+  std::vector<float> g(env_off + nenv);
   e = cudaMemcpyAsync(g.data(), r->adj_grad.ptr, g.size() * 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(e, "backward");
@@ -1017,7 +1019,8 @@ lucent_status lucent_renderer_backward(lucent_renderer* r, uint32_t samples, uin
     return fail(LUCENT_ERR_DEVICE, "backward raised device error word 0x%x", word);
   }
   for (size_t i = 0; i < nmat; i++) d_materials[i] += g[i];
-  for (size_t i = 0; i < nenv; i++) d_env[i] += g[nmat + i];
+  for (size_t i = 0; i < texels; i++)
+    for (int c = 0; c < 3; c++) d_env[3 * i + c] += g[env_off + 4 * i + c];
   return LUCENT_OK;
 }
 

@@ -159,7 +159,7 @@ struct AdjointDevHost {
   const float4* dl;
   float4 *lrem, *gcont, *gslot, *genv;
   float* dmat;
-  float* denv;
+  float* denv;  // environment texel gradients, 4 floats (RGB, pad) per texel, 16-byte aligned
 };
 // Gradient of sum_px dl[px] . (mean of the wave's samples) with respect to
 // material parameters (6 per material) and environment texels, for a launch
