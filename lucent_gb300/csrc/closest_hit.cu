@@ -27,6 +27,9 @@ struct ApiPolicy {
   __device__ uint32_t key(uint32_t) const { return 0; }
   static constexpr bool kMultiScene = false;
   static constexpr int kThreads = 128, kMinBlocks = 7;  // closest-hit block shape
+  // Lanes of a wide-kernel warp that wait before it fetches new rays
+  // (measured on 10^6 random rays into a 65,536-triangle soup: 4 over 1, 8, 16).
+  static constexpr int kRefillMin = 4;
   __device__ bool alpha(int, int, uint32_t, float, float) const { return true; }
   __device__ AlphaAnswer alpha_fast(int, int, uint32_t) const { return kAlphaBlock; }
   __device__ bool alpha_any() const { return false; }

@@ -23,6 +23,7 @@
 //                                                 true if a hit on `slot` at barycentrics (bu, bv) counts
 //   AlphaAnswer alpha_fast(int scene, int slot, uint32_t key)
 //                                                 the same without texture lookups (kAlphaDefer: ask alpha)
+//   static constexpr int kRefillMin               (closest hit) lanes a warp lets wait before it fetches rays
 //   static constexpr bool kMultiScene             rays of several scenes in one launch:
 //   BvhView bvh(uint32_t k) const                 then the k-th ray's BVH (else TravArgs'),
 //   BvhView scene_bvh(int s) const                and scene s's BVH
@@ -269,7 +270,9 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_fast
   while (true) {
     const bool need = !active && !exhausted;
     const unsigned m = __ballot_sync(FULL, need);
-    if (m) {
+    // Refill once Pol::kRefillMin lanes wait (or none is busy): each refill
+    // stalls the whole warp on the atomic and the new rays' loads.
+    if (m && (__popc(m) >= Pol::kRefillMin || __ballot_sync(FULL, active) == 0)) {
       const int leader = __ffs(m) - 1;
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(A.work, (uint32_t)__popc(m));

@@ -151,7 +151,9 @@ __global__ void __launch_bounds__(Pol::kThreads, Pol::kMinBlocks) k_closest_wide
   while (true) {
     const bool need = !active && !exhausted;
     const unsigned m = __ballot_sync(FULL, need);
-    if (m) {
+    // Refill once Pol::kRefillMin lanes wait (or none is busy): each refill
+    // stalls the whole warp on the atomic and the new rays' loads.
+    if (m && (__popc(m) >= Pol::kRefillMin || __ballot_sync(FULL, active) == 0)) {
       const int leader = __ffs(m) - 1;
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(A.work, (uint32_t)__popc(m));
