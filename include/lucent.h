@@ -302,7 +302,12 @@ lucent_status lucent_renderer_reset(lucent_renderer* r);
 /* Sets the next RNG stream index (uSeed); the reference starts at 0. */
 lucent_status lucent_renderer_set_seed(lucent_renderer* r, uint32_t seed);
 /* traceSamples(count) (renderer.ts:702-737): `samples` more samples per
- * pixel into the running average. Asynchronous on `stream`. */
+ * pixel into the running average. Asynchronous on `stream`: the samples are
+ * in the targets for work queued on `stream` after the call. With pipelining
+ * (lucent_renderer_set_pipelining, default on) the paths themselves are
+ * traced on the renderer's own streams and may start before work queued on
+ * `stream` earlier; they read only the renderer's scene, lighting, camera and
+ * settings, and the calls that change those wait for the waves in flight. */
 lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* stream);
 /* Synchronises and reports the device error word. */
 lucent_status lucent_renderer_check(lucent_renderer* r, void* stream);
@@ -310,6 +315,12 @@ lucent_status lucent_renderer_check(lucent_renderer* r, void* stream);
  * color4 / albedo4 / normal4 as width*height*4 floats, history width*height.
  * Row 0 is the bottom row (gl_FragCoord convention). */
 lucent_status lucent_renderer_read(lucent_renderer* r, float* color4, float* albedo4, float* normal4, float* history);
+/* Queues a copy of the colour target (width*height*4 floats, as
+ * lucent_renderer_read) to host memory on `stream` and returns without
+ * waiting; color4 must stay valid until the stream reaches the copy (pinned
+ * memory keeps the copy asynchronous). The counterpart of the reference's
+ * asynchronous readback; lucent_renderer_check(stream) waits for it. */
+lucent_status lucent_renderer_read_color_async(lucent_renderer* r, float* color4, void* stream);
 lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out);
 /* Records CUDA events between the kernels of each trace (the counterpart of
  * the reference's GPU timer queries, renderer.ts:668-700); results appear in
@@ -359,6 +370,14 @@ lucent_status lucent_renderer_set_top_levels(lucent_renderer* r, int32_t enabled
  * grandchildren's boxes lie inside their parents', so the reference's cull
  * decisions and visiting order are unchanged. */
 lucent_status lucent_renderer_set_wide_bvh(lucent_renderer* r, int32_t enabled);
+/* Pipelined waves (default on): successive waves (of one trace or of
+ * successive traces) alternate between two path-state buffers and are traced
+ * on the renderer's own streams, so one wave's last bounces (short launches
+ * that leave most of the GPU idle) run beside the next wave's first bounces;
+ * the accumulation stays on the caller's stream, in call order. Images are the
+ * same either way. Costs a second path buffer (about 400 bytes per path of a
+ * wave). Profiling and ray capture trace without it. */
+lucent_status lucent_renderer_set_pipelining(lucent_renderer* r, int32_t enabled);
 /* A renderer of width x height that renders `src`'s scene: geometry, BVH
  * and its wide view, triangle attributes, materials, spheres, lights and
  * texture arrays are read from src's device memory, not copied. The view

@@ -59,6 +59,7 @@ def declare(L, sig):
     sig(L, "lucent_renderer_trace", [VP, C.c_uint32, VP])
     sig(L, "lucent_renderer_check", [VP, VP])
     sig(L, "lucent_renderer_read", [VP, F32P, F32P, F32P, F32P])
+    sig(L, "lucent_renderer_read_color_async", [VP, F32P, VP])
     sig(L, "lucent_renderer_stats", [VP, P(RenderStats)])
     sig(L, "lucent_renderer_set_profiling", [VP, C.c_int32])
     sig(L, "lucent_renderer_trim", [VP])
@@ -67,6 +68,7 @@ def declare(L, sig):
     sig(L, "lucent_renderer_set_ray_sort", [VP, C.c_int32])
     sig(L, "lucent_renderer_set_top_levels", [VP, C.c_int32])
     sig(L, "lucent_renderer_set_wide_bvh", [VP, C.c_int32])
+    sig(L, "lucent_renderer_set_pipelining", [VP, C.c_int32])
     sig(L, "lucent_renderer_create_view", [VP, C.c_uint32, C.c_uint32, C.POINTER(VP)])
     sig(L, "lucent_renderer_read_textures", [VP, U32P, U8P, U8P])
     sig(L, "lucent_renderer_set_materials", [VP, F32P, C.c_uint32])

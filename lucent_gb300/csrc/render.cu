@@ -1189,7 +1189,7 @@ static void launch_shadow_multi(int wide, int blocks, int top, const TravArgs& A
     k_anyhit_fast_t<PathShadowMulti><<<blocks, 256, top_smem_bytes(top), s>>>(A, ps);
 }
 
-int render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
+int render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe, bool accumulate) {
   int nl = 0;  // kernels launched
   Paths P = M.paths;  // queue buffers swap with the sort buffer below
   PhaseEvents none{nullptr, nullptr, 0, 0};
@@ -1289,10 +1289,16 @@ int render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe) {
     }
   }
   E.mark(kPhResolve, s);
-  k_accumulate_multi<<<grid_for(M.total_pixels, 256), 256, 0, s>>>(P, M.recs, M.pix_base, M.path_base, M.n, M.S);
-  k_advance_seeds<<<1, 64, 0, s>>>(M.recs, M.n, M.S);
+  if (accumulate) nl += accumulate_wave(M, s);
   E.mark(kPhAccumulate, s);
-  return nl + 2;
+  return nl;
+}
+
+int accumulate_wave(const MultiLaunch& M, cudaStream_t s) {
+  k_accumulate_multi<<<grid_for(M.total_pixels, 256), 256, 0, s>>>(M.paths, M.recs, M.pix_base, M.path_base, M.n,
+                                                                     M.S);
+  k_advance_seeds<<<1, 64, 0, s>>>(M.recs, M.n, M.S);
+  return 2;
 }
 
 // ------------------------------------------------------------ path replay backpropagation

@@ -194,7 +194,7 @@ struct WaveGraph {
     if (cap) cudaStreamDestroy(cap);
     cap = nullptr;
   }
-  lucent_status run(const MultiLaunch& M, const uint64_t k[4], cudaStream_t s) {
+  lucent_status run(const MultiLaunch& M, const uint64_t k[4], cudaStream_t s, bool accumulate = true) {
     cudaError_t e;
     if (!exec || std::memcmp(k, key, sizeof key) != 0) {
       drop();
@@ -202,7 +202,7 @@ struct WaveGraph {
         return cuda_fail(e, "capture stream");
       if ((e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
         return cuda_fail(e, "begin capture");
-      launches = render_wave_multi(M, cap);
+      launches = render_wave_multi(M, cap, nullptr, accumulate);
       e = cudaStreamEndCapture(cap, &graph);
       if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
       if (e != cudaSuccess) {
@@ -245,6 +245,48 @@ struct SideStream {
   }
 };
 
+// The path state of one wave and what launches it. A renderer keeps two:
+// successive waves alternate between them, each traced on its set's own
+// stream, so one wave's deep bounces (short, latency-bound launches that
+// leave most SMs idle) run beside the next wave's first bounces. Only the
+// accumulation into the targets runs on the caller's stream, after the wave
+// and in call order.
+struct WaveSet {
+  DeviceBuffer paths, ctr;
+  DeviceBuffer rec, base;  // the wave's SceneRec and path / pixel bases (full and last wave)
+  uint32_t path_cap = 0;
+  Paths P{};
+  WaveGraph graph;  // full waves replay a captured graph (not while profiling)
+  SideStream side;  // second stream of the wave
+  cudaStream_t stream = nullptr;
+  cudaEvent_t traced = nullptr;  // on `stream`: the wave's last bounce is done
+  cudaEvent_t done = nullptr;    // on the caller's stream: the wave is accumulated
+  bool used = false;             // `done` has been recorded
+  lucent_status ensure() {
+    if (stream) return LUCENT_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&traced, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
+    return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "wave stream");
+  }
+  void release_paths() {
+    paths.release();
+    path_cap = 0;
+    P = Paths{};
+    P.ctr = (uint32_t*)ctr.ptr;
+  }
+  void destroy() {
+    for (DeviceBuffer* b : {&paths, &ctr, &rec, &base}) b->release();
+    graph.destroy();
+    side.destroy();
+    if (done) cudaEventDestroy(done);
+    if (traced) cudaEventDestroy(traced);
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+    traced = done = nullptr;
+  }
+};
+
 // Everything a captured wave bakes in besides the buffer contents.
 static void wave_key(const MultiLaunch& M, uint64_t key[4]) {
   key[0] = (uint64_t)(uint32_t)M.S | ((uint64_t)(uint32_t)M.n << 32);
@@ -282,12 +324,14 @@ struct lucent_renderer {
   uint32_t max_bounces = 6;
   float clamp = 8.f;
   // targets and path state
-  DeviceBuffer color, albedo, normal, history, paths, ctr;
-  uint32_t path_cap = 0;
-  Paths P{};
+  DeviceBuffer color, albedo, normal, history;
+  WaveSet set[2];   // set 0 also serves every wave that is not pipelined
+  int next_set = 0;  // set of the next pipelined wave
+  int pipeline = 1;  // alternate the waves between the sets (lucent_renderer_set_pipelining)
   uint32_t frame = 0, seed = 0;
   double last_ms = 0;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // around the last trace (recorded once it traced)
+  bool timed = false;
   // optional per-phase timing (lucent_renderer_set_profiling)
   bool profiling = false;
   bool trav_counters = false;  // closest-hit traversal counters (profiling mode 2)
@@ -299,11 +343,9 @@ struct lucent_renderer {
   DeviceBuffer den_a, den_b, guide0, guide1, disp;
   // path-replay backward pass
   DeviceBuffer adj_dl, adj_path, adj_grad;
-  // a renderer traces as a launch of one scene: its SceneRec, path/pixel bases (full and last wave), scene index per path
-  DeviceBuffer rec1, base1, sid1;
+  // a renderer traces as a launch of one scene: scene index per path (all 0)
+  DeviceBuffer sid1;
   uint32_t sid_cap = 0;
-  WaveGraph wave_graph;  // full waves of a trace replay a captured graph (not while profiling)
-  SideStream side;       // second stream of the waves
   uint32_t waves = 0;
   uint64_t kernel_launches = 0;  // by reset and trace (lucent_render_stats)
   int sort_rays = 1;   // sort the rays of bounces 1 and 2 (lucent_renderer_set_ray_sort)
@@ -404,8 +446,23 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
   return LUCENT_OK;
 }
 
-static lucent_status alloc_paths(lucent_renderer* r, uint32_t cap) {
-  return alloc_path_buffers(r->paths, r->ctr, r->path_cap, r->P, cap);
+static lucent_status alloc_paths(WaveSet& w, uint32_t cap) {
+  return alloc_path_buffers(w.paths, w.ctr, w.path_cap, w.P, cap);
+}
+
+// Orders stream s after every wave of r in flight: the accumulations stay in
+// call order, and a set's buffers are reused only after its wave is done.
+static void after_waves(lucent_renderer* r, cudaStream_t s) {
+  for (WaveSet& w : r->set)
+    if (w.used) cudaStreamWaitEvent(s, w.done, 0);
+}
+
+// Calls that change what a wave reads (geometry, materials, lighting) wait for
+// the waves in flight, which run on streams of their own, and return only
+// once the change is on the device, so a later wave needs no wait for it.
+static lucent_status settle(const char* what) {
+  cudaError_t e = cudaDeviceSynchronize();
+  return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, what);
 }
 
 // buildTextureArrays (renderer.ts:314-333): every referenced image resampled
@@ -503,31 +560,33 @@ static void record_history(lucent_renderer* r) {
   r->hist_h = r->H;
 }
 
-// The renderer as a launch of one scene: uploads its SceneRec (sample seed
-// `seed0`) and the path/pixel bases of a full wave of S samples and of a last
-// wave of `tail` samples; fills M for the full wave.
-static lucent_status single_launch(lucent_renderer* r, uint32_t S, uint32_t tail, uint32_t seed0, cudaStream_t s,
-                                   MultiLaunch& M) {
+// The renderer as a launch of one scene on path set w: uploads its SceneRec
+// (sample seed `seed0`; a pending reprojection only with `first`) and the
+// path/pixel bases of a full wave of S samples and of a last wave of `tail`
+// samples; fills M for the full wave.
+static lucent_status single_launch(lucent_renderer* r, WaveSet& w, uint32_t S, uint32_t tail, uint32_t seed0,
+                                   bool first, cudaStream_t s, MultiLaunch& M) {
   const uint32_t WH = r->W * r->H;
-  lucent_status st = alloc_paths(r, S * WH);
+  lucent_status st = alloc_paths(w, S * WH);
   if (st) return st;
-  if (r->path_cap > r->sid_cap) {
-    if ((st = r->sid1.reserve((size_t)r->path_cap * 2))) return st;
-    if (clear_now(r->sid1.ptr, (size_t)r->path_cap * 2) != cudaSuccess) return cuda_fail(cudaGetLastError(), "clear sid");
-    r->sid_cap = r->path_cap;
+  if (w.path_cap > r->sid_cap) {
+    if ((st = r->sid1.reserve((size_t)w.path_cap * 2))) return st;
+    if (clear_now(r->sid1.ptr, (size_t)w.path_cap * 2) != cudaSuccess) return cuda_fail(cudaGetLastError(), "clear sid");
+    r->sid_cap = w.path_cap;
   }
-  if ((st = r->rec1.reserve(sizeof(SceneRec))) || (st = r->base1.reserve(32))) return st;
+  if ((st = w.rec.reserve(sizeof(SceneRec))) || (st = w.base.reserve(32))) return st;
   SceneRec rec = scene_rec(r);
   rec.seed0 = seed0;
+  if (!first) rec.reproject = 0;
   const uint32_t bases[8] = {0, WH * S, 0, WH, 0, WH * tail, 0, WH};
   // pageable host-to-device copies are staged before the call returns, so the locals may go
-  cudaError_t e = cudaMemcpyAsync(r->rec1.ptr, &rec, sizeof rec, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(r->base1.ptr, bases, sizeof bases, cudaMemcpyHostToDevice, s);
+  cudaError_t e = cudaMemcpyAsync(w.rec.ptr, &rec, sizeof rec, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(w.base.ptr, bases, sizeof bases, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "upload scene record");
   M = MultiLaunch{};
-  M.paths = r->P;
-  M.recs = (SceneRec*)r->rec1.ptr;
-  M.path_base = (const uint32_t*)r->base1.ptr;
+  M.paths = w.P;
+  M.recs = (SceneRec*)w.rec.ptr;
+  M.path_base = (const uint32_t*)w.base.ptr;
   M.pix_base = M.path_base + 2;
   M.sid = (uint16_t*)r->sid1.ptr;
   M.n = 1;
@@ -547,16 +606,16 @@ static lucent_status single_launch(lucent_renderer* r, uint32_t S, uint32_t tail
     M.cap_count = (uint32_t*)r->cap_count.ptr;
     M.cap_stride = r->cap_rays;
   }
-  if (lucent_status st = r->side.ensure()) return st;
-  r->side.set(M);
+  if (lucent_status st = w.side.ensure()) return st;
+  w.side.set(M);
   return LUCENT_OK;
 }
 
 // Switches M to the last wave of `tail` samples.
-static void single_tail(lucent_renderer* r, uint32_t tail, MultiLaunch& M) {
+static void single_tail(lucent_renderer* r, const WaveSet& w, uint32_t tail, MultiLaunch& M) {
   M.S = (int)tail;
   M.total_paths = r->W * r->H * tail;
-  M.path_base = (const uint32_t*)r->base1.ptr + 4;
+  M.path_base = (const uint32_t*)w.base.ptr + 4;
   M.pix_base = M.path_base + 2;
 }
 
@@ -608,11 +667,10 @@ void lucent_renderer_destroy(lucent_renderer* r) {
   if (r->src) r->src->n_views--;
   for (DeviceBuffer* b : {&r->nodes, &r->wide, &r->geo, &r->attr, &r->mats, &r->spheres, &r->sph_mat, &r->sph_light,
                           &r->lights, &r->env_rgb, &r->env_alias, &r->sheen, &r->color, &r->albedo, &r->normal,
-                          &r->history, &r->paths, &r->ctr, &r->den_a, &r->den_b, &r->guide0, &r->guide1, &r->disp, &r->adj_dl, &r->adj_path, &r->adj_grad, &r->rec1, &r->base1, &r->sid1, &r->prev,
+                          &r->history, &r->den_a, &r->den_b, &r->guide0, &r->guide1, &r->disp, &r->adj_dl, &r->adj_path, &r->adj_grad, &r->sid1, &r->prev,
                           &r->color_maps, &r->data_maps, &r->texel_lut})
     b->release();
-  r->wave_graph.destroy();
-  r->side.destroy();
+  for (WaveSet& w : r->set) w.destroy();
   if (r->ev0) cudaEventDestroy(r->ev0);
   if (r->ev1) cudaEventDestroy(r->ev1);
   for (cudaEvent_t e : r->pev) cudaEventDestroy(e);
@@ -641,6 +699,7 @@ lucent_status lucent_renderer_load_scene(lucent_renderer* r, const lucent_scene_
   if (n > (1u << 23)) return fail(LUCENT_ERR_UNSUPPORTED, "%u triangles; the limit is 2^23", n);
   if (d->sphere_count > 64) return fail(LUCENT_ERR_INVALID, "scene has %u spheres; max is 64", d->sphere_count);
   if (d->light_count > 8) return fail(LUCENT_ERR_INVALID, "scene has %u lights; max is 8", d->light_count);
+  if (lucent_status st = settle("load scene")) return st;
   if (d->material_count == 0 || !d->materials) return fail(LUCENT_ERR_INVALID, "scene has no materials");
   const uint32_t M = d->material_count;
   // Map fields hold layer indices: base colour and emissive into the colour
@@ -764,6 +823,7 @@ lucent_status lucent_renderer_load_scene(lucent_renderer* r, const lucent_scene_
   r->any_alpha = any_alpha;
   r->has_scene = true;
   cleanup(LUCENT_OK);
+  if ((st = settle("load scene"))) return st;
   return lucent_renderer_reset(r);
 }
 
@@ -781,7 +841,8 @@ lucent_status lucent_renderer_upload_lighting(lucent_renderer* r, const lucent_l
   if (!env_sampler(l->env_rgb, l->env_width, l->env_height, 1024, gw, gh, table, total))
     return fail(LUCENT_ERR_INVALID, "environment sampler failed");
   lucent_status st;
-  if ((st = upload(r->env_rgb, l->env_rgb, texels * 12)) || (st = upload(r->env_alias, table.data(), table.size() * 4)))
+  if ((st = settle("upload lighting")) || (st = upload(r->env_rgb, l->env_rgb, texels * 12)) ||
+      (st = upload(r->env_alias, table.data(), table.size() * 4)) || (st = settle("upload lighting")))
     return st;
   sh::LightingDev& L = r->light;
   L.sun_enabled = l->sun_enabled;
@@ -814,7 +875,8 @@ static lucent_status set_env_gpu(lucent_renderer* r, const float* rgb, bool on_d
   const size_t texels = (size_t)width * height;
   uint32_t gw, gh;
   env_grid(width, height, 1024, gw, gh);
-  lucent_status st = r->env_rgb.reserve(texels * 12);
+  lucent_status st = settle("set environment");
+  if (!st) st = r->env_rgb.reserve(texels * 12);
   if (!st) st = r->env_alias.reserve((size_t)gw * gh * 16);
   if (st) return st;
   cudaError_t e = cudaMemcpyAsync(r->env_rgb.ptr, rgb, texels * 12,
@@ -832,6 +894,7 @@ static lucent_status set_env_gpu(lucent_renderer* r, const float* rgb, bool on_d
   L.grid_w = (int)gw;
   L.grid_h = (int)gh;
   L.env_sampling = total > 0 ? 1 : 0;  // renderer.ts:412
+  if ((st = settle("set environment"))) return st;
   return lucent_renderer_reset(r);
 }
 
@@ -924,30 +987,67 @@ lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* 
   const uint32_t full = samples / batch, tail = samples % batch;
   MultiLaunch M{};
   lucent_status st = prepare_reprojection(r, s);
-  if (!st) st = single_launch(r, batch, tail, r->seed, s, M);
   if (st) return st;
-  M.trav_stats = r->trav_counters ? (unsigned long long*)((uint32_t*)r->ctr.ptr + kCtrTrav) : nullptr;
-  cudaEventRecord(r->ev0, s);
-  PhaseEvents pe{r->pev.data(), r->ptag.data(), (int)r->pev.size(), 0};
-  uint64_t key[4];
-  wave_key(M, key);
-  for (uint32_t w = 0; w < full + (tail ? 1 : 0); w++) {
-    if (w == full) single_tail(r, tail, M);
-    // The first wave ever runs uncaptured (one-time setup); profiling and ray
-    // capture launch directly.
-    if (w < full && !r->profiling && !r->cap_mask && r->waves > 0) {
-      if ((st = r->wave_graph.run(M, key, s))) return st;
-      r->kernel_launches += r->wave_graph.launches;
-    } else {
-      r->kernel_launches += render_wave_multi(M, s, r->profiling ? &pe : nullptr);  // seeds advance on the device
+  after_waves(r, s);
+  // Profiling (phase events on one stream, traversal counters) and ray
+  // capture keep every wave on the caller's stream, in path set 0.
+  const bool pipelined = r->pipeline && !r->profiling && !r->cap_mask && !r->trav_counters;
+  if (pipelined) {
+    for (uint32_t w = 0; w < full + (tail ? 1 : 0); w++) {
+      WaveSet& X = r->set[r->next_set];
+      r->next_set ^= 1;
+      if ((st = X.ensure())) return st;
+      // The set's previous wave is accumulated (its buffers and record are free).
+      if (X.used) cudaStreamWaitEvent(X.stream, X.done, 0);
+      const uint32_t S = w < full ? batch : tail;
+      if ((st = single_launch(r, X, S, 0, r->seed + w * batch, w == 0, X.stream, M))) return st;
+      if (w == 0) cudaEventRecord(r->ev0, X.stream);
+      // The first wave ever runs uncaptured (one-time setup).
+      if (w < full && r->waves > 0) {
+        uint64_t key[4];
+        wave_key(M, key);
+        key[0] |= 1ull << 63;  // captured without the accumulation
+        if ((st = X.graph.run(M, key, X.stream, false))) return st;
+        r->kernel_launches += X.graph.launches;
+      } else {
+        r->kernel_launches += render_wave_multi(M, X.stream, nullptr, false);
+      }
+      cudaEventRecord(X.traced, X.stream);
+      cudaStreamWaitEvent(s, X.traced, 0);
+      r->kernel_launches += accumulate_wave(M, s);
+      cudaEventRecord(X.done, s);
+      X.used = true;
+      r->waves++;
     }
-    r->waves++;
+  } else {
+    WaveSet& X = r->set[0];
+    if ((st = X.ensure()) || (st = single_launch(r, X, batch, tail, r->seed, true, s, M))) return st;
+    M.trav_stats = r->trav_counters ? (unsigned long long*)((uint32_t*)X.ctr.ptr + kCtrTrav) : nullptr;
+    cudaEventRecord(r->ev0, s);
+    PhaseEvents pe{r->pev.data(), r->ptag.data(), (int)r->pev.size(), 0};
+    uint64_t key[4];
+    wave_key(M, key);
+    for (uint32_t w = 0; w < full + (tail ? 1 : 0); w++) {
+      if (w == full) single_tail(r, X, tail, M);
+      // The first wave ever runs uncaptured (one-time setup); profiling and ray
+      // capture launch directly.
+      if (w < full && !r->profiling && !r->cap_mask && r->waves > 0) {
+        if ((st = X.graph.run(M, key, s))) return st;
+        r->kernel_launches += X.graph.launches;
+      } else {
+        r->kernel_launches += render_wave_multi(M, s, r->profiling ? &pe : nullptr);  // seeds advance on the device
+      }
+      r->waves++;
+    }
+    cudaEventRecord(X.done, s);
+    X.used = true;
+    r->pn = pe.n;
   }
   r->seed += samples;
   r->frame += samples;
   record_history(r);
   cudaEventRecord(r->ev1, s);
-  r->pn = pe.n;
+  r->timed = true;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "trace launch");
 }
@@ -961,8 +1061,10 @@ lucent_status lucent_renderer_set_materials(lucent_renderer* r, const float* mat
     return fail(LUCENT_ERR_INVALID, "scene has %u materials, got %u", o->material_count, count);
   for (size_t i = 0; i < (size_t)count * 40; i++)
     if (!std::isfinite(materials[i])) return fail(LUCENT_ERR_INVALID, "material value %zu is not finite", i);
+  if (lucent_status st = settle("upload materials")) return st;
   cudaError_t e = cudaMemcpy(o->mats.ptr, materials, (size_t)count * 160, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(e, "upload materials");
+  if (lucent_status st = settle("upload materials")) return st;
   return lucent_renderer_reset(r);
 }
 
@@ -979,9 +1081,10 @@ lucent_status lucent_renderer_backward(lucent_renderer* r, uint32_t samples, uin
   const uint32_t WH = r->W * r->H;
   const uint32_t max_paths = 1u << 23;
   const uint32_t batch = std::max(1u, std::min(samples, max_paths / std::max(1u, WH)));
-  lucent_status st = alloc_paths(r, batch * WH);
+  WaveSet& X = r->set[0];
+  lucent_status st = alloc_paths(X, batch * WH);
   if (st) return st;
-  const size_t cap = r->path_cap;
+  const size_t cap = X.path_cap;
   const size_t nmat = (size_t)scene_owner(r)->material_count * 6;
   const size_t texels = d_env ? (size_t)r->light.env_w * r->light.env_h : 0;
   const size_t env_off = (nmat + 3) & ~(size_t)3;  // the env gradients: float4 per texel, 16-byte aligned
@@ -996,6 +1099,7 @@ lucent_status lucent_renderer_backward(lucent_renderer* r, uint32_t samples, uin
     if (!std::isfinite(dl_dimage[i])) return fail(LUCENT_ERR_INVALID, "dl_dimage value %zu is not finite", i);
     dl[i] = dl_dimage[i] * inv;
   }
+  after_waves(r, s);
   cudaError_t e = cudaMemcpyAsync(r->adj_dl.ptr, dl.data(), dl.size() * 4, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(r->adj_grad.ptr, 0, (env_off + nenv) * 4, s);
   if (e != cudaSuccess) return cuda_fail(e, "backward setup");
@@ -1005,7 +1109,7 @@ lucent_status lucent_renderer_backward(lucent_renderer* r, uint32_t samples, uin
   for (uint32_t done = 0; done < samples; done += batch) {
     const uint32_t S = std::min(batch, samples - done);
     MultiLaunch M{};
-    if ((st = single_launch(r, S, 0, seed + done, s, M))) return st;
+    if ((st = single_launch(r, X, S, 0, seed + done, true, s, M))) return st;
     render_backward(M, H, s);
   }
   std::vector<float> g(env_off + nenv);
@@ -1013,9 +1117,9 @@ lucent_status lucent_renderer_backward(lucent_renderer* r, uint32_t samples, uin
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(e, "backward");
   uint32_t word = 0;
-  cudaMemcpy(&word, (uint32_t*)r->ctr.ptr + kCtrErr, 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(&word, (uint32_t*)X.ctr.ptr + kCtrErr, 4, cudaMemcpyDeviceToHost);
   if (word) {
-    clear_now((uint32_t*)r->ctr.ptr + kCtrErr, 4);
+    clear_now((uint32_t*)X.ctr.ptr + kCtrErr, 4);
     return fail(LUCENT_ERR_DEVICE, "backward raised device error word 0x%x", word);
   }
   for (size_t i = 0; i < nmat; i++) d_materials[i] += g[i];
@@ -1058,15 +1162,19 @@ lucent_status lucent_renderer_set_wide_bvh(lucent_renderer* r, int32_t enabled) 
   return LUCENT_OK;
 }
 
+lucent_status lucent_renderer_set_pipelining(lucent_renderer* r, int32_t enabled) {
+  clear_error();
+  if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  r->pipeline = enabled ? 1 : 0;
+  return LUCENT_OK;
+}
+
 lucent_status lucent_renderer_trim(lucent_renderer* r) {
   clear_error();
   if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
   cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return cuda_fail(e, "synchronize");
-  r->paths.release();
-  r->path_cap = 0;
-  r->P = Paths{};
-  r->P.ctr = (uint32_t*)r->ctr.ptr;
+  for (WaveSet& w : r->set) w.release_paths();
   return LUCENT_OK;
 }
 
@@ -1147,12 +1255,16 @@ lucent_status lucent_renderer_check(lucent_renderer* r, void* stream) {
   if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
   cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "synchronize");
-  if (!r->ctr.ptr) return LUCENT_OK;
   uint32_t word = 0;
-  e = cudaMemcpy(&word, (uint32_t*)r->ctr.ptr + kCtrErr, 4, cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return cuda_fail(e, "read error word");
+  WaveSet* bad = nullptr;
+  for (WaveSet& w : r->set) {
+    if (!w.ctr.ptr || word) continue;
+    e = cudaMemcpy(&word, (uint32_t*)w.ctr.ptr + kCtrErr, 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "read error word");
+    if (word) bad = &w;
+  }
   float ms = 0;
-  if (cudaEventElapsedTime(&ms, r->ev0, r->ev1) == cudaSuccess) r->last_ms = ms;
+  if (r->timed && cudaEventElapsedTime(&ms, r->ev0, r->ev1) == cudaSuccess) r->last_ms = ms;
   if (r->profiling && r->pn > 1) {
     for (double& v : r->phase_ms) v = 0;
     for (int i = 1; i < r->pn; i++) {
@@ -1163,7 +1275,7 @@ lucent_status lucent_renderer_check(lucent_renderer* r, void* stream) {
     r->pn = 0;
   }
   if (word) {
-    clear_now((uint32_t*)r->ctr.ptr + kCtrErr, 4);
+    clear_now((uint32_t*)bad->ctr.ptr + kCtrErr, 4);
     return fail(LUCENT_ERR_DEVICE, "render raised device error word 0x%x", word);
   }
   return LUCENT_OK;
@@ -1187,6 +1299,14 @@ lucent_status lucent_renderer_read(lucent_renderer* r, float* color4, float* alb
     tmp.release();
   }
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "read targets");
+}
+
+lucent_status lucent_renderer_read_color_async(lucent_renderer* r, float* color4, void* stream) {
+  clear_error();
+  if (!r || !color4) return fail(LUCENT_ERR_INVALID, "null argument");
+  cudaError_t e = cudaMemcpyAsync(color4, r->color.ptr, (size_t)r->W * r->H * 16, cudaMemcpyDeviceToHost,
+                                  (cudaStream_t)stream);
+  return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "read colour target");
 }
 
 lucent_status lucent_renderer_denoise(lucent_renderer* r, uint32_t levels, float sigma_l, float sigma_n,
@@ -1257,18 +1377,19 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
   out->height = r->H;
   out->triangles = scene_owner(r)->tri_count;
   out->bvh_nodes = scene_owner(r)->node_count;
-  if (r->ctr.ptr) {
+  for (WaveSet& w : r->set) {
+    if (!w.ctr.ptr) continue;
     uint64_t c[2] = {0, 0};
-    cudaError_t e = cudaMemcpy(c, (uint32_t*)r->ctr.ptr + kCtrStatClosest, 16, cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaMemcpy(c, (uint32_t*)w.ctr.ptr + kCtrStatClosest, 16, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "read stats");
-    out->closest_rays = c[0];
-    out->shadow_rays = c[1];
+    out->closest_rays += c[0];
+    out->shadow_rays += c[1];
   }
   out->last_trace_ms = r->last_ms;
   out->kernel_launches = r->kernel_launches;
   for (int k = 0; k < kPhases; k++) out->phase_ms[k] = r->phase_ms[k];
-  if (r->ctr.ptr) {
-    cudaError_t e = cudaMemcpy(out->traversal, (uint32_t*)r->ctr.ptr + kCtrTrav, 40, cudaMemcpyDeviceToHost);
+  if (r->set[0].ctr.ptr) {  // profiling mode 2 traces in set 0
+    cudaError_t e = cudaMemcpy(out->traversal, (uint32_t*)r->set[0].ctr.ptr + kCtrTrav, 40, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "read traversal counters");
   }
   return LUCENT_OK;

@@ -150,8 +150,11 @@ struct PhaseEvents {
 // One wave of S samples for every scene of a launch (a single renderer is a
 // launch of one scene: the same kernels, so a batch reproduces it bit for
 // bit). Graph-safe: no host synchronisation, every count stays on the device.
-// Returns the number of kernels it launched.
-int render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe = nullptr);
+// Returns the number of kernels it launched. Without `accumulate` it stops
+// after the last bounce: accumulate_wave then adds the wave's samples to the
+// targets (and advances the seeds), on any stream ordered after it.
+int render_wave_multi(const MultiLaunch& M, cudaStream_t s, PhaseEvents* pe = nullptr, bool accumulate = true);
+int accumulate_wave(const MultiLaunch& M, cudaStream_t s);
 
 // Device buffers of a path-replay backward pass (per path: lrem 1, gcont 5,
 // genv 2 float4; per shadow slot: gslot 2 float4; dl per pixel).

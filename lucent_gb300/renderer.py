@@ -239,6 +239,18 @@ class Renderer:
         """Closest hit over the four-wide BVH view (lucent_renderer_set_wide_bvh)."""
         N.check(N.lib().lucent_renderer_set_wide_bvh(self._h, 1 if enabled else 0))
 
+    def set_pipelining(self, enabled=True):
+        """Alternate successive waves between two path buffers traced on the
+        renderer's own streams (lucent_renderer_set_pipelining; default on)."""
+        N.check(N.lib().lucent_renderer_set_pipelining(self._h, 1 if enabled else 0))
+
+    def read_color_async(self, out, stream=None):
+        """Queues a copy of the colour target into `out` (a pinned torch or
+        numpy float32 buffer of width*height*4, alive until the stream reaches
+        the copy) and returns; check(stream) waits for it."""
+        ptr = out.data_ptr() if hasattr(out, "data_ptr") else out.ctypes.data
+        N.check(N.lib().lucent_renderer_read_color_async(self._h, C.cast(ptr, N.F32P), stream))
+
     def set_top_levels(self, enabled=True):
         """Stage the top BVH levels in shared memory (lucent_renderer_set_top_levels)."""
         N.check(N.lib().lucent_renderer_set_top_levels(self._h, 1 if enabled else 0))

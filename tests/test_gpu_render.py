@@ -181,6 +181,43 @@ def test_graph_replay_changes_no_pixel():
     assert all(np.array_equal(a, b) for a, b in zip(*out))
 
 
+def test_pipelined_waves_change_no_pixel():
+    # Pipelining alternates successive waves between two path buffers traced
+    # on the renderer's own streams; only the accumulation runs on the
+    # caller's stream, in call order. The images equal wave-by-wave tracing
+    # bit for bit: across the waves of one trace (full waves and a last
+    # partial one), across traces, through a camera move that reprojects the
+    # history, a material change and an accumulation reset.
+    import copy
+    sc = W.box_scene(2, 3)
+    cam2 = copy.deepcopy(sc.camera)
+    cam2.position = (sc.camera.position[0] + 0.05, sc.camera.position[1], sc.camera.position[2])
+    out = []
+    for on in (True, False):
+        r = Renderer(1024, 1024)  # 2^23 paths a wave: waves of 8 samples
+        r.settings.max_bounces = 4
+        r.load_scene(sc)
+        r.set_pipelining(on)
+        r.set_seed(3)
+        r.trace_samples(20)  # 8 + 8 + 4
+        r.trace_samples(3)
+        r.trace_samples(5)
+        r.upload_camera(cam2)  # temporal on: the next sample reprojects the history
+        r.trace_samples(2)
+        r.trace_samples(9)  # 8 + 1
+        imgs = [a.copy() for a in r.read()]
+        from lucent_gb300 import adjoint as AD
+        m = np.array(r.packed.materials, np.float32).reshape(-1, 40)
+        m[:, 0] *= 0.5  # albedo red
+        AD.set_materials(r, m)
+        r.trace_samples(4)
+        r.reset()
+        r.trace_samples(11)
+        out.append(imgs + list(r.read()))
+        r.dispose()
+    assert all(np.array_equal(a, b) for a, b in zip(*out))
+
+
 def test_kernel_launch_count():
     # lucent_render_stats.kernel_launches: a wave launches the camera kernel,
     # 7 kernels a bounce, a shade-counter reset for each bounce after the
