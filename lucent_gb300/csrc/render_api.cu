@@ -253,8 +253,9 @@ struct SideStream {
 // and in call order.
 struct WaveSet {
   DeviceBuffer paths, ctr;
-  DeviceBuffer rec, base;  // the wave's SceneRec and path / pixel bases (full and last wave)
-  uint32_t path_cap = 0;
+  DeviceBuffer rec, base;  // the wave's scene records and path / pixel bases
+  DeviceBuffer sid;        // scene index per path (written by the camera kernel)
+  uint32_t path_cap = 0, sid_cap = 0;
   Paths P{};
   WaveGraph graph;  // full waves replay a captured graph (not while profiling)
   SideStream side;  // second stream of the wave
@@ -275,8 +276,11 @@ struct WaveSet {
     P = Paths{};
     P.ctr = (uint32_t*)ctr.ptr;
   }
+  // Path buffers and scene indices for `cap` paths.
+  lucent_status reserve(uint32_t cap);
   void destroy() {
-    for (DeviceBuffer* b : {&paths, &ctr, &rec, &base}) b->release();
+    for (DeviceBuffer* b : {&paths, &ctr, &rec, &base, &sid}) b->release();
+    sid_cap = 0;
     graph.destroy();
     side.destroy();
     if (done) cudaEventDestroy(done);
@@ -343,9 +347,6 @@ struct lucent_renderer {
   DeviceBuffer den_a, den_b, guide0, guide1, disp;
   // path-replay backward pass
   DeviceBuffer adj_dl, adj_path, adj_grad;
-  // a renderer traces as a launch of one scene: scene index per path (all 0)
-  DeviceBuffer sid1;
-  uint32_t sid_cap = 0;
   uint32_t waves = 0;
   uint64_t kernel_launches = 0;  // by reset and trace (lucent_render_stats)
   int sort_rays = 1;   // sort the rays of bounces 1 and 2 (lucent_renderer_set_ray_sort)
@@ -446,8 +447,13 @@ static lucent_status alloc_path_buffers(DeviceBuffer& paths, DeviceBuffer& ctr, 
   return LUCENT_OK;
 }
 
-static lucent_status alloc_paths(WaveSet& w, uint32_t cap) {
-  return alloc_path_buffers(w.paths, w.ctr, w.path_cap, w.P, cap);
+lucent_status WaveSet::reserve(uint32_t cap) {
+  lucent_status st = alloc_path_buffers(paths, ctr, path_cap, P, cap);
+  if (st || cap <= sid_cap) return st;
+  if ((st = sid.reserve((size_t)cap * 2))) return st;
+  if (clear_now(sid.ptr, (size_t)cap * 2) != cudaSuccess) return cuda_fail(cudaGetLastError(), "clear sid");
+  sid_cap = cap;
+  return LUCENT_OK;
 }
 
 // Orders stream s after every wave of r in flight: the accumulations stay in
@@ -567,13 +573,8 @@ static void record_history(lucent_renderer* r) {
 static lucent_status single_launch(lucent_renderer* r, WaveSet& w, uint32_t S, uint32_t tail, uint32_t seed0,
                                    bool first, cudaStream_t s, MultiLaunch& M) {
   const uint32_t WH = r->W * r->H;
-  lucent_status st = alloc_paths(w, S * WH);
+  lucent_status st = w.reserve(S * WH);
   if (st) return st;
-  if (w.path_cap > r->sid_cap) {
-    if ((st = r->sid1.reserve((size_t)w.path_cap * 2))) return st;
-    if (clear_now(r->sid1.ptr, (size_t)w.path_cap * 2) != cudaSuccess) return cuda_fail(cudaGetLastError(), "clear sid");
-    r->sid_cap = w.path_cap;
-  }
   if ((st = w.rec.reserve(sizeof(SceneRec))) || (st = w.base.reserve(32))) return st;
   SceneRec rec = scene_rec(r);
   rec.seed0 = seed0;
@@ -588,7 +589,7 @@ static lucent_status single_launch(lucent_renderer* r, WaveSet& w, uint32_t S, u
   M.recs = (SceneRec*)w.rec.ptr;
   M.path_base = (const uint32_t*)w.base.ptr;
   M.pix_base = M.path_base + 2;
-  M.sid = (uint16_t*)r->sid1.ptr;
+  M.sid = (uint16_t*)w.sid.ptr;
   M.n = 1;
   M.S = (int)S;
   M.max_bounces = (int)r->max_bounces;
@@ -667,7 +668,7 @@ void lucent_renderer_destroy(lucent_renderer* r) {
   if (r->src) r->src->n_views--;
   for (DeviceBuffer* b : {&r->nodes, &r->wide, &r->geo, &r->attr, &r->mats, &r->spheres, &r->sph_mat, &r->sph_light,
                           &r->lights, &r->env_rgb, &r->env_alias, &r->sheen, &r->color, &r->albedo, &r->normal,
-                          &r->history, &r->den_a, &r->den_b, &r->guide0, &r->guide1, &r->disp, &r->adj_dl, &r->adj_path, &r->adj_grad, &r->sid1, &r->prev,
+                          &r->history, &r->den_a, &r->den_b, &r->guide0, &r->guide1, &r->disp, &r->adj_dl, &r->adj_path, &r->adj_grad, &r->prev,
                           &r->color_maps, &r->data_maps, &r->texel_lut})
     b->release();
   for (WaveSet& w : r->set) w.destroy();
@@ -1082,7 +1083,7 @@ lucent_status lucent_renderer_backward(lucent_renderer* r, uint32_t samples, uin
   const uint32_t max_paths = 1u << 23;
   const uint32_t batch = std::max(1u, std::min(samples, max_paths / std::max(1u, WH)));
   WaveSet& X = r->set[0];
-  lucent_status st = alloc_paths(X, batch * WH);
+  lucent_status st = X.reserve(batch * WH);
   if (st) return st;
   const size_t cap = X.path_cap;
   const size_t nmat = (size_t)scene_owner(r)->material_count * 6;
@@ -1403,11 +1404,11 @@ lucent_status lucent_renderer_stats(lucent_renderer* r, lucent_render_stats* out
 struct lucent_batch {
   std::vector<lucent_renderer*> rs;
   lucent_batch_options opt{0, 1u << 25, 1, 0, 0, 1, 1, 1, 0, 1};
-  DeviceBuffer recs, bases, sid, paths, ctr;
-  uint32_t path_cap = 0, sid_cap = 0;
-  Paths P{};
-  std::vector<WaveGraph> graphs;  // a captured full wave per group of scenes
-  SideStream side;                // second stream of the waves
+  // Pipelined as a renderer's waves: successive waves alternate between the
+  // two sets, each traced on its set's stream, accumulated on the caller's.
+  WaveSet set[2];
+  int next_set = 0;
+  std::vector<WaveGraph> graphs[2];  // per set: a captured full wave per group of scenes
   // opt.streams > 1: consecutive parts of the renderers traced as batches of
   // their own, side by side on their own streams
   std::vector<lucent_batch*> parts;
@@ -1415,11 +1416,14 @@ struct lucent_batch {
   uint32_t waves = 0, graph_waves = 0;
   uint64_t kernel_launches = 0;  // by its traces (lucent_batch_stats)
   void drop_graphs() {
-    for (WaveGraph& g : graphs) g.drop();
+    for (std::vector<WaveGraph>& gs : graphs)
+      for (WaveGraph& g : gs) g.drop();
   }
   void destroy_graphs() {
-    for (WaveGraph& g : graphs) g.destroy();
-    graphs.clear();
+    for (std::vector<WaveGraph>& gs : graphs) {
+      for (WaveGraph& g : gs) g.destroy();
+      gs.clear();
+    }
   }
 };
 
@@ -1453,8 +1457,7 @@ void lucent_batch_destroy(lucent_batch* b) {
   if (!b) return;
   drop_parts(b);
   b->destroy_graphs();
-  b->side.destroy();
-  for (DeviceBuffer* d : {&b->recs, &b->bases, &b->sid, &b->paths, &b->ctr}) d->release();
+  for (WaveSet& w : b->set) w.destroy();
   delete b;
 }
 
@@ -1582,27 +1585,26 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
   (void)max_bounces;
   (void)any_alpha;
   const uint32_t cap = (uint32_t)cap64;
-  lucent_status st = alloc_path_buffers(b->paths, b->ctr, b->path_cap, b->P, cap);
-  if (st) return st;
-  if (cap > b->sid_cap) {
-    if ((st = b->sid.reserve((size_t)cap * 2))) return st;
-    if (clear_now(b->sid.ptr, (size_t)cap * 2) != cudaSuccess) return cuda_fail(cudaGetLastError(), "clear sid");
-    b->sid_cap = cap;
-    b->drop_graphs();
+  lucent_status st;
+  for (WaveSet& X : b->set) {
+    if ((st = X.ensure()) || (st = X.side.ensure())) return st;
+    if (X.used) cudaStreamWaitEvent(X.stream, X.done, 0);  // the set's last wave is accumulated
+    const uint32_t had = X.path_cap;
+    if ((st = X.reserve(cap))) return st;
+    if (X.path_cap != had) b->drop_graphs();  // new buffer addresses
+    if ((st = X.rec.reserve(sizeof(SceneRec) * n)) || (st = X.base.reserve(4 * hb.size()))) return st;
+    cudaError_t e = cudaMemcpyAsync(X.base.ptr, hb.data(), 4 * hb.size(), cudaMemcpyHostToDevice, X.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "upload batch tables");
   }
-  if ((st = b->recs.reserve(sizeof(SceneRec) * n)) || (st = b->bases.reserve(4 * hb.size()))) return st;
-  cudaError_t e = cudaMemcpyAsync(b->recs.ptr, recs.data(), sizeof(SceneRec) * n, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(b->bases.ptr, hb.data(), 4 * hb.size(), cudaMemcpyHostToDevice, s);
-  if (e != cudaSuccess) return cuda_fail(e, "upload batch tables");
-  if (b->graphs.size() != gs.size()) {
-    b->destroy_graphs();
-    b->graphs.resize(gs.size());
-  }
-  if ((st = b->side.ensure())) return st;
+  for (lucent_renderer* r : b->rs) after_waves(r, s);  // the renderers' own traces accumulate first
+  for (std::vector<WaveGraph>& g : b->graphs)
+    if (g.size() != gs.size()) {
+      b->destroy_graphs();
+      b->graphs[0].resize(gs.size());
+      b->graphs[1].resize(gs.size());
+      break;
+    }
   MultiLaunch M{};
-  b->side.set(M);
-  M.paths = b->P;
-  M.sid = (uint16_t*)b->sid.ptr;
   M.trace_blocks = (int)b->opt.trace_blocks;
   M.shade_blocks = (int)b->opt.shade_blocks;
   M.sort_rays = b->opt.sort_rays;
@@ -1611,36 +1613,51 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
   for (size_t g = 0; g < gs.size(); g++) {
     const Group& G = gs[g];
     const int ng = G.i1 - G.i0;
-    M.recs = (SceneRec*)b->recs.ptr + G.i0;
     M.n = ng;
     M.max_bounces = G.max_bounces;
     M.any_alpha = G.any_alpha;
     M.any_tex = G.any_tex;
     M.total_pixels = (uint32_t)G.pixels;
     M.sort_classes = G.classes;
-    auto setup = [&](uint32_t s_wave, size_t base) {
-      M.S = (int)s_wave;
-      M.total_paths = (uint32_t)(G.pixels * s_wave);
-      M.path_base = (const uint32_t*)b->bases.ptr + base;
-      M.pix_base = M.path_base + (ng + 1);
-    };
-    for (uint32_t w = 0; w < G.full; w++) {
-      setup(G.S, G.base);
-      uint64_t key[4];
-      wave_key(M, key);
-      if (b->opt.use_graph && b->waves > 0) {  // first wave ever runs uncaptured (one-time setup inside)
-        const lucent_status gst = b->graphs[g].run(M, key, s);
-        if (gst) return gst;
-        b->graph_waves++;
-        b->kernel_launches += b->graphs[g].launches;
-      } else {
-        b->kernel_launches += render_wave_multi(M, s);
+    for (uint32_t w = 0; w < G.full + (G.tail ? 1u : 0u); w++) {
+      const int x = b->next_set;
+      WaveSet& X = b->set[x];
+      b->next_set ^= 1;
+      if (X.used) cudaStreamWaitEvent(X.stream, X.done, 0);
+      // the group's scene records with this wave's sample seeds (a pending
+      // reprojection in the group's first wave only)
+      std::vector<SceneRec> wr(recs.begin() + G.i0, recs.begin() + G.i1);
+      for (int i = 0; i < ng; i++) {
+        wr[i].seed0 = b->rs[G.i0 + i]->seed + w * G.S;
+        if (w > 0) wr[i].reproject = 0;
       }
-      b->waves++;
-    }
-    if (G.tail) {
-      setup(G.tail, G.base + 2 * (ng + 1));
-      b->kernel_launches += render_wave_multi(M, s);
+      cudaError_t e = cudaMemcpyAsync((SceneRec*)X.rec.ptr + G.i0, wr.data(), sizeof(SceneRec) * ng,
+                                      cudaMemcpyHostToDevice, X.stream);
+      if (e != cudaSuccess) return cuda_fail(e, "upload scene records");
+      M.paths = X.P;
+      M.sid = (uint16_t*)X.sid.ptr;
+      X.side.set(M);
+      M.recs = (SceneRec*)X.rec.ptr + G.i0;
+      const bool full = w < G.full;
+      M.S = (int)(full ? G.S : G.tail);
+      M.total_paths = (uint32_t)(G.pixels * (uint32_t)M.S);
+      M.path_base = (const uint32_t*)X.base.ptr + G.base + (full ? 0 : 2 * (ng + 1));
+      M.pix_base = M.path_base + (ng + 1);
+      if (full && b->opt.use_graph && b->waves > 0) {  // first wave ever runs uncaptured (one-time setup inside)
+        uint64_t key[4];
+        wave_key(M, key);
+        key[0] |= 1ull << 63;  // captured without the accumulation
+        if ((st = b->graphs[x][g].run(M, key, X.stream, false))) return st;
+        b->graph_waves++;
+        b->kernel_launches += b->graphs[x][g].launches;
+      } else {
+        b->kernel_launches += render_wave_multi(M, X.stream, nullptr, false);
+      }
+      cudaEventRecord(X.traced, X.stream);
+      cudaStreamWaitEvent(s, X.traced, 0);
+      b->kernel_launches += accumulate_wave(M, s);
+      cudaEventRecord(X.done, s);
+      X.used = true;
       b->waves++;
     }
   }
@@ -1649,7 +1666,7 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
     r->frame += samples;
     record_history(r);
   }
-  e = cudaGetLastError();
+  cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "batch trace launch");
 }
 
@@ -1670,25 +1687,29 @@ lucent_status lucent_batch_check(lucent_batch* b, void* stream, lucent_batch_sta
     acc.wave_paths += ps.wave_paths;
     acc.kernel_launches += ps.kernel_launches;
   }
-  if (out) *out = acc;
-  if (!b->ctr.ptr) return LUCENT_OK;
-  uint32_t words[kCtrWords];
-  e = cudaMemcpy(words, b->ctr.ptr, sizeof words, cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return cuda_fail(e, "read batch counters");
   if (out) {
-    uint64_t c = 0, sh = 0;
-    std::memcpy(&c, words + kCtrStatClosest, 8);
-    std::memcpy(&sh, words + kCtrStatShadow, 8);
-    out->closest_rays += c;
-    out->shadow_rays += sh;
+    *out = acc;
     out->waves += b->waves;
     out->graph_waves += b->graph_waves;
-    out->wave_paths += b->path_cap;
+    out->wave_paths += std::max(b->set[0].path_cap, b->set[1].path_cap);
     out->kernel_launches += b->kernel_launches;
   }
-  if (words[kCtrErr]) {
-    clear_now((uint32_t*)b->ctr.ptr + kCtrErr, 4);
-    return fail(LUCENT_ERR_DEVICE, "batch raised device error word 0x%x", words[kCtrErr]);
+  for (WaveSet& X : b->set) {
+    if (!X.ctr.ptr) continue;
+    uint32_t words[kCtrWords];
+    e = cudaMemcpy(words, X.ctr.ptr, sizeof words, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "read batch counters");
+    if (out) {
+      uint64_t c = 0, sh = 0;
+      std::memcpy(&c, words + kCtrStatClosest, 8);
+      std::memcpy(&sh, words + kCtrStatShadow, 8);
+      out->closest_rays += c;
+      out->shadow_rays += sh;
+    }
+    if (words[kCtrErr]) {
+      clear_now((uint32_t*)X.ctr.ptr + kCtrErr, 4);
+      return fail(LUCENT_ERR_DEVICE, "batch raised device error word 0x%x", words[kCtrErr]);
+    }
   }
   return LUCENT_OK;
 }
