@@ -665,6 +665,7 @@ lucent_status lucent_renderer_create_view(lucent_renderer* src, uint32_t width, 
 
 void lucent_renderer_destroy(lucent_renderer* r) {
   if (!r) return;
+  cudaDeviceSynchronize();  // waves in flight on the renderer's own streams read its buffers
   if (r->src) r->src->n_views--;
   for (DeviceBuffer* b : {&r->nodes, &r->wide, &r->geo, &r->attr, &r->mats, &r->spheres, &r->sph_mat, &r->sph_light,
                           &r->lights, &r->env_rgb, &r->env_alias, &r->sheen, &r->color, &r->albedo, &r->normal,
@@ -1455,6 +1456,7 @@ static void drop_parts(lucent_batch* b) {
 
 void lucent_batch_destroy(lucent_batch* b) {
   if (!b) return;
+  cudaDeviceSynchronize();  // waves in flight on the batch's own streams read its buffers
   drop_parts(b);
   b->destroy_graphs();
   for (WaveSet& w : b->set) w.destroy();
