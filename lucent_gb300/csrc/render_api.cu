@@ -265,10 +265,17 @@ struct WaveSet {
   bool used = false;             // `done` has been recorded
   lucent_status ensure() {
     if (stream) return LUCENT_OK;
-    cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&traced, cudaEventDisableTiming);
+    cudaError_t e = cudaEventCreateWithFlags(&traced, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
-    return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "wave stream");
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {  // nothing half made: the next call tries again
+      if (done) cudaEventDestroy(done);
+      if (traced) cudaEventDestroy(traced);
+      traced = done = nullptr;
+      stream = nullptr;
+      return cuda_fail(e, "wave stream");
+    }
+    return LUCENT_OK;
   }
   void release_paths() {
     paths.release();
