@@ -117,6 +117,18 @@ export class NativeRenderer {
     native.resize(this.handle, width, height);
   }
 
+  /** traceSamples (renderer.ts:702): with wait = false the call returns once the samples are queued,
+   *  so a frame loop's next trace starts beside this one's last bounces; render, stats and the
+   *  read-back wait for them. */
+  trace(samples: number, wait = true): void {
+    native.trace(this.handle, samples, wait);
+  }
+
+  /** Pipelined waves (default on; images identical either way). */
+  setPipelining(on: boolean): void {
+    native.setPipelining(this.handle, on);
+  }
+
   /** render() (renderer.ts:552): accumulate, denoise, display into an RGBA8 canvas. */
   render(samples: number, denoiseLevels: number, denoiseWeight: number, tonemap: keyof typeof TONEMAPS,
          exposure: number): Uint8Array {

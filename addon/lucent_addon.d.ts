@@ -129,7 +129,10 @@ export interface LucentAddon {
   applySettings(r: NativeHandle, settings: NativeSettings): void;
   reset(r: NativeHandle): void;
   resize(r: NativeHandle, width: number, height: number): void;
-  trace(r: NativeHandle, samples: number): void;
+  /** wait = false: return once the samples are queued (read, display and stats wait for them). */
+  trace(r: NativeHandle, samples: number, wait?: boolean): void;
+  /** Successive waves alternate between two path buffers on the renderer's own streams (default on). */
+  setPipelining(r: NativeHandle, on: boolean): void;
   denoise(r: NativeHandle, levels: number, sigmaL?: number, sigmaN?: number, sigmaP?: number): void;
   /** viewWidth/viewHeight: show the image in a canvas of that size (Catmull-Rom preview upsampling). */
   display(r: NativeHandle, denoiseWeight: number, tonemap: 0 | 1 | 2, exposure: number, viewWidth?: number,

@@ -581,17 +581,36 @@ static napi_value Resize(napi_env env, napi_callback_info info) {
   return undefined(env);
 }
 
-/* trace(r, samples): the accumulation half of render() (renderer.ts:552-620,
- * the traceSamples draw loop :702-736); returns after the samples finished. */
+/* trace(r, samples, wait = true): the accumulation half of render()
+ * (renderer.ts:552-620, the traceSamples draw loop :702-736). With wait it
+ * returns after the samples finished; with wait = false it returns once they
+ * are queued, so that the next frame's waves can start beside this frame's
+ * last bounces (pipelined waves); read, display and stats wait for them. */
 static napi_value Trace(napi_env env, napi_callback_info info) {
+  napi_value argv[3];
+  size_t argc;
+  args(env, info, 3, argv, &argc);
+  lucent_renderer* r = argc >= 2 ? renderer_arg(env, argv[0]) : NULL;
+  if (!r) return NULL;
+  uint32_t samples = 0;
+  bool wait = true;
+  napi_get_value_uint32(env, argv[1], &samples);
+  if (argc >= 3) napi_get_value_bool(env, argv[2], &wait);  /* undefined keeps the default */
+  if (lucent_renderer_trace(r, samples, NULL) || (wait && lucent_renderer_check(r, NULL))) return throw_last(env);
+  return undefined(env);
+}
+
+/* setPipelining(r, on): successive waves on two path buffers and the
+ * renderer's own streams (default on; images identical either way). */
+static napi_value SetPipelining(napi_env env, napi_callback_info info) {
   napi_value argv[2];
   size_t argc;
   args(env, info, 2, argv, &argc);
   lucent_renderer* r = argc >= 2 ? renderer_arg(env, argv[0]) : NULL;
   if (!r) return NULL;
-  uint32_t samples = 0;
-  napi_get_value_uint32(env, argv[1], &samples);
-  if (lucent_renderer_trace(r, samples, NULL) || lucent_renderer_check(r, NULL)) return throw_last(env);
+  bool on = true;
+  napi_get_value_bool(env, argv[1], &on);
+  if (lucent_renderer_set_pipelining(r, on ? 1 : 0)) return throw_last(env);
   return undefined(env);
 }
 
@@ -839,6 +858,7 @@ static napi_value Init(napi_env env, napi_value exports) {
       {"reset", NULL, Reset, NULL, NULL, NULL, napi_default, NULL},
       {"resize", NULL, Resize, NULL, NULL, NULL, napi_default, NULL},
       {"trace", NULL, Trace, NULL, NULL, NULL, napi_default, NULL},
+      {"setPipelining", NULL, SetPipelining, NULL, NULL, NULL, napi_default, NULL},
       {"denoise", NULL, Denoise, NULL, NULL, NULL, napi_default, NULL},
       {"display", NULL, Display, NULL, NULL, NULL, napi_default, NULL},
       {"stats", NULL, Stats, NULL, NULL, NULL, napi_default, NULL},
