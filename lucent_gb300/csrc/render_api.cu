@@ -995,9 +995,9 @@ lucent_status lucent_renderer_trace(lucent_renderer* r, uint32_t samples, void* 
   const uint32_t batch = std::max(1u, std::min(samples, max_paths / std::max(1u, WH)));
   const uint32_t full = samples / batch, tail = samples % batch;
   MultiLaunch M{};
+  after_waves(r, s);  // the previous traces' accumulations first (the reprojection copies their result)
   lucent_status st = prepare_reprojection(r, s);
   if (st) return st;
-  after_waves(r, s);
   // Profiling (phase events on one stream, traversal counters) and ray
   // capture keep every wave on the caller's stream, in path set 0.
   const bool pipelined = r->pipeline && !r->profiling && !r->cap_mask && !r->trav_counters;
@@ -1531,6 +1531,7 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
     lucent_renderer* r = b->rs[i];
     if (!scene_owner(r)->has_scene || !r->has_lighting)
       return fail(LUCENT_ERR_INVALID, "renderer %d: trace before load_scene / upload_lighting", i);
+    after_waves(r, s);  // the renderer's own traces accumulate first
     lucent_status st = prepare_reprojection(r, s);
     if (st) return st;
     recs[i] = scene_rec(r);
@@ -1605,7 +1606,6 @@ lucent_status lucent_batch_trace(lucent_batch* b, uint32_t samples, void* stream
     cudaError_t e = cudaMemcpyAsync(X.base.ptr, hb.data(), 4 * hb.size(), cudaMemcpyHostToDevice, X.stream);
     if (e != cudaSuccess) return cuda_fail(e, "upload batch tables");
   }
-  for (lucent_renderer* r : b->rs) after_waves(r, s);  // the renderers' own traces accumulate first
   for (std::vector<WaveGraph>& g : b->graphs)
     if (g.size() != gs.size()) {
       b->destroy_graphs();
