@@ -1262,6 +1262,7 @@ lucent_status lucent_renderer_set_profiling(lucent_renderer* r, int32_t enabled)
 lucent_status lucent_renderer_check(lucent_renderer* r, void* stream) {
   clear_error();
   if (!r) return fail(LUCENT_ERR_INVALID, "null renderer");
+  after_waves(r, (cudaStream_t)stream);  // and so the waves themselves
   cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "synchronize");
   uint32_t word = 0;
@@ -1313,6 +1314,7 @@ lucent_status lucent_renderer_read(lucent_renderer* r, float* color4, float* alb
 lucent_status lucent_renderer_read_color_async(lucent_renderer* r, float* color4, void* stream) {
   clear_error();
   if (!r || !color4) return fail(LUCENT_ERR_INVALID, "null argument");
+  after_waves(r, (cudaStream_t)stream);
   cudaError_t e = cudaMemcpyAsync(color4, r->color.ptr, (size_t)r->W * r->H * 16, cudaMemcpyDeviceToHost,
                                   (cudaStream_t)stream);
   return e == cudaSuccess ? LUCENT_OK : cuda_fail(e, "read colour target");
@@ -1328,6 +1330,7 @@ lucent_status lucent_renderer_denoise(lucent_renderer* r, uint32_t levels, float
   if ((st = r->den_a.reserve(n * 16)) || (st = r->den_b.reserve(n * 16)) || (st = r->guide0.reserve(n * 16)) ||
       (st = r->guide1.reserve(n * 16)))
     return st;
+  after_waves(r, (cudaStream_t)stream);  // the traces' accumulations, wherever they were queued
   r->denoised = denoise_run(accum_of(r), r->cam, (int)r->W, (int)r->H, (int)levels, sigma_l, sigma_n, sigma_p,
                             (float4*)r->den_a.ptr, (float4*)r->den_b.ptr, (float4*)r->guide0.ptr,
                             (float4*)r->guide1.ptr, (cudaStream_t)stream);
@@ -1367,6 +1370,7 @@ lucent_status lucent_renderer_display_view(lucent_renderer* r, uint32_t view_w, 
   uchar4* d8 = (uchar4*)r->disp.ptr;
   float* drgb = (float*)((char*)r->disp.ptr + n * 4);
   cudaStream_t s = (cudaStream_t)stream;
+  after_waves(r, s);
   display_run(accum_of(r), denoise_weight > 0.f ? r->denoised : nullptr, (int)r->W, (int)r->H, (int)view_w,
               (int)view_h, denoise_weight, exposure, tonemap, rgba8_out ? d8 : nullptr, rgb_out ? drgb : nullptr, s);
   cudaError_t e = cudaGetLastError();
