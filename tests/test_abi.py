@@ -28,3 +28,17 @@ def test_null_arguments_rejected_before_any_device_work():
     assert st == 1 and b"null" in L.lucent_last_error()
     with pytest.raises(N.LucentError):
         N.check(st)
+
+
+def test_renderer_calls_reject_null_handles_without_device_work():
+    # Argument checks run before any CUDA call, so they hold without a GPU;
+    # the pipelining switch and the asynchronous read-back included.
+    from lucent_gb300 import _native_render  # noqa: F401  (declares the renderer signatures)
+    L = N.lib()
+    buf = (ctypes.c_float * 4)()
+    for st in (L.lucent_renderer_set_pipelining(None, 1),
+               L.lucent_renderer_read_color_async(None, buf, None),
+               L.lucent_renderer_set_wide_bvh(None, 1),
+               L.lucent_renderer_set_ray_sort(None, 1),
+               L.lucent_renderer_trace(None, 1, None)):
+        assert st == 1 and b"null" in L.lucent_last_error()
