@@ -193,7 +193,11 @@ class Renderer:
 
     # ------------------------------------------------------------------ work
     def trace_samples(self, count, stream=None):
-        """traceSamples (renderer.ts:702-737), asynchronous on `stream`."""
+        """traceSamples (renderer.ts:702-737), asynchronous on `stream`: the
+        samples are in the targets for work queued on `stream` afterwards.
+        With pipelining (default) the waves run on the renderer's own streams,
+        so successive calls overlap one wave's last bounces with the next's
+        first; only the accumulation is queued on `stream`."""
         N.check(N.lib().lucent_renderer_trace(self._h, count, stream))
 
     def check(self, stream=None):
